@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Benchmark of the vortex-particle FMM hot path on GB300.
+
+One step = one full RK stage of the reference's FMMCalculator::advance
+(fmmCalculator.hpp:919-1005) on device-resident bodies: tree build, interaction
+lists, P2M/M2M, M2L, L2L, L2P + P2P, stretching and the stage update.  The
+workload is the uniform cloud: N = 1,048,576 positions uniform in [-1, 1]^3,
+strengths N(0, 1e-3), sigma = 1.3 * 2 * N^(-1/3), theta = 0.5, leaf 64, RK2;
+synthetic inputs from a seed.  Metric: particle evaluations (velocity + J +
+dalpha/dt at one body for one RHS evaluation) per second, whole job.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With torchrun, each rank runs an independent replica on its own GPU (the
+single-system FMM does not shard without a halo exchange the reference does
+not have); value = sum of all ranks' particle evaluations / max rank time.
+--impl reference times the CPU implementation of the same path (the oracle
+restatement of the reference's own FMM, OpenMP, all host cores) on a bounded
+sample of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-evals/sec at N=1M, mixed vs FP64 GPU FMM at <=1e-6 rel L2 err"
+UNIT = "particle-evals/s"
+
+
+def parse(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--p", type=int, default=10)
+    ap.add_argument("--ncrit", type=int, default=64)
+    ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--dt", type=float, default=0.01)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 17, help="bodies in the CPU baseline's sample cloud")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--out", default=None, help="also write the JSON line to this file")
+    return ap.parse_args(argv)
+
+
+# ----------------------------------------------------------------- distributed
+class Dist:
+    """Replica bookkeeping: rank/world from torchrun's environment; barriers and
+    max-reductions over gloo (no data-path collective exists)."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples (SM clock, throttle reasons) during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) >= 9 for k in range(4) if "Active" in r[5 + k]
+                          and "Not" not in r[5 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ----------------------------------------------------------------- helpers
+def m2l_flops_per_pair(p: int) -> int:
+    """Useful complex multiply-adds of one M2L (j + n <= p - 1, all k <= j,
+    all m), 8 flops each, 3 components: 24 * sum_j (j+1)(p-j)^2."""
+    return 24 * sum((j + 1) * (p - j) ** 2 for j in range(p))
+
+
+P2P_FLOPS = 84  # per body-body interaction, counted from multipoleKernels.hpp:239-283
+
+
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def cpu_baseline(args, threads: int | None = None) -> dict:
+    """The oracle restatement of the reference's FMM (OpenMP, host cores): one
+    full stage (tree, lists, evaluation, Euler update) of a bounded sample."""
+    from oracle import oracle as O
+    from uvlm_gb300 import workloads
+    lib = O.oracle()
+    cores = lib.vo_set_threads(threads or os.cpu_count() or 1)
+    n = args.cpu_sample
+    b = workloads.cloud(n, seed=11)
+    t0 = time.perf_counter()
+    O.advance(b, args.p, args.ncrit, args.theta, args.dt, 1, 0)
+    t = time.perf_counter() - t0
+    return {"value": n / t, "unit": UNIT, "cores": cores, "kind": "port", "seconds": t,
+            "sample": f"one stage (tree, lists, FMM evaluation, update) of a {n}-body cloud of the same recipe "
+                      f"(p={args.p}, theta={args.theta}, leaf {args.ncrit}); FMM cost per body is ~independent of N"}
+
+
+def config_of(args, l2: str) -> dict:
+    return {"workload": "uniform cloud, one RK2 stage", "n_bodies": args.n, "p": args.p, "theta": args.theta,
+            "ncrit": args.ncrit, "integrator": "RK2", "precision": args.precision, "l2": l2}
+
+
+# ----------------------------------------------------------------- arms
+def run_reference(args, dist: Dist) -> dict | None:
+    if dist.rank != 0:
+        return None
+    from oracle import oracle as O
+    O.build_oracle()
+    for _ in range(args.warmup):
+        cpu_baseline(args)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        r = cpu_baseline(args)
+        vals.append(r["value"])
+        secs.append(r["seconds"])
+    value = args.cpu_sample * len(secs) / sum(secs)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform cloud)",
+            "config": config_of(args, "n/a (CPU)"), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": "port", "sample": r["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return line
+
+
+def run_ours(args, dist: Dist) -> dict | None:
+    from uvlm_gb300 import FMMCalculator, direct, lib, workloads
+    from uvlm_gb300._lib import BODY_DTYPE
+    n = args.n
+    calc = FMMCalculator(p=args.p, ncrit=args.ncrit, theta=args.theta, integration="RK2", precision=args.precision,
+                         device=dist.local_rank)
+    h = calc.handle
+    L = lib()
+    bodies = workloads.cloud(n, seed=1000 + dist.rank)
+    calc.load(bodies)
+    for w in range(args.warmup):
+        calc.stage(w % 2, args.dt)
+    L.vfmm_synchronize(h)
+    dist.barrier()
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    launches0 = L.vfmm_launch_count(h)
+    times = []
+    ms = ctypes.c_float()
+    for k in range(args.steps):
+        L.vfmm_flush_l2(h)  # evict L2 between timed steps (untimed)
+        L.vfmm_event_record(h, 0)
+        calc.stage((args.warmup + k) % 2, args.dt)
+        L.vfmm_event_record(h, 1)
+        L.vfmm_event_elapsed(h, 0, 1, ctypes.byref(ms))
+        times.append(ms.value * 1e-3)
+    launches = L.vfmm_launch_count(h) - launches0 - args.steps  # minus the L2 flushes
+    L.vfmm_synchronize(h)
+    clk = clocks.stop()
+    dist.barrier()
+    total = sum(times)
+    tmax = dist.max(total)
+    value = dist.world * n * args.steps / tmax
+    phases = calc.phase_times()
+    stats = calc.stats()
+
+    # roofline of the dominant kernel (phase timings of the last step, CUDA events on the handle's stream)
+    peak_fp = ctypes.c_double()
+    L.vfmm_measure_fma_peak(h, 0 if args.precision == "fp64" else 1, ctypes.byref(peak_fp))
+    m2l_flops = m2l_flops_per_pair(args.p) * stats["m2l_pairs"]
+    p2p_flops = P2P_FLOPS * stats["p2p_interactions"]
+    cand = {"m2l": (phases["m2l"], m2l_flops), "l2p_p2p": (phases["l2p_p2p"], p2p_flops)}
+    dom = max(cand, key=lambda k: cand[k][0])
+    t_dom, f_dom = cand[dom]
+    achieved = f_dom / (t_dom * 1e-3) / 1e12
+    roof = {"bound": "fp64" if args.precision == "fp64" else "fp32", "kernel": dom, "achieved": achieved,
+            "peak": peak_fp.value, "unit": "TFLOP/s", "frac": achieved / peak_fp.value if peak_fp.value else None,
+            "traffic": None,
+            "peak_source": "measured on this GPU in this run: FMA-chain probe kernel (vfmm_measure_fma_peak); "
+                           "MEASURED_PEAKS.json has no CUDA-core figure",
+            "algorithmic_flops_per_launch": f_dom, "kernel_ms": t_dom}
+
+    # end to end through the public API: vfmm_advance on pinned host AoS bodies
+    host = workloads.cloud(n, seed=2000 + dist.rank)
+    L.vfmm_host_register(host.ctypes.data, host.nbytes)
+    calc.advance(host, args.dt)  # warm-up
+    dist.barrier()
+    e2e_t = []
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        calc.advance(host, args.dt)
+        e2e_t.append(time.perf_counter() - t0)
+    L.vfmm_host_unregister(host.ctypes.data)
+    e2e_total = dist.max(sum(e2e_t))
+    stages = calc.num_stages
+    e2e_value = dist.world * n * stages * len(e2e_t) / e2e_total
+
+    accuracy = None
+    if not args.no_accuracy and dist.rank == 0:
+        accuracy = measure_accuracy(args, calc)
+    calc.close()
+    if dist.rank != 0:
+        return None
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (seeded uniform cloud; no dataset)",
+            "config": config_of(args, "flushed between steps (256 MB write)"),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * BODY_DTYPE.itemsize,
+                    "d2h_bytes_per_step": n * BODY_DTYPE.itemsize,
+                    "note": f"vfmm_advance (RK2 = {stages} stages) on pinned host exafmm::Body arrays, wall clock"},
+            "gpu_launches": int(launches),
+            "roofline": roof, "clocks": clk, "phases_ms": phases, "tree": stats}
+    if accuracy:
+        line["accuracy"] = accuracy
+    if not args.no_cpu_baseline and dist.world == 1:
+        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(args).items() if k != "seconds"}
+    return line
+
+
+def measure_accuracy(args, calc) -> dict:
+    """rel-L2 velocity and J errors of this run's FMM on 4096 targets against the
+    FP64 direct sum with the reference's regularised kernel."""
+    from uvlm_gb300 import direct, workloads
+    b = workloads.cloud(args.n, seed=3000)
+    b["drdt_old"] = np.arange(b.size)  # survives init/calculate: recovers the tree permutation
+    calc.init(b)
+    calc.calculate()
+    calc.copyBodies2Host(b)
+    order = np.argsort(b["drdt_old"].astype(np.int64))
+    fmm = b[order][:4096]
+    src = workloads.cloud(args.n, seed=3000)
+    ref = direct(src[:4096].copy(), src)
+
+    def rl2(a, r):
+        return float(np.linalg.norm(a - r) / np.linalg.norm(r))
+    return {"targets": 4096, "vs": "FP64 direct sum (regularised kernel, all pairs)",
+            "velocity_rel_l2": rl2(fmm["velocity"], ref["velocity"]), "J_rel_l2": rl2(fmm["J"], ref["J"]),
+            "note": "the reference's far field is the singular kernel, so this error includes the model's "
+                    "un-regularised far field, independent of arithmetic precision"}
+
+
+def main(argv=None):
+    args = parse(argv)
+    dist = Dist()
+    if args.impl == "reference":
+        line = run_reference(args, dist)
+    else:
+        from uvlm_gb300 import _build, _lib
+        if not os.path.exists(_lib.LIB_PATH):
+            _build.build()
+        line = run_ours(args, dist)
+    if line is not None:
+        s = json.dumps(line)
+        print(s, flush=True)
+        if args.out:
+            with open(args.out, "w") as f:
+                f.write(s + "\n")
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

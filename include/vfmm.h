@@ -1,0 +1,203 @@
+/* vfmm — GB300-native vortex-particle FMM: the C ABI.
+ *
+ * Drop-in for the particle velocity-and-stretching evaluation of
+ * kursatyurt/UVLM, whose call surface is the header-only class template
+ * Vortex::FMMCalculator<Host, Device, Integration, Viscous, Formulation,
+ * Stretching> (src/fmmCalculator.hpp:25-26) and the free functions
+ * exafmm::buildTree (src/tree.hpp:101) and exafmm::getList
+ * (src/traverse.hpp:32).  The reference has no FFI of its own; each entry
+ * point below names the reference function it replaces.  include/vfmm.hpp
+ * wraps these calls in a class with the reference's method names.
+ *
+ * Conventions
+ *  - Every function returns a vfmm_status; VFMM_OK is 0.  After an error,
+ *    vfmm_last_error(h) describes it.  A handle owns one CUDA stream and all
+ *    of its device memory; calls on one handle must not overlap.
+ *  - Bodies cross the boundary as arrays of vfmm_body, byte-compatible with
+ *    the reference's exafmm::Body (37 doubles, 296 bytes).
+ *  - Compile-time constants of the reference (P, ncrit, MAC_theta,
+ *    exafmmTypes.hpp:12-15) and its template policy tags
+ *    (fmmCalculator.hpp:9-23) are fields of vfmm_config.
+ */
+#ifndef VFMM_H
+#define VFMM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  VFMM_OK               = 0,
+  VFMM_ERR_INVALID      = 1, /* bad argument or configuration */
+  VFMM_ERR_NONFINITE    = 2, /* NaN/Inf in positions, strengths or radii */
+  VFMM_ERR_DEPTH        = 3, /* more than ncrit bodies closer than the deepest level can split */
+  VFMM_ERR_CAPACITY     = 4, /* an internal list outgrew its capacity (handled internally; reported only if growth fails) */
+  VFMM_ERR_CUDA         = 5, /* a CUDA call failed */
+  VFMM_ERR_TIMEOUT      = 6, /* a bounded device-side wait gave up */
+  VFMM_ERR_UNSUPPORTED  = 7, /* configuration not implemented (e.g. an expansion order outside 2..16) */
+  VFMM_ERR_STATE        = 8  /* call order violated (e.g. calculate before init) */
+} vfmm_status;
+
+/* Integration scheme: Vortex::Euler / RK2 / RK3 / RK4 (fmmCalculator.hpp:14-17). */
+enum { VFMM_EULER = 0, VFMM_RK2 = 1, VFMM_RK3 = 2, VFMM_RK4 = 3 };
+/* Stretching formulation: Vortex::Transposed / Classic (fmmCalculator.hpp:22-23). */
+enum { VFMM_TRANSPOSED = 0, VFMM_CLASSIC = 1 };
+/* VPM formulation: Vortex::cVPM / rVPM (fmmCalculator.hpp:19-20). */
+enum { VFMM_CVPM = 0, VFMM_RVPM = 1 };
+/* Arithmetic of the evaluation: FP64 throughout (the drop-in), or mixed
+ * (FP32 P2P with compensated sums, FP32 P2M/M2L/L2P with per-level scaling,
+ * FP64 tree, and FP64 M2M/L2L when p >= 10). */
+enum { VFMM_FP64 = 0, VFMM_MIXED = 1 };
+
+typedef struct {
+  int    p;           /* expansion terms n = 0..p-1; reference P (exafmmTypes.hpp:12); 2..16 */
+  int    ncrit;       /* bodies per leaf; reference ncrit (exafmmTypes.hpp:14); 1..256 */
+  double theta;       /* multipole acceptance criterion; reference MAC_theta (exafmmTypes.hpp:15) */
+  int    precision;   /* VFMM_FP64 or VFMM_MIXED */
+  int    integrator;  /* VFMM_EULER .. VFMM_RK4 */
+  int    stretching;  /* VFMM_TRANSPOSED or VFMM_CLASSIC */
+  int    formulation; /* VFMM_CVPM or VFMM_RVPM */
+  double relax;       /* relaxation factor f in [0,1]; 0 = off (relaxation.hpp:8-19) */
+  int    rk4_fixed;   /* 1: RK4 stage 3 uses dt; 0: 0.5*dt as the reference (fmmCalculator.hpp:683-689) */
+  int    device;      /* CUDA device ordinal; -1 = the caller's current device */
+  int    reserved[6];
+} vfmm_config;
+
+/* exafmm::Body (exafmmTypes.hpp:18-32), 296 bytes. J[a][b] = du_a/dx_b. */
+typedef struct {
+  double J[3][3];
+  double X[3];
+  double alpha[3];
+  double velocity[3];
+  double dadt[3];
+  double velocity_old[3];
+  double dadt_old[3];
+  double X_old[3];
+  double alpha_old[3];
+  double radius;
+  double drdt;
+  double radius_old;
+  double drdt_old;
+} vfmm_body;
+
+/* exafmm::Cell without its pointers (exafmmTypes.hpp:36-46), 72 bytes. */
+typedef struct {
+  uint64_t NCHILD;
+  uint64_t NBODY;
+  uint64_t ChildOffset;
+  uint64_t BodyOffset;
+  double   X[3];
+  double   R;
+  uint64_t level;
+} vfmm_cell;
+
+typedef struct vfmm_handle_s *vfmm_handle;
+
+/* Defaults of the reference: p=4, ncrit=128, theta=0.3, RK3, Transposed,
+ * cVPM, FP64, no relaxation (exafmmTypes.hpp:12-15, main.cpp:119), current device. */
+void vfmm_default_config(vfmm_config *cfg);
+
+/* Create / destroy a calculator on the current CUDA device (the reference
+ * constructs Vortex::FMMCalculator by value, fmmCalculator.hpp:25-26). */
+int vfmm_create(const vfmm_config *cfg, vfmm_handle *out);
+int vfmm_destroy(vfmm_handle h);
+const char *vfmm_last_error(vfmm_handle h);
+int vfmm_get_config(vfmm_handle h, vfmm_config *cfg);
+
+/* FMMCalculator::init (fmmCalculator.hpp:282-288): copy the bodies to the
+ * device, build the octree (exafmm::buildTree, tree.hpp:101-113) and the
+ * interaction lists (exafmm::getList, traverse.hpp:32-85).  As in the
+ * reference, `bodies` is permuted in place into tree order. */
+int vfmm_init(vfmm_handle h, vfmm_body *bodies, size_t n);
+
+/* FMMCalculator::calculate (fmmCalculator.hpp:420-467): velocity, J and
+ * dadt (stretching, plus rVPM terms when configured) of the bodies given to
+ * the last vfmm_init, left on the device. */
+int vfmm_calculate(vfmm_handle h);
+
+/* FMMCalculator::copyBodies2Host (fmmCalculator.hpp:235-243): the device
+ * bodies, in tree order, into `bodies` (n must match the last init). */
+int vfmm_copy_bodies_to_host(vfmm_handle h, vfmm_body *bodies, size_t n);
+
+/* FMMCalculator::advance (fmmCalculator.hpp:919-1005): one time step of the
+ * configured scheme; each stage rebuilds the tree from the current
+ * positions.  `bodies` is read, then overwritten with the bodies after the
+ * step in the last stage's tree order (velocity, J, dadt from the last stage's
+ * evaluation).  With relax > 0, relaxation follows the step (using that J). */
+int vfmm_advance(vfmm_handle h, vfmm_body *bodies, size_t n, double dt);
+
+/* FMMCalculator::getSensorData (fmmCalculator.hpp:726-731): velocity (and,
+ * from the far field, J) at probe points from the particles of the last
+ * init/calculate.  `sensors` is permuted into its own tree order. */
+int vfmm_get_sensor_data(vfmm_handle h, vfmm_body *sensors, size_t n);
+
+/* Relaxation (relaxation.hpp:8-19, written 0-based) of the device bodies with
+ * factor f, using the J of the last evaluation. */
+int vfmm_relax(vfmm_handle h, double f);
+
+/* The tree of the last init (exafmm::buildTree output, tree.hpp:101): cells in
+ * the reference's order.  *ncells receives the count; at most `cap` are written. */
+int vfmm_get_tree(vfmm_handle h, vfmm_cell *cells, size_t cap, size_t *ncells);
+
+/* The interaction lists of the last init (exafmm::getList, traverse.hpp:32):
+ * (target, source) cell pairs, sorted by target then source.  Counts are
+ * always written; pairs are written when the capacities suffice. */
+int vfmm_get_lists(vfmm_handle h, uint64_t *p2p, size_t cap_p2p, size_t *n_p2p, uint64_t *m2l, size_t cap_m2l, size_t *n_m2l);
+
+/* Multipole and local expansions of the last calculate, as
+ * ncells * 3*p(p+1)/2 complex doubles (interleaved re, im) in the reference's
+ * layout [cell][3*(n(n+1)/2+m) + d] (multipoleKernels.hpp:468-471). */
+int vfmm_get_expansions(vfmm_handle h, double *M, double *L, size_t cap_cells);
+
+/* ---- device-resident stepping (inputs already in HBM) ------------------- */
+
+/* Upload bodies once (no tree yet); later stages work on the device copy. */
+int vfmm_load(vfmm_handle h, const vfmm_body *bodies, size_t n);
+/* One stage of the configured scheme on the device copy: tree, lists,
+ * evaluation, stretching and the stage update (stage = 0 .. stages-1). */
+int vfmm_stage(vfmm_handle h, int stage, double dt);
+/* Number of stages per step of the configured scheme (1, 2, 3 or 4). */
+int vfmm_num_stages(vfmm_handle h);
+
+/* ---- direct sum ---------------------------------------------------------- */
+
+/* FP64 all-pairs sum with the reference's regularised kernel
+ * (multipoleKernels.hpp:239-283): velocity and J at `nt` targets from `ns`
+ * sources, all arrays on the host; the targets' velocity and J are
+ * overwritten.  The reference's exafmm::direct (traverse.hpp:88) computes
+ * the same velocity. */
+int vfmm_direct(vfmm_handle h, vfmm_body *targets, size_t nt, const vfmm_body *sources, size_t ns);
+
+/* ---- instrumentation ----------------------------------------------------- */
+
+/* Record event `slot` (0..15) on the handle's stream; elapsed ms between two
+ * recorded slots (waits for the later one). */
+int vfmm_event_record(vfmm_handle h, int slot);
+int vfmm_event_elapsed(vfmm_handle h, int slot_a, int slot_b, float *ms);
+int vfmm_synchronize(vfmm_handle h);
+/* Kernel launches issued by this handle since creation. */
+uint64_t vfmm_launch_count(vfmm_handle h);
+/* Per-phase device time of the last calculate/stage, ms: [0] tree+lists,
+ * [1] upward, [2] M2L, [3] downward L2L, [4] L2P+P2P, [5] update. */
+int vfmm_phase_times(vfmm_handle h, float *ms, int n);
+/* Sizes of the last tree: cells, leaves, P2P pairs, M2L pairs, P2P body-body
+ * interactions (self pairs excluded), max level. */
+int vfmm_tree_stats(vfmm_handle h, uint64_t *stats, int n);
+/* Page-lock a host range for fast copies (cudaHostRegister). */
+int vfmm_host_register(void *ptr, size_t bytes);
+int vfmm_host_unregister(void *ptr);
+/* Fill a device scratch buffer larger than L2 to evict cached data. */
+int vfmm_flush_l2(vfmm_handle h);
+/* Measured CUDA-core throughput of independent FMA chains on this GPU, in
+ * TFLOP/s (2 flops per FMA): precision VFMM_FP64 or VFMM_MIXED (FP32).  The
+ * roofline denominator for the compute-bound FMM kernels, which run on the
+ * FP64/FP32 pipes rather than on tensor cores. */
+int vfmm_measure_fma_peak(vfmm_handle h, int precision, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1042,3 +1042,24 @@ void vo_relax(Body *b, long n, double f)
 }
 
 } // extern "C"
+
+extern "C" {
+// L2P alone (complex-step form of multipoleKernels.hpp:630-742) for one body:
+// local expansion Lc (3K complex, reference layout) about centre C, body at X;
+// adds the far-field velocity (3) and J (9, row-major) into out[12].
+void vo_l2p_body(int P, const double *Lc, const double *C, const double *X, double *out)
+{
+  vo::FMM f(P, 1, 0.5);
+  vo::Cell c{};
+  for (int d = 0; d < 3; d++)
+    c.X[d] = C[d];
+  vo::Body b{};
+  for (int d = 0; d < 3; d++)
+    b.X[d] = X[d];
+  f.L2P_body(reinterpret_cast<const vo::cd *>(Lc), c, b);
+  for (int d = 0; d < 3; d++)
+    out[d] = b.velocity[d];
+  for (int k = 0; k < 9; k++)
+    out[3 + k] = b.J[k / 3][k % 3];
+}
+}

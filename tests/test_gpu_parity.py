@@ -1,0 +1,158 @@
+"""CUDA path (libvfmm.so through the C ABI) against the reference's golden
+fixtures and the oracle restatement.  Bit-exact for the tree, the body order
+and the interaction lists; FP64 fields within 1e-10 (max-abs relative), the
+bar the drop-in must meet against the reference's own FMM."""
+import numpy as np
+import pytest
+
+from conftest import golden, golden_bodies, rel
+
+pytestmark = pytest.mark.gpu
+
+EVAL = ["cloud_p6_c16_t05", "ring_p8_c32_t05", "cloud_p10_c64_t05", "cloud_p4_c128_t03", "cloud_p14_c32_t05",
+        "classic_rvpm_p6", "root_leaf", "coincident", "lattice_ties"]
+ADV = ["advance_rk2_ring", "advance_rk3_cloud", "advance_euler_cloud", "advance_rk4_cloud"]
+TOL = 1e-10
+SCHEMES = {0: "Euler", 1: "RK2", 2: "RK3", 3: "RK4"}
+
+
+def calc_for(d, **kw):
+    from uvlm_gb300 import FMMCalculator
+    form = int(d["formulation"]) if "formulation" in d.files else 0
+    return FMMCalculator(p=int(d["P"]), ncrit=int(d["ncrit"]), theta=float(d["theta"]),
+                         stretching="Classic" if int(d["stretching"]) else "Transposed",
+                         formulation="rVPM" if form else "cVPM", **kw)
+
+
+def near_axis_mask(cells, X, limit=1e-4):
+    """Bodies (tree order) whose offset from their leaf centre is within
+    sin(theta) < limit of the leaf's z axis.  There the reference's L2P, which
+    differentiates in spherical coordinates by a complex step and divides by
+    sin(theta) (multipoleKernels.hpp:44-47, :94-134), loses up to ~1e-8 of
+    J's absolute accuracy; the Cartesian derivatives used here do not."""
+    mask = np.zeros(len(X), bool)
+    for c in cells[cells["NCHILD"] == 0]:
+        s = slice(int(c["BodyOffset"]), int(c["BodyOffset"] + c["NBODY"]))
+        d = X[s] - c["X"]
+        r = np.sqrt((d ** 2).sum(1))
+        mask[s] = np.hypot(d[:, 0], d[:, 1]) < limit * np.maximum(r, 1e-300)
+    return mask
+
+
+@pytest.mark.parametrize("name", EVAL)
+def test_tree_lists_exact(vfmm_lib, name):
+    d = golden(name)
+    b = golden_bodies(d)
+    with calc_for(d) as c:
+        bb = b.copy()
+        c.init(bb)
+        assert (bb["X"] == b["X"][d["perm"]]).all(), "body order"
+        cells = c.tree()
+        ref = d["cells"]
+        assert cells.shape == ref.shape
+        for f in ["NCHILD", "NBODY", "ChildOffset", "BodyOffset", "level"]:
+            assert (cells[f] == ref[f]).all(), f
+        assert (cells["X"] == ref["X"]).all() and (cells["R"] == ref["R"]).all()
+        p2p, m2l = c.lists()
+        assert (p2p == d["p2p"]).all()
+        assert (m2l == d["m2l"]).all()
+
+
+@pytest.mark.parametrize("name", EVAL)
+def test_evaluation_matches_reference(vfmm_lib, name):
+    d = golden(name)
+    b = golden_bodies(d)
+    with calc_for(d) as c:
+        bb = b.copy()
+        c.init(bb)
+        c.calculate()
+        c.copyBodies2Host(bb)
+        if "M" in d.files:
+            M, L = c.expansions()
+            sel = d["cell_sel"]
+            assert rel(M[sel], d["M"]) < TOL
+            assert rel(L[sel], d["L"]) < TOL
+    axis = near_axis_mask(d["cells"], bb["X"])
+    for f in ["velocity", "J", "dadt", "drdt"]:
+        assert rel(bb[f][~axis], d[f][~axis]) < TOL, f
+        assert rel(bb[f], d[f]) < 1e-6, f
+
+
+@pytest.mark.parametrize("name", ADV)
+def test_advance_matches_reference(vfmm_lib, name):
+    d = golden(name)
+    b = golden_bodies(d)
+    with calc_for(d, integration=SCHEMES[int(d["scheme"])]) as c:
+        for _ in range(int(d["steps"])):
+            c.advance(b, float(d["dt"]))
+    for f in ["X", "alpha", "radius", "velocity", "J"]:
+        assert rel(b[f], d["out_" + f]) < TOL, f
+
+
+@pytest.mark.parametrize("kind,n,P,ncrit", [("cloud", 20000, 8, 32), ("ring", 64, 8, 32), ("cloud", 30000, 12, 64)])
+def test_larger_against_oracle(vfmm_lib, kind, n, P, ncrit):
+    from oracle import oracle as O
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(n, seed=21) if kind == "cloud" else workloads.ring(n, seed=21)
+    ob, oc = O.build_tree(b, ncrit)
+    ref = O.calculate(b, P, ncrit, 0.5)
+    with FMMCalculator(p=P, ncrit=ncrit, theta=0.5) as c:
+        bb = b.copy()
+        c.init(bb)
+        assert (bb["X"] == ob["X"]).all()
+        cells = c.tree()
+        assert cells.shape == oc.shape and (cells == oc).all()
+        p2p, m2l = c.lists()
+        op2p, om2l = O.lists(oc, 0.5)
+        assert (p2p == op2p[np.lexsort((op2p[:, 1], op2p[:, 0]))]).all()
+        assert (m2l == om2l[np.lexsort((om2l[:, 1], om2l[:, 0]))]).all()
+        c.calculate()
+        c.copyBodies2Host(bb)
+    for f in ["velocity", "J", "dadt"]:
+        assert rel(bb[f], ref[f]) < TOL, f
+
+
+def test_direct_sum_against_oracle(vfmm_lib):
+    from oracle import oracle as O
+    from uvlm_gb300 import direct, workloads
+    src = workloads.cloud(5000, seed=3)
+    tgt = src[:700].copy()
+    out = direct(tgt, src)
+    ref = O.direct(tgt, src)
+    assert rel(out["velocity"], ref["velocity"]) < 1e-13
+    assert rel(out["J"], ref["J"]) < 1e-13
+
+
+def test_relaxation_matches_oracle(vfmm_lib):
+    from oracle import oracle as O
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.ring(16, seed=4)
+    ref = O.advance(b, 6, 32, 0.5, 0.01, 2, 1, relax=0.3)
+    with FMMCalculator(p=6, ncrit=32, theta=0.5, integration="RK2", relax=0.3) as c:
+        for _ in range(2):
+            c.advance(b, 0.01)
+    for f in ["X", "alpha", "velocity"]:
+        assert rel(b[f], ref[f]) < TOL, f
+
+
+def test_errors_are_reported(vfmm_lib):
+    from uvlm_gb300 import FMMCalculator, VfmmError, workloads
+    b = workloads.cloud(500, seed=1)
+    b["X"][17, 1] = np.nan
+    with FMMCalculator(p=6, ncrit=16, theta=0.5) as c:
+        with pytest.raises(VfmmError) as e:
+            c.init(b.copy())
+        assert e.value.code == 2
+        dup = workloads.cloud(100, seed=2)
+        dup["X"][:40] = dup["X"][0]  # 40 coincident bodies > ncrit: no depth splits them
+        with pytest.raises(VfmmError) as e:
+            c.init(dup)
+        assert e.value.code == 3
+        with pytest.raises(VfmmError) as e:
+            c.calculate()  # no valid tree after the failed init
+        # a good call still works on the same handle afterwards
+        good = workloads.cloud(300, seed=3)
+        c.init(good)
+        c.calculate()
+    with pytest.raises(VfmmError):
+        FMMCalculator(p=40)

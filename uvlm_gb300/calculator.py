@@ -1,0 +1,163 @@
+"""Host-side mirror of the reference's Vortex::FMMCalculator (src/fmmCalculator.hpp).
+
+The reference selects its behaviour with template policy tags
+(fmmCalculator.hpp:9-26): integration scheme Euler/RK2/RK3/RK4, viscous
+scheme Inviscid/PSE/CSM, formulation cVPM/rVPM, stretching Transposed/Classic;
+and with compile-time constants P, ncrit, MAC_theta (exafmmTypes.hpp:12-15).
+Here they are constructor arguments.  Methods keep the reference's names and
+meaning: `init(bodies)` builds the tree and permutes `bodies` into tree order,
+`calculate()` evaluates velocity, J and dadt on the device,
+`copyBodies2Host(bodies)` brings them back, `advance(bodies, dt)` runs one
+time step and overwrites `bodies`.  Every call goes through libvfmm.so.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import BODY_DTYPE, CELL_DTYPE, check, lib
+
+_SCHEMES = {"Euler": _lib.EULER, "RK2": _lib.RK2, "RK3": _lib.RK3, "RK4": _lib.RK4}
+_STRETCH = {"Transposed": _lib.TRANSPOSED, "Classic": _lib.CLASSIC}
+_FORM = {"cVPM": _lib.CVPM, "rVPM": _lib.RVPM}
+_PREC = {"fp64": _lib.FP64, "mixed": _lib.MIXED}
+
+
+class FMMCalculator:
+    def __init__(self, p: int = 4, ncrit: int = 128, theta: float = 0.3, integration: str = "RK3",
+                 viscous: str = "Inviscid", formulation: str = "cVPM", stretching: str = "Transposed",
+                 precision: str = "fp64", relax: float = 0.0, rk4_fixed: bool = False, device: int = -1):
+        if viscous != "Inviscid":
+            raise NotImplementedError("only the Inviscid scheme is implemented (PSE/CSM are not on this path)")
+        cfg = _lib.vfmm_config()
+        lib().vfmm_default_config(ctypes.byref(cfg))
+        cfg.p, cfg.ncrit, cfg.theta = int(p), int(ncrit), float(theta)
+        cfg.precision = _PREC[precision]
+        cfg.integrator = _SCHEMES[integration]
+        cfg.stretching = _STRETCH[stretching]
+        cfg.formulation = _FORM[formulation]
+        cfg.relax = float(relax)
+        cfg.rk4_fixed = int(bool(rk4_fixed))
+        cfg.device = int(device)
+        h = ctypes.c_void_p()
+        code = lib().vfmm_create(ctypes.byref(cfg), ctypes.byref(h))
+        if code != 0:
+            raise _lib.VfmmError(code, "vfmm_create failed")
+        self._h = h
+        self.config = cfg
+        self.n = 0
+
+    # -- lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().vfmm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, code: int) -> None:
+        check(self._h, code)
+
+    # -- FMMCalculator surface (fmmCalculator.hpp)
+    def init(self, bodies: np.ndarray) -> None:
+        b = _lib.as_bodies(bodies)
+        self._check(lib().vfmm_init(self._h, b.ctypes.data, b.size))
+        self.n = b.size
+
+    def calculate(self) -> None:
+        self._check(lib().vfmm_calculate(self._h))
+
+    def copyBodies2Host(self, bodies: np.ndarray) -> None:
+        b = _lib.as_bodies(bodies)
+        self._check(lib().vfmm_copy_bodies_to_host(self._h, b.ctypes.data, b.size))
+
+    def advance(self, bodies: np.ndarray, dt: float) -> None:
+        b = _lib.as_bodies(bodies)
+        self._check(lib().vfmm_advance(self._h, b.ctypes.data, b.size, float(dt)))
+        self.n = b.size
+
+    def getSensorData(self, sensors: np.ndarray) -> None:
+        s = _lib.as_bodies(sensors)
+        self._check(lib().vfmm_get_sensor_data(self._h, s.ctypes.data, s.size))
+
+    def relax(self, f: float) -> None:
+        self._check(lib().vfmm_relax(self._h, float(f)))
+
+    # -- inspection
+    def tree(self) -> np.ndarray:
+        n = ctypes.c_size_t()
+        self._check(lib().vfmm_get_tree(self._h, None, 0, ctypes.byref(n)))
+        cells = np.zeros(n.value, CELL_DTYPE)
+        self._check(lib().vfmm_get_tree(self._h, cells.ctypes.data, cells.size, ctypes.byref(n)))
+        return cells
+
+    def lists(self) -> tuple[np.ndarray, np.ndarray]:
+        a, b = ctypes.c_size_t(), ctypes.c_size_t()
+        self._check(lib().vfmm_get_lists(self._h, None, 0, ctypes.byref(a), None, 0, ctypes.byref(b)))
+        p2p = np.zeros((a.value, 2), np.uint64)
+        m2l = np.zeros((b.value, 2), np.uint64)
+        self._check(lib().vfmm_get_lists(self._h, p2p.ctypes.data, a.value, ctypes.byref(a),
+                                         m2l.ctypes.data, b.value, ctypes.byref(b)))
+        return p2p, m2l
+
+    def expansions(self) -> tuple[np.ndarray, np.ndarray]:
+        nc = self.stats()["cells"]
+        p = self.config.p
+        K3 = 3 * p * (p + 1) // 2
+        M = np.zeros((nc, K3), np.complex128)
+        L = np.zeros((nc, K3), np.complex128)
+        self._check(lib().vfmm_get_expansions(self._h, M.ctypes.data, L.ctypes.data, nc))
+        return M, L
+
+    def stats(self) -> dict:
+        v = (ctypes.c_uint64 * 6)()
+        self._check(lib().vfmm_tree_stats(self._h, v, 6))
+        return dict(zip(["cells", "leaves", "p2p_pairs", "m2l_pairs", "p2p_interactions", "max_level"], map(int, v)))
+
+    def phase_times(self) -> dict:
+        v = (ctypes.c_float * 6)()
+        self._check(lib().vfmm_phase_times(self._h, v, 6))
+        return dict(zip(["tree_lists", "upward", "m2l", "l2l", "l2p_p2p", "update"], map(float, v)))
+
+    # -- device-resident stepping
+    def load(self, bodies: np.ndarray) -> None:
+        b = _lib.as_bodies(bodies)
+        self._check(lib().vfmm_load(self._h, b.ctypes.data, b.size))
+        self.n = b.size
+
+    def stage(self, stage: int, dt: float) -> None:
+        self._check(lib().vfmm_stage(self._h, int(stage), float(dt)))
+
+    @property
+    def num_stages(self) -> int:
+        return int(lib().vfmm_num_stages(self._h))
+
+    @property
+    def handle(self):
+        return self._h
+
+
+def direct(targets: np.ndarray, sources: np.ndarray) -> np.ndarray:
+    """FP64 all-pairs velocity and J on the GPU (regularised kernel); returns a
+    copy of `targets` with velocity and J filled."""
+    t = np.ascontiguousarray(_lib.as_bodies(targets).copy())
+    s = _lib.as_bodies(np.ascontiguousarray(sources))
+    with FMMCalculator() as c:
+        c._check(lib().vfmm_direct(c._h, t.ctypes.data, t.size, s.ctypes.data, s.size))
+    return t
+
+
+def new_bodies(n: int) -> np.ndarray:
+    return np.zeros(n, BODY_DTYPE)

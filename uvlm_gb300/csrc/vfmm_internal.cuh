@@ -1,0 +1,193 @@
+// Internal declarations shared by the vfmm CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include "../../include/vfmm.h"
+
+namespace vfmm {
+
+// Tree depth limit: a 63-bit key holds 21 octant digits.
+constexpr int MAXL = 21;
+constexpr int PMIN = 2, PMAX = 16;
+constexpr int NCRIT_MAX = 256;
+
+// Body fields in device memory, field-major (field f of body i at
+// f*cap + i), in the order of exafmm::Body (exafmmTypes.hpp:18-32) so that the
+// 296-byte records transpose directly.
+enum BodyField {
+  F_J = 0, // 9: J[a][b] at F_J + 3a + b
+  F_X = 9,
+  F_A = 12,
+  F_U = 15,
+  F_DADT = 18,
+  F_VOLD = 21,
+  F_DOLD = 24,
+  F_XOLD = 27,
+  F_AOLD = 30,
+  F_R = 33,
+  F_DRDT = 34,
+  F_ROLD = 35,
+  F_DRDTOLD = 36,
+  NFIELD = 37
+};
+
+// Device-side scalars of one tree build and evaluation.  Counters are
+// written by kernels and read back by the host at the two sync points of a
+// stage (after node enumeration, after traversal).
+struct DevInfo {
+  double   X0[3];
+  double   R0;
+  int      err;         // VFMM_ERR_* raised by a kernel
+  int      nnodes;      // cells of the tree
+  int      nleaves;
+  int      maxLevel;
+  int      front_n[2];  // traversal frontier sizes (ping-pong)
+  int      n_p2p, n_m2l;
+  int      overflow;    // 1 if a capacity was exceeded
+  int      nonfinite;   // 1 if an input was NaN/Inf
+  unsigned long long p2p_interactions;
+  int      pad[6];
+};
+
+// Cells in the reference's order (tree.hpp:29-99), structure of arrays.
+struct CellsView {
+  int    *nchild, *nbody, *child, *body, *level, *parent;
+  double *x, *y, *z, *R;
+};
+
+// Launch bookkeeping (kernel count for instrumentation).
+extern thread_local unsigned long long *g_launch_counter;
+inline void count_launch()
+{
+  if (g_launch_counter)
+    (*g_launch_counter)++;
+}
+
+#define VFMM_CUDA_TRY(expr)                                                                            \
+  do {                                                                                                 \
+    cudaError_t e_ = (expr);                                                                           \
+    if (e_ != cudaSuccess) {                                                                           \
+      throw ::vfmm::Error(VFMM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_));         \
+    }                                                                                                  \
+  } while (0)
+
+#define VFMM_LAUNCH_CHECK() VFMM_CUDA_TRY(cudaGetLastError())
+
+struct Error {
+  int         code;
+  std::string msg;
+  Error(int c, std::string m) : code(c), msg(std::move(m)) {}
+};
+
+// Grow-only device buffer.
+template <class T>
+struct DevBuf {
+  T     *p   = nullptr;
+  size_t cap = 0;
+  void   reserve(size_t n)
+  {
+    if (n <= cap)
+      return;
+    if (p)
+      cudaFree(p);
+    p   = nullptr;
+    cap = 0;
+    size_t want = n + n / 4 + 64;
+    VFMM_CUDA_TRY(cudaMalloc((void **)&p, want * sizeof(T)));
+    cap = want;
+  }
+  void release()
+  {
+    if (p)
+      cudaFree(p);
+    p   = nullptr;
+    cap = 0;
+  }
+};
+
+inline int grid_for(long n, int block, int maxBlocks = 152 * 16)
+{
+  long g = (n + block - 1) / block;
+  if (g < 1)
+    g = 1;
+  if (g > maxBlocks)
+    g = maxBlocks;
+  return (int)g;
+}
+
+// ---- tree.cu
+struct TreeScratch {
+  DevBuf<uint64_t> keys, skeys;
+  DevBuf<uint32_t> idx, sidx, perm;
+  DevBuf<int>      lvl, lo, hi, cnt, off;
+  DevBuf<int>      nlevel, nstart, ncount, nparent, nchild, nrank, nref, nbs, nsortidx, nsortlvl, nflag, noff;
+  DevBuf<double>   bbox_part;
+  DevBuf<unsigned char> cub_tmp;
+  size_t           cub_bytes = 0;
+};
+void tree_bounds(cudaStream_t s, const double *X, size_t cap, int n, DevInfo *info, TreeScratch &ts);
+void tree_sort_bodies(cudaStream_t s, const double *X, size_t cap, int n, int ncrit, DevInfo *info, TreeScratch &ts);
+void tree_build_cells(cudaStream_t s, int n, int ncrit, int nnodes, DevInfo *info, TreeScratch &ts, CellsView cv, int *level_cells,
+                      int *level_start, int *leaf_cells);
+
+// ---- traverse.cu
+struct ListScratch {
+  DevBuf<int2>               front[2];
+  DevBuf<unsigned long long> p2p_raw, m2l_raw, p2p_sorted, m2l_sorted;
+  DevBuf<unsigned char>      cub_tmp;
+  size_t                     cub_bytes = 0;
+};
+void traverse(cudaStream_t s, CellsView tc, CellsView sc, int ntc, int maxLevelT, int maxLevelS, double theta, DevInfo *info, ListScratch &ls,
+              size_t cap_front, size_t cap_p2p, size_t cap_m2l);
+void lists_to_csr(cudaStream_t s, ListScratch &ls, int n_p2p, int n_m2l, int ncells_t, int cell_bits, int *p2p_start, int *p2p_src, int *m2l_start,
+                  int *m2l_src, const int *nbody_t, unsigned long long *interactions);
+
+// ---- bodies.cu
+void aos_to_soa(cudaStream_t s, const double *aos, double *soa, size_t cap, int n);
+void soa_to_aos(cudaStream_t s, const double *soa, size_t cap, double *aos, int n);
+void gather_bodies(cudaStream_t s, const double *src, double *dst, size_t cap, const uint32_t *perm, int n, uint64_t fieldMask);
+void check_finite(cudaStream_t s, const double *soa, size_t cap, int n, DevInfo *info);
+void reset_rates(cudaStream_t s, double *soa, size_t cap, int n);
+// Stage update kernel variants: scheme and stage index select the formula of
+// fmmCalculator.hpp:493-711; stretching/formulation complete the rates first.
+struct StageArgs {
+  int    scheme, stage, stretching, formulation, rk4_fixed, store_initial, do_update;
+  double dt, relax;
+};
+void finish_and_update(cudaStream_t s, double *soa, size_t cap, int n, const StageArgs &a);
+void relax_bodies(cudaStream_t s, double *soa, size_t cap, int n, double f);
+void fill_bytes(cudaStream_t s, void *p, size_t bytes, int value);
+double fma_probe(cudaStream_t s, bool fp64, void *scratch, int iters, float *ms_out, cudaEvent_t e0, cudaEvent_t e1);
+
+// ---- expansions.cu (FP64 path)
+struct ExpArgs {
+  int           P;
+  CellsView     cells;
+  int           ncells;
+  const int    *level_cells;
+  const int    *level_start_host; // host copy: [MAXL+2]
+  int           maxLevel;
+  const int    *leaf_cells;
+  int           nleaves;
+  const double *soa;
+  size_t        cap;
+  double2      *M, *L, *Mprep;
+  const int    *m2l_start, *m2l_src;
+  const int    *p2p_start, *p2p_src;
+  const int4   *m2l_items; // per-lane schedule, see m2l_schedule
+  int           m2l_nitems_per_lane;
+  int           stretching, formulation;
+};
+void upward_pass(cudaStream_t s, const ExpArgs &a);
+void m2l_pass(cudaStream_t s, const ExpArgs &a);
+void downward_l2l(cudaStream_t s, const ExpArgs &a);
+void l2p_p2p_pass(cudaStream_t s, const ExpArgs &a, double *soa_out);
+std::vector<int4> m2l_schedule(int P, int lanes, int kb, int maxItems, int *itemsPerLane);
+
+// ---- direct.cu
+void direct_sum(cudaStream_t s, const double *tx, const double *ty, const double *tz, int nt, const double *src, size_t scap, int ns, double *out /*12*nt*/);
+
+} // namespace vfmm
