@@ -45,7 +45,8 @@ def parse(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--fp64-steps", type=int, default=2, help="timed FP64 steps for the mixed-vs-FP64 comparison (0: skip)")
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--p", type=int, default=10)
     ap.add_argument("--ncrit", type=int, default=64)
@@ -281,11 +282,15 @@ def run_ours(args, dist: Dist) -> dict | None:
     if not args.no_accuracy and dist.rank == 0:
         accuracy = measure_accuracy(args, calc)
     calc.close()
+
+    fp64 = None
+    if args.precision == "mixed" and args.fp64_steps > 0:
+        fp64 = time_fp64(args, dist, bodies)
     if dist.rank != 0:
         return None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
             "data": "synthetic (seeded uniform cloud; no dataset)",
             "config": config_of(args, "flushed between steps (256 MB write)"),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * BODY_DTYPE.itemsize,
@@ -295,9 +300,38 @@ def run_ours(args, dist: Dist) -> dict | None:
             "roofline": roof, "clocks": clk, "phases_ms": phases, "tree": stats}
     if accuracy:
         line["accuracy"] = accuracy
+    if fp64:
+        line["fp64"] = fp64
+        line["fp64"]["speedup_mixed_vs_fp64"] = fp64["ms_per_step"] / line["ms_per_step"]
     if not args.no_cpu_baseline and dist.world == 1:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(args).items() if k != "seconds"}
     return line
+
+
+def time_fp64(args, dist: Dist, bodies) -> dict:
+    """The plain FP64 GPU FMM on the same workload (the drop-in mode), timed the
+    same way for the mixed-vs-FP64 comparison."""
+    from uvlm_gb300 import FMMCalculator, lib
+    L = lib()
+    c = FMMCalculator(p=args.p, ncrit=args.ncrit, theta=args.theta, integration="RK2", precision="fp64",
+                      device=dist.local_rank)
+    h = c.handle
+    c.load(bodies)
+    c.stage(0, args.dt)
+    ms = ctypes.c_float()
+    t = []
+    for k in range(args.fp64_steps):
+        L.vfmm_flush_l2(h)
+        L.vfmm_event_record(h, 0)
+        c.stage((1 + k) % 2, args.dt)
+        L.vfmm_event_record(h, 1)
+        L.vfmm_event_elapsed(h, 0, 1, ctypes.byref(ms))
+        t.append(ms.value)
+    ph = c.phase_times()
+    c.close()
+    tot = dist.max(sum(t))
+    return {"ms_per_step": tot / len(t), "value": dist.world * args.n * len(t) / (tot * 1e-3), "steps": len(t),
+            "phases_ms": ph}
 
 
 def measure_accuracy(args, calc) -> dict:
@@ -306,20 +340,34 @@ def measure_accuracy(args, calc) -> dict:
     from uvlm_gb300 import direct, workloads
     b = workloads.cloud(args.n, seed=3000)
     b["drdt_old"] = np.arange(b.size)  # survives init/calculate: recovers the tree permutation
-    calc.init(b)
-    calc.calculate()
-    calc.copyBodies2Host(b)
-    order = np.argsort(b["drdt_old"].astype(np.int64))
-    fmm = b[order][:4096]
-    src = workloads.cloud(args.n, seed=3000)
-    ref = direct(src[:4096].copy(), src)
+    from uvlm_gb300 import FMMCalculator
+
+    def evaluate(c):
+        bb = b.copy()
+        c.init(bb)
+        c.calculate()
+        c.copyBodies2Host(bb)
+        return bb[np.argsort(bb["drdt_old"].astype(np.int64))]
 
     def rl2(a, r):
         return float(np.linalg.norm(a - r) / np.linalg.norm(r))
-    return {"targets": 4096, "vs": "FP64 direct sum (regularised kernel, all pairs)",
-            "velocity_rel_l2": rl2(fmm["velocity"], ref["velocity"]), "J_rel_l2": rl2(fmm["J"], ref["J"]),
-            "note": "the reference's far field is the singular kernel, so this error includes the model's "
-                    "un-regularised far field, independent of arithmetic precision"}
+    fmm = evaluate(calc)
+    src = workloads.cloud(args.n, seed=3000)
+    ref = direct(src[:4096].copy(), src)
+    acc = {"direct_targets": 4096,
+           "velocity_rel_l2_vs_direct": rl2(fmm["velocity"][:4096], ref["velocity"]),
+           "J_rel_l2_vs_direct": rl2(fmm["J"][:4096], ref["J"]),
+           "note_direct": "FP64 all-pairs sum with the regularised kernel; the reference's far field uses the "
+                          "singular kernel, so this error is the model's (same for FP64 and mixed)"}
+    if args.precision == "mixed":
+        with FMMCalculator(p=args.p, ncrit=args.ncrit, theta=args.theta, precision="fp64") as c64:
+            f64 = evaluate(c64)
+        acc.update({"velocity_rel_l2_vs_fp64_fmm": rl2(fmm["velocity"], f64["velocity"]),
+                    "J_rel_l2_vs_fp64_fmm": rl2(fmm["J"], f64["J"]),
+                    "dadt_rel_l2_vs_fp64_fmm": rl2(fmm["dadt"], f64["dadt"]),
+                    "fp64_velocity_rel_l2_vs_direct": rl2(f64["velocity"][:4096], ref["velocity"]),
+                    "bodies_compared": int(args.n)})
+    return acc
 
 
 def main(argv=None):

@@ -156,3 +156,31 @@ def test_errors_are_reported(vfmm_lib):
         c.calculate()
     with pytest.raises(VfmmError):
         FMMCalculator(p=40)
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("kind,n,P,ncrit", [("cloud", 40000, 10, 64), ("cloud", 20000, 14, 64), ("cloud", 20000, 6, 64),
+                                            ("ring", 96, 8, 32)])
+def test_mixed_matches_fp64_fmm(vfmm_lib, kind, n, P, ncrit):
+    """The mixed path (FP32 P2M/M2L/L2P/P2P, FP64 tree and M2M/L2L) against the
+    FP64 path on the same tree: relative L2 error of velocity and of J below
+    1e-6 (the precision bar of the mixed mode)."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(n, seed=5) if kind == "cloud" else workloads.ring(n, seed=5)
+    out = {}
+    for prec in ["fp64", "mixed"]:
+        with FMMCalculator(p=P, ncrit=ncrit, theta=0.5, precision=prec) as c:
+            bb = b.copy()
+            c.init(bb)
+            c.calculate()
+            c.copyBodies2Host(bb)
+            out[prec] = bb
+    assert (out["fp64"]["X"] == out["mixed"]["X"]).all()
+    ev = rel_l2(out["mixed"]["velocity"], out["fp64"]["velocity"])
+    eJ = rel_l2(out["mixed"]["J"], out["fp64"]["J"])
+    ed = rel_l2(out["mixed"]["dadt"], out["fp64"]["dadt"])
+    print(f"{kind} n={n} P={P}: velocity {ev:.3e}  J {eJ:.3e}  dadt {ed:.3e}")
+    assert ev < 1e-6 and eJ < 1e-6 and ed < 1e-6, (ev, eJ, ed)

@@ -56,8 +56,10 @@ struct vfmm_handle_s {
 
   // expansions
   DevBuf<double2> M, L, Mprep;
-  DevBuf<int4>    items;
+  DevBuf<int4>    items, items32;
   int             items_P = 0, items_per_lane = 0;
+  DevBuf<float2>  Mp32;
+  DevBuf<float4>  pos32, alp32;
 
   DevBuf<unsigned char> flushbuf;
   DevBuf<double>        dtmp;
@@ -255,6 +257,10 @@ void ensure_items(vfmm_handle h)
   auto tab = m2l_schedule(h->cfg.p, 32, 2, 4, &per);
   h->items.reserve(tab.size());
   VFMM_CUDA_TRY(cudaMemcpy(h->items.p, tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  int  per32 = 0;
+  auto tab32 = m2l_schedule(h->cfg.p, 32, 4, 3, &per32);
+  h->items32.reserve(tab32.size());
+  VFMM_CUDA_TRY(cudaMemcpy(h->items32.p, tab32.data(), tab32.size() * sizeof(int4), cudaMemcpyHostToDevice));
   h->items_P        = h->cfg.p;
   h->items_per_lane = per;
 }
@@ -292,14 +298,35 @@ void calculate(vfmm_handle h)
   e.m2l_nitems_per_lane = h->items_per_lane;
   e.stretching          = h->cfg.stretching;
   e.formulation         = h->cfg.formulation;
-  upward_pass(s, e);
-  VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
-  m2l_pass(s, e);
-  VFMM_CUDA_TRY(cudaEventRecord(h->ph[3], s));
-  downward_l2l(s, e);
-  VFMM_CUDA_TRY(cudaEventRecord(h->ph[4], s));
-  l2p_p2p_pass(s, e, h->soa[h->cur].p);
-  VFMM_CUDA_TRY(cudaEventRecord(h->ph[5], s));
+  if (h->cfg.precision == VFMM_MIXED) {
+    h->Mp32.reserve((size_t)h->ncells * 3 * h->cfg.p * h->cfg.p);
+    h->pos32.reserve(h->n);
+    h->alp32.reserve(h->n);
+    MixedArgs m{};
+    m.Mp32    = h->Mp32.p;
+    m.pos32   = h->pos32.p;
+    m.alp32   = h->alp32.p;
+    m.items32 = h->items32.p;
+    m.R0      = h->hinfo->R0;
+    p2m_mixed(s, e, m);
+    m2m_pass(s, e);
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
+    m2l_mixed(s, e, m);
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[3], s));
+    downward_l2l(s, e);
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[4], s));
+    l2p_p2p_mixed(s, e, m, h->soa[h->cur].p);
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[5], s));
+  } else {
+    upward_pass(s, e);
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
+    m2l_pass(s, e);
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[3], s));
+    downward_l2l(s, e);
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[4], s));
+    l2p_p2p_pass(s, e, h->soa[h->cur].p);
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[5], s));
+  }
   h->has_eval = true;
 }
 
@@ -393,6 +420,10 @@ int vfmm_destroy(vfmm_handle h)
   h->L.release();
   h->Mprep.release();
   h->items.release();
+  h->items32.release();
+  h->Mp32.release();
+  h->pos32.release();
+  h->alp32.release();
   h->flushbuf.release();
   for (auto *b : {&h->ts.keys, &h->ts.skeys})
     b->release();

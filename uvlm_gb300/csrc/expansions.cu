@@ -610,6 +610,20 @@ static void upward_P(cudaStream_t s, const ExpArgs &e)
 }
 
 template <int P>
+static void m2m_P(cudaStream_t s, const ExpArgs &e)
+{
+  DevExp d = dev_args(e);
+  for (int l = e.maxLevel - 1; l >= 1; l--) {
+    const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
+    if (n1 > n0) {
+      k_m2m<P><<<std::min(n1 - n0, 152 * 16), 64, 0, s>>>(d, e.level_cells + n0, n1 - n0);
+      count_launch();
+    }
+  }
+  VFMM_LAUNCH_CHECK();
+}
+
+template <int P>
 static void m2l_P(cudaStream_t s, const ExpArgs &e)
 {
   DevExp    d  = dev_args(e);
@@ -679,6 +693,7 @@ static void l2p_P(cudaStream_t s, const ExpArgs &e, double *out)
   }
 
 void upward_pass(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(upward_P, s, e) }
+void m2m_pass(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(m2m_P, s, e) }
 void m2l_pass(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(m2l_P, s, e) }
 void downward_l2l(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(l2l_P, s, e) }
 void l2p_p2p_pass(cudaStream_t s, const ExpArgs &e, double *out) { VFMM_DISPATCH(l2p_P, s, e, out) }

@@ -1,0 +1,632 @@
+// Mixed-precision expansion kernels: FP32 P2M, M2L, L2P and P2P with FP64
+// tree, M2M/L2L (expansions.cu) and FP64 outputs.
+//
+// Scaling.  FP32 cannot hold the raw expansions at high order (rho^n/(n+m)!
+// and (n-m)!/rho^(n+1) leave its exponent range), so inside these kernels a
+// cell c of half-width R_c = R0/2^level carries
+//   scaled multipole  Mt_n^m = M_n^m / R_c^n,
+//   scaled local      Lt_j^k = L_j^k * R_c^j,
+// and harmonics are evaluated at offsets divided by the cell size.  The FP64
+// arrays M and L between kernels stay unscaled (the reference's values).
+//   P2M:  Mt_n^m(c) = sum_b alpha_b conj(Y_n^m((x_b - X_c)/R_c)).
+//   M2L:  Lt_j^k(t) += (R_t/R_s)^j / R_s * (-1)^j sum M't_n^m S'_{j+n}^{m-k}(d/R_s),
+//         d = X_t - X_s; (R_t/R_s) is a power of two.
+//   L2P:  u = (1/R) sum (D Lt)(y), J = (1/R^2) sum (D D Lt)(y), y = (x - X_c)/R.
+// P2P uses leaf-relative FP32 coordinates, a series form of the regularised
+// kernel for close pairs (no cancellation), and per-source-leaf FP32 partial
+// sums folded into a float-float (two-sum) accumulator.
+#include <algorithm>
+#include "harmonics.cuh"
+#include "vfmm_internal.cuh"
+
+namespace vfmm {
+
+typedef cx<float>  zf;
+typedef cx<double> zd;
+
+struct DevMixed {
+  CellsView     cv;
+  const double *soa;
+  size_t        cap;
+  double2      *M, *L;
+  float2       *Mp;      // prepared scaled multipoles [cell][P*P][3]
+  const float4 *pos32;   // per body: (x - X_leaf, y - Y_leaf, z - Z_leaf, 1/(2 sigma^2))
+  const float4 *alp32;   // per body: (alpha, 1/sigma)
+  const int    *leaf_cells;
+  int           nleaves;
+  const int    *m2l_start, *m2l_src;
+  const int    *p2p_start, *p2p_src;
+  const int4   *items;
+  double        R0;
+  int           stretching, formulation;
+};
+
+__device__ __forceinline__ void jk_of_m(int jks, int &j, int &k)
+{
+  j = 0;
+  while ((j + 1) * (j + 2) / 2 <= jks)
+    j++;
+  k = jks - j * (j + 1) / 2;
+}
+__device__ __forceinline__ double cell_R(double R0, int level) { return ldexp(R0, -level); }
+
+// ------------------------------------------------------------------ prep
+// Leaf-relative FP32 body data for the P2P sources and targets.
+__global__ void k_prep_bodies(DevMixed a)
+{
+  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+    const int    c  = a.leaf_cells[li];
+    const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
+    const double cx_ = a.cv.x[c], cy_ = a.cv.y[c], cz_ = a.cv.z[c];
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+      const int    b  = b0 + t;
+      const double sg = a.soa[F_R * a.cap + b];
+      float4       p, q;
+      p.x = (float)(a.soa[F_X * a.cap + b] - cx_);
+      p.y = (float)(a.soa[(F_X + 1) * a.cap + b] - cy_);
+      p.z = (float)(a.soa[(F_X + 2) * a.cap + b] - cz_);
+      p.w = (float)(0.5 / (sg * sg));
+      q.x = (float)a.soa[F_A * a.cap + b];
+      q.y = (float)a.soa[(F_A + 1) * a.cap + b];
+      q.z = (float)a.soa[(F_A + 2) * a.cap + b];
+      q.w = (float)(1.0 / sg);
+      const_cast<float4 *>(a.pos32)[b] = p;
+      const_cast<float4 *>(a.alp32)[b] = q;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ P2M
+template <int P>
+__global__ void __launch_bounds__(64) k_p2m32(DevMixed a)
+{
+  constexpr int K = nterms(P), NO = (3 * K + 63) / 64;
+  extern __shared__ float4 smem32[];
+  zf    *Ys = reinterpret_cast<zf *>(smem32);
+  float *As = reinterpret_cast<float *>(Ys + 32 * K);
+  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+    const int c = a.leaf_cells[li];
+    if (a.cv.level[c] == 0)
+      continue; // the reference's upward pass skips level 0 (fmmCalculator.hpp:427)
+    const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
+    const double R = cell_R(a.R0, a.cv.level[c]);
+    const float  iR = (float)(1.0 / R);
+    zf           acc[NO];
+#pragma unroll
+    for (int i = 0; i < NO; i++)
+      acc[i] = {0.f, 0.f};
+    for (int c0 = 0; c0 < nb; c0 += 32) {
+      const int nbc = min(32, nb - c0);
+      const int t   = threadIdx.x;
+      if (t < nbc) {
+        const float4 p = a.pos32[b0 + c0 + t];
+        regular_harmonics<float, P>(p.x * iR, p.y * iR, p.z * iR, Ys + t * K);
+        const float4 q = a.alp32[b0 + c0 + t];
+        As[t * 3 + 0]  = q.x;
+        As[t * 3 + 1]  = q.y;
+        As[t * 3 + 2]  = q.z;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < NO; i++) {
+        const int o = threadIdx.x + 64 * i;
+        if (o < 3 * K) {
+          const int nms = o / 3, d = o % 3;
+          for (int tt = 0; tt < nbc; tt++) {
+            const zf    y  = Ys[tt * K + nms];
+            const float al = As[tt * 3 + d];
+            acc[i].r       = fmaf(al, y.r, acc[i].r);
+            acc[i].i       = fmaf(-al, y.i, acc[i].i);
+          }
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < NO; i++) {
+      const int o = threadIdx.x + 64 * i;
+      if (o < 3 * K) {
+        int n, m;
+        jk_of_m(o / 3, n, m);
+        const double s = pow(R, n);
+        a.M[(size_t)c * 3 * K + o] = make_double2(acc[i].r * s, acc[i].i * s);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ M2L
+// Prepared scaled multipoles, sign- and conjugation-folded as in k_mprep:
+// Mp[cell][n^2+n+m][d] = ((-1)^m M_n^m (m>=0) | conj(M_n^|m|) (m<0)) / R_c^n.
+template <int P>
+__global__ void k_mprep32(const double2 *__restrict__ M, float2 *__restrict__ Mp, const int *__restrict__ level, double R0, int ncells)
+{
+  constexpr int K = nterms(P), PP = P * P;
+  const long    total = (long)ncells * PP * 3;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(e / (PP * 3)), r = (int)(e % (PP * 3)), idx = r / 3, d = r % 3;
+    int       n = 0;
+    while ((n + 1) * (n + 1) <= idx)
+      n++;
+    const int    m  = idx - n * n - n;
+    const double2 v = M[(size_t)c * 3 * K + tri(n, m >= 0 ? m : -m) * 3 + d];
+    const double s  = pow(ldexp(R0, -level[c]), -n);
+    double       re = v.x * s, im = v.y * s;
+    if (m >= 0) {
+      if (m & 1) {
+        re = -re;
+        im = -im;
+      }
+    } else
+      im = -im;
+    Mp[e] = make_float2((float)re, (float)im);
+  }
+}
+
+// One warp per target cell (4 per block); lane work items as in k_m2l.  Per
+// source, each item's partial sums are scaled by (R_t/R_s)^j / R_s before
+// they join the target's accumulators.
+template <int P, int KB, int MAXI>
+__global__ void __launch_bounds__(128) k_m2l32(DevMixed a, int ncells)
+{
+  constexpr int K = nterms(P), PP = P * P;
+  extern __shared__ float4 smem32[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  zf       *Ms = reinterpret_cast<zf *>(smem32) + w * (4 * PP);
+  zf       *Ys = Ms + 3 * PP;
+  int4      it[MAXI];
+#pragma unroll
+  for (int i = 0; i < MAXI; i++)
+    it[i] = a.items[i * 32 + lane];
+  for (int t = blockIdx.x * 4 + w; t < ncells; t += gridDim.x * 4) {
+    zf acc[MAXI][KB][3];
+#pragma unroll
+    for (int i = 0; i < MAXI; i++)
+#pragma unroll
+      for (int kk = 0; kk < KB; kk++)
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+          acc[i][kk][d] = {0.f, 0.f};
+    const int    q0 = a.m2l_start[t], q1 = a.m2l_start[t + 1];
+    const double tx = a.cv.x[t], ty = a.cv.y[t], tz = a.cv.z[t];
+    const int    lt = a.cv.level[t];
+    for (int q = q0; q < q1; q++) {
+      const int s = a.m2l_src[q], ls = a.cv.level[s];
+      __syncwarp();
+      for (int e = lane; e < 3 * PP; e += 32) {
+        const float2 v = a.Mp[(size_t)s * 3 * PP + e];
+        Ms[e]          = {v.x, v.y};
+      }
+      const double iRs = 1.0 / cell_R(a.R0, ls);
+      if (lane < P) {
+        const float dx = (float)((tx - a.cv.x[s]) * iRs), dy = (float)((ty - a.cv.y[s]) * iRs), dz = (float)((tz - a.cv.z[s]) * iRs);
+        const float r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.0f / r2, S00 = rsqrtf(r2);
+        zf          col[P];
+        singular_column<float, P>(lane, dx, dy, dz, ir2, S00, col);
+        const int m = lane;
+        for (int n = m; n < P; n++) {
+          const zf v        = col[n];
+          Ys[n * n + n + m] = (m & 1) ? zf{-v.r, -v.i} : v;
+          if (m > 0)
+            Ys[n * n + n - m] = conj(v);
+        }
+      }
+      __syncwarp();
+      const float fs = (float)iRs; // 1/R_s
+#pragma unroll
+      for (int i = 0; i < MAXI; i++) {
+        const int j = it[i].x;
+        if (j < 0)
+          continue;
+        const int k0 = it[i].y & 255, kb = it[i].y >> 8, n0 = it[i].z, n1 = it[i].w;
+        zf        tmp[KB][3];
+#pragma unroll
+        for (int kk = 0; kk < KB; kk++)
+#pragma unroll
+          for (int d = 0; d < 3; d++)
+            tmp[kk][d] = {0.f, 0.f};
+        for (int n = n0; n <= n1; n++) {
+          const int base = (j + n) * (j + n) + (j + n) - k0;
+          for (int m = -n; m <= n; m++) {
+            const zf m0 = Ms[(n * n + n + m) * 3 + 0], m1 = Ms[(n * n + n + m) * 3 + 1], m2 = Ms[(n * n + n + m) * 3 + 2];
+#pragma unroll
+            for (int kk = 0; kk < KB; kk++) {
+              if (kk < kb) {
+                const zf y = Ys[base + m - kk];
+                cfma(tmp[kk][0], m0, y);
+                cfma(tmp[kk][1], m1, y);
+                cfma(tmp[kk][2], m2, y);
+              }
+            }
+          }
+        }
+        const float f = ldexpf(fs, (ls - lt) * j); // (R_t/R_s)^j / R_s
+#pragma unroll
+        for (int kk = 0; kk < KB; kk++)
+#pragma unroll
+          for (int d = 0; d < 3; d++) {
+            acc[i][kk][d].r = fmaf(f, tmp[kk][d].r, acc[i][kk][d].r);
+            acc[i][kk][d].i = fmaf(f, tmp[kk][d].i, acc[i][kk][d].i);
+          }
+      }
+    }
+    __syncwarp();
+    zf *Lr = Ms;
+    for (int e = lane; e < 3 * K; e += 32)
+      Lr[e] = {0.f, 0.f};
+    __syncwarp();
+    for (int src = 0; src < 32; src++) {
+      if (lane == src) {
+#pragma unroll
+        for (int i = 0; i < MAXI; i++) {
+          const int j = it[i].x;
+          if (j < 0)
+            continue;
+          const int k0 = it[i].y & 255, kb = it[i].y >> 8;
+#pragma unroll
+          for (int kk = 0; kk < KB; kk++)
+            if (kk < kb)
+              for (int d = 0; d < 3; d++) {
+                zf &o = Lr[tri(j, k0 + kk) * 3 + d];
+                o     = o + acc[i][kk][d];
+              }
+        }
+      }
+      __syncwarp();
+    }
+    const double Rt = cell_R(a.R0, lt);
+    for (int e = lane; e < 3 * K; e += 32) {
+      int j, k;
+      jk_of_m(e / 3, j, k);
+      const zf     v = Lr[e];
+      const double s = ((j & 1) ? -1.0 : 1.0) * pow(Rt, -j);
+      a.L[(size_t)t * 3 * K + e] = make_double2(v.r * s, v.i * s);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ L2P + P2P
+__device__ __forceinline__ zf coef_full32(const zf *c, int n, int m, int stride, int comp)
+{
+  if (m > 0)
+    return c[tri(n, m) * stride + comp];
+  if (m == 0)
+    return {c[tri(n, 0) * stride + comp].r, 0.f};
+  return conj(c[tri(n, -m) * stride + comp]);
+}
+__device__ __forceinline__ zf deriv_coef32(const zf *c, int n, int mu, int axis, int stride, int comp)
+{
+  if (axis == 2) {
+    zf v = coef_full32(c, n + 1, mu, stride, comp);
+    return {-v.r, -v.i};
+  }
+  const float s = (mu - 1 >= 0) ? -1.f : 1.f;
+  const float t = (mu + 1 >= 1) ? 1.f : -1.f;
+  const zf    A = s * coef_full32(c, n + 1, mu - 1, stride, comp);
+  const zf    B = t * coef_full32(c, n + 1, mu + 1, stride, comp);
+  if (axis == 0)
+    return {0.5f * (A.r + B.r), 0.5f * (A.i + B.i)};
+  return {0.5f * (A.i - B.i), -0.5f * (A.r - B.r)};
+}
+
+template <int P>
+struct L2P32Sizes {
+  static constexpr int    K  = nterms(P);
+  static constexpr int    K1 = nterms(P - 1) > 0 ? nterms(P - 1) : 1;
+  static constexpr int    K2 = nterms(P - 2) > 0 ? nterms(P - 2) : 1;
+  static constexpr size_t bytes = (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zf) + 2 * 128 * 12 * sizeof(double);
+};
+
+// two-sum: s + e = a + b exactly
+__device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v)
+{
+  const float s  = hi + v;
+  const float bb = s - hi;
+  const float e  = (hi - (s - bb)) + (v - bb);
+  hi             = s;
+  lo += e;
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
+{
+  using S = L2P32Sizes<P>;
+  constexpr int K = S::K, K1 = S::K1, K2 = S::K2;
+  constexpr int D1 = P - 1, D2 = P - 2;
+  extern __shared__ float4 smem32[];
+  zf     *Lc  = reinterpret_cast<zf *>(smem32);
+  zf     *U   = Lc + 3 * K;
+  zf     *JJ  = U + 3 * K1;
+  double *far = reinterpret_cast<double *>(JJ + 9 * K2);
+  double *red = far + 128 * 12;
+  (void)K1;
+  (void)K2;
+  const float inv4pi = 0.0795774715459476679f;
+  const float c2spi  = 1.12837916709551257f; // 2/sqrt(pi)
+  // series constants: G = ghat(RS) * KS / sigma^3, A = hhat(RS) * KS / sigma^5, KS = (2/sqrt(pi)) / (8 sqrt(2) pi)
+  const float KS = 0.0317468755f;
+
+  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+    const int    c  = a.leaf_cells[li];
+    const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
+    const double R  = cell_R(a.R0, a.cv.level[c]);
+    const float  iR = (float)(1.0 / R);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * K; e += 128) {
+      int n, m;
+      jk_of_m(e / 3, n, m);
+      const double2 v = a.L[(size_t)c * 3 * K + e];
+      const double  s = pow(R, n); // scaled local Lt = L R^n
+      Lc[e]           = {(float)(v.x * s), (float)(v.y * s)};
+    }
+    __syncthreads();
+    if (D1 > 0)
+      for (int e = threadIdx.x; e < 3 * nterms(D1); e += 128) {
+        const int idx = e / 3, ax = e % 3;
+        int       n, mu;
+        jk_of_m(idx, n, mu);
+        const int b1 = (ax + 1) % 3, c1 = (ax + 2) % 3;
+        const zf  p = deriv_coef32(Lc, n, mu, b1, 3, c1), q = deriv_coef32(Lc, n, mu, c1, 3, b1);
+        U[idx * 3 + ax] = {inv4pi * (p.r - q.r), inv4pi * (p.i - q.i)};
+      }
+    __syncthreads();
+    if (D2 > 0)
+      for (int e = threadIdx.x; e < 9 * nterms(D2); e += 128) {
+        const int idx = e / 9, ae = e % 9, ax = ae / 3, ex = ae % 3;
+        int       n, mu;
+        jk_of_m(idx, n, mu);
+        JJ[idx * 9 + ae] = deriv_coef32(U, n, mu, ex, 3, ax);
+      }
+    __syncthreads();
+
+    for (int tc = 0; tc < nb; tc += 128) {
+      const int nbc = min(128, nb - tc);
+      if (threadIdx.x < nbc) {
+        const float4 p = a.pos32[b0 + tc + threadIdx.x];
+        const float  x = p.x * iR, y = p.y * iR, z = p.z * iR;
+        const float  r2 = x * x + y * y + z * z;
+        float        f[12];
+        for (int k = 0; k < 12; k++)
+          f[k] = 0.f;
+        zf diag{1.f, 0.f};
+        for (int m = 0; m < D1; m++) {
+          if (m > 0) {
+            const float s = 1.f / float(2 * m);
+            diag          = {(diag.r * x - diag.i * y) * s, (diag.r * y + diag.i * x) * s};
+          }
+          const float w  = m == 0 ? 1.f : 2.f;
+          zf          ya = diag, yb{0.f, 0.f};
+          for (int n = m; n < D1; n++) {
+            const int t = tri(n, m);
+            for (int ax = 0; ax < 3; ax++) {
+              const zf u = U[t * 3 + ax];
+              f[ax] += w * (u.r * ya.r - u.i * ya.i);
+            }
+            if (n < D2)
+              for (int ae = 0; ae < 9; ae++) {
+                const zf u = JJ[t * 9 + ae];
+                f[3 + ae] += w * (u.r * ya.r - u.i * ya.i);
+              }
+            const float cc = -1.f / float((n + m + 1) * (n - m + 1));
+            const float zz = float(2 * n + 1) * z;
+            const zf    nx = {cc * (zz * ya.r + r2 * yb.r), cc * (zz * ya.i + r2 * yb.i)};
+            yb             = ya;
+            ya             = nx;
+          }
+        }
+        const double s1 = 1.0 / R, s2 = s1 * s1;
+        for (int k = 0; k < 3; k++)
+          far[threadIdx.x * 12 + k] = (double)f[k] * s1;
+        for (int k = 3; k < 12; k++)
+          far[threadIdx.x * 12 + k] = (double)f[k] * s2;
+      }
+      const int TG = nbc <= 32 ? 32 : (nbc <= 64 ? 64 : 128), G = 128 / TG;
+      const int tt = threadIdx.x % TG, g = threadIdx.x / TG;
+      float     hi[12], lo[12];
+      for (int k = 0; k < 12; k++)
+        hi[k] = lo[k] = 0.f;
+      if (tt < nbc) {
+        const float4 pt = a.pos32[b0 + tc + tt];
+        const double ctx = a.cv.x[c], cty = a.cv.y[c], ctz = a.cv.z[c];
+        const int    q0 = a.p2p_start[c], q1 = a.p2p_start[c + 1];
+        for (int q = q0 + g; q < q1; q += G) {
+          const int   sc = a.p2p_src[q], sb = a.cv.body[sc], sn = a.cv.nbody[sc];
+          const float ox = pt.x - (float)(a.cv.x[sc] - ctx), oy = pt.y - (float)(a.cv.y[sc] - cty), oz = pt.z - (float)(a.cv.z[sc] - ctz);
+          float       s[12];
+          for (int k = 0; k < 12; k++)
+            s[k] = 0.f;
+          for (int jb = sb; jb < sb + sn; jb++) {
+            const float4 ps = __ldg(a.pos32 + jb);
+            const float  dx = ox - ps.x, dy = oy - ps.y, dz = oz - ps.z;
+            const float  R2 = dx * dx + dy * dy + dz * dz;
+            if (R2 != 0.f) {
+              const float4 al = __ldg(a.alp32 + jb);
+              const float  RS = R2 * ps.w; // R^2 / (2 sigma^2)
+              float        Gc, Ac;
+              if (RS < 0.25f) {
+                // x^3-scaled series: no cancellation for close pairs
+                const float gpoly = ((((((1.f / 5400.f) * RS - 1.f / 780.f) * RS + 1.f / 132.f) * RS - 1.f / 27.f) * RS + 1.f / 7.f) * RS - 0.4f) * RS +
+                                    2.f / 3.f;
+                const float hpoly = ((((((-1.f / 6120.f) * RS + 1.f / 900.f) * RS - 1.f / 156.f) * RS + 1.f / 33.f) * RS - 1.f / 9.f) * RS + 2.f / 7.f) *
+                                        RS -
+                                    0.4f;
+                const float is = al.w, is2 = is * is, is3 = is2 * is;
+                Gc             = gpoly * KS * is3;
+                Ac             = hpoly * KS * is3 * is2;
+              } else {
+                const float xs   = sqrtf(RS);
+                const float erfS = erff(xs);
+                const float t2   = c2spi * xs * __expf(-RS);
+                const float rinv = rsqrtf(R2);
+                const float c4   = inv4pi * rinv * rinv * rinv;
+                const float gg   = erfS - t2;
+                Gc               = gg * c4;
+                Ac               = (t2 * 2.f * ps.w - 3.f * gg * rinv * rinv) * c4;
+              }
+              const float cr0 = dy * al.z - dz * al.y, cr1 = dz * al.x - dx * al.z, cr2 = dx * al.y - dy * al.x;
+              s[0] = fmaf(Gc, cr0, s[0]);
+              s[1] = fmaf(Gc, cr1, s[1]);
+              s[2] = fmaf(Gc, cr2, s[2]);
+              const float a0 = Ac * cr0, a1 = Ac * cr1, a2 = Ac * cr2;
+              s[3]  = fmaf(a0, dx, s[3]);
+              s[4]  = fmaf(a0, dy, s[4]);
+              s[5]  = fmaf(a0, dz, s[5]);
+              s[6]  = fmaf(a1, dx, s[6]);
+              s[7]  = fmaf(a1, dy, s[7]);
+              s[8]  = fmaf(a1, dz, s[8]);
+              s[9]  = fmaf(a2, dx, s[9]);
+              s[10] = fmaf(a2, dy, s[10]);
+              s[11] = fmaf(a2, dz, s[11]);
+              s[6] -= Gc * al.z;
+              s[9] += Gc * al.y;
+              s[4] += Gc * al.z;
+              s[10] -= Gc * al.x;
+              s[5] -= Gc * al.y;
+              s[8] += Gc * al.x;
+            }
+          }
+          for (int k = 0; k < 12; k++)
+            two_sum_add(hi[k], lo[k], s[k]);
+        }
+      }
+      for (int k = 0; k < 12; k++)
+        red[threadIdx.x * 12 + k] = (double)hi[k] + (double)lo[k];
+      __syncthreads();
+      if (threadIdx.x < nbc) {
+        const int t = threadIdx.x, b = b0 + tc + t;
+        double    r[12];
+        for (int k = 0; k < 12; k++) {
+          double nearv = 0;
+          for (int gg = 0; gg < G; gg++)
+            nearv += red[(gg * TG + t) * 12 + k];
+          r[k] = far[t * 12 + k] - nearv;
+        }
+        const double al[3] = {a.soa[F_A * a.cap + b], a.soa[(F_A + 1) * a.cap + b], a.soa[(F_A + 2) * a.cap + b]};
+        double       dadt[3];
+        for (int aa = 0; aa < 3; aa++) {
+          double v = 0;
+          for (int cc = 0; cc < 3; cc++)
+            v += (a.stretching == VFMM_TRANSPOSED ? r[3 + 3 * cc + aa] : r[3 + 3 * aa + cc]) * al[cc];
+          dadt[aa] = v;
+        }
+        double drdt = 0;
+        if (a.formulation == VFMM_RVPM) {
+          const double na = sqrt(al[0] * al[0] + al[1] * al[1] + al[2] * al[2]);
+          const double ah[3] = {al[0] / na, al[1] / na, al[2] / na};
+          const double dot   = dadt[0] * ah[0] + dadt[1] * ah[1] + dadt[2] * ah[2];
+          for (int aa = 0; aa < 3; aa++)
+            dadt[aa] -= 3. / 5. * dot * ah[aa];
+          drdt -= 1.0 / 5.0 * a.soa[F_R * a.cap + b] / na * dot;
+        }
+        for (int d = 0; d < 3; d++) {
+          out[(F_U + d) * a.cap + b]    = r[d];
+          out[(F_DADT + d) * a.cap + b] = dadt[d];
+        }
+        for (int k = 0; k < 9; k++)
+          out[(F_J + k) * a.cap + b] = r[3 + k];
+        out[F_DRDT * a.cap + b] = drdt;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host side
+static DevMixed dev_mixed(const ExpArgs &e, const MixedArgs &m)
+{
+  DevMixed d;
+  d.cv          = e.cells;
+  d.soa         = e.soa;
+  d.cap         = e.cap;
+  d.M           = e.M;
+  d.L           = e.L;
+  d.Mp          = m.Mp32;
+  d.pos32       = m.pos32;
+  d.alp32       = m.alp32;
+  d.leaf_cells  = e.leaf_cells;
+  d.nleaves     = e.nleaves;
+  d.m2l_start   = e.m2l_start;
+  d.m2l_src     = e.m2l_src;
+  d.p2p_start   = e.p2p_start;
+  d.p2p_src     = e.p2p_src;
+  d.items       = m.items32;
+  d.R0          = m.R0;
+  d.stretching  = e.stretching;
+  d.formulation = e.formulation;
+  return d;
+}
+
+template <int P>
+static void p2m32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+{
+  DevMixed     d     = dev_mixed(e, m);
+  const size_t bytes = (size_t)32 * nterms(P) * sizeof(zf) + 32 * 3 * sizeof(float);
+  if (e.nleaves > 0) {
+    k_prep_bodies<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
+    count_launch();
+    k_p2m32<P><<<std::min(e.nleaves, 152 * 16), 64, bytes, s>>>(d);
+    count_launch();
+  }
+  VFMM_LAUNCH_CHECK();
+}
+
+template <int P>
+static void m2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+{
+  DevMixed  d  = dev_mixed(e, m);
+  const int PP = P * P;
+  k_mprep32<P><<<grid_for((long)e.ncells * PP * 3, 256), 256, 0, s>>>(e.M, m.Mp32, e.cells.level, m.R0, e.ncells);
+  count_launch();
+  const size_t bytes = (size_t)4 * 4 * PP * sizeof(zf);
+  static bool  once  = false;
+  if (!once) {
+    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2l32<P, 4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    once = true;
+  }
+  k_m2l32<P, 4, 3><<<grid_for(e.ncells, 4, 152 * 32), 128, bytes, s>>>(d, e.ncells);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+template <int P>
+static void l2p32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out)
+{
+  DevMixed     d     = dev_mixed(e, m);
+  const size_t bytes = L2P32Sizes<P>::bytes;
+  static bool  once  = false;
+  if (!once) {
+    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_l2p_p2p32<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    once = true;
+  }
+  if (e.nleaves > 0) {
+    k_l2p_p2p32<P><<<std::min(e.nleaves, 152 * 16), 128, bytes, s>>>(d, out);
+    count_launch();
+  }
+  VFMM_LAUNCH_CHECK();
+}
+
+#define VFMM_DISPATCH_M(fn, ...)                                                                                                 \
+  switch (e.P) {                                                                                                                \
+  case 2: fn<2>(__VA_ARGS__); break;                                                                                            \
+  case 3: fn<3>(__VA_ARGS__); break;                                                                                            \
+  case 4: fn<4>(__VA_ARGS__); break;                                                                                            \
+  case 5: fn<5>(__VA_ARGS__); break;                                                                                            \
+  case 6: fn<6>(__VA_ARGS__); break;                                                                                            \
+  case 7: fn<7>(__VA_ARGS__); break;                                                                                            \
+  case 8: fn<8>(__VA_ARGS__); break;                                                                                            \
+  case 9: fn<9>(__VA_ARGS__); break;                                                                                            \
+  case 10: fn<10>(__VA_ARGS__); break;                                                                                          \
+  case 11: fn<11>(__VA_ARGS__); break;                                                                                          \
+  case 12: fn<12>(__VA_ARGS__); break;                                                                                          \
+  case 13: fn<13>(__VA_ARGS__); break;                                                                                          \
+  case 14: fn<14>(__VA_ARGS__); break;                                                                                          \
+  case 15: fn<15>(__VA_ARGS__); break;                                                                                          \
+  case 16: fn<16>(__VA_ARGS__); break;                                                                                          \
+  default: throw Error(VFMM_ERR_UNSUPPORTED, "expansion order p must be in 2..16");                                            \
+  }
+
+void p2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(p2m32_P, s, e, m) }
+void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(m2l32_P, s, e, m) }
+void l2p_p2p_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out) { VFMM_DISPATCH_M(l2p32_P, s, e, m, out) }
+
+} // namespace vfmm

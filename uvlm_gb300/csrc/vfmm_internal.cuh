@@ -181,11 +181,23 @@ struct ExpArgs {
   int           m2l_nitems_per_lane;
   int           stretching, formulation;
 };
-void upward_pass(cudaStream_t s, const ExpArgs &a);
+void upward_pass(cudaStream_t s, const ExpArgs &a); // P2M + M2M (FP64)
+void m2m_pass(cudaStream_t s, const ExpArgs &a);    // M2M only (FP64)
 void m2l_pass(cudaStream_t s, const ExpArgs &a);
 void downward_l2l(cudaStream_t s, const ExpArgs &a);
 void l2p_p2p_pass(cudaStream_t s, const ExpArgs &a, double *soa_out);
 std::vector<int4> m2l_schedule(int P, int lanes, int kb, int maxItems, int *itemsPerLane);
+
+// ---- mixed.cu (FP32 P2M / M2L / L2P+P2P around the FP64 M2M / L2L)
+struct MixedArgs {
+  float2       *Mp32;
+  float4       *pos32, *alp32;
+  const int4   *items32;
+  double        R0;
+};
+void p2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
+void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
+void l2p_p2p_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out);
 
 // ---- direct.cu
 void direct_sum(cudaStream_t s, const double *tx, const double *ty, const double *tz, int nt, const double *src, size_t scap, int ns, double *out /*12*nt*/);
