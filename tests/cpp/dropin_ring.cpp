@@ -1,0 +1,38 @@
+// A caller written against the reference's FMMCalculator API, compiled
+// against include/vfmm.hpp and linked with libvfmm.so.  Builds a small ring
+// of particles, takes one RK3 step and prints the mean velocity; exit code 0
+// on success.
+#include <cmath>
+#include <cstdio>
+#include "vfmm.hpp"
+
+int main()
+{
+  typedef Vortex::FMMCalculator<int, int, Vortex::RK3, Vortex::Inviscid, Vortex::cVPM, Vortex::Transposed> FMMCalculator;
+  exafmm::Bodies particles;
+  const int      n  = 2000;
+  const double   ds = 2 * M_PI / n;
+  for (int i = 0; i < n; i++) {
+    exafmm::Body b;
+    const double ph = i * ds;
+    b.X[0]          = std::cos(ph);
+    b.X[1]          = std::sin(ph);
+    b.X[2]          = 1e-3 * std::sin(7 * ph);
+    b.alpha[0]      = -std::sin(ph) * ds;
+    b.alpha[1]      = std::cos(ph) * ds;
+    b.radius        = 3 * ds;
+    particles.push_back(b);
+  }
+  try {
+    FMMCalculator calc(8, 32, 0.5);
+    calc.advance(particles, 0.01);
+  } catch (const Vortex::Error &e) {
+    std::fprintf(stderr, "vfmm error %d: %s\n", e.code, e.what());
+    return 1;
+  }
+  double uz = 0;
+  for (const auto &b : particles)
+    uz += b.velocity[2];
+  std::printf("mean uz %.6e\n", uz / n);
+  return std::isfinite(uz) ? 0 : 2;
+}

@@ -101,61 +101,57 @@ __global__ void __launch_bounds__(64) k_p2m(DevExp a)
 
 // ------------------------------------------------------------------ M2M
 // Parent pulls its children's multipoles (multipoleKernels.hpp:479-516),
-// dX = X_parent - X_child.
+// dX = X_parent - X_child.  Block of 128 threads per parent: all children's
+// multipoles (contiguous, the children form one block of cells) and their
+// harmonics are staged once; each thread then sums its outputs over all
+// children without further synchronisation.
 template <int P>
-__global__ void __launch_bounds__(64) k_m2m(DevExp a, const int *cells, int count)
+__device__ __forceinline__ zd m2m_term_sum(int j, int k, int d, const zd *Mc, const zd *Y)
 {
-  constexpr int K = nterms(P), NJ = (K + 63) / 64;
-  __shared__ zd Ms[3 * K], Ys[K];
+  zd acc{0, 0};
+  for (int n = 0; n <= j; n++) {
+    for (int m = max(-n, -j + k + n); m <= min(k - 1, n); m++) {
+      const zd     y = m > 0 ? conj(Y[tri(n, m)]) : Y[tri(n, -m)];
+      const double s = double(ipow2n(m) * sgn_odd(n));
+      cfma(acc, s * Mc[tri(j - n, k - m) * 3 + d], y);
+    }
+    for (int m = k; m <= min(n, j + k - n); m++) {
+      const zd     y = conj(Y[tri(n, m)]);
+      const double s = double(sgn_odd(k + n + m));
+      cfma(acc, s * conj(Mc[tri(j - n, m - k) * 3 + d]), y);
+    }
+  }
+  return acc;
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) k_m2m(DevExp a, const int *cells, int count)
+{
+  constexpr int K = nterms(P);
+  extern __shared__ double2 smem_raw[];
+  zd *Ms = reinterpret_cast<zd *>(smem_raw); // [8][3K]
+  zd *Ys = Ms + 8 * 3 * K;                   // [8][K]
   for (int pi = blockIdx.x; pi < count; pi += gridDim.x) {
     const int c = cells[pi], nch = a.cv.nchild[c], ch0 = a.cv.child[c];
     if (nch == 0)
       continue;
-    zd acc[NJ][3];
-#pragma unroll
-    for (int i = 0; i < NJ; i++)
-      for (int d = 0; d < 3; d++)
-        acc[i][d] = {0, 0};
-    for (int ch = ch0; ch < ch0 + nch; ch++) {
-      __syncthreads();
-      for (int e = threadIdx.x; e < 3 * K; e += 64)
-        Ms[e] = ldz(a.M + (size_t)ch * 3 * K + e);
-      if (threadIdx.x == 0)
-        regular_harmonics<double, P>(a.cv.x[c] - a.cv.x[ch], a.cv.y[c] - a.cv.y[ch], a.cv.z[c] - a.cv.z[ch], Ys);
-      __syncthreads();
-#pragma unroll
-      for (int i = 0; i < NJ; i++) {
-        const int jks = threadIdx.x + 64 * i;
-        if (jks >= K)
-          continue;
-        int j, k;
-        jk_of(jks, j, k);
-        for (int n = 0; n <= j; n++) {
-          for (int m = max(-n, -j + k + n); m <= min(k - 1, n); m++) {
-            const zd     y = m > 0 ? conj(Ys[tri(n, m)]) : Ys[tri(n, -m)];
-            const double s = double(ipow2n(m) * sgn_odd(n));
-            const int    src = tri(j - n, k - m);
-            for (int d = 0; d < 3; d++)
-              cfma(acc[i][d], s * Ms[src * 3 + d], y);
-          }
-          for (int m = k; m <= min(n, j + k - n); m++) {
-            const zd     y = conj(Ys[tri(n, m)]);
-            const double s = double(sgn_odd(k + n + m));
-            const int    src = tri(j - n, m - k);
-            for (int d = 0; d < 3; d++)
-              cfma(acc[i][d], s * conj(Ms[src * 3 + d]), y);
-          }
-        }
-      }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nch * 3 * K; e += blockDim.x)
+      Ms[e] = ldz(a.M + (size_t)ch0 * 3 * K + e);
+    if (threadIdx.x < nch) {
+      const int ch = ch0 + threadIdx.x;
+      regular_harmonics<double, P>(a.cv.x[c] - a.cv.x[ch], a.cv.y[c] - a.cv.y[ch], a.cv.z[c] - a.cv.z[ch], Ys + threadIdx.x * K);
     }
-#pragma unroll
-    for (int i = 0; i < NJ; i++) {
-      const int jks = threadIdx.x + 64 * i;
-      if (jks < K)
-        for (int d = 0; d < 3; d++) {
-          double2 *p = a.M + (size_t)c * 3 * K + jks * 3 + d;
-          stz(p, ldz(p) + acc[i][d]);
-        }
+    __syncthreads();
+    for (int o = threadIdx.x; o < 3 * K; o += blockDim.x) {
+      const int jks = o / 3, d = o % 3;
+      int       j, k;
+      jk_of(jks, j, k);
+      zd acc{0, 0};
+      for (int t = 0; t < nch; t++)
+        acc = acc + m2m_term_sum<P>(j, k, d, Ms + t * 3 * K, Ys + t * K);
+      double2 *p = a.M + (size_t)c * 3 * K + o;
+      stz(p, ldz(p) + acc);
     }
   }
 }
@@ -293,51 +289,56 @@ __global__ void __launch_bounds__(128) k_m2l(DevExp a, int ncells)
 }
 
 // ------------------------------------------------------------------ L2L
-// Child pulls its parent's local expansion (multipoleKernels.hpp:591-628),
-// dX = X_child - X_parent.
+// Children pull their parent's local expansion (multipoleKernels.hpp:591-628),
+// dX = X_child - X_parent.  Block of 128 threads per parent: the parent's L
+// and all children's harmonics are staged once; threads own (child, output).
 template <int P>
-__global__ void __launch_bounds__(64) k_l2l(DevExp a, const int *cells, int count)
+__device__ __forceinline__ zd l2l_term_sum(int j, int k, int d, const zd *Lp, const zd *Y)
 {
-  constexpr int K = nterms(P), NJ = (K + 63) / 64;
-  __shared__ zd Ls[3 * K], Ys[K];
-  for (int ci = blockIdx.x; ci < count; ci += gridDim.x) {
-    const int c = cells[ci], p = a.cv.parent[c];
-    if (p < 0)
+  zd acc{0, 0};
+  for (int n = j; n < P; n++) {
+    for (int m = j + k - n; m < 0; m++) {
+      const zd     y = conj(Y[tri(n - j, k - m)]);
+      const double s = double(sgn_odd(k));
+      cfma(acc, s * conj(Lp[tri(n, -m) * 3 + d]), y);
+    }
+    for (int m = 0; m <= n; m++) {
+      if (n - j >= abs(m - k)) {
+        const zd     y = m >= k ? Y[tri(n - j, m - k)] : conj(Y[tri(n - j, k - m)]);
+        const double s = double(sgn_odd((m - k) * (m < k)));
+        cfma(acc, s * Lp[tri(n, m) * 3 + d], y);
+      }
+    }
+  }
+  return acc;
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) k_l2l(DevExp a, const int *cells, int count)
+{
+  constexpr int K = nterms(P);
+  extern __shared__ double2 smem_raw[];
+  zd *Ls = reinterpret_cast<zd *>(smem_raw); // [3K]
+  zd *Ys = Ls + 3 * K;                       // [8][K]
+  for (int pi = blockIdx.x; pi < count; pi += gridDim.x) {
+    const int p = cells[pi], nch = a.cv.nchild[p], ch0 = a.cv.child[p];
+    if (nch == 0)
       continue;
     __syncthreads();
-    for (int e = threadIdx.x; e < 3 * K; e += 64)
+    for (int e = threadIdx.x; e < 3 * K; e += blockDim.x)
       Ls[e] = ldz(a.L + (size_t)p * 3 * K + e);
-    if (threadIdx.x == 0)
-      regular_harmonics<double, P>(a.cv.x[c] - a.cv.x[p], a.cv.y[c] - a.cv.y[p], a.cv.z[c] - a.cv.z[p], Ys);
+    if (threadIdx.x < nch) {
+      const int ch = ch0 + threadIdx.x;
+      regular_harmonics<double, P>(a.cv.x[ch] - a.cv.x[p], a.cv.y[ch] - a.cv.y[p], a.cv.z[ch] - a.cv.z[p], Ys + threadIdx.x * K);
+    }
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < NJ; i++) {
-      const int jks = threadIdx.x + 64 * i;
-      if (jks >= K)
-        continue;
-      int j, k;
+    for (int o = threadIdx.x; o < nch * 3 * K; o += blockDim.x) {
+      const int t = o / (3 * K), r = o % (3 * K), jks = r / 3, d = r % 3;
+      int       j, k;
       jk_of(jks, j, k);
-      zd acc[3] = {{0, 0}, {0, 0}, {0, 0}};
-      for (int n = j; n < P; n++) {
-        for (int m = j + k - n; m < 0; m++) {
-          const zd     y = conj(Ys[tri(n - j, k - m)]);
-          const double s = double(sgn_odd(k));
-          for (int d = 0; d < 3; d++)
-            cfma(acc[d], s * conj(Ls[tri(n, -m) * 3 + d]), y);
-        }
-        for (int m = 0; m <= n; m++) {
-          if (n - j >= abs(m - k)) {
-            const zd     y = m >= k ? Ys[tri(n - j, m - k)] : conj(Ys[tri(n - j, k - m)]);
-            const double s = double(sgn_odd((m - k) * (m < k)));
-            for (int d = 0; d < 3; d++)
-              cfma(acc[d], s * Ls[tri(n, m) * 3 + d], y);
-          }
-        }
-      }
-      for (int d = 0; d < 3; d++) {
-        double2 *q = a.L + (size_t)c * 3 * K + jks * 3 + d;
-        stz(q, ldz(q) + acc[d]);
-      }
+      const zd acc = l2l_term_sum<P>(j, k, d, Ls, Ys + t * K);
+      double2 *q   = a.L + (size_t)(ch0 + t) * 3 * K + r;
+      stz(q, ldz(q) + acc);
     }
   }
 }
@@ -585,6 +586,27 @@ static DevExp dev_args(const ExpArgs &e)
 
 #define VFMM_FOR_EACH_P(X) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16)
 
+// M2M into parents at levels maxLevel-1 .. 1 (the root is skipped, as the
+// reference's upward pass skips level 0, fmmCalculator.hpp:427).
+template <int P>
+static void m2m_levels(cudaStream_t s, const ExpArgs &e, const DevExp &d)
+{
+  const size_t bytes = (size_t)(8 * 3 + 8) * nterms(P) * sizeof(zd);
+  static bool  once  = false;
+  if (!once) {
+    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2m<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    once = true;
+  }
+  for (int l = e.maxLevel - 1; l >= 1; l--) {
+    const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
+    if (n1 > n0) {
+      k_m2m<P><<<std::min(n1 - n0, 152 * 16), 128, bytes, s>>>(d, e.level_cells + n0, n1 - n0);
+      count_launch();
+    }
+  }
+  VFMM_LAUNCH_CHECK();
+}
+
 template <int P>
 static void upward_P(cudaStream_t s, const ExpArgs &e)
 {
@@ -599,28 +621,14 @@ static void upward_P(cudaStream_t s, const ExpArgs &e)
     k_p2m<P><<<std::min(e.nleaves, 152 * 16), 64, bytes, s>>>(d);
     count_launch();
   }
-  for (int l = e.maxLevel - 1; l >= 1; l--) {
-    const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
-    if (n1 > n0) {
-      k_m2m<P><<<std::min(n1 - n0, 152 * 16), 64, 0, s>>>(d, e.level_cells + n0, n1 - n0);
-      count_launch();
-    }
-  }
-  VFMM_LAUNCH_CHECK();
+  m2m_levels<P>(s, e, d);
 }
 
 template <int P>
 static void m2m_P(cudaStream_t s, const ExpArgs &e)
 {
   DevExp d = dev_args(e);
-  for (int l = e.maxLevel - 1; l >= 1; l--) {
-    const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
-    if (n1 > n0) {
-      k_m2m<P><<<std::min(n1 - n0, 152 * 16), 64, 0, s>>>(d, e.level_cells + n0, n1 - n0);
-      count_launch();
-    }
-  }
-  VFMM_LAUNCH_CHECK();
+  m2m_levels<P>(s, e, d);
 }
 
 template <int P>
@@ -641,14 +649,21 @@ static void m2l_P(cudaStream_t s, const ExpArgs &e)
   VFMM_LAUNCH_CHECK();
 }
 
+// L2L from parents at levels 0 .. maxLevel-1 into their children.
 template <int P>
 static void l2l_P(cudaStream_t s, const ExpArgs &e)
 {
-  DevExp d = dev_args(e);
-  for (int l = 1; l <= e.maxLevel; l++) {
+  DevExp       d     = dev_args(e);
+  const size_t bytes = (size_t)(3 + 8) * nterms(P) * sizeof(zd);
+  static bool  once  = false;
+  if (!once) {
+    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_l2l<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    once = true;
+  }
+  for (int l = 0; l < e.maxLevel; l++) {
     const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
     if (n1 > n0) {
-      k_l2l<P><<<std::min(n1 - n0, 152 * 16), 64, 0, s>>>(d, e.level_cells + n0, n1 - n0);
+      k_l2l<P><<<std::min(n1 - n0, 152 * 16), 128, bytes, s>>>(d, e.level_cells + n0, n1 - n0);
       count_launch();
     }
   }
