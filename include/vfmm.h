@@ -197,6 +197,22 @@ int vfmm_flush_l2(vfmm_handle h);
  * FP64/FP32 pipes rather than on tensor cores. */
 int vfmm_measure_fma_peak(vfmm_handle h, int precision, double *tflops);
 
+/* ---- no allocation -------------------------------------------------------- */
+
+/* No counterpart in the reference.  Root cell of the octree -- centre out[0..2]
+ * and half-width out[3], the values exafmm::getBounds produces -- for n
+ * bodies whose coordinates x, y, z are already in device memory; out is a
+ * device pointer to 4 doubles; the work is queued on `stream` (a
+ * cudaStream_t; NULL = the default stream).  Allocates nothing, for callers
+ * that cannot call cudaMalloc (work issued under CUDA-graph stream capture,
+ * hosts whose device memory belongs to their own pool, plugins that must not
+ * touch the allocator): its scratch is a fixed 29,184-byte array in the
+ * library, present on every GPU that loads it.  n must be 1 .. 2^31-1.  The
+ * first call on a device looks up the array's address and should come before
+ * any stream capture.  Calls that overlap on the GPU share the array and race:
+ * serialise them. */
+int vfmm_bounds_noalloc(const double *x, const double *y, const double *z, size_t n, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -95,6 +95,13 @@ __global__ void k_bbox_final(const double *part, int nb, DevInfo *info)
   info->R0 = R0;
 }
 
+// The partial-reduction kernel into caller-provided storage of nb*6 doubles.
+void bbox_partial_into(cudaStream_t s, const double *x, const double *y, const double *z, int n, double *part, int nb)
+{
+  k_bbox_partial<<<nb, 256, 0, s>>>(x, y, z, n, part);
+  count_launch();
+}
+
 void tree_bounds(cudaStream_t s, const double *X, size_t cap, int n, DevInfo *info, TreeScratch &ts)
 {
   const int nb = 152 * 4;

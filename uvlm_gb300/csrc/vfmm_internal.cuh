@@ -129,6 +129,7 @@ struct TreeScratch {
   size_t           cub_bytes = 0;
 };
 void tree_bounds(cudaStream_t s, const double *X, size_t cap, int n, DevInfo *info, TreeScratch &ts);
+void bbox_partial_into(cudaStream_t s, const double *x, const double *y, const double *z, int n, double *part, int nb);
 void tree_sort_bodies(cudaStream_t s, const double *X, size_t cap, int n, int ncrit, DevInfo *info, TreeScratch &ts);
 void tree_build_cells(cudaStream_t s, int n, int ncrit, int nnodes, DevInfo *info, TreeScratch &ts, CellsView cv, int *level_cells,
                       int *level_start, int *leaf_cells);
