@@ -56,7 +56,7 @@ struct vfmm_handle_s {
 
   // expansions
   DevBuf<double2> M, L, Mprep;
-  DevBuf<int4>    items, items32;
+  DevBuf<int4>    items, items32, lanes32;
   int             items_P = 0, items_per_lane = 0;
   DevBuf<float2>  Mp32;
   DevBuf<float4>  pos32, alp32;
@@ -261,6 +261,9 @@ void ensure_items(vfmm_handle h)
   auto tab32 = m2l_schedule(h->cfg.p, 32, 4, 3, &per32);
   h->items32.reserve(tab32.size());
   VFMM_CUDA_TRY(cudaMemcpy(h->items32.p, tab32.data(), tab32.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  auto lt32 = m2l_lane_table(h->cfg.p, h->cfg.p >= 15 ? 8 : 4, 8); // tile width and batch of k_m2l32v2
+  h->lanes32.reserve(lt32.size());
+  VFMM_CUDA_TRY(cudaMemcpy(h->lanes32.p, lt32.data(), lt32.size() * sizeof(int4), cudaMemcpyHostToDevice));
   h->items_P        = h->cfg.p;
   h->items_per_lane = per;
 }
@@ -307,6 +310,7 @@ void calculate(vfmm_handle h)
     m.pos32   = h->pos32.p;
     m.alp32   = h->alp32.p;
     m.items32 = h->items32.p;
+    m.lanes32 = h->lanes32.p;
     m.R0      = h->hinfo->R0;
     p2m_mixed(s, e, m);
     m2m_pass(s, e);
@@ -421,6 +425,7 @@ int vfmm_destroy(vfmm_handle h)
   h->Mprep.release();
   h->items.release();
   h->items32.release();
+  h->lanes32.release();
   h->Mp32.release();
   h->pos32.release();
   h->alp32.release();

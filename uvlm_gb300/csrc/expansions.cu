@@ -713,6 +713,35 @@ void m2l_pass(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(m2l_P, s, e) }
 void downward_l2l(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(l2l_P, s, e) }
 void l2p_p2p_pass(cudaStream_t s, const ExpArgs &e, double *out) { VFMM_DISPATCH(l2p_P, s, e, out) }
 
+// Lane table of the lockstep M2L (k_m2l32v2): warp n (input degree n) splits
+// the output rows j <= P-1-n into tiles of kb columns; with T tiles, R =
+// min(32 / T, sb) replicas of them take turns over the batch's sources.
+// Entry [n * 32 + lane] = {j, k0 | kbn << 8, replica, R | T << 8}, j = -1 idle.
+std::vector<int4> m2l_lane_table(int P, int kb, int sb)
+{
+  std::vector<int4> tab((size_t)P * 32, make_int4(-1, 0, 0, 1));
+  for (int n = 0; n < P; n++) {
+    std::vector<int4> tiles;
+    for (int j = 0; j <= P - 1 - n; j++)
+      for (int k0 = 0; k0 <= j; k0 += kb)
+        tiles.push_back(make_int4(j, k0 | (std::min(kb, j + 1 - k0) << 8), 0, 0));
+    const int T = (int)tiles.size();
+    if (T > 32)
+      throw Error(VFMM_ERR_UNSUPPORTED, "M2L lane table: more than 32 tiles for one degree");
+    const int R = std::max(1, std::min(32 / T, sb));
+    for (int l = 0; l < 32; l++) {
+      int4 e = make_int4(-1, 0, 0, R | (T << 8));
+      if (l < T * R) {
+        e   = tiles[l % T];
+        e.z = l / T;
+        e.w = R | (T << 8);
+      }
+      tab[(size_t)n * 32 + l] = e;
+    }
+  }
+  return tab;
+}
+
 // Balanced static schedule for k_m2l: items (j, k0..k0+kb-1, n0..n1) whose
 // cost is kb * sum_{n0..n1}(2n+1) complex multiply-adds per component, packed
 // onto `lanes` lanes with at most `maxItems` each (longest-processing-time

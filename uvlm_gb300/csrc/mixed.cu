@@ -285,6 +285,161 @@ __global__ void __launch_bounds__(128) k_m2l32(DevMixed a, int ncells)
   }
 }
 
+// M2L, lockstep form.  One block per target cell, one warp per input degree
+// n (P warps).  Within warp n every lane runs the same m-loop (-n..n), so
+// there is no divergence; a lane owns an output tile (row j, columns
+// k0..k0+3, all 3 components) and keeps a sliding register window over the
+// singular harmonics S'_{j+n}^{m-k}.  Warps whose degree has few tiles
+// replicate them over several sources of the batch.  The per-pair factor
+// (R_t/R_s)^j / R_s is split exactly into 2^{(lt-ls) n} on the staged
+// multipole and 2^{(ls-lt) q} / R_s on the staged harmonics (q = j + n).
+// Lane table entry: {j, k0 | kb << 8, replica, replicas | tiles << 8}; j < 0
+// marks an idle lane.
+constexpr int M2L_SB = 8;  // sources per batch
+constexpr int M2L_YOFF = 4; // leading pad of each staged harmonic table
+
+template <int P>
+struct M2LV2 {
+  static constexpr int KB = P >= 15 ? 8 : 4; // k columns per lane tile: at most 32 tiles per degree
+  static constexpr int K = nterms(P), PP = P * P;
+  static constexpr int MSTR = 3 * PP + 1;            // complex stride of a staged multipole
+  static constexpr int YSTR = PP + M2L_YOFF + 1;     // complex stride of a staged harmonic table
+  static constexpr size_t bytes = (size_t)(M2L_SB * (MSTR + YSTR) + 3 * K) * sizeof(zf) + M2L_SB * 2 * sizeof(int);
+};
+
+template <int P>
+__global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__restrict__ lanes, int ncells)
+{
+  using G = M2LV2<P>;
+  constexpr int K = G::K, PP = G::PP, MSTR = G::MSTR, YSTR = G::YSTR, SB = M2L_SB, KB = G::KB;
+  extern __shared__ float4 smem32[];
+  zf  *Ms  = reinterpret_cast<zf *>(smem32);
+  zf  *Ys  = Ms + SB * MSTR;
+  zf  *Lsm = Ys + SB * YSTR;
+  int *Src = reinterpret_cast<int *>(Lsm + 3 * K);
+  int *Lvl = Src + SB;
+  const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int4 me = lanes[n * 32 + lane];
+  const int  j = me.x, k0 = me.y & 255, kb = me.y >> 8, rep = me.z, R = me.w & 255;
+  const int  nthreads = P * 32;
+  for (int t = blockIdx.x; t < ncells; t += gridDim.x) {
+    zf acc[KB][3];
+#pragma unroll
+    for (int kk = 0; kk < KB; kk++)
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+        acc[kk][d] = {0.f, 0.f};
+    const int    q0 = a.m2l_start[t], q1 = a.m2l_start[t + 1];
+    const double tx = a.cv.x[t], ty = a.cv.y[t], tz = a.cv.z[t];
+    const int    lt = a.cv.level[t];
+    for (int qb = q0; qb < q1; qb += SB) {
+      const int nb = min(SB, q1 - qb);
+      __syncthreads();
+      if (threadIdx.x < nb) {
+        const int s       = a.m2l_src[qb + threadIdx.x];
+        Src[threadIdx.x] = s;
+        Lvl[threadIdx.x] = a.cv.level[s];
+      }
+      __syncthreads();
+      // stage multipoles: Mp32 * 2^{(lt - ls) n}
+      for (int e = threadIdx.x; e < nb * 3 * PP; e += nthreads) {
+        const int b = e / (3 * PP), r = e - b * (3 * PP);
+        int       nn = 0;
+        while ((nn + 1) * (nn + 1) <= r / 3)
+          nn++;
+        const float2 v  = a.Mp[(size_t)Src[b] * 3 * PP + r];
+        const int    sh = (lt - Lvl[b]) * nn;
+        Ms[b * MSTR + r] = {ldexpf(v.x, sh), ldexpf(v.y, sh)};
+      }
+      // stage singular harmonics at d / R_s, folded and scaled by 2^{(ls - lt) q} / R_s
+      if (threadIdx.x < nb * P) {
+        const int    b = threadIdx.x / P, m = threadIdx.x - b * P, s = Src[b], ls = Lvl[b];
+        const double iRs = 1.0 / cell_R(a.R0, ls);
+        const float  dx = (float)((tx - a.cv.x[s]) * iRs), dy = (float)((ty - a.cv.y[s]) * iRs), dz = (float)((tz - a.cv.z[s]) * iRs);
+        const float  r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.0f / r2, S00 = rsqrtf(r2);
+        zf           col[P];
+        singular_column<float, P>(m, dx, dy, dz, ir2, S00, col);
+        zf *Y = Ys + b * YSTR + M2L_YOFF;
+        for (int q = m; q < P; q++) {
+          const float f  = ldexpf((float)iRs, (ls - lt) * q);
+          const zf    v  = {col[q].r * f, col[q].i * f};
+          Y[q * q + q + m] = (m & 1) ? zf{-v.r, -v.i} : v;
+          if (m > 0)
+            Y[q * q + q - m] = conj(v);
+        }
+      }
+      __syncthreads();
+      if (j >= 0) {
+        const int q    = j + n;
+        const int base = M2L_YOFF + q * q + q - k0;
+        for (int b = rep; b < nb; b += R) {
+          const zf *Y  = Ys + b * YSTR + base;
+          const zf *Mb = Ms + b * MSTR + (n * n + n) * 3;
+          zf        y[KB];
+#pragma unroll
+          for (int kk = 0; kk < KB; kk++)
+            y[kk] = Y[-n - kk];
+          for (int m = -n; m <= n; m++) {
+            const zf m0 = Mb[m * 3 + 0], m1 = Mb[m * 3 + 1], m2 = Mb[m * 3 + 2];
+#pragma unroll
+            for (int kk = 0; kk < KB; kk++) {
+              cfma(acc[kk][0], m0, y[kk]);
+              cfma(acc[kk][1], m1, y[kk]);
+              cfma(acc[kk][2], m2, y[kk]);
+            }
+            if (m < n) {
+#pragma unroll
+              for (int kk = KB - 1; kk > 0; kk--)
+                y[kk] = y[kk - 1];
+              y[0] = Y[m + 1];
+            }
+          }
+        }
+      }
+    }
+    // combine: replicas inside the warp (deterministic tree), then warps in order
+    const int T = me.w >> 8;
+    for (int st = 1; st < R; st <<= 1) {
+#pragma unroll
+      for (int kk = 0; kk < KB; kk++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const float vr = __shfl_down_sync(0xffffffffu, acc[kk][d].r, T * st);
+          const float vi = __shfl_down_sync(0xffffffffu, acc[kk][d].i, T * st);
+          if (j >= 0 && (rep % (2 * st)) == 0 && rep + st < R) {
+            acc[kk][d].r += vr;
+            acc[kk][d].i += vi;
+          }
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * K; e += nthreads)
+      Lsm[e] = {0.f, 0.f};
+    for (int w = 0; w < P; w++) {
+      __syncthreads();
+      if (n == w && j >= 0 && rep == 0) {
+#pragma unroll
+        for (int kk = 0; kk < KB; kk++)
+          if (kk < kb)
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+              zf &o = Lsm[tri(j, k0 + kk) * 3 + d];
+              o     = o + acc[kk][d];
+            }
+      }
+    }
+    __syncthreads();
+    const double Rt = cell_R(a.R0, lt);
+    for (int e = threadIdx.x; e < 3 * K; e += nthreads) {
+      int jj, kk;
+      jk_of_m(e / 3, jj, kk);
+      const zf     v = Lsm[e];
+      const double s = ((jj & 1) ? -1.0 : 1.0) * pow(Rt, -jj);
+      a.L[(size_t)t * 3 * K + e] = make_double2(v.r * s, v.i * s);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ L2P + P2P
 __device__ __forceinline__ zf coef_full32(const zf *c, int n, int m, int stride, int comp)
 {
@@ -550,6 +705,7 @@ static DevMixed dev_mixed(const ExpArgs &e, const MixedArgs &m)
   d.p2p_start   = e.p2p_start;
   d.p2p_src     = e.p2p_src;
   d.items       = m.items32;
+  (void)m.lanes32;
   d.R0          = m.R0;
   d.stretching  = e.stretching;
   d.formulation = e.formulation;
@@ -577,14 +733,16 @@ static void m2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   const int PP = P * P;
   k_mprep32<P><<<grid_for((long)e.ncells * PP * 3, 256), 256, 0, s>>>(e.M, m.Mp32, e.cells.level, m.R0, e.ncells);
   count_launch();
-  const size_t bytes = (size_t)4 * 4 * PP * sizeof(zf);
+  const size_t bytes = M2LV2<P>::bytes;
   static bool  once  = false;
   if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2l32<P, 4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2l32v2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     once = true;
   }
-  k_m2l32<P, 4, 3><<<grid_for(e.ncells, 4, 152 * 32), 128, bytes, s>>>(d, e.ncells);
-  count_launch();
+  if (e.ncells > 0) {
+    k_m2l32v2<P><<<std::min(e.ncells, 152 * 8), P * 32, bytes, s>>>(d, m.lanes32, e.ncells);
+    count_launch();
+  }
   VFMM_LAUNCH_CHECK();
 }
 

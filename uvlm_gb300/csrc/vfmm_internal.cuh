@@ -194,8 +194,10 @@ struct MixedArgs {
   float2       *Mp32;
   float4       *pos32, *alp32;
   const int4   *items32;
+  const int4   *lanes32; // k_m2l32v2 lane table, see m2l_lane_table
   double        R0;
 };
+std::vector<int4> m2l_lane_table(int P, int kb, int sb);
 void p2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
 void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
 void l2p_p2p_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out);
