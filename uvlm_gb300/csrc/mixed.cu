@@ -37,9 +37,15 @@ struct DevMixed {
   const int    *m2l_start, *m2l_src;
   const int    *p2p_start, *p2p_src;
   const int4   *items;
-  double        R0;
+  double        R0, iR0;
+  double        R0pow[PMAX + 1], iR0pow[PMAX + 1]; // R0^n, R0^-n
   int           stretching, formulation;
 };
+
+// R_c^n and R_c^-n for a cell at `level` (R_c = R0 / 2^level): exact
+// power-of-two rescalings of the per-tree tables.
+__device__ __forceinline__ double cell_Rpow(const DevMixed &a, int level, int n) { return ldexp(a.R0pow[n], -level * n); }
+__device__ __forceinline__ double cell_iRpow(const DevMixed &a, int level, int n) { return ldexp(a.iR0pow[n], level * n); }
 
 __device__ __forceinline__ void jk_of_m(int jks, int &j, int &k)
 {
@@ -48,7 +54,6 @@ __device__ __forceinline__ void jk_of_m(int jks, int &j, int &k)
     j++;
   k = jks - j * (j + 1) / 2;
 }
-__device__ __forceinline__ double cell_R(double R0, int level) { return ldexp(R0, -level); }
 
 // ------------------------------------------------------------------ prep
 // Leaf-relative FP32 body data for the P2P sources and targets.
@@ -89,9 +94,9 @@ __global__ void __launch_bounds__(64) k_p2m32(DevMixed a)
     if (a.cv.level[c] == 0)
       continue; // the reference's upward pass skips level 0 (fmmCalculator.hpp:427)
     const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
-    const double R = cell_R(a.R0, a.cv.level[c]);
-    const float  iR = (float)(1.0 / R);
-    zf           acc[NO];
+    const int   lev = a.cv.level[c];
+    const float iR  = (float)ldexp(a.iR0, lev);
+    zf          acc[NO];
 #pragma unroll
     for (int i = 0; i < NO; i++)
       acc[i] = {0.f, 0.f};
@@ -128,7 +133,7 @@ __global__ void __launch_bounds__(64) k_p2m32(DevMixed a)
       if (o < 3 * K) {
         int n, m;
         jk_of_m(o / 3, n, m);
-        const double s = pow(R, n);
+        const double s = cell_Rpow(a, lev, n);
         a.M[(size_t)c * 3 * K + o] = make_double2(acc[i].r * s, acc[i].i * s);
       }
     }
@@ -139,7 +144,7 @@ __global__ void __launch_bounds__(64) k_p2m32(DevMixed a)
 // Prepared scaled multipoles, sign- and conjugation-folded as in k_mprep:
 // Mp[cell][n^2+n+m][d] = ((-1)^m M_n^m (m>=0) | conj(M_n^|m|) (m<0)) / R_c^n.
 template <int P>
-__global__ void k_mprep32(const double2 *__restrict__ M, float2 *__restrict__ Mp, const int *__restrict__ level, double R0, int ncells)
+__global__ void k_mprep32(DevMixed a, int ncells)
 {
   constexpr int K = nterms(P), PP = P * P;
   const long    total = (long)ncells * PP * 3;
@@ -148,10 +153,10 @@ __global__ void k_mprep32(const double2 *__restrict__ M, float2 *__restrict__ Mp
     int       n = 0;
     while ((n + 1) * (n + 1) <= idx)
       n++;
-    const int    m  = idx - n * n - n;
-    const double2 v = M[(size_t)c * 3 * K + tri(n, m >= 0 ? m : -m) * 3 + d];
-    const double s  = pow(ldexp(R0, -level[c]), -n);
-    double       re = v.x * s, im = v.y * s;
+    const int     m = idx - n * n - n;
+    const double2 v = a.M[(size_t)c * 3 * K + tri(n, m >= 0 ? m : -m) * 3 + d];
+    const double  s = cell_iRpow(a, a.cv.level[c], n);
+    double        re = v.x * s, im = v.y * s;
     if (m >= 0) {
       if (m & 1) {
         re = -re;
@@ -159,129 +164,7 @@ __global__ void k_mprep32(const double2 *__restrict__ M, float2 *__restrict__ Mp
       }
     } else
       im = -im;
-    Mp[e] = make_float2((float)re, (float)im);
-  }
-}
-
-// One warp per target cell (4 per block); lane work items as in k_m2l.  Per
-// source, each item's partial sums are scaled by (R_t/R_s)^j / R_s before
-// they join the target's accumulators.
-template <int P, int KB, int MAXI>
-__global__ void __launch_bounds__(128) k_m2l32(DevMixed a, int ncells)
-{
-  constexpr int K = nterms(P), PP = P * P;
-  extern __shared__ float4 smem32[];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  zf       *Ms = reinterpret_cast<zf *>(smem32) + w * (4 * PP);
-  zf       *Ys = Ms + 3 * PP;
-  int4      it[MAXI];
-#pragma unroll
-  for (int i = 0; i < MAXI; i++)
-    it[i] = a.items[i * 32 + lane];
-  for (int t = blockIdx.x * 4 + w; t < ncells; t += gridDim.x * 4) {
-    zf acc[MAXI][KB][3];
-#pragma unroll
-    for (int i = 0; i < MAXI; i++)
-#pragma unroll
-      for (int kk = 0; kk < KB; kk++)
-#pragma unroll
-        for (int d = 0; d < 3; d++)
-          acc[i][kk][d] = {0.f, 0.f};
-    const int    q0 = a.m2l_start[t], q1 = a.m2l_start[t + 1];
-    const double tx = a.cv.x[t], ty = a.cv.y[t], tz = a.cv.z[t];
-    const int    lt = a.cv.level[t];
-    for (int q = q0; q < q1; q++) {
-      const int s = a.m2l_src[q], ls = a.cv.level[s];
-      __syncwarp();
-      for (int e = lane; e < 3 * PP; e += 32) {
-        const float2 v = a.Mp[(size_t)s * 3 * PP + e];
-        Ms[e]          = {v.x, v.y};
-      }
-      const double iRs = 1.0 / cell_R(a.R0, ls);
-      if (lane < P) {
-        const float dx = (float)((tx - a.cv.x[s]) * iRs), dy = (float)((ty - a.cv.y[s]) * iRs), dz = (float)((tz - a.cv.z[s]) * iRs);
-        const float r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.0f / r2, S00 = rsqrtf(r2);
-        zf          col[P];
-        singular_column<float, P>(lane, dx, dy, dz, ir2, S00, col);
-        const int m = lane;
-        for (int n = m; n < P; n++) {
-          const zf v        = col[n];
-          Ys[n * n + n + m] = (m & 1) ? zf{-v.r, -v.i} : v;
-          if (m > 0)
-            Ys[n * n + n - m] = conj(v);
-        }
-      }
-      __syncwarp();
-      const float fs = (float)iRs; // 1/R_s
-#pragma unroll
-      for (int i = 0; i < MAXI; i++) {
-        const int j = it[i].x;
-        if (j < 0)
-          continue;
-        const int k0 = it[i].y & 255, kb = it[i].y >> 8, n0 = it[i].z, n1 = it[i].w;
-        zf        tmp[KB][3];
-#pragma unroll
-        for (int kk = 0; kk < KB; kk++)
-#pragma unroll
-          for (int d = 0; d < 3; d++)
-            tmp[kk][d] = {0.f, 0.f};
-        for (int n = n0; n <= n1; n++) {
-          const int base = (j + n) * (j + n) + (j + n) - k0;
-          for (int m = -n; m <= n; m++) {
-            const zf m0 = Ms[(n * n + n + m) * 3 + 0], m1 = Ms[(n * n + n + m) * 3 + 1], m2 = Ms[(n * n + n + m) * 3 + 2];
-#pragma unroll
-            for (int kk = 0; kk < KB; kk++) {
-              if (kk < kb) {
-                const zf y = Ys[base + m - kk];
-                cfma(tmp[kk][0], m0, y);
-                cfma(tmp[kk][1], m1, y);
-                cfma(tmp[kk][2], m2, y);
-              }
-            }
-          }
-        }
-        const float f = ldexpf(fs, (ls - lt) * j); // (R_t/R_s)^j / R_s
-#pragma unroll
-        for (int kk = 0; kk < KB; kk++)
-#pragma unroll
-          for (int d = 0; d < 3; d++) {
-            acc[i][kk][d].r = fmaf(f, tmp[kk][d].r, acc[i][kk][d].r);
-            acc[i][kk][d].i = fmaf(f, tmp[kk][d].i, acc[i][kk][d].i);
-          }
-      }
-    }
-    __syncwarp();
-    zf *Lr = Ms;
-    for (int e = lane; e < 3 * K; e += 32)
-      Lr[e] = {0.f, 0.f};
-    __syncwarp();
-    for (int src = 0; src < 32; src++) {
-      if (lane == src) {
-#pragma unroll
-        for (int i = 0; i < MAXI; i++) {
-          const int j = it[i].x;
-          if (j < 0)
-            continue;
-          const int k0 = it[i].y & 255, kb = it[i].y >> 8;
-#pragma unroll
-          for (int kk = 0; kk < KB; kk++)
-            if (kk < kb)
-              for (int d = 0; d < 3; d++) {
-                zf &o = Lr[tri(j, k0 + kk) * 3 + d];
-                o     = o + acc[i][kk][d];
-              }
-        }
-      }
-      __syncwarp();
-    }
-    const double Rt = cell_R(a.R0, lt);
-    for (int e = lane; e < 3 * K; e += 32) {
-      int j, k;
-      jk_of_m(e / 3, j, k);
-      const zf     v = Lr[e];
-      const double s = ((j & 1) ? -1.0 : 1.0) * pow(Rt, -j);
-      a.L[(size_t)t * 3 * K + e] = make_double2(v.r * s, v.i * s);
-    }
+    a.Mp[e] = make_float2((float)re, (float)im);
   }
 }
 
@@ -304,7 +187,7 @@ struct M2LV2 {
   static constexpr int K = nterms(P), PP = P * P;
   static constexpr int MSTR = 3 * PP + 1;            // complex stride of a staged multipole
   static constexpr int YSTR = PP + M2L_YOFF + 1;     // complex stride of a staged harmonic table
-  static constexpr size_t bytes = (size_t)(M2L_SB * (MSTR + YSTR) + 3 * K) * sizeof(zf) + M2L_SB * 2 * sizeof(int);
+  static constexpr size_t bytes = (size_t)(M2L_SB * (MSTR + YSTR) + 3 * K) * sizeof(zf) + M2L_SB * (sizeof(float4) + 2 * sizeof(int));
 };
 
 template <int P>
@@ -313,11 +196,14 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
   using G = M2LV2<P>;
   constexpr int K = G::K, PP = G::PP, MSTR = G::MSTR, YSTR = G::YSTR, SB = M2L_SB, KB = G::KB;
   extern __shared__ float4 smem32[];
-  zf  *Ms  = reinterpret_cast<zf *>(smem32);
-  zf  *Ys  = Ms + SB * MSTR;
-  zf  *Lsm = Ys + SB * YSTR;
-  int *Src = reinterpret_cast<int *>(Lsm + 3 * K);
-  int *Lvl = Src + SB;
+  // 16-byte-aligned fields first: per source (d / R_s, 1 / R_s), source index, level
+  float4 *Off = smem32;
+  int    *Src = reinterpret_cast<int *>(Off + SB);
+  int    *Lvl = Src + SB;
+  static_assert((SB * (sizeof(float4) + 2 * sizeof(int))) % 16 == 0, "keeps the complex arrays aligned");
+  zf *Ms  = reinterpret_cast<zf *>(Lvl + SB);
+  zf *Ys  = Ms + SB * MSTR;
+  zf *Lsm = Ys + SB * YSTR;
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int4 me = lanes[n * 32 + lane];
   const int  j = me.x, k0 = me.y & 255, kb = me.y >> 8, rep = me.z, R = me.w & 255;
@@ -336,32 +222,34 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
       const int nb = min(SB, q1 - qb);
       __syncthreads();
       if (threadIdx.x < nb) {
-        const int s       = a.m2l_src[qb + threadIdx.x];
+        const int    s   = a.m2l_src[qb + threadIdx.x];
+        const int    ls  = a.cv.level[s];
+        const double iRs = ldexp(a.iR0, ls);
         Src[threadIdx.x] = s;
-        Lvl[threadIdx.x] = a.cv.level[s];
+        Lvl[threadIdx.x] = ls;
+        Off[threadIdx.x] = make_float4((float)((tx - a.cv.x[s]) * iRs), (float)((ty - a.cv.y[s]) * iRs), (float)((tz - a.cv.z[s]) * iRs),
+                                       (float)iRs);
       }
       __syncthreads();
       // stage multipoles: Mp32 * 2^{(lt - ls) n}
       for (int e = threadIdx.x; e < nb * 3 * PP; e += nthreads) {
         const int b = e / (3 * PP), r = e - b * (3 * PP);
-        int       nn = 0;
-        while ((nn + 1) * (nn + 1) <= r / 3)
-          nn++;
+        const int nn = (int)sqrtf((float)(r / 3)); // degree of entry n^2+n+m (exact for these small integers)
         const float2 v  = a.Mp[(size_t)Src[b] * 3 * PP + r];
         const int    sh = (lt - Lvl[b]) * nn;
         Ms[b * MSTR + r] = {ldexpf(v.x, sh), ldexpf(v.y, sh)};
       }
       // stage singular harmonics at d / R_s, folded and scaled by 2^{(ls - lt) q} / R_s
       if (threadIdx.x < nb * P) {
-        const int    b = threadIdx.x / P, m = threadIdx.x - b * P, s = Src[b], ls = Lvl[b];
-        const double iRs = 1.0 / cell_R(a.R0, ls);
-        const float  dx = (float)((tx - a.cv.x[s]) * iRs), dy = (float)((ty - a.cv.y[s]) * iRs), dz = (float)((tz - a.cv.z[s]) * iRs);
+        const int    b = threadIdx.x / P, m = threadIdx.x - b * P, ls = Lvl[b];
+        const float4 o = Off[b];
+        const float  dx = o.x, dy = o.y, dz = o.z;
         const float  r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.0f / r2, S00 = rsqrtf(r2);
         zf           col[P];
         singular_column<float, P>(m, dx, dy, dz, ir2, S00, col);
         zf *Y = Ys + b * YSTR + M2L_YOFF;
         for (int q = m; q < P; q++) {
-          const float f  = ldexpf((float)iRs, (ls - lt) * q);
+          const float f  = ldexpf(o.w, (ls - lt) * q);
           const zf    v  = {col[q].r * f, col[q].i * f};
           Y[q * q + q + m] = (m & 1) ? zf{-v.r, -v.i} : v;
           if (m > 0)
@@ -429,12 +317,11 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
       }
     }
     __syncthreads();
-    const double Rt = cell_R(a.R0, lt);
     for (int e = threadIdx.x; e < 3 * K; e += nthreads) {
       int jj, kk;
       jk_of_m(e / 3, jj, kk);
       const zf     v = Lsm[e];
-      const double s = ((jj & 1) ? -1.0 : 1.0) * pow(Rt, -jj);
+      const double s = ((jj & 1) ? -1.0 : 1.0) * cell_iRpow(a, lt, jj);
       a.L[(size_t)t * 3 * K + e] = make_double2(v.r * s, v.i * s);
     }
   }
@@ -504,14 +391,14 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
     const int    c  = a.leaf_cells[li];
     const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
-    const double R  = cell_R(a.R0, a.cv.level[c]);
-    const float  iR = (float)(1.0 / R);
+    const int    lev = a.cv.level[c];
+    const float  iR  = (float)ldexp(a.iR0, lev);
     __syncthreads();
     for (int e = threadIdx.x; e < 3 * K; e += 128) {
       int n, m;
       jk_of_m(e / 3, n, m);
       const double2 v = a.L[(size_t)c * 3 * K + e];
-      const double  s = pow(R, n); // scaled local Lt = L R^n
+      const double  s = cell_Rpow(a, lev, n); // scaled local Lt = L R^n
       Lc[e]           = {(float)(v.x * s), (float)(v.y * s)};
     }
     __syncthreads();
@@ -569,7 +456,7 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
             ya             = nx;
           }
         }
-        const double s1 = 1.0 / R, s2 = s1 * s1;
+        const double s1 = ldexp(a.iR0, lev), s2 = s1 * s1;
         for (int k = 0; k < 3; k++)
           far[threadIdx.x * 12 + k] = (double)f[k] * s1;
         for (int k = 3; k < 12; k++)
@@ -707,6 +594,12 @@ static DevMixed dev_mixed(const ExpArgs &e, const MixedArgs &m)
   d.items       = m.items32;
   (void)m.lanes32;
   d.R0          = m.R0;
+  d.iR0         = 1.0 / m.R0;
+  d.R0pow[0] = d.iR0pow[0] = 1.0;
+  for (int n = 1; n <= PMAX; n++) {
+    d.R0pow[n]  = d.R0pow[n - 1] * m.R0;
+    d.iR0pow[n] = d.iR0pow[n - 1] * d.iR0;
+  }
   d.stretching  = e.stretching;
   d.formulation = e.formulation;
   return d;
@@ -731,7 +624,7 @@ static void m2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
 {
   DevMixed  d  = dev_mixed(e, m);
   const int PP = P * P;
-  k_mprep32<P><<<grid_for((long)e.ncells * PP * 3, 256), 256, 0, s>>>(e.M, m.Mp32, e.cells.level, m.R0, e.ncells);
+  k_mprep32<P><<<grid_for((long)e.ncells * PP * 3, 256), 256, 0, s>>>(d, e.ncells);
   count_launch();
   const size_t bytes = M2LV2<P>::bytes;
   static bool  once  = false;
