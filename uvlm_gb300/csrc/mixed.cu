@@ -356,10 +356,13 @@ struct L2P32Sizes {
   static constexpr int    K  = nterms(P);
   static constexpr int    K1 = nterms(P - 1) > 0 ? nterms(P - 1) : 1;
   static constexpr int    K2 = nterms(P - 2) > 0 ? nterms(P - 2) : 1;
-  static constexpr size_t bytes = (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zf) + 2 * 128 * 12 * sizeof(double);
+  static constexpr int    CH = 1024; // near-field source bodies staged per chunk
+  static constexpr size_t bytes =
+      (size_t)CH * 2 * sizeof(float4) + 128 * (sizeof(float4) + sizeof(int)) + (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zf);
+  static_assert((size_t)CH * 2 * sizeof(float4) >= 2 * 128 * 12 * sizeof(float), "the staging buffer holds the reduction");
 };
 
-// two-sum: s + e = a + b exactly
+// two-sum: hi + lo accumulates v without losing its low-order bits
 __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v)
 {
   const float s  = hi + v;
@@ -369,30 +372,47 @@ __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v)
   lo += e;
 }
 
+// One block (128 threads) per target leaf.  Thread l works for target
+// t = l % nt (nt targets in this chunk) as member g = l / nt of G = 128 / nt
+// threads:
+//  * far field: member g evaluates the columns m = g, g+G, ... of the leaf's
+//    derivative expansions at the target;
+//  * near field: the bodies of the leaf's P2P source leaves are staged in
+//    shared memory as one flat array in coordinates relative to the target
+//    leaf's centre (each source leaf's centre offset computed once, in FP64),
+//    and member g takes every G-th staged body; groups of 16 are summed in FP32.
+// Everything is folded into a two-sum (float-float) accumulator, the G members
+// are combined in a fixed order, and the result becomes FP64 for the
+// stretching epilogue.  All lanes run the same trip counts.
 template <int P>
 __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
 {
   using S = L2P32Sizes<P>;
-  constexpr int K = S::K, K1 = S::K1, K2 = S::K2;
+  constexpr int K = S::K, K1 = S::K1, K2 = S::K2, CH = S::CH, LG = 128;
   constexpr int D1 = P - 1, D2 = P - 2;
   extern __shared__ float4 smem32[];
-  zf     *Lc  = reinterpret_cast<zf *>(smem32);
-  zf     *U   = Lc + 3 * K;
-  zf     *JJ  = U + 3 * K1;
-  double *far = reinterpret_cast<double *>(JJ + 9 * K2);
-  double *red = far + 128 * 12;
+  float4 *Sp   = smem32;   // staged source positions (rel. to target leaf), w = 1/(2 sigma^2)
+  float4 *Sa   = Sp + CH;  // staged strengths, w = 1/sigma
+  float4 *Loff = Sa + CH;  // per source leaf of the current group: centre offset, w = body start (int bits)
+  int    *Lcnt = reinterpret_cast<int *>(Loff + LG);
+  zf     *Lc   = reinterpret_cast<zf *>(Lcnt + LG);
+  zf     *U    = Lc + 3 * K;
+  zf     *JJ   = U + 3 * K1;
+  float  *rhi  = reinterpret_cast<float *>(Sp); // [128][12] partial sums (hi), reusing the staging buffer
+  float  *rlo  = rhi + 128 * 12;                // [128][12] partial sums (lo)
   (void)K1;
   (void)K2;
   const float inv4pi = 0.0795774715459476679f;
   const float c2spi  = 1.12837916709551257f; // 2/sqrt(pi)
-  // series constants: G = ghat(RS) * KS / sigma^3, A = hhat(RS) * KS / sigma^5, KS = (2/sqrt(pi)) / (8 sqrt(2) pi)
-  const float KS = 0.0317468755f;
+  const float KS     = 0.0317468755f;        // (2/sqrt(pi)) / (8 sqrt(2) pi)
+  const float isq2   = 0.707106781186547524f;
 
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
-    const int    c  = a.leaf_cells[li];
+    const int    c = a.leaf_cells[li];
     const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
     const int    lev = a.cv.level[c];
     const float  iR  = (float)ldexp(a.iR0, lev);
+    const int    q0 = a.p2p_start[c], q1 = a.p2p_start[c + 1];
     __syncthreads();
     for (int e = threadIdx.x; e < 3 * K; e += 128) {
       int n, m;
@@ -422,20 +442,29 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
     __syncthreads();
 
     for (int tc = 0; tc < nb; tc += 128) {
-      const int nbc = min(128, nb - tc);
-      if (threadIdx.x < nbc) {
-        const float4 p = a.pos32[b0 + tc + threadIdx.x];
-        const float  x = p.x * iR, y = p.y * iR, z = p.z * iR;
-        const float  r2 = x * x + y * y + z * z;
-        float        f[12];
+      const int  nt = min(128, nb - tc);
+      const int  G = 128 / nt, tt = threadIdx.x % nt, g = threadIdx.x / nt;
+      const bool active = g < G;
+      float      hi[12], lo[12];
+      for (int k = 0; k < 12; k++)
+        hi[k] = lo[k] = 0.f;
+      float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (active) {
+        pt = a.pos32[b0 + tc + tt];
+        // far field: columns m = g, g + G, ... (u scaled by 1/R, J by 1/R^2)
+        const float x = pt.x * iR, y = pt.y * iR, z = pt.z * iR;
+        const float r2 = x * x + y * y + z * z;
+        float       f[12];
         for (int k = 0; k < 12; k++)
           f[k] = 0.f;
         zf diag{1.f, 0.f};
         for (int m = 0; m < D1; m++) {
           if (m > 0) {
-            const float s = 1.f / float(2 * m);
-            diag          = {(diag.r * x - diag.i * y) * s, (diag.r * y + diag.i * x) * s};
+            const float sc = 1.f / float(2 * m);
+            diag           = {(diag.r * x - diag.i * y) * sc, (diag.r * y + diag.i * x) * sc};
           }
+          if ((m - g) % G != 0)
+            continue;
           const float w  = m == 0 ? 1.f : 2.f;
           zf          ya = diag, yb{0.f, 0.f};
           for (int n = m; n < D1; n++) {
@@ -456,92 +485,125 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
             ya             = nx;
           }
         }
-        const double s1 = ldexp(a.iR0, lev), s2 = s1 * s1;
         for (int k = 0; k < 3; k++)
-          far[threadIdx.x * 12 + k] = (double)f[k] * s1;
+          two_sum_add(hi[k], lo[k], f[k] * iR);
         for (int k = 3; k < 12; k++)
-          far[threadIdx.x * 12 + k] = (double)f[k] * s2;
+          two_sum_add(hi[k], lo[k], f[k] * (iR * iR));
       }
-      const int TG = nbc <= 32 ? 32 : (nbc <= 64 ? 64 : 128), G = 128 / TG;
-      const int tt = threadIdx.x % TG, g = threadIdx.x / TG;
-      float     hi[12], lo[12];
-      for (int k = 0; k < 12; k++)
-        hi[k] = lo[k] = 0.f;
-      if (tt < nbc) {
-        const float4 pt = a.pos32[b0 + tc + tt];
-        const double ctx = a.cv.x[c], cty = a.cv.y[c], ctz = a.cv.z[c];
-        const int    q0 = a.p2p_start[c], q1 = a.p2p_start[c + 1];
-        for (int q = q0 + g; q < q1; q += G) {
-          const int   sc = a.p2p_src[q], sb = a.cv.body[sc], sn = a.cv.nbody[sc];
-          const float ox = pt.x - (float)(a.cv.x[sc] - ctx), oy = pt.y - (float)(a.cv.y[sc] - cty), oz = pt.z - (float)(a.cv.z[sc] - ctz);
-          float       s[12];
-          for (int k = 0; k < 12; k++)
-            s[k] = 0.f;
-          for (int jb = sb; jb < sb + sn; jb++) {
-            const float4 ps = __ldg(a.pos32 + jb);
-            const float  dx = ox - ps.x, dy = oy - ps.y, dz = oz - ps.z;
-            const float  R2 = dx * dx + dy * dy + dz * dz;
-            if (R2 != 0.f) {
-              const float4 al = __ldg(a.alp32 + jb);
-              const float  RS = R2 * ps.w; // R^2 / (2 sigma^2)
-              float        Gc, Ac;
-              if (RS < 0.25f) {
-                // x^3-scaled series: no cancellation for close pairs
-                const float gpoly = ((((((1.f / 5400.f) * RS - 1.f / 780.f) * RS + 1.f / 132.f) * RS - 1.f / 27.f) * RS + 1.f / 7.f) * RS - 0.4f) * RS +
-                                    2.f / 3.f;
-                const float hpoly = ((((((-1.f / 6120.f) * RS + 1.f / 900.f) * RS - 1.f / 156.f) * RS + 1.f / 33.f) * RS - 1.f / 9.f) * RS + 2.f / 7.f) *
-                                        RS -
-                                    0.4f;
-                const float is = al.w, is2 = is * is, is3 = is2 * is;
-                Gc             = gpoly * KS * is3;
-                Ac             = hpoly * KS * is3 * is2;
-              } else {
-                const float xs   = sqrtf(RS);
-                const float erfS = erff(xs);
-                const float t2   = c2spi * xs * __expf(-RS);
-                const float rinv = rsqrtf(R2);
-                const float c4   = inv4pi * rinv * rinv * rinv;
-                const float gg   = erfS - t2;
-                Gc               = gg * c4;
-                Ac               = (t2 * 2.f * ps.w - 3.f * gg * rinv * rinv) * c4;
-              }
-              const float cr0 = dy * al.z - dz * al.y, cr1 = dz * al.x - dx * al.z, cr2 = dx * al.y - dy * al.x;
-              s[0] = fmaf(Gc, cr0, s[0]);
-              s[1] = fmaf(Gc, cr1, s[1]);
-              s[2] = fmaf(Gc, cr2, s[2]);
-              const float a0 = Ac * cr0, a1 = Ac * cr1, a2 = Ac * cr2;
-              s[3]  = fmaf(a0, dx, s[3]);
-              s[4]  = fmaf(a0, dy, s[4]);
-              s[5]  = fmaf(a0, dz, s[5]);
-              s[6]  = fmaf(a1, dx, s[6]);
-              s[7]  = fmaf(a1, dy, s[7]);
-              s[8]  = fmaf(a1, dz, s[8]);
-              s[9]  = fmaf(a2, dx, s[9]);
-              s[10] = fmaf(a2, dy, s[10]);
-              s[11] = fmaf(a2, dz, s[11]);
-              s[6] -= Gc * al.z;
-              s[9] += Gc * al.y;
-              s[4] += Gc * al.z;
-              s[10] -= Gc * al.x;
-              s[5] -= Gc * al.y;
-              s[8] += Gc * al.x;
+      // near field, source leaves in groups of LG
+      for (int qg = q0; qg < q1; qg += LG) {
+        const int ng = min(LG, q1 - qg);
+        __syncthreads();
+        if (threadIdx.x < ng) {
+          const int sc      = a.p2p_src[qg + threadIdx.x];
+          Loff[threadIdx.x] = make_float4((float)(a.cv.x[sc] - a.cv.x[c]), (float)(a.cv.y[sc] - a.cv.y[c]), (float)(a.cv.z[sc] - a.cv.z[c]),
+                                          __int_as_float(a.cv.body[sc]));
+          Lcnt[threadIdx.x] = a.cv.nbody[sc];
+        }
+        __syncthreads();
+        int lq = 0, lo_off = 0; // next leaf of the group, body offset inside it (uniform)
+        while (lq < ng) {
+          int cnt = 0;
+          while (lq < ng && cnt < CH) {
+            const float4 o = Loff[lq];
+            const int    sn = Lcnt[lq], take = min(sn - lo_off, CH - cnt), sb = __float_as_int(o.w) + lo_off;
+            for (int i = threadIdx.x; i < take; i += 128) {
+              float4 p = a.pos32[sb + i];
+              p.x += o.x;
+              p.y += o.y;
+              p.z += o.z;
+              Sp[cnt + i] = p;
+              Sa[cnt + i] = a.alp32[sb + i];
+            }
+            cnt += take;
+            lo_off += take;
+            if (lo_off == sn) {
+              lq++;
+              lo_off = 0;
             }
           }
-          for (int k = 0; k < 12; k++)
-            two_sum_add(hi[k], lo[k], s[k]);
+          __syncthreads();
+          if (active) {
+            for (int j0 = g; j0 < cnt; j0 += 16 * G) {
+              float sacc[12];
+              for (int k = 0; k < 12; k++)
+                sacc[k] = 0.f;
+              const int jend = min(cnt, j0 + 16 * G);
+              for (int jb = j0; jb < jend; jb += G) {
+                const float4 ps = Sp[jb];
+                const float  dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
+                const float  R2 = dx * dx + dy * dy + dz * dz;
+                if (R2 != 0.f) {
+                  const float4 al = Sa[jb];
+                  const float  RS = R2 * ps.w; // R^2 / (2 sigma^2)
+                  float        Gc, Ac;
+                  if (RS < 0.25f) {
+                    // x^3-scaled series of the regularised kernel: no cancellation for close pairs
+                    const float gpoly = ((((((1.f / 5400.f) * RS - 1.f / 780.f) * RS + 1.f / 132.f) * RS - 1.f / 27.f) * RS + 1.f / 7.f) * RS - 0.4f) *
+                                            RS +
+                                        2.f / 3.f;
+                    const float hpoly = ((((((-1.f / 6120.f) * RS + 1.f / 900.f) * RS - 1.f / 156.f) * RS + 1.f / 33.f) * RS - 1.f / 9.f) * RS +
+                                         2.f / 7.f) *
+                                            RS -
+                                        0.4f;
+                    const float is = al.w, is2 = is * is, is3 = is2 * is;
+                    Gc             = gpoly * KS * is3;
+                    Ac             = hpoly * KS * is3 * is2;
+                  } else {
+                    const float rinv = rsqrtf(R2);
+                    const float xs   = R2 * rinv * al.w * isq2; // R / (sqrt(2) sigma)
+                    const float erfS = erff(xs);
+                    const float t2   = c2spi * xs * __expf(-RS);
+                    const float c4   = inv4pi * rinv * rinv * rinv;
+                    const float gg   = erfS - t2;
+                    Gc               = gg * c4;
+                    Ac               = (t2 * 2.f * ps.w - 3.f * gg * rinv * rinv) * c4;
+                  }
+                  const float cr0 = dy * al.z - dz * al.y, cr1 = dz * al.x - dx * al.z, cr2 = dx * al.y - dy * al.x;
+                  sacc[0] = fmaf(Gc, cr0, sacc[0]);
+                  sacc[1] = fmaf(Gc, cr1, sacc[1]);
+                  sacc[2] = fmaf(Gc, cr2, sacc[2]);
+                  const float a0 = Ac * cr0, a1 = Ac * cr1, a2 = Ac * cr2;
+                  sacc[3]  = fmaf(a0, dx, sacc[3]);
+                  sacc[4]  = fmaf(a0, dy, sacc[4]);
+                  sacc[5]  = fmaf(a0, dz, sacc[5]);
+                  sacc[6]  = fmaf(a1, dx, sacc[6]);
+                  sacc[7]  = fmaf(a1, dy, sacc[7]);
+                  sacc[8]  = fmaf(a1, dz, sacc[8]);
+                  sacc[9]  = fmaf(a2, dx, sacc[9]);
+                  sacc[10] = fmaf(a2, dy, sacc[10]);
+                  sacc[11] = fmaf(a2, dz, sacc[11]);
+                  sacc[6]  = fmaf(-Gc, al.z, sacc[6]);
+                  sacc[9]  = fmaf(Gc, al.y, sacc[9]);
+                  sacc[4]  = fmaf(Gc, al.z, sacc[4]);
+                  sacc[10] = fmaf(-Gc, al.x, sacc[10]);
+                  sacc[5]  = fmaf(-Gc, al.y, sacc[5]);
+                  sacc[8]  = fmaf(Gc, al.x, sacc[8]);
+                }
+              }
+              for (int k = 0; k < 12; k++)
+                two_sum_add(hi[k], lo[k], -sacc[k]); // the near field enters with a minus sign
+            }
+          }
+          __syncthreads();
         }
       }
-      for (int k = 0; k < 12; k++)
-        red[threadIdx.x * 12 + k] = (double)hi[k] + (double)lo[k];
+      __syncthreads(); // staging buffer free: reuse it for the partial sums
+      for (int k = 0; k < 12; k++) {
+        rhi[threadIdx.x * 12 + k] = hi[k];
+        rlo[threadIdx.x * 12 + k] = lo[k];
+      }
       __syncthreads();
-      if (threadIdx.x < nbc) {
+      if (threadIdx.x < nt) {
         const int t = threadIdx.x, b = b0 + tc + t;
         double    r[12];
         for (int k = 0; k < 12; k++) {
-          double nearv = 0;
-          for (int gg = 0; gg < G; gg++)
-            nearv += red[(gg * TG + t) * 12 + k];
-          r[k] = far[t * 12 + k] - nearv;
+          float h = 0.f, l = 0.f;
+          for (int gg = 0; gg < G; gg++) {
+            two_sum_add(h, l, rhi[(gg * nt + t) * 12 + k]);
+            l += rlo[(gg * nt + t) * 12 + k];
+          }
+          r[k] = (double)h + (double)l;
         }
         const double al[3] = {a.soa[F_A * a.cap + b], a.soa[(F_A + 1) * a.cap + b], a.soa[(F_A + 2) * a.cap + b]};
         double       dadt[3];
@@ -568,7 +630,6 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
           out[(F_J + k) * a.cap + b] = r[3 + k];
         out[F_DRDT * a.cap + b] = drdt;
       }
-      __syncthreads();
     }
   }
 }
