@@ -6,6 +6,7 @@
 // All work runs on the handle's stream; the host synchronises twice per
 // tree build (node counts, pair counts) and at the end of each API call.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <exception>
 #include "vfmm_internal.cuh"
@@ -57,6 +58,7 @@ struct vfmm_handle_s {
   // expansions
   DevBuf<double2> M, L, Mprep;
   DevBuf<int4>    items, items32, lanes32;
+  int             m2l_batch = 16; // sources per mixed-M2L batch; VFMM_M2L_BATCH = 8, 16 or 32 overrides
   int             items_P = 0, items_per_lane = 0;
   DevBuf<float2>  Mp32;
   DevBuf<float4>  pos32, alp32;
@@ -261,7 +263,9 @@ void ensure_items(vfmm_handle h)
   auto tab32 = m2l_schedule(h->cfg.p, 32, 4, 3, &per32);
   h->items32.reserve(tab32.size());
   VFMM_CUDA_TRY(cudaMemcpy(h->items32.p, tab32.data(), tab32.size() * sizeof(int4), cudaMemcpyHostToDevice));
-  auto lt32 = m2l_lane_table(h->cfg.p, h->cfg.p >= 15 ? 8 : 4, 8); // tile width and batch of k_m2l32v2
+  const char *sb = getenv("VFMM_M2L_BATCH");
+  h->m2l_batch   = sb && (atoi(sb) == 8 || atoi(sb) == 32) ? atoi(sb) : 16;
+  auto lt32      = m2l_lane_table(h->cfg.p, h->cfg.p >= 15 ? 8 : 4, h->m2l_batch); // tile width and batch of k_m2l32v2
   h->lanes32.reserve(lt32.size());
   VFMM_CUDA_TRY(cudaMemcpy(h->lanes32.p, lt32.data(), lt32.size() * sizeof(int4), cudaMemcpyHostToDevice));
   h->items_P        = h->cfg.p;
@@ -310,7 +314,8 @@ void calculate(vfmm_handle h)
     m.pos32   = h->pos32.p;
     m.alp32   = h->alp32.p;
     m.items32 = h->items32.p;
-    m.lanes32 = h->lanes32.p;
+    m.lanes32   = h->lanes32.p;
+    m.m2l_batch = h->m2l_batch;
     m.R0      = h->hinfo->R0;
     p2m_mixed(s, e, m);
     m2m_pass(s, e);

@@ -105,23 +105,36 @@ __global__ void __launch_bounds__(64) k_p2m(DevExp a)
 // multipoles (contiguous, the children form one block of cells) and their
 // harmonics are staged once; each thread then sums its outputs over all
 // children without further synchronisation.
-template <int P>
-__device__ __forceinline__ zd m2m_term_sum(int j, int k, int d, const zd *Mc, const zd *Y)
+__device__ __forceinline__ zd neg_if(zd v, bool neg) { return neg ? zd{-v.r, -v.i} : v; }
+
+// One output (j, k, d) of M2M for NC children at once (children t0..t0+NC-1
+// that exist): the index arithmetic is shared and the NC accumulators are
+// independent, which keeps the FP64 pipe fed.  Signs ipow2n(m) * oddOrEven(n)
+// and oddOrEven(k+n+m) negate an operand instead of costing a multiply.
+template <int P, int NC>
+__device__ __forceinline__ void m2m_term_sum(int j, int k, int d, const zd *Ms, const zd *Ys, int t0, int nch, zd *acc)
 {
-  zd acc{0, 0};
+  constexpr int K = nterms(P);
   for (int n = 0; n <= j; n++) {
     for (int m = max(-n, -j + k + n); m <= min(k - 1, n); m++) {
-      const zd     y = m > 0 ? conj(Y[tri(n, m)]) : Y[tri(n, -m)];
-      const double s = double(ipow2n(m) * sgn_odd(n));
-      cfma(acc, s * Mc[tri(j - n, k - m) * 3 + d], y);
+      const int  yi = tri(n, m > 0 ? m : -m), mi = tri(j - n, k - m) * 3 + d;
+      const bool cj = m > 0, neg = ((m < 0 ? (m & 1) : 0) ^ (n & 1)) != 0;
+#pragma unroll
+      for (int c = 0; c < NC; c++)
+        if (t0 + c < nch) {
+          const zd y = Ys[(t0 + c) * K + yi];
+          cfma(acc[c], neg_if(Ms[(t0 + c) * 3 * K + mi], neg), cj ? conj(y) : y);
+        }
     }
     for (int m = k; m <= min(n, j + k - n); m++) {
-      const zd     y = conj(Y[tri(n, m)]);
-      const double s = double(sgn_odd(k + n + m));
-      cfma(acc, s * conj(Mc[tri(j - n, m - k) * 3 + d]), y);
+      const int  yi = tri(n, m), mi = tri(j - n, m - k) * 3 + d;
+      const bool neg = ((k + n + m) & 1) != 0;
+#pragma unroll
+      for (int c = 0; c < NC; c++)
+        if (t0 + c < nch)
+          cfma(acc[c], neg_if(conj(Ms[(t0 + c) * 3 * K + mi]), neg), conj(Ys[(t0 + c) * K + yi]));
     }
   }
-  return acc;
 }
 
 template <int P>
@@ -147,11 +160,11 @@ __global__ void __launch_bounds__(128) k_m2m(DevExp a, const int *cells, int cou
       const int jks = o / 3, d = o % 3;
       int       j, k;
       jk_of(jks, j, k);
-      zd acc{0, 0};
-      for (int t = 0; t < nch; t++)
-        acc = acc + m2m_term_sum<P>(j, k, d, Ms + t * 3 * K, Ys + t * K);
+      zd acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+      for (int t0 = 0; t0 < nch; t0 += 4)
+        m2m_term_sum<P, 4>(j, k, d, Ms, Ys, t0, nch, acc);
       double2 *p = a.M + (size_t)c * 3 * K + o;
-      stz(p, ldz(p) + acc);
+      stz(p, ldz(p) + ((acc[0] + acc[1]) + (acc[2] + acc[3])));
     }
   }
 }
@@ -292,25 +305,35 @@ __global__ void __launch_bounds__(128) k_m2l(DevExp a, int ncells)
 // Children pull their parent's local expansion (multipoleKernels.hpp:591-628),
 // dX = X_child - X_parent.  Block of 128 threads per parent: the parent's L
 // and all children's harmonics are staged once; threads own (child, output).
-template <int P>
-__device__ __forceinline__ zd l2l_term_sum(int j, int k, int d, const zd *Lp, const zd *Y)
+// One output (j, k, d) of L2L for NC children at once (shared parent operand
+// and index arithmetic, independent accumulators).
+template <int P, int NC>
+__device__ __forceinline__ void l2l_term_sum(int j, int k, int d, const zd *Lp, const zd *Ys, int t0, int nch, zd *acc)
 {
-  zd acc{0, 0};
+  constexpr int K = nterms(P);
   for (int n = j; n < P; n++) {
+    const bool negk = (k & 1) != 0;
     for (int m = j + k - n; m < 0; m++) {
-      const zd     y = conj(Y[tri(n - j, k - m)]);
-      const double s = double(sgn_odd(k));
-      cfma(acc, s * conj(Lp[tri(n, -m) * 3 + d]), y);
+      const zd  l  = neg_if(conj(Lp[tri(n, -m) * 3 + d]), negk);
+      const int yi = tri(n - j, k - m);
+#pragma unroll
+      for (int c = 0; c < NC; c++)
+        if (t0 + c < nch)
+          cfma(acc[c], l, conj(Ys[(t0 + c) * K + yi]));
     }
-    for (int m = 0; m <= n; m++) {
-      if (n - j >= abs(m - k)) {
-        const zd     y = m >= k ? Y[tri(n - j, m - k)] : conj(Y[tri(n - j, k - m)]);
-        const double s = double(sgn_odd((m - k) * (m < k)));
-        cfma(acc, s * Lp[tri(n, m) * 3 + d], y);
-      }
+    const int mlo = max(0, k - (n - j)), mhi = min(n, k + (n - j)); // n - j >= |m - k|
+    for (int m = mlo; m <= mhi; m++) {
+      const bool neg = m < k && ((k - m) & 1);
+      const zd   l   = neg_if(Lp[tri(n, m) * 3 + d], neg);
+      const int  yi  = tri(n - j, m >= k ? m - k : k - m);
+#pragma unroll
+      for (int c = 0; c < NC; c++)
+        if (t0 + c < nch) {
+          const zd y = Ys[(t0 + c) * K + yi];
+          cfma(acc[c], l, m >= k ? y : conj(y));
+        }
     }
   }
-  return acc;
 }
 
 template <int P>
@@ -332,13 +355,19 @@ __global__ void __launch_bounds__(128) k_l2l(DevExp a, const int *cells, int cou
       regular_harmonics<double, P>(a.cv.x[ch] - a.cv.x[p], a.cv.y[ch] - a.cv.y[p], a.cv.z[ch] - a.cv.z[p], Ys + threadIdx.x * K);
     }
     __syncthreads();
-    for (int o = threadIdx.x; o < nch * 3 * K; o += blockDim.x) {
-      const int t = o / (3 * K), r = o % (3 * K), jks = r / 3, d = r % 3;
+    const int ngroups = (nch + 3) / 4;
+    for (int o = threadIdx.x; o < ngroups * 3 * K; o += blockDim.x) {
+      const int t0 = (o / (3 * K)) * 4, r = o % (3 * K), jks = r / 3, d = r % 3;
       int       j, k;
       jk_of(jks, j, k);
-      const zd acc = l2l_term_sum<P>(j, k, d, Ls, Ys + t * K);
-      double2 *q   = a.L + (size_t)(ch0 + t) * 3 * K + r;
-      stz(q, ldz(q) + acc);
+      zd acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+      l2l_term_sum<P, 4>(j, k, d, Ls, Ys, t0, nch, acc);
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        if (t0 + c < nch) {
+          double2 *q = a.L + (size_t)(ch0 + t0 + c) * 3 * K + r;
+          stz(q, ldz(q) + acc[c]);
+        }
     }
   }
 }

@@ -178,23 +178,22 @@ __global__ void k_mprep32(DevMixed a, int ncells)
 // multipole and 2^{(ls-lt) q} / R_s on the staged harmonics (q = j + n).
 // Lane table entry: {j, k0 | kb << 8, replica, replicas | tiles << 8}; j < 0
 // marks an idle lane.
-constexpr int M2L_SB = 8;  // sources per batch
 constexpr int M2L_YOFF = 4; // leading pad of each staged harmonic table
 
-template <int P>
+template <int P, int SB>
 struct M2LV2 {
   static constexpr int KB = P >= 15 ? 8 : 4; // k columns per lane tile: at most 32 tiles per degree
   static constexpr int K = nterms(P), PP = P * P;
   static constexpr int MSTR = 3 * PP + 1;            // complex stride of a staged multipole
   static constexpr int YSTR = PP + M2L_YOFF + 1;     // complex stride of a staged harmonic table
-  static constexpr size_t bytes = (size_t)(M2L_SB * (MSTR + YSTR) + 3 * K) * sizeof(zf) + M2L_SB * (sizeof(float4) + 2 * sizeof(int));
+  static constexpr size_t bytes = (size_t)(SB * (MSTR + YSTR) + 3 * K) * sizeof(zf) + SB * (sizeof(float4) + 2 * sizeof(int));
 };
 
-template <int P>
+template <int P, int SB>
 __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__restrict__ lanes, int ncells)
 {
-  using G = M2LV2<P>;
-  constexpr int K = G::K, PP = G::PP, MSTR = G::MSTR, YSTR = G::YSTR, SB = M2L_SB, KB = G::KB;
+  using G = M2LV2<P, SB>;
+  constexpr int K = G::K, PP = G::PP, MSTR = G::MSTR, YSTR = G::YSTR, KB = G::KB;
   extern __shared__ float4 smem32[];
   // 16-byte-aligned fields first: per source (d / R_s, 1 / R_s), source index, level
   float4 *Off = smem32;
@@ -680,6 +679,21 @@ static void p2m32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   VFMM_LAUNCH_CHECK();
 }
 
+template <int P, int SB>
+static void m2l32_launch(cudaStream_t s, const DevMixed &d, const ExpArgs &e, const MixedArgs &m)
+{
+  const size_t bytes = M2LV2<P, SB>::bytes;
+  static bool  once  = false;
+  if (!once) {
+    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2l32v2<P, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    once = true;
+  }
+  if (e.ncells > 0) {
+    k_m2l32v2<P, SB><<<std::min(e.ncells, 152 * 8), P * 32, bytes, s>>>(d, m.lanes32, e.ncells);
+    count_launch();
+  }
+}
+
 template <int P>
 static void m2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
 {
@@ -687,16 +701,12 @@ static void m2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   const int PP = P * P;
   k_mprep32<P><<<grid_for((long)e.ncells * PP * 3, 256), 256, 0, s>>>(d, e.ncells);
   count_launch();
-  const size_t bytes = M2LV2<P>::bytes;
-  static bool  once  = false;
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2l32v2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
-  if (e.ncells > 0) {
-    k_m2l32v2<P><<<std::min(e.ncells, 152 * 8), P * 32, bytes, s>>>(d, m.lanes32, e.ncells);
-    count_launch();
-  }
+  if (m.m2l_batch == 32)
+    m2l32_launch<P, 32>(s, d, e, m);
+  else if (m.m2l_batch == 8)
+    m2l32_launch<P, 8>(s, d, e, m);
+  else
+    m2l32_launch<P, 16>(s, d, e, m);
   VFMM_LAUNCH_CHECK();
 }
 

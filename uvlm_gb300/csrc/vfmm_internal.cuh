@@ -195,6 +195,7 @@ struct MixedArgs {
   float4       *pos32, *alp32;
   const int4   *items32;
   const int4   *lanes32; // k_m2l32v2 lane table, see m2l_lane_table
+  int           m2l_batch; // sources staged per batch in k_m2l32v2 (8, 16 or 32)
   double        R0;
 };
 std::vector<int4> m2l_lane_table(int P, int kb, int sb);
