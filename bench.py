@@ -156,6 +156,11 @@ def m2l_flops_per_pair(p: int) -> int:
 
 P2P_FLOPS = 84  # per body-body interaction, counted from multipoleKernels.hpp:239-283
 
+# DRAM bytes (read + write) per unit of the two mixed-precision evaluation
+# kernels at p = 10, from one ncu capture of a 2^19-body cloud
+# (profiles/k_m2l32v2_k_l2p_p2p32_cloud512K_p10.md): per M2L pair, per body.
+NCU_TRAFFIC_MIXED_P10 = {"m2l": 378.8e6 / 3843856, "l2p_p2p": 171.5e6 / 524288}
+
 
 def measured_peaks() -> dict:
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -256,9 +261,15 @@ def run_ours(args, dist: Dist) -> dict | None:
     dom = max(cand, key=lambda k: cand[k][0])
     t_dom, f_dom = cand[dom]
     achieved = f_dom / (t_dom * 1e-3) / 1e12
+    traffic = None
+    if args.precision == "mixed" and args.p == 10:
+        units = stats["m2l_pairs"] if dom == "m2l" else n
+        traffic = NCU_TRAFFIC_MIXED_P10[dom] * units
     roof = {"bound": "fp64" if args.precision == "fp64" else "fp32", "kernel": dom, "achieved": achieved,
             "peak": peak_fp.value, "unit": "TFLOP/s", "frac": achieved / peak_fp.value if peak_fp.value else None,
-            "traffic": None,
+            "traffic": traffic,
+            "traffic_source": "DRAM bytes per unit from an ncu capture of a 2^19-body cloud at p = 10, scaled by "
+                              "this launch's units (M2L pairs or bodies); null for other orders",
             "peak_source": "measured on this GPU in this run: FMA-chain probe kernel (vfmm_measure_fma_peak); "
                            "MEASURED_PEAKS.json has no CUDA-core figure",
             "algorithmic_flops_per_launch": f_dom, "kernel_ms": t_dom}

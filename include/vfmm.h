@@ -129,9 +129,12 @@ int vfmm_copy_bodies_to_host(vfmm_handle h, vfmm_body *bodies, size_t n);
  * evaluation).  With relax > 0, relaxation follows the step (using that J). */
 int vfmm_advance(vfmm_handle h, vfmm_body *bodies, size_t n, double dt);
 
-/* FMMCalculator::getSensorData (fmmCalculator.hpp:726-731): velocity (and,
- * from the far field, J) at probe points from the particles of the last
- * init/calculate.  `sensors` is permuted into its own tree order. */
+/* FMMCalculator::getSensorData (fmmCalculator.hpp:726-731): velocity at probe
+ * points from the particles (multipoles of the last calculate, near field
+ * from the particles as they are now); velocity and dadt are overwritten, the
+ * far-field J is added to the sensors' J.  `sensors` is permuted into its own
+ * tree order, as the reference's buildTree does.  Evaluated in FP64.
+ * VFMM_ERR_STATE before the first calculate/advance. */
 int vfmm_get_sensor_data(vfmm_handle h, vfmm_body *sensors, size_t n);
 
 /* Relaxation (relaxation.hpp:8-19, written 0-based) of the device bodies with

@@ -1,7 +1,8 @@
 // A caller written against the reference's FMMCalculator API, compiled
 // against include/vfmm.hpp and linked with libvfmm.so.  Builds a small ring
-// of particles, takes one RK3 step and prints the mean velocity; exit code 0
-// on success.
+// of particles, takes one RK3 step, prints the mean velocity and reads the
+// velocity at the ring's centre through getSensorData (Gamma / 2R = 0.5 for
+// this ring); exit code 0 on success.
 #include <cmath>
 #include <cstdio>
 #include "vfmm.hpp"
@@ -23,9 +24,11 @@ int main()
     b.radius        = 3 * ds;
     particles.push_back(b);
   }
+  exafmm::Bodies sensors(1);
   try {
     FMMCalculator calc(8, 32, 0.5);
     calc.advance(particles, 0.01);
+    calc.getSensorData(sensors);
   } catch (const Vortex::Error &e) {
     std::fprintf(stderr, "vfmm error %d: %s\n", e.code, e.what());
     return 1;
@@ -33,6 +36,7 @@ int main()
   double uz = 0;
   for (const auto &b : particles)
     uz += b.velocity[2];
-  std::printf("mean uz %.6e\n", uz / n);
-  return std::isfinite(uz) ? 0 : 2;
+  const double uc = sensors[0].velocity[2];
+  std::printf("mean uz %.6e centre uz %.6e\n", uz / n, uc);
+  return std::isfinite(uz) && std::fabs(uc - 0.5) < 0.01 ? 0 : 2;
 }

@@ -30,6 +30,8 @@ CELL_DTYPE = np.dtype([
 assert CELL_DTYPE.itemsize == 72
 
 VFMM_OK = 0
+(VFMM_ERR_INVALID, VFMM_ERR_NONFINITE, VFMM_ERR_DEPTH, VFMM_ERR_CAPACITY, VFMM_ERR_CUDA, VFMM_ERR_TIMEOUT,
+ VFMM_ERR_UNSUPPORTED, VFMM_ERR_STATE) = range(1, 9)
 STATUS = {0: "OK", 1: "ERR_INVALID", 2: "ERR_NONFINITE", 3: "ERR_DEPTH", 4: "ERR_CAPACITY", 5: "ERR_CUDA",
           6: "ERR_TIMEOUT", 7: "ERR_UNSUPPORTED", 8: "ERR_STATE"}
 EULER, RK2, RK3, RK4 = 0, 1, 2, 3

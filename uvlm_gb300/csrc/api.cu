@@ -13,7 +13,47 @@
 
 namespace vfmm {
 thread_local unsigned long long *g_launch_counter = nullptr;
-}
+
+// One octree in the reference's cell order (tree.hpp:29-99) with its
+// per-level tables.
+struct Tree {
+  DevBuf<int>    nchild, nbody, child, body, level, parent;
+  DevBuf<double> x, y, z, R;
+  DevBuf<int>    level_cells, level_start, leaf_cells;
+  int            level_start_host[MAXL + 2]{};
+  int            ncells = 0, nleaves = 0, maxLevel = 0;
+  double         R0 = 0;
+
+  CellsView view() { return CellsView{nchild.p, nbody.p, child.p, body.p, level.p, parent.p, x.p, y.p, z.p, R.p}; }
+  void      release()
+  {
+    for (auto *b : {&nchild, &nbody, &child, &body, &level, &parent, &level_cells, &level_start, &leaf_cells})
+      b->release();
+    for (auto *b : {&x, &y, &z, &R})
+      b->release();
+  }
+};
+
+// P2P and M2L lists of a (target tree, source tree) traversal as CSR rows
+// over the target cells; the sorted (target << 32 | source) keys stay in ls.
+struct Lists {
+  DevBuf<int> p2p_start, p2p_src, m2l_start, m2l_src;
+  int         n_p2p = 0, n_m2l = 0;
+  size_t      cap_front = 0, cap_p2p = 0, cap_m2l = 0;
+  ListScratch ls;
+
+  void release()
+  {
+    for (auto *b : {&p2p_start, &p2p_src, &m2l_start, &m2l_src})
+      b->release();
+    ls.front[0].release();
+    ls.front[1].release();
+    for (auto *b : {&ls.p2p_raw, &ls.m2l_raw, &ls.p2p_sorted, &ls.m2l_sorted})
+      b->release();
+    ls.cub_tmp.release();
+  }
+};
+} // namespace vfmm
 
 using namespace vfmm;
 
@@ -38,22 +78,22 @@ struct vfmm_handle_s {
   int            cur = 0;
   DevBuf<double> aos; // device staging for 296-byte records
 
-  // tree
-  DevInfo       *info  = nullptr; // device
-  DevInfo       *hinfo = nullptr; // pinned host
-  TreeScratch    ts;
-  ListScratch    ls;
-  DevBuf<int>    c_nchild, c_nbody, c_child, c_body, c_level, c_parent;
-  DevBuf<double> c_x, c_y, c_z, c_R;
-  DevBuf<int>    level_cells, level_start, leaf_cells;
-  int            level_start_host[MAXL + 2]{};
-  int            ncells = 0, nleaves = 0, maxLevel = 0;
+  // particle tree and its self-interaction lists
+  DevInfo    *info  = nullptr; // device
+  DevInfo    *hinfo = nullptr; // pinned host
+  TreeScratch ts;
+  Tree        tree;
+  Lists       lists;
 
-  // lists
-  DevBuf<int>        p2p_start, p2p_src, m2l_start, m2l_src;
-  int                n_p2p = 0, n_m2l = 0;
-  unsigned long long interactions = 0;
-  size_t             cap_front = 0, cap_p2p = 0, cap_m2l = 0;
+  // sensor points: bodies (field-major, double-buffered), tree, lists
+  // against the particle tree, local expansions
+  size_t          scap = 0;
+  int             ns = 0, scur = 0;
+  DevBuf<double>  ssoa[2];
+  DevInfo        *sinfo = nullptr, *shinfo = nullptr;
+  Tree            stree;
+  Lists           slists;
+  DevBuf<double2> sL;
 
   // expansions
   DevBuf<double2> M, L, Mprep;
@@ -66,11 +106,6 @@ struct vfmm_handle_s {
   DevBuf<unsigned char> flushbuf;
   DevBuf<double>        dtmp;
   bool                  has_tree = false, has_eval = false;
-
-  CellsView cells()
-  {
-    return CellsView{c_nchild.p, c_nbody.p, c_child.p, c_body.p, c_level.p, c_parent.p, c_x.p, c_y.p, c_z.p, c_R.p};
-  }
 };
 
 namespace {
@@ -166,86 +201,97 @@ void download(vfmm_handle h, vfmm_body *b, size_t n)
   VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
 }
 
-void read_info(vfmm_handle h)
+void read_info(cudaStream_t s, DevInfo *info, DevInfo *hinfo)
 {
-  VFMM_CUDA_TRY(cudaMemcpyAsync(h->hinfo, h->info, sizeof(DevInfo), cudaMemcpyDeviceToHost, h->stream));
-  VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  VFMM_CUDA_TRY(cudaMemcpyAsync(hinfo, info, sizeof(DevInfo), cudaMemcpyDeviceToHost, s));
+  VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+}
+
+void read_info(vfmm_handle h) { read_info(h->stream, h->info, h->hinfo); }
+
+// Tree of the n bodies in soa[cur] (field-major, capacity cap).  The bodies
+// are gathered into tree order in soa[cur ^ 1] and cur flips, as buildTree
+// permutes its bodies (tree.hpp:101-113).  One host sync (node counts).
+void build_tree(cudaStream_t s, DevBuf<double> *soa, int &cur, size_t cap, int n, int ncrit, DevInfo *info, DevInfo *hinfo, TreeScratch &ts,
+                Tree &t)
+{
+  VFMM_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(DevInfo), s));
+  check_finite(s, soa[cur].p, cap, n, info);
+  tree_bounds(s, soa[cur].p + (size_t)F_X * cap, cap, n, info, ts);
+  tree_sort_bodies(s, soa[cur].p + (size_t)F_X * cap, cap, n, ncrit, info, ts);
+  gather_bodies(s, soa[cur].p, soa[cur ^ 1].p, cap, ts.perm.p, n, (1ull << NFIELD) - 1);
+  cur ^= 1;
+  const int nncap = n + MAXL * (n / (ncrit + 1)) + 64;
+  for (auto *b : {&t.nchild, &t.nbody, &t.child, &t.body, &t.level, &t.parent, &t.level_cells, &t.leaf_cells})
+    b->reserve(nncap);
+  for (auto *b : {&t.x, &t.y, &t.z, &t.R})
+    b->reserve(nncap);
+  t.level_start.reserve(MAXL + 2);
+  tree_build_cells(s, n, ncrit, nncap, info, ts, t.view(), t.level_cells.p, t.level_start.p, t.leaf_cells.p);
+  VFMM_CUDA_TRY(cudaMemcpyAsync(t.level_start_host, t.level_start.p, sizeof(int) * (MAXL + 2), cudaMemcpyDeviceToHost, s));
+  read_info(s, info, hinfo);
+  if (hinfo->nonfinite)
+    throw Error(VFMM_ERR_NONFINITE, "non-finite position, strength or radius");
+  if (hinfo->err)
+    throw Error(hinfo->err, "tree deeper than 21 levels: more than ncrit bodies (nearly) coincide");
+  if (hinfo->overflow)
+    throw Error(VFMM_ERR_CAPACITY, "tree node capacity exceeded");
+  t.ncells   = hinfo->nnodes;
+  t.nleaves  = hinfo->nleaves;
+  t.maxLevel = hinfo->maxLevel;
+  t.R0       = hinfo->R0;
+}
+
+// Lists of the traversal of targets tt against sources st (traverse.hpp:
+// 32-85), growing the capacities until nothing overflows (one host sync per
+// attempt), then sorted into CSR rows.  interactions (device counter, may be
+// null) receives the body-body P2P count of a self traversal.
+void build_lists(cudaStream_t s, Tree &tt, Tree &st, double theta, DevInfo *info, DevInfo *hinfo, Lists &L, unsigned long long *interactions)
+{
+  if (L.cap_front == 0) {
+    const size_t nc = (size_t)std::max(tt.ncells, st.ncells), nl = (size_t)std::max(tt.nleaves, st.nleaves);
+    L.cap_front     = std::max<size_t>(4096, nc * 16);
+    L.cap_p2p       = std::max<size_t>(4096, nl * 48);
+    L.cap_m2l       = std::max<size_t>(4096, nc * 240);
+  }
+  for (int attempt = 0;; attempt++) {
+    L.ls.front[0].reserve(L.cap_front);
+    L.ls.front[1].reserve(L.cap_front);
+    L.ls.p2p_raw.reserve(L.cap_p2p);
+    L.ls.m2l_raw.reserve(L.cap_m2l);
+    traverse(s, tt.view(), st.view(), tt.ncells, tt.maxLevel, st.maxLevel, theta, info, L.ls, L.ls.front[0].cap, L.ls.p2p_raw.cap,
+             L.ls.m2l_raw.cap);
+    read_info(s, info, hinfo);
+    if (!hinfo->overflow)
+      break;
+    if (attempt > 8)
+      throw Error(VFMM_ERR_CAPACITY, "interaction lists keep overflowing");
+    L.cap_front = std::max(L.cap_front * 2, L.ls.front[0].cap * 2);
+    L.cap_p2p   = std::max(L.cap_p2p * 2, L.ls.p2p_raw.cap * 2);
+    L.cap_m2l   = std::max(L.cap_m2l * 2, L.ls.m2l_raw.cap * 2);
+    VFMM_CUDA_TRY(cudaMemsetAsync(&info->overflow, 0, sizeof(int), s));
+  }
+  L.n_p2p = hinfo->n_p2p;
+  L.n_m2l = hinfo->n_m2l;
+  L.p2p_start.reserve(tt.ncells + 1);
+  L.m2l_start.reserve(tt.ncells + 1);
+  L.p2p_src.reserve(L.n_p2p + 1);
+  L.m2l_src.reserve(L.n_m2l + 1);
+  if (interactions)
+    VFMM_CUDA_TRY(cudaMemsetAsync(interactions, 0, sizeof(unsigned long long), s));
+  lists_to_csr(s, L.ls, L.n_p2p, L.n_m2l, tt.ncells, 32, L.p2p_start.p, L.p2p_src.p, L.m2l_start.p, L.m2l_src.p,
+               interactions ? tt.nbody.p : nullptr, interactions);
 }
 
 // Tree and lists of the bodies in soa[cur]; bodies are reordered into tree order.
 void build_tree_and_lists(vfmm_handle h)
 {
   cudaStream_t s = h->stream;
-  const int    n = h->n;
-  const auto  &c = h->cfg;
   h->has_tree    = false;
   h->has_eval    = false;
   VFMM_CUDA_TRY(cudaEventRecord(h->ph[0], s));
-  VFMM_CUDA_TRY(cudaMemsetAsync(h->info, 0, sizeof(DevInfo), s));
-  check_finite(s, h->soa[h->cur].p, h->cap, n, h->info);
-  tree_bounds(s, h->soa[h->cur].p + (size_t)F_X * h->cap, h->cap, n, h->info, h->ts);
-  tree_sort_bodies(s, h->soa[h->cur].p + (size_t)F_X * h->cap, h->cap, n, c.ncrit, h->info, h->ts);
-  gather_bodies(s, h->soa[h->cur].p, h->soa[h->cur ^ 1].p, h->cap, h->ts.perm.p, n, (1ull << NFIELD) - 1);
-  h->cur ^= 1;
-  const int nncap = n + MAXL * (n / (c.ncrit + 1)) + 64;
-  h->c_nchild.reserve(nncap);
-  h->c_nbody.reserve(nncap);
-  h->c_child.reserve(nncap);
-  h->c_body.reserve(nncap);
-  h->c_level.reserve(nncap);
-  h->c_parent.reserve(nncap);
-  h->c_x.reserve(nncap);
-  h->c_y.reserve(nncap);
-  h->c_z.reserve(nncap);
-  h->c_R.reserve(nncap);
-  h->level_cells.reserve(nncap);
-  h->leaf_cells.reserve(nncap);
-  h->level_start.reserve(MAXL + 2);
-  tree_build_cells(s, n, c.ncrit, nncap, h->info, h->ts, h->cells(), h->level_cells.p, h->level_start.p, h->leaf_cells.p);
-  VFMM_CUDA_TRY(cudaMemcpyAsync(h->level_start_host, h->level_start.p, sizeof(int) * (MAXL + 2), cudaMemcpyDeviceToHost, s));
-  read_info(h);
-  if (h->hinfo->nonfinite)
-    throw Error(VFMM_ERR_NONFINITE, "non-finite position, strength or radius");
-  if (h->hinfo->err)
-    throw Error(h->hinfo->err, "tree deeper than 21 levels: more than ncrit bodies (nearly) coincide");
-  if (h->hinfo->overflow)
-    throw Error(VFMM_ERR_CAPACITY, "tree node capacity exceeded");
-  h->ncells   = h->hinfo->nnodes;
-  h->nleaves  = h->hinfo->nleaves;
-  h->maxLevel = h->hinfo->maxLevel;
-
-  // traversal, growing the list capacities until nothing overflows
-  if (h->cap_front == 0) {
-    h->cap_front = std::max<size_t>(4096, (size_t)h->ncells * 16);
-    h->cap_p2p   = std::max<size_t>(4096, (size_t)h->nleaves * 48);
-    h->cap_m2l   = std::max<size_t>(4096, (size_t)h->ncells * 240);
-  }
-  for (int attempt = 0;; attempt++) {
-    h->ls.front[0].reserve(h->cap_front);
-    h->ls.front[1].reserve(h->cap_front);
-    h->ls.p2p_raw.reserve(h->cap_p2p);
-    h->ls.m2l_raw.reserve(h->cap_m2l);
-    traverse(s, h->cells(), h->cells(), h->ncells, h->maxLevel, h->maxLevel, c.theta, h->info, h->ls, h->ls.front[0].cap, h->ls.p2p_raw.cap,
-             h->ls.m2l_raw.cap);
-    read_info(h);
-    if (!h->hinfo->overflow)
-      break;
-    if (attempt > 8)
-      throw Error(VFMM_ERR_CAPACITY, "interaction lists keep overflowing");
-    h->cap_front = std::max(h->cap_front * 2, h->ls.front[0].cap * 2);
-    h->cap_p2p   = std::max(h->cap_p2p * 2, h->ls.p2p_raw.cap * 2);
-    h->cap_m2l   = std::max(h->cap_m2l * 2, h->ls.m2l_raw.cap * 2);
-    VFMM_CUDA_TRY(cudaMemsetAsync(&h->info->overflow, 0, sizeof(int), s));
-  }
-  h->n_p2p = h->hinfo->n_p2p;
-  h->n_m2l = h->hinfo->n_m2l;
-  h->p2p_start.reserve(h->ncells + 1);
-  h->m2l_start.reserve(h->ncells + 1);
-  h->p2p_src.reserve(h->n_p2p + 1);
-  h->m2l_src.reserve(h->n_m2l + 1);
-  VFMM_CUDA_TRY(cudaMemsetAsync(&h->info->p2p_interactions, 0, sizeof(unsigned long long), s));
-  lists_to_csr(s, h->ls, h->n_p2p, h->n_m2l, h->ncells, 32, h->p2p_start.p, h->p2p_src.p, h->m2l_start.p, h->m2l_src.p, h->c_nbody.p,
-               &h->info->p2p_interactions);
+  build_tree(s, h->soa, h->cur, h->cap, h->n, h->cfg.ncrit, h->info, h->hinfo, h->ts, h->tree);
+  build_lists(s, h->tree, h->tree, h->cfg.theta, h->info, h->hinfo, h->lists, &h->info->p2p_interactions);
   VFMM_CUDA_TRY(cudaEventRecord(h->ph[1], s));
   h->has_tree = true;
   h->has_eval = false;
@@ -272,6 +318,34 @@ void ensure_items(vfmm_handle h)
   h->items_per_lane = per;
 }
 
+// Expansion arguments of the particle tree and its self lists.
+ExpArgs particle_args(vfmm_handle h)
+{
+  ExpArgs e{};
+  e.P                   = h->cfg.p;
+  e.cells               = h->tree.view();
+  e.ncells              = h->tree.ncells;
+  e.level_cells         = h->tree.level_cells.p;
+  e.level_start_host    = h->tree.level_start_host;
+  e.maxLevel            = h->tree.maxLevel;
+  e.leaf_cells          = h->tree.leaf_cells.p;
+  e.nleaves             = h->tree.nleaves;
+  e.soa                 = h->soa[h->cur].p;
+  e.cap                 = h->cap;
+  e.M                   = h->M.p;
+  e.L                   = h->L.p;
+  e.Mprep               = h->Mprep.p;
+  e.m2l_start           = h->lists.m2l_start.p;
+  e.m2l_src             = h->lists.m2l_src.p;
+  e.p2p_start           = h->lists.p2p_start.p;
+  e.p2p_src             = h->lists.p2p_src.p;
+  e.m2l_items           = h->items.p;
+  e.m2l_nitems_per_lane = h->items_per_lane;
+  e.stretching          = h->cfg.stretching;
+  e.formulation         = h->cfg.formulation;
+  return e;
+}
+
 void calculate(vfmm_handle h)
 {
   if (!h->has_tree)
@@ -279,34 +353,13 @@ void calculate(vfmm_handle h)
   cudaStream_t s  = h->stream;
   const int    K3 = 3 * h->cfg.p * (h->cfg.p + 1) / 2;
   ensure_items(h);
-  h->M.reserve((size_t)h->ncells * K3);
-  h->L.reserve((size_t)h->ncells * K3);
-  h->Mprep.reserve((size_t)h->ncells * 3 * h->cfg.p * h->cfg.p);
-  VFMM_CUDA_TRY(cudaMemsetAsync(h->M.p, 0, sizeof(double2) * (size_t)h->ncells * K3, s));
-  ExpArgs e{};
-  e.P                   = h->cfg.p;
-  e.cells               = h->cells();
-  e.ncells              = h->ncells;
-  e.level_cells         = h->level_cells.p;
-  e.level_start_host    = h->level_start_host;
-  e.maxLevel            = h->maxLevel;
-  e.leaf_cells          = h->leaf_cells.p;
-  e.nleaves             = h->nleaves;
-  e.soa                 = h->soa[h->cur].p;
-  e.cap                 = h->cap;
-  e.M                   = h->M.p;
-  e.L                   = h->L.p;
-  e.Mprep               = h->Mprep.p;
-  e.m2l_start           = h->m2l_start.p;
-  e.m2l_src             = h->m2l_src.p;
-  e.p2p_start           = h->p2p_start.p;
-  e.p2p_src             = h->p2p_src.p;
-  e.m2l_items           = h->items.p;
-  e.m2l_nitems_per_lane = h->items_per_lane;
-  e.stretching          = h->cfg.stretching;
-  e.formulation         = h->cfg.formulation;
+  h->M.reserve((size_t)h->tree.ncells * K3);
+  h->L.reserve((size_t)h->tree.ncells * K3);
+  h->Mprep.reserve((size_t)h->tree.ncells * 3 * h->cfg.p * h->cfg.p);
+  VFMM_CUDA_TRY(cudaMemsetAsync(h->M.p, 0, sizeof(double2) * (size_t)h->tree.ncells * K3, s));
+  const ExpArgs e = particle_args(h);
   if (h->cfg.precision == VFMM_MIXED) {
-    h->Mp32.reserve((size_t)h->ncells * 3 * h->cfg.p * h->cfg.p);
+    h->Mp32.reserve((size_t)h->tree.ncells * 3 * h->cfg.p * h->cfg.p);
     h->pos32.reserve(h->n);
     h->alp32.reserve(h->n);
     MixedArgs m{};
@@ -316,7 +369,7 @@ void calculate(vfmm_handle h)
     m.items32 = h->items32.p;
     m.lanes32   = h->lanes32.p;
     m.m2l_batch = h->m2l_batch;
-    m.R0      = h->hinfo->R0;
+    m.R0      = h->tree.R0;
     p2m_mixed(s, e, m);
     m2m_pass(s, e);
     VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
@@ -337,6 +390,67 @@ void calculate(vfmm_handle h)
     VFMM_CUDA_TRY(cudaEventRecord(h->ph[5], s));
   }
   h->has_eval = true;
+}
+
+// getSensorData (fmmCalculator.hpp:726-731 with :117-161, :469-491): a tree
+// of the sensors (buildTree permutes them), the traversal of the sensor tree
+// as targets against the particle tree, M2L from the particles' multipoles
+// of the last calculate, the velocity-only P2P against the particles as they
+// are now, then L2L and L2P down the sensor tree.  The sensors come back in
+// sensor-tree order.  FP64 in both precision modes.
+void sensor_data(vfmm_handle h, vfmm_body *sens, size_t n)
+{
+  if (!h->has_eval)
+    throw Error(VFMM_ERR_STATE, "sensor data needs the particles' multipoles: call calculate or advance first");
+  if (n == 0)
+    throw Error(VFMM_ERR_INVALID, "no sensors");
+  if (n > (size_t)0x7fffffff)
+    throw Error(VFMM_ERR_INVALID, "too many sensors");
+  cudaStream_t s = h->stream;
+  if (n > h->scap) {
+    const size_t cap = n + n / 8 + 256;
+    h->ssoa[0].release();
+    h->ssoa[1].release();
+    h->ssoa[0].reserve(cap * NFIELD);
+    h->ssoa[1].reserve(cap * NFIELD);
+    h->scap = cap;
+  }
+  h->aos.reserve(std::max(n, (size_t)h->n) * NFIELD);
+  h->ns = (int)n;
+  VFMM_CUDA_TRY(cudaMemcpyAsync(h->aos.p, sens, n * sizeof(vfmm_body), cudaMemcpyHostToDevice, s));
+  aos_to_soa(s, h->aos.p, h->ssoa[h->scur].p, h->scap, (int)n);
+  build_tree(s, h->ssoa, h->scur, h->scap, (int)n, h->cfg.ncrit, h->sinfo, h->shinfo, h->ts, h->stree);
+  build_lists(s, h->stree, h->tree, h->cfg.theta, h->sinfo, h->shinfo, h->slists, nullptr);
+
+  const int K3 = 3 * h->cfg.p * (h->cfg.p + 1) / 2;
+  h->sL.reserve((size_t)h->stree.ncells * K3);
+  h->Mprep.reserve((size_t)h->tree.ncells * 3 * h->cfg.p * h->cfg.p);
+  const ExpArgs pe = particle_args(h);
+  mprep_pass(s, pe);
+  ExpArgs se          = pe;
+  se.cells            = h->stree.view();
+  se.ncells           = h->stree.ncells;
+  se.level_cells      = h->stree.level_cells.p;
+  se.level_start_host = h->stree.level_start_host;
+  se.maxLevel         = h->stree.maxLevel;
+  se.leaf_cells       = h->stree.leaf_cells.p;
+  se.nleaves          = h->stree.nleaves;
+  se.soa              = h->ssoa[h->scur].p;
+  se.cap              = h->scap;
+  se.L                = h->sL.p;
+  se.m2l_start        = h->slists.m2l_start.p;
+  se.m2l_src          = h->slists.m2l_src.p;
+  se.p2p_start        = h->slists.p2p_start.p;
+  se.p2p_src          = h->slists.p2p_src.p;
+  se.src_cells        = h->tree.view();
+  se.src_soa          = h->soa[h->cur].p;
+  se.src_cap          = h->cap;
+  m2l_sensor_pass(s, se);
+  downward_l2l(s, se);
+  l2p_sensor_pass(s, se, h->ssoa[h->scur].p);
+  soa_to_aos(s, h->ssoa[h->scur].p, h->scap, h->aos.p, (int)n);
+  VFMM_CUDA_TRY(cudaMemcpyAsync(sens, h->aos.p, n * sizeof(vfmm_body), cudaMemcpyDeviceToHost, s));
+  VFMM_CUDA_TRY(cudaStreamSynchronize(s));
 }
 
 void stage_update(vfmm_handle h, int stage, double dt)
@@ -404,6 +518,9 @@ int vfmm_create(const vfmm_config *cfg, vfmm_handle *out)
     VFMM_CUDA_TRY(cudaMalloc((void **)&h->info, sizeof(DevInfo)));
     VFMM_CUDA_TRY(cudaMallocHost((void **)&h->hinfo, sizeof(DevInfo)));
     std::memset(h->hinfo, 0, sizeof(DevInfo));
+    VFMM_CUDA_TRY(cudaMalloc((void **)&h->sinfo, sizeof(DevInfo)));
+    VFMM_CUDA_TRY(cudaMallocHost((void **)&h->shinfo, sizeof(DevInfo)));
+    std::memset(h->shinfo, 0, sizeof(DevInfo));
   } catch (const Error &e) {
     const int code = e.code;
     vfmm_destroy(h);
@@ -420,11 +537,13 @@ int vfmm_destroy(vfmm_handle h)
   cudaSetDevice(h->device);
   if (h->stream)
     cudaStreamSynchronize(h->stream);
-  for (auto *b : {&h->soa[0], &h->soa[1], &h->aos, &h->c_x, &h->c_y, &h->c_z, &h->c_R, &h->dtmp})
+  for (auto *b : {&h->soa[0], &h->soa[1], &h->aos, &h->dtmp, &h->ssoa[0], &h->ssoa[1]})
     b->release();
-  for (auto *b : {&h->c_nchild, &h->c_nbody, &h->c_child, &h->c_body, &h->c_level, &h->c_parent, &h->level_cells, &h->level_start, &h->leaf_cells,
-                  &h->p2p_start, &h->p2p_src, &h->m2l_start, &h->m2l_src})
-    b->release();
+  h->tree.release();
+  h->lists.release();
+  h->stree.release();
+  h->slists.release();
+  h->sL.release();
   h->M.release();
   h->L.release();
   h->Mprep.release();
@@ -444,15 +563,14 @@ int vfmm_destroy(vfmm_handle h)
     b->release();
   h->ts.bbox_part.release();
   h->ts.cub_tmp.release();
-  h->ls.front[0].release();
-  h->ls.front[1].release();
-  for (auto *b : {&h->ls.p2p_raw, &h->ls.m2l_raw, &h->ls.p2p_sorted, &h->ls.m2l_sorted})
-    b->release();
-  h->ls.cub_tmp.release();
   if (h->info)
     cudaFree(h->info);
   if (h->hinfo)
     cudaFreeHost(h->hinfo);
+  if (h->sinfo)
+    cudaFree(h->sinfo);
+  if (h->shinfo)
+    cudaFreeHost(h->shinfo);
   for (auto &e : h->ev)
     if (e)
       cudaEventDestroy(e);
@@ -519,9 +637,9 @@ int vfmm_advance(vfmm_handle h, vfmm_body *bodies, size_t n, double dt)
 int vfmm_get_sensor_data(vfmm_handle h, vfmm_body *sensors, size_t n)
 {
   return guarded(h, [&] {
-    (void)sensors;
-    (void)n;
-    throw Error(VFMM_ERR_UNSUPPORTED, "sensor evaluation is not implemented yet");
+    if (!sensors)
+      throw Error(VFMM_ERR_INVALID, "null sensors");
+    sensor_data(h, sensors, n);
   });
 }
 
@@ -543,21 +661,21 @@ int vfmm_get_tree(vfmm_handle h, vfmm_cell *cells, size_t cap, size_t *ncells)
     if (!h->has_tree)
       throw Error(VFMM_ERR_STATE, "no tree: call init first");
     if (ncells)
-      *ncells = (size_t)h->ncells;
-    if (!cells || cap < (size_t)h->ncells)
+      *ncells = (size_t)h->tree.ncells;
+    if (!cells || cap < (size_t)h->tree.ncells)
       return;
-    const int        nc = h->ncells;
+    const int        nc = h->tree.ncells;
     std::vector<int> ni(nc), nb(nc), ch(nc), bo(nc), lv(nc);
     std::vector<double> x(nc), y(nc), z(nc), R(nc);
-    VFMM_CUDA_TRY(cudaMemcpy(ni.data(), h->c_nchild.p, nc * sizeof(int), cudaMemcpyDeviceToHost));
-    VFMM_CUDA_TRY(cudaMemcpy(nb.data(), h->c_nbody.p, nc * sizeof(int), cudaMemcpyDeviceToHost));
-    VFMM_CUDA_TRY(cudaMemcpy(ch.data(), h->c_child.p, nc * sizeof(int), cudaMemcpyDeviceToHost));
-    VFMM_CUDA_TRY(cudaMemcpy(bo.data(), h->c_body.p, nc * sizeof(int), cudaMemcpyDeviceToHost));
-    VFMM_CUDA_TRY(cudaMemcpy(lv.data(), h->c_level.p, nc * sizeof(int), cudaMemcpyDeviceToHost));
-    VFMM_CUDA_TRY(cudaMemcpy(x.data(), h->c_x.p, nc * sizeof(double), cudaMemcpyDeviceToHost));
-    VFMM_CUDA_TRY(cudaMemcpy(y.data(), h->c_y.p, nc * sizeof(double), cudaMemcpyDeviceToHost));
-    VFMM_CUDA_TRY(cudaMemcpy(z.data(), h->c_z.p, nc * sizeof(double), cudaMemcpyDeviceToHost));
-    VFMM_CUDA_TRY(cudaMemcpy(R.data(), h->c_R.p, nc * sizeof(double), cudaMemcpyDeviceToHost));
+    VFMM_CUDA_TRY(cudaMemcpy(ni.data(), h->tree.nchild.p, nc * sizeof(int), cudaMemcpyDeviceToHost));
+    VFMM_CUDA_TRY(cudaMemcpy(nb.data(), h->tree.nbody.p, nc * sizeof(int), cudaMemcpyDeviceToHost));
+    VFMM_CUDA_TRY(cudaMemcpy(ch.data(), h->tree.child.p, nc * sizeof(int), cudaMemcpyDeviceToHost));
+    VFMM_CUDA_TRY(cudaMemcpy(bo.data(), h->tree.body.p, nc * sizeof(int), cudaMemcpyDeviceToHost));
+    VFMM_CUDA_TRY(cudaMemcpy(lv.data(), h->tree.level.p, nc * sizeof(int), cudaMemcpyDeviceToHost));
+    VFMM_CUDA_TRY(cudaMemcpy(x.data(), h->tree.x.p, nc * sizeof(double), cudaMemcpyDeviceToHost));
+    VFMM_CUDA_TRY(cudaMemcpy(y.data(), h->tree.y.p, nc * sizeof(double), cudaMemcpyDeviceToHost));
+    VFMM_CUDA_TRY(cudaMemcpy(z.data(), h->tree.z.p, nc * sizeof(double), cudaMemcpyDeviceToHost));
+    VFMM_CUDA_TRY(cudaMemcpy(R.data(), h->tree.R.p, nc * sizeof(double), cudaMemcpyDeviceToHost));
     for (int i = 0; i < nc; i++) {
       cells[i].NCHILD      = (uint64_t)ni[i];
       cells[i].NBODY       = (uint64_t)nb[i];
@@ -578,9 +696,9 @@ int vfmm_get_lists(vfmm_handle h, uint64_t *p2p, size_t cap_p2p, size_t *n_p2p, 
     if (!h->has_tree)
       throw Error(VFMM_ERR_STATE, "no lists: call init first");
     if (n_p2p)
-      *n_p2p = (size_t)h->n_p2p;
+      *n_p2p = (size_t)h->lists.n_p2p;
     if (n_m2l)
-      *n_m2l = (size_t)h->n_m2l;
+      *n_m2l = (size_t)h->lists.n_m2l;
     auto fetch = [&](const unsigned long long *src, int cnt, uint64_t *dst, size_t cap) {
       if (!dst || cap < (size_t)cnt || cnt == 0)
         return;
@@ -592,8 +710,8 @@ int vfmm_get_lists(vfmm_handle h, uint64_t *p2p, size_t cap_p2p, size_t *n_p2p, 
       }
     };
     VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
-    fetch(h->ls.p2p_sorted.p, h->n_p2p, p2p, cap_p2p);
-    fetch(h->ls.m2l_sorted.p, h->n_m2l, m2l, cap_m2l);
+    fetch(h->lists.ls.p2p_sorted.p, h->lists.n_p2p, p2p, cap_p2p);
+    fetch(h->lists.ls.m2l_sorted.p, h->lists.n_m2l, m2l, cap_m2l);
   });
 }
 
@@ -602,9 +720,9 @@ int vfmm_get_expansions(vfmm_handle h, double *M, double *L, size_t cap_cells)
   return guarded(h, [&] {
     if (!h->has_eval)
       throw Error(VFMM_ERR_STATE, "no expansions: call calculate first");
-    if (cap_cells < (size_t)h->ncells)
+    if (cap_cells < (size_t)h->tree.ncells)
       throw Error(VFMM_ERR_INVALID, "capacity below the cell count");
-    const size_t cnt = (size_t)h->ncells * 3 * h->cfg.p * (h->cfg.p + 1) / 2;
+    const size_t cnt = (size_t)h->tree.ncells * 3 * h->cfg.p * (h->cfg.p + 1) / 2;
     VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
     if (M)
       VFMM_CUDA_TRY(cudaMemcpy(M, h->M.p, cnt * sizeof(double2), cudaMemcpyDeviceToHost));
@@ -711,8 +829,8 @@ int vfmm_tree_stats(vfmm_handle h, uint64_t *st, int n)
     if (!h->has_tree)
       throw Error(VFMM_ERR_STATE, "no tree");
     read_info(h);
-    const uint64_t v[6] = {(uint64_t)h->ncells, (uint64_t)h->nleaves, (uint64_t)h->n_p2p, (uint64_t)h->n_m2l, h->hinfo->p2p_interactions,
-                           (uint64_t)h->maxLevel};
+    const uint64_t v[6] = {(uint64_t)h->tree.ncells, (uint64_t)h->tree.nleaves, (uint64_t)h->lists.n_p2p, (uint64_t)h->lists.n_m2l, h->hinfo->p2p_interactions,
+                           (uint64_t)h->tree.maxLevel};
     for (int i = 0; i < n && i < 6; i++)
       st[i] = v[i];
   });

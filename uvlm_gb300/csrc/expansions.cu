@@ -31,9 +31,12 @@ __device__ __forceinline__ void jk_of(int jks, int &j, int &k)
 }
 
 struct DevExp {
-  CellsView     cv;
+  CellsView     cv;  // target cells (L, L2P bodies)
+  CellsView     scv; // source cells (M2L sources, P2P source leaves); cv except for sensors
   const double *soa;
   size_t        cap;
+  const double *ssoa; // source bodies of P2P; soa except for sensors
+  size_t        scap;
   double2      *M, *L, *Mprep;
   const int    *leaf_cells;
   int           nleaves;
@@ -229,7 +232,7 @@ __global__ void __launch_bounds__(128) k_m2l(DevExp a, int ncells)
       for (int e = lane; e < 3 * PP; e += 32)
         Ms[e] = ldz(a.Mprep + (size_t)s * 3 * PP + e);
       if (lane < P) {
-        const double dx = tx - a.cv.x[s], dy = ty - a.cv.y[s], dz = tz - a.cv.z[s];
+        const double dx = tx - a.scv.x[s], dy = ty - a.scv.y[s], dz = tz - a.scv.z[s];
         const double r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.0 / r2, S00 = sqrt(ir2);
         zd           col[P];
         singular_column<double, P>(lane, dx, dy, dz, ir2, S00, col);
@@ -418,7 +421,14 @@ struct L2PSizes {
   static constexpr size_t bytes = (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zd) + 2 * 128 * 12 * sizeof(double);
 };
 
-template <int P>
+// SENS = false: the bodies' own evaluation; velocity and J are overwritten
+// and dadt/drdt completed by the stretching (and rVPM) functors.
+// SENS = true: sensor points (fmmCalculator.hpp:469-491): the near field is
+// the velocity-only P2P of multipoleKernels.hpp:304-338 against the particle
+// leaves, the far field is L2P (multipoleKernels.hpp:631-742), which adds to
+// J; velocity and dadt start from zero (resetSensors, fmmCalculator.hpp:380-
+// 389), J and drdt keep their input values.
+template <int P, bool SENS>
 __global__ void __launch_bounds__(128) k_l2p_p2p(DevExp a, double *out)
 {
   using S = L2PSizes<P>;
@@ -513,13 +523,15 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(DevExp a, double *out)
         const double xi = a.soa[F_X * a.cap + i], yi = a.soa[(F_X + 1) * a.cap + i], zi = a.soa[(F_X + 2) * a.cap + i];
         const int    q0 = a.p2p_start[c], q1 = a.p2p_start[c + 1];
         for (int q = q0 + g; q < q1; q += G) {
-          const int sc = a.p2p_src[q], sb = a.cv.body[sc], sn = a.cv.nbody[sc];
+          const int sc = a.p2p_src[q], sb = a.scv.body[sc], sn = a.scv.nbody[sc];
+          const double *__restrict__ src = a.ssoa;
+          const size_t scap = a.scap;
           for (int jb = sb; jb < sb + sn; jb++) {
-            const double dx = xi - a.soa[F_X * a.cap + jb], dy = yi - a.soa[(F_X + 1) * a.cap + jb], dz = zi - a.soa[(F_X + 2) * a.cap + jb];
+            const double dx = xi - src[F_X * scap + jb], dy = yi - src[(F_X + 1) * scap + jb], dz = zi - src[(F_X + 2) * scap + jb];
             const double R2 = dx * dx + dy * dy + dz * dz;
             if (R2 != 0) {
-              const double ax = a.soa[F_A * a.cap + jb], ay = a.soa[(F_A + 1) * a.cap + jb], az = a.soa[(F_A + 2) * a.cap + jb];
-              const double sg = a.soa[F_R * a.cap + jb];
+              const double ax = src[F_A * scap + jb], ay = src[(F_A + 1) * scap + jb], az = src[(F_A + 2) * scap + jb];
+              const double sg = src[F_R * scap + jb];
               const double S2 = sg * sg, RS = R2 / S2 / 2.0, sqrtRS = sqrt(RS);
               const double erfS = erf(sqrtRS), expm = exp(-RS), invSqrtR2 = 1.0 / sqrt(R2);
               const double t2 = 2.0 * inv_sqrtpi * sqrtRS * expm, c4 = 0.25 * inv_pi / R2 * invSqrtR2;
@@ -528,6 +540,8 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(DevExp a, double *out)
               s[0] += cr0 * gg;
               s[1] += cr1 * gg;
               s[2] += cr2 * gg;
+              if (SENS)
+                continue;
               double aux = t2 / S2 - 3.0 * gg / R2;
               s[3] += aux * cr0 * dx;
               s[4] += aux * cr0 * dy;
@@ -561,30 +575,39 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(DevExp a, double *out)
             nearv += red[(gg * TG + t) * 12 + k];
           r[k] = far[t * 12 + k] - nearv;
         }
-        const double al[3] = {a.soa[F_A * a.cap + b], a.soa[(F_A + 1) * a.cap + b], a.soa[(F_A + 2) * a.cap + b]};
-        double       dadt[3];
-        for (int aa = 0; aa < 3; aa++) {
-          double v = 0;
-          for (int cc = 0; cc < 3; cc++)
-            v += (a.stretching == VFMM_TRANSPOSED ? r[3 + 3 * cc + aa] : r[3 + 3 * aa + cc]) * al[cc];
-          dadt[aa] = v;
+        if (SENS) {
+          for (int d = 0; d < 3; d++) {
+            out[(F_U + d) * a.cap + b]    = r[d];
+            out[(F_DADT + d) * a.cap + b] = 0.0;
+          }
+          for (int k = 0; k < 9; k++)
+            out[(F_J + k) * a.cap + b] = a.soa[(F_J + k) * a.cap + b] + far[t * 12 + 3 + k];
+        } else {
+          const double al[3] = {a.soa[F_A * a.cap + b], a.soa[(F_A + 1) * a.cap + b], a.soa[(F_A + 2) * a.cap + b]};
+          double       dadt[3];
+          for (int aa = 0; aa < 3; aa++) {
+            double v = 0;
+            for (int cc = 0; cc < 3; cc++)
+              v += (a.stretching == VFMM_TRANSPOSED ? r[3 + 3 * cc + aa] : r[3 + 3 * aa + cc]) * al[cc];
+            dadt[aa] = v;
+          }
+          double drdt = 0;
+          if (a.formulation == VFMM_RVPM) {
+            const double na = sqrt(al[0] * al[0] + al[1] * al[1] + al[2] * al[2]);
+            const double ah[3] = {al[0] / na, al[1] / na, al[2] / na};
+            const double dot   = dadt[0] * ah[0] + dadt[1] * ah[1] + dadt[2] * ah[2];
+            for (int aa = 0; aa < 3; aa++)
+              dadt[aa] -= 3. / 5. * dot * ah[aa];
+            drdt -= 1.0 / 5.0 * a.soa[F_R * a.cap + b] / na * dot;
+          }
+          for (int d = 0; d < 3; d++) {
+            out[(F_U + d) * a.cap + b]    = r[d];
+            out[(F_DADT + d) * a.cap + b] = dadt[d];
+          }
+          for (int k = 0; k < 9; k++)
+            out[(F_J + k) * a.cap + b] = r[3 + k];
+          out[F_DRDT * a.cap + b] = drdt;
         }
-        double drdt = 0;
-        if (a.formulation == VFMM_RVPM) {
-          const double na = sqrt(al[0] * al[0] + al[1] * al[1] + al[2] * al[2]);
-          const double ah[3] = {al[0] / na, al[1] / na, al[2] / na};
-          const double dot   = dadt[0] * ah[0] + dadt[1] * ah[1] + dadt[2] * ah[2];
-          for (int aa = 0; aa < 3; aa++)
-            dadt[aa] -= 3. / 5. * dot * ah[aa];
-          drdt -= 1.0 / 5.0 * a.soa[F_R * a.cap + b] / na * dot;
-        }
-        for (int d = 0; d < 3; d++) {
-          out[(F_U + d) * a.cap + b]    = r[d];
-          out[(F_DADT + d) * a.cap + b] = dadt[d];
-        }
-        for (int k = 0; k < 9; k++)
-          out[(F_J + k) * a.cap + b] = r[3 + k];
-        out[F_DRDT * a.cap + b] = drdt;
       }
       __syncthreads();
     }
@@ -596,8 +619,11 @@ static DevExp dev_args(const ExpArgs &e)
 {
   DevExp d;
   d.cv          = e.cells;
+  d.scv         = e.src_soa ? e.src_cells : e.cells;
   d.soa         = e.soa;
   d.cap         = e.cap;
+  d.ssoa        = e.src_soa ? e.src_soa : e.soa;
+  d.scap        = e.src_soa ? e.src_cap : e.cap;
   d.M           = e.M;
   d.L           = e.L;
   d.Mprep       = e.Mprep;
@@ -661,12 +687,22 @@ static void m2m_P(cudaStream_t s, const ExpArgs &e)
 }
 
 template <int P>
-static void m2l_P(cudaStream_t s, const ExpArgs &e)
+static void mprep_P(cudaStream_t s, const ExpArgs &e)
+{
+  k_mprep<P><<<grid_for((long)e.ncells * P * P * 3, 256), 256, 0, s>>>(e.M, e.Mprep, e.ncells);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+// M2L into every target cell of e.cells; with prep, the sign-folded source
+// multipoles are made first from e.M (same tree as the targets).
+template <int P>
+static void m2l_P(cudaStream_t s, const ExpArgs &e, bool prep)
 {
   DevExp    d  = dev_args(e);
   const int PP = P * P;
-  k_mprep<P><<<grid_for((long)e.ncells * PP * 3, 256), 256, 0, s>>>(e.M, e.Mprep, e.ncells);
-  count_launch();
+  if (prep)
+    mprep_P<P>(s, e);
   const size_t bytes = (size_t)4 * 4 * PP * sizeof(zd);
   static bool  once  = false;
   if (!once) {
@@ -699,22 +735,27 @@ static void l2l_P(cudaStream_t s, const ExpArgs &e)
   VFMM_LAUNCH_CHECK();
 }
 
-template <int P>
+template <int P, bool SENS>
 static void l2p_P(cudaStream_t s, const ExpArgs &e, double *out)
 {
   DevExp       d     = dev_args(e);
   const size_t bytes = L2PSizes<P>::bytes;
   static bool  once  = false;
   if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_l2p_p2p<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_l2p_p2p<P, SENS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     once = true;
   }
   if (e.nleaves > 0) {
-    k_l2p_p2p<P><<<std::min(e.nleaves, 152 * 16), 128, bytes, s>>>(d, out);
+    k_l2p_p2p<P, SENS><<<std::min(e.nleaves, 152 * 16), 128, bytes, s>>>(d, out);
     count_launch();
   }
   VFMM_LAUNCH_CHECK();
 }
+
+template <int P>
+static void l2p_bodies_P(cudaStream_t s, const ExpArgs &e, double *out) { l2p_P<P, false>(s, e, out); }
+template <int P>
+static void l2p_sensors_P(cudaStream_t s, const ExpArgs &e, double *out) { l2p_P<P, true>(s, e, out); }
 
 #define VFMM_DISPATCH(fn, ...)                                                                                                   \
   switch (e.P) {                                                                                                                \
@@ -738,9 +779,12 @@ static void l2p_P(cudaStream_t s, const ExpArgs &e, double *out)
 
 void upward_pass(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(upward_P, s, e) }
 void m2m_pass(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(m2m_P, s, e) }
-void m2l_pass(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(m2l_P, s, e) }
+void m2l_pass(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(m2l_P, s, e, true) }
+void mprep_pass(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(mprep_P, s, e) }
+void m2l_sensor_pass(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(m2l_P, s, e, false) }
 void downward_l2l(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(l2l_P, s, e) }
-void l2p_p2p_pass(cudaStream_t s, const ExpArgs &e, double *out) { VFMM_DISPATCH(l2p_P, s, e, out) }
+void l2p_p2p_pass(cudaStream_t s, const ExpArgs &e, double *out) { VFMM_DISPATCH(l2p_bodies_P, s, e, out) }
+void l2p_sensor_pass(cudaStream_t s, const ExpArgs &e, double *out) { VFMM_DISPATCH(l2p_sensors_P, s, e, out) }
 
 // Lane table of the lockstep M2L (k_m2l32v2): warp n (input degree n) splits
 // the output rows j <= P-1-n into tiles of kb columns; with T tiles, R =

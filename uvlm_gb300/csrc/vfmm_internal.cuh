@@ -181,12 +181,25 @@ struct ExpArgs {
   const int4   *m2l_items; // per-lane schedule, see m2l_schedule
   int           m2l_nitems_per_lane;
   int           stretching, formulation;
+  // Sources when they are another tree than the targets (sensors): source
+  // cells for M2L and P2P, source bodies for P2P.  src_soa == nullptr means
+  // the targets' own cells and bodies.
+  CellsView     src_cells;
+  const double *src_soa;
+  size_t        src_cap;
 };
 void upward_pass(cudaStream_t s, const ExpArgs &a); // P2M + M2M (FP64)
 void m2m_pass(cudaStream_t s, const ExpArgs &a);    // M2M only (FP64)
 void m2l_pass(cudaStream_t s, const ExpArgs &a);
 void downward_l2l(cudaStream_t s, const ExpArgs &a);
 void l2p_p2p_pass(cudaStream_t s, const ExpArgs &a, double *soa_out);
+// Sensor evaluation (FP64): mprep_pass makes the sign-folded multipoles of
+// the particle tree (e.M -> e.Mprep over e.ncells); m2l_sensor_pass runs M2L
+// into the sensor cells from e.Mprep of e.src_cells; l2p_sensor_pass is the
+// sensors' L2P plus velocity-only P2P against e.src_soa.
+void mprep_pass(cudaStream_t s, const ExpArgs &a);
+void m2l_sensor_pass(cudaStream_t s, const ExpArgs &a);
+void l2p_sensor_pass(cudaStream_t s, const ExpArgs &a, double *soa_out);
 std::vector<int4> m2l_schedule(int P, int lanes, int kb, int maxItems, int *itemsPerLane);
 
 // ---- mixed.cu (FP32 P2M / M2L / L2P+P2P around the FP64 M2M / L2L)
