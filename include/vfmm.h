@@ -48,8 +48,8 @@ enum { VFMM_TRANSPOSED = 0, VFMM_CLASSIC = 1 };
 /* VPM formulation: Vortex::cVPM / rVPM (fmmCalculator.hpp:19-20). */
 enum { VFMM_CVPM = 0, VFMM_RVPM = 1 };
 /* Arithmetic of the evaluation: FP64 throughout (the drop-in), or mixed
- * (FP32 P2P with compensated sums, FP32 P2M/M2L/L2P with per-level scaling,
- * FP64 tree, and FP64 M2M/L2L when p >= 10). */
+ * (FP32 P2P with compensated sums, FP32 P2M/M2M/M2L/L2L/L2P with per-cell
+ * scaling, FP64 tree and FP64 expansion arrays between the kernels). */
 enum { VFMM_FP64 = 0, VFMM_MIXED = 1 };
 
 typedef struct {

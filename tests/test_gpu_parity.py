@@ -165,7 +165,7 @@ def rel_l2(a, b):
 @pytest.mark.parametrize("kind,n,P,ncrit", [("cloud", 40000, 10, 64), ("cloud", 20000, 14, 64), ("cloud", 20000, 6, 64),
                                             ("ring", 96, 8, 32), ("cloud", 15000, 16, 64), ("ring", 48, 15, 32), ("cloud", 3000, 3, 16)])
 def test_mixed_matches_fp64_fmm(vfmm_lib, kind, n, P, ncrit):
-    """The mixed path (FP32 P2M/M2L/L2P/P2P, FP64 tree and M2M/L2L) against the
+    """The mixed path (FP32 expansion kernels and P2P, FP64 tree) against the
     FP64 path on the same tree: relative L2 error of velocity and of J below
     1e-6 (the precision bar of the mixed mode)."""
     from uvlm_gb300 import FMMCalculator, workloads

@@ -371,11 +371,11 @@ void calculate(vfmm_handle h)
     m.m2l_batch = h->m2l_batch;
     m.R0      = h->tree.R0;
     p2m_mixed(s, e, m);
-    m2m_pass(s, e);
+    m2m_mixed(s, e, m);
     VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
     m2l_mixed(s, e, m);
     VFMM_CUDA_TRY(cudaEventRecord(h->ph[3], s));
-    downward_l2l(s, e);
+    l2l_mixed(s, e, m);
     VFMM_CUDA_TRY(cudaEventRecord(h->ph[4], s));
     l2p_p2p_mixed(s, e, m, h->soa[h->cur].p);
     VFMM_CUDA_TRY(cudaEventRecord(h->ph[5], s));

@@ -108,38 +108,6 @@ __global__ void __launch_bounds__(64) k_p2m(DevExp a)
 // multipoles (contiguous, the children form one block of cells) and their
 // harmonics are staged once; each thread then sums its outputs over all
 // children without further synchronisation.
-__device__ __forceinline__ zd neg_if(zd v, bool neg) { return neg ? zd{-v.r, -v.i} : v; }
-
-// One output (j, k, d) of M2M for NC children at once (children t0..t0+NC-1
-// that exist): the index arithmetic is shared and the NC accumulators are
-// independent, which keeps the FP64 pipe fed.  Signs ipow2n(m) * oddOrEven(n)
-// and oddOrEven(k+n+m) negate an operand instead of costing a multiply.
-template <int P, int NC>
-__device__ __forceinline__ void m2m_term_sum(int j, int k, int d, const zd *Ms, const zd *Ys, int t0, int nch, zd *acc)
-{
-  constexpr int K = nterms(P);
-  for (int n = 0; n <= j; n++) {
-    for (int m = max(-n, -j + k + n); m <= min(k - 1, n); m++) {
-      const int  yi = tri(n, m > 0 ? m : -m), mi = tri(j - n, k - m) * 3 + d;
-      const bool cj = m > 0, neg = ((m < 0 ? (m & 1) : 0) ^ (n & 1)) != 0;
-#pragma unroll
-      for (int c = 0; c < NC; c++)
-        if (t0 + c < nch) {
-          const zd y = Ys[(t0 + c) * K + yi];
-          cfma(acc[c], neg_if(Ms[(t0 + c) * 3 * K + mi], neg), cj ? conj(y) : y);
-        }
-    }
-    for (int m = k; m <= min(n, j + k - n); m++) {
-      const int  yi = tri(n, m), mi = tri(j - n, m - k) * 3 + d;
-      const bool neg = ((k + n + m) & 1) != 0;
-#pragma unroll
-      for (int c = 0; c < NC; c++)
-        if (t0 + c < nch)
-          cfma(acc[c], neg_if(conj(Ms[(t0 + c) * 3 * K + mi]), neg), conj(Ys[(t0 + c) * K + yi]));
-    }
-  }
-}
-
 template <int P>
 __global__ void __launch_bounds__(128) k_m2m(DevExp a, const int *cells, int count)
 {
@@ -308,37 +276,6 @@ __global__ void __launch_bounds__(128) k_m2l(DevExp a, int ncells)
 // Children pull their parent's local expansion (multipoleKernels.hpp:591-628),
 // dX = X_child - X_parent.  Block of 128 threads per parent: the parent's L
 // and all children's harmonics are staged once; threads own (child, output).
-// One output (j, k, d) of L2L for NC children at once (shared parent operand
-// and index arithmetic, independent accumulators).
-template <int P, int NC>
-__device__ __forceinline__ void l2l_term_sum(int j, int k, int d, const zd *Lp, const zd *Ys, int t0, int nch, zd *acc)
-{
-  constexpr int K = nterms(P);
-  for (int n = j; n < P; n++) {
-    const bool negk = (k & 1) != 0;
-    for (int m = j + k - n; m < 0; m++) {
-      const zd  l  = neg_if(conj(Lp[tri(n, -m) * 3 + d]), negk);
-      const int yi = tri(n - j, k - m);
-#pragma unroll
-      for (int c = 0; c < NC; c++)
-        if (t0 + c < nch)
-          cfma(acc[c], l, conj(Ys[(t0 + c) * K + yi]));
-    }
-    const int mlo = max(0, k - (n - j)), mhi = min(n, k + (n - j)); // n - j >= |m - k|
-    for (int m = mlo; m <= mhi; m++) {
-      const bool neg = m < k && ((k - m) & 1);
-      const zd   l   = neg_if(Lp[tri(n, m) * 3 + d], neg);
-      const int  yi  = tri(n - j, m >= k ? m - k : k - m);
-#pragma unroll
-      for (int c = 0; c < NC; c++)
-        if (t0 + c < nch) {
-          const zd y = Ys[(t0 + c) * K + yi];
-          cfma(acc[c], l, m >= k ? y : conj(y));
-        }
-    }
-  }
-}
-
 template <int P>
 __global__ void __launch_bounds__(128) k_l2l(DevExp a, const int *cells, int count)
 {

@@ -90,4 +90,70 @@ __device__ __forceinline__ void singular_column(int m, T x, T y, T z, T inv_r2, 
   }
 }
 
+template <class T>
+__device__ __forceinline__ cx<T> neg_if(cx<T> v, bool neg) { return neg ? cx<T>{-v.r, -v.i} : v; }
+
+// One output (j, k, d) of M2M for NC children at once (children t0..t0+NC-1
+// that exist): the index arithmetic is shared and the NC accumulators are
+// independent, which keeps the arithmetic pipe fed.  M2M of
+// multipoleKernels.hpp:479-516 with dX = X_parent - X_child.  Signs ipow2n(m) * oddOrEven(n)
+// and oddOrEven(k+n+m) negate an operand instead of costing a multiply.
+template <int P, int NC, class T>
+__device__ __forceinline__ void m2m_term_sum(int j, int k, int d, const cx<T> *Ms, const cx<T> *Ys, int t0, int nch, cx<T> *acc)
+{
+  constexpr int K = nterms(P);
+  for (int n = 0; n <= j; n++) {
+    for (int m = max(-n, -j + k + n); m <= min(k - 1, n); m++) {
+      const int  yi = tri(n, m > 0 ? m : -m), mi = tri(j - n, k - m) * 3 + d;
+      const bool cj = m > 0, neg = ((m < 0 ? (m & 1) : 0) ^ (n & 1)) != 0;
+#pragma unroll
+      for (int c = 0; c < NC; c++)
+        if (t0 + c < nch) {
+          const cx<T> y = Ys[(t0 + c) * K + yi];
+          cfma(acc[c], neg_if(Ms[(t0 + c) * 3 * K + mi], neg), cj ? conj(y) : y);
+        }
+    }
+    for (int m = k; m <= min(n, j + k - n); m++) {
+      const int  yi = tri(n, m), mi = tri(j - n, m - k) * 3 + d;
+      const bool neg = ((k + n + m) & 1) != 0;
+#pragma unroll
+      for (int c = 0; c < NC; c++)
+        if (t0 + c < nch)
+          cfma(acc[c], neg_if(conj(Ms[(t0 + c) * 3 * K + mi]), neg), conj(Ys[(t0 + c) * K + yi]));
+    }
+  }
+}
+
+// One output (j, k, d) of L2L for NC children at once (shared parent operand
+// and index arithmetic, independent accumulators).  L2L of
+// multipoleKernels.hpp:591-628 with dX = X_child - X_parent.
+template <int P, int NC, class T>
+__device__ __forceinline__ void l2l_term_sum(int j, int k, int d, const cx<T> *Lp, const cx<T> *Ys, int t0, int nch, cx<T> *acc)
+{
+  constexpr int K = nterms(P);
+  for (int n = j; n < P; n++) {
+    const bool negk = (k & 1) != 0;
+    for (int m = j + k - n; m < 0; m++) {
+      const cx<T> l  = neg_if(conj(Lp[tri(n, -m) * 3 + d]), negk);
+      const int yi = tri(n - j, k - m);
+#pragma unroll
+      for (int c = 0; c < NC; c++)
+        if (t0 + c < nch)
+          cfma(acc[c], l, conj(Ys[(t0 + c) * K + yi]));
+    }
+    const int mlo = max(0, k - (n - j)), mhi = min(n, k + (n - j)); // n - j >= |m - k|
+    for (int m = mlo; m <= mhi; m++) {
+      const bool neg = m < k && ((k - m) & 1);
+      const cx<T> l   = neg_if(Lp[tri(n, m) * 3 + d], neg);
+      const int  yi  = tri(n - j, m >= k ? m - k : k - m);
+#pragma unroll
+      for (int c = 0; c < NC; c++)
+        if (t0 + c < nch) {
+          const cx<T> y = Ys[(t0 + c) * K + yi];
+          cfma(acc[c], l, m >= k ? y : conj(y));
+        }
+    }
+  }
+}
+
 } // namespace vfmm

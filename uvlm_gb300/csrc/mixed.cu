@@ -1,5 +1,6 @@
-// Mixed-precision expansion kernels: FP32 P2M, M2L, L2P and P2P with FP64
-// tree, M2M/L2L (expansions.cu) and FP64 outputs.
+// Mixed-precision expansion kernels: FP32 P2M, M2M, M2L, L2L, L2P and P2P;
+// the tree (tree.cu), the expansion arrays between kernels and the outputs
+// stay FP64.
 //
 // Scaling.  FP32 cannot hold the raw expansions at high order (rho^n/(n+m)!
 // and (n-m)!/rho^(n+1) leave its exponent range), so inside these kernels a
@@ -11,6 +12,7 @@
 //   P2M:  Mt_n^m(c) = sum_b alpha_b conj(Y_n^m((x_b - X_c)/R_c)).
 //   M2L:  Lt_j^k(t) += (R_t/R_s)^j / R_s * (-1)^j sum M't_n^m S'_{j+n}^{m-k}(d/R_s),
 //         d = X_t - X_s; (R_t/R_s) is a power of two.
+//   M2M, L2L: scaled by the parent's half-width R_p instead (see k_m2m32).
 //   L2P:  u = (1/R) sum (D Lt)(y), J = (1/R^2) sum (D D Lt)(y), y = (x - X_c)/R.
 // P2P uses leaf-relative FP32 coordinates, a series form of the regularised
 // kernel for close pairs (no cancellation), and per-source-leaf FP32 partial
@@ -165,6 +167,99 @@ __global__ void k_mprep32(DevMixed a, int ncells)
     } else
       im = -im;
     a.Mp[e] = make_float2((float)re, (float)im);
+  }
+}
+
+// M2M and L2L in FP32 (multipoleKernels.hpp:479-516, :591-628) with every
+// operand scaled by the parent's half-width R_p: the child multipoles enter
+// as M_c / R_p^n and the parent's local expansion as L_p R_p^n, the offset
+// harmonics are Y(dX / R_p), and the outputs are rescaled by R_p^j (M2M) or
+// R_p^-j (L2L) in FP64 when they are added to the FP64 expansions.  Block of
+// 128 threads per parent, as the FP64 kernels.
+template <int P>
+__global__ void __launch_bounds__(128) k_m2m32(DevMixed a, const int *cells, int count)
+{
+  constexpr int K = nterms(P);
+  extern __shared__ float4 smem32[];
+  zf *Ms = reinterpret_cast<zf *>(smem32); // [8][3K]
+  zf *Ys = Ms + 8 * 3 * K;                  // [8][K]
+  for (int pi = blockIdx.x; pi < count; pi += gridDim.x) {
+    const int c = cells[pi], nch = a.cv.nchild[c], ch0 = a.cv.child[c], lev = a.cv.level[c];
+    if (nch == 0)
+      continue;
+    __syncthreads();
+    for (int e = threadIdx.x; e < nch * 3 * K; e += blockDim.x) {
+      int n, m;
+      jk_of_m((e % (3 * K)) / 3, n, m);
+      const double2 v = a.M[(size_t)ch0 * 3 * K + e];
+      const double  s = cell_iRpow(a, lev, n);
+      Ms[e]           = {(float)(v.x * s), (float)(v.y * s)};
+    }
+    if (threadIdx.x < nch) {
+      const int    ch = ch0 + threadIdx.x;
+      const double iR = ldexp(a.iR0, lev);
+      regular_harmonics<float, P>((float)((a.cv.x[c] - a.cv.x[ch]) * iR), (float)((a.cv.y[c] - a.cv.y[ch]) * iR),
+                                  (float)((a.cv.z[c] - a.cv.z[ch]) * iR), Ys + threadIdx.x * K);
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < 3 * K; o += blockDim.x) {
+      const int jks = o / 3, d = o % 3;
+      int       j, k;
+      jk_of_m(jks, j, k);
+      zf acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      for (int t0 = 0; t0 < nch; t0 += 4)
+        m2m_term_sum<P, 4>(j, k, d, Ms, Ys, t0, nch, acc);
+      const zf     sum = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+      const double s   = cell_Rpow(a, lev, j);
+      double2     *q   = a.M + (size_t)c * 3 * K + o;
+      const double2 old = *q;
+      *q                = make_double2(old.x + (double)sum.r * s, old.y + (double)sum.i * s);
+    }
+  }
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) k_l2l32(DevMixed a, const int *cells, int count)
+{
+  constexpr int K = nterms(P);
+  extern __shared__ float4 smem32[];
+  zf *Ls = reinterpret_cast<zf *>(smem32); // [3K]
+  zf *Ys = Ls + 3 * K;                      // [8][K]
+  for (int pi = blockIdx.x; pi < count; pi += gridDim.x) {
+    const int p = cells[pi], nch = a.cv.nchild[p], ch0 = a.cv.child[p], lev = a.cv.level[p];
+    if (nch == 0)
+      continue;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * K; e += blockDim.x) {
+      int n, m;
+      jk_of_m(e / 3, n, m);
+      const double2 v = a.L[(size_t)p * 3 * K + e];
+      const double  s = cell_Rpow(a, lev, n);
+      Ls[e]           = {(float)(v.x * s), (float)(v.y * s)};
+    }
+    if (threadIdx.x < nch) {
+      const int    ch = ch0 + threadIdx.x;
+      const double iR = ldexp(a.iR0, lev);
+      regular_harmonics<float, P>((float)((a.cv.x[ch] - a.cv.x[p]) * iR), (float)((a.cv.y[ch] - a.cv.y[p]) * iR),
+                                  (float)((a.cv.z[ch] - a.cv.z[p]) * iR), Ys + threadIdx.x * K);
+    }
+    __syncthreads();
+    const int ngroups = (nch + 3) / 4;
+    for (int o = threadIdx.x; o < ngroups * 3 * K; o += blockDim.x) {
+      const int t0 = (o / (3 * K)) * 4, r = o % (3 * K), jks = r / 3, d = r % 3;
+      int       j, k;
+      jk_of_m(jks, j, k);
+      zf acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      l2l_term_sum<P, 4>(j, k, d, Ls, Ys, t0, nch, acc);
+      const double s = cell_iRpow(a, lev, j);
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        if (t0 + c < nch) {
+          double2      *q   = a.L + (size_t)(ch0 + t0 + c) * 3 * K + r;
+          const double2 old = *q;
+          *q                = make_double2(old.x + (double)acc[c].r * s, old.y + (double)acc[c].i * s);
+        }
+    }
   }
 }
 
@@ -727,6 +822,49 @@ static void l2p32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double
   VFMM_LAUNCH_CHECK();
 }
 
+// M2M into parents at levels maxLevel-1 .. 1 (level 0 skipped as in the
+// reference's upward pass, fmmCalculator.hpp:427); L2L from parents at levels
+// 0 .. maxLevel-1.
+template <int P>
+static void m2m32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+{
+  const DevMixed d     = dev_mixed(e, m);
+  const size_t   bytes = (size_t)(8 * 3 + 8) * nterms(P) * sizeof(zf);
+  static bool    once  = false;
+  if (!once) {
+    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2m32<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    once = true;
+  }
+  for (int l = e.maxLevel - 1; l >= 1; l--) {
+    const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
+    if (n1 > n0) {
+      k_m2m32<P><<<std::min(n1 - n0, 152 * 16), 128, bytes, s>>>(d, e.level_cells + n0, n1 - n0);
+      count_launch();
+    }
+  }
+  VFMM_LAUNCH_CHECK();
+}
+
+template <int P>
+static void l2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+{
+  const DevMixed d     = dev_mixed(e, m);
+  const size_t   bytes = (size_t)(3 + 8) * nterms(P) * sizeof(zf);
+  static bool    once  = false;
+  if (!once) {
+    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_l2l32<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    once = true;
+  }
+  for (int l = 0; l < e.maxLevel; l++) {
+    const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
+    if (n1 > n0) {
+      k_l2l32<P><<<std::min(n1 - n0, 152 * 16), 128, bytes, s>>>(d, e.level_cells + n0, n1 - n0);
+      count_launch();
+    }
+  }
+  VFMM_LAUNCH_CHECK();
+}
+
 #define VFMM_DISPATCH_M(fn, ...)                                                                                                 \
   switch (e.P) {                                                                                                                \
   case 2: fn<2>(__VA_ARGS__); break;                                                                                            \
@@ -749,6 +887,8 @@ static void l2p32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double
 
 void p2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(p2m32_P, s, e, m) }
 void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(m2l32_P, s, e, m) }
+void m2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(m2m32_P, s, e, m) }
+void l2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(l2l32_P, s, e, m) }
 void l2p_p2p_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out) { VFMM_DISPATCH_M(l2p32_P, s, e, m, out) }
 
 } // namespace vfmm

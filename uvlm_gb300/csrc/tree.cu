@@ -72,16 +72,22 @@ __global__ void k_bbox_partial(const double *__restrict__ x, const double *__res
 
 // getBounds, tree.hpp:7-26: centre = (max+min)/2, R0 = largest half extent
 // about the centre, times 1.00001.
+// One warp; min/max are exact, so the lane split does not change the result.
 __global__ void k_bbox_final(const double *part, int nb, DevInfo *info)
 {
-  if (threadIdx.x != 0)
-    return;
   double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (int b = 0; b < nb; b++)
+  for (int b = threadIdx.x; b < nb; b += 32)
     for (int d = 0; d < 3; d++) {
       mn[d] = fmin(part[b * 6 + d], mn[d]);
       mx[d] = fmax(part[b * 6 + 3 + d], mx[d]);
     }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int d = 0; d < 3; d++) {
+      mn[d] = fmin(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+      mx[d] = fmax(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+    }
+  if (threadIdx.x != 0)
+    return;
   double X0[3], R0 = 0;
   for (int d = 0; d < 3; d++)
     X0[d] = __ddiv_rn(__dadd_rn(mx[d], mn[d]), 2.0);
@@ -117,7 +123,11 @@ void tree_bounds(cudaStream_t s, const double *X, size_t cap, int n, DevInfo *in
 __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, int n, const DevInfo *info,
                        uint64_t *keys, uint32_t *idx)
 {
-  const double R0 = info->R0;
+  // the centre chain's half-widths R0 / 2^(l+1), the same division for every body
+  __shared__ double half[MAXL];
+  if (threadIdx.x < MAXL)
+    half[threadIdx.x] = __ddiv_rn(info->R0, (double)(1 << (threadIdx.x + 1)));
+  __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double p[3] = {x[i], y[i], z[i]};
     double       c[3] = {info->X0[0], info->X0[1], info->X0[2]};
@@ -126,7 +136,7 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
     for (int l = 0; l < MAXL; l++) {
       const int b0 = p[0] > c[0], b1 = p[1] > c[1], b2 = p[2] > c[2];
       key          = (key << 3) | (uint64_t)(b0 | (b1 << 1) | (b2 << 2));
-      const double r = __ddiv_rn(R0, (double)(1 << (l + 1)));
+      const double r = half[l];
       c[0]           = __dadd_rn(c[0], b0 ? r : -r);
       c[1]           = __dadd_rn(c[1], b1 ? r : -r);
       c[2]           = __dadd_rn(c[2], b2 ? r : -r);

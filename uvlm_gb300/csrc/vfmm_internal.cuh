@@ -202,7 +202,7 @@ void m2l_sensor_pass(cudaStream_t s, const ExpArgs &a);
 void l2p_sensor_pass(cudaStream_t s, const ExpArgs &a, double *soa_out);
 std::vector<int4> m2l_schedule(int P, int lanes, int kb, int maxItems, int *itemsPerLane);
 
-// ---- mixed.cu (FP32 P2M / M2L / L2P+P2P around the FP64 M2M / L2L)
+// ---- mixed.cu (FP32 P2M / M2M / M2L / L2L / L2P+P2P, FP64 expansion arrays)
 struct MixedArgs {
   float2       *Mp32;
   float4       *pos32, *alp32;
@@ -214,6 +214,8 @@ struct MixedArgs {
 std::vector<int4> m2l_lane_table(int P, int kb, int sb);
 void p2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
 void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
+void m2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m); // FP32, scaled
+void l2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m); // FP32, scaled
 void l2p_p2p_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out);
 
 // ---- direct.cu
