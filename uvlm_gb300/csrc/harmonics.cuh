@@ -69,9 +69,10 @@ __device__ __forceinline__ void regular_harmonics(T x, T y, T z, cx<T> *Y, int s
 }
 
 // One column m of the singular harmonics S_n^m, n = m..NDEG-1 (lane-parallel
-// use: lane m computes column m).  inv_r2 = 1/r^2, S00 = 1/r.
-template <class T, int NDEG>
-__device__ __forceinline__ void singular_column(int m, T x, T y, T z, T inv_r2, T S00, cx<T> *out /* indexed by n */)
+// use: lane m computes column m), handed to emit(n, S_n^m) in order of n.
+// inv_r2 = 1/r^2, S00 = 1/r.
+template <class T, int NDEG, class F>
+__device__ __forceinline__ void singular_column_emit(int m, T x, T y, T z, T inv_r2, T S00, F &&emit)
 {
   cx<T> d{S00, T(0)};
   for (int k = 1; k <= m; k++) {
@@ -79,15 +80,22 @@ __device__ __forceinline__ void singular_column(int m, T x, T y, T z, T inv_r2, 
     d         = mk<T>((d.r * x - d.i * y) * s, (d.r * y + d.i * x) * s);
   }
   cx<T> a = d, b{T(0), T(0)};
-  out[m] = a;
+  emit(m, a);
   for (int n = m; n + 1 < NDEG; n++) {
     const T zz = T(2 * n + 1) * z;
     const T c2 = T((n + m) * (n - m));
     cx<T>   nx = mk<T>(-(zz * a.r + c2 * b.r) * inv_r2, -(zz * a.i + c2 * b.i) * inv_r2);
-    out[n + 1] = nx;
+    emit(n + 1, nx);
     b = a;
     a = nx;
   }
+}
+
+// The same column written to out[n].
+template <class T, int NDEG>
+__device__ __forceinline__ void singular_column(int m, T x, T y, T z, T inv_r2, T S00, cx<T> *out /* indexed by n */)
+{
+  singular_column_emit<T, NDEG>(m, x, y, z, inv_r2, S00, [&](int n, cx<T> v) { out[n] = v; });
 }
 
 template <class T>

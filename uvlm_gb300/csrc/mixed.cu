@@ -275,13 +275,22 @@ __global__ void __launch_bounds__(128) k_l2l32(DevMixed a, const int *cells, int
 // marks an idle lane.
 constexpr int M2L_YOFF = 4; // leading pad of each staged harmonic table
 
+// v * 2^e, equal to ldexpf(v, e): a multiply by the exactly built power of
+// two inside the normal exponent range, ldexpf outside it.
+__device__ __forceinline__ float scale2f(float v, int e)
+{
+  return (e >= -126 && e <= 127) ? v * __int_as_float((e + 127) << 23) : ldexpf(v, e);
+}
+
 template <int P, int SB>
 struct M2LV2 {
   static constexpr int KB = P >= 15 ? 8 : 4; // k columns per lane tile: at most 32 tiles per degree
   static constexpr int K = nterms(P), PP = P * P;
   static constexpr int MSTR = 3 * PP + 1;            // complex stride of a staged multipole
   static constexpr int YSTR = PP + M2L_YOFF + 1;     // complex stride of a staged harmonic table
-  static constexpr size_t bytes = (size_t)(SB * (MSTR + YSTR) + 3 * K) * sizeof(zf) + SB * (sizeof(float4) + 2 * sizeof(int));
+  static constexpr size_t bytes = (size_t)(SB * (MSTR + YSTR)) * sizeof(zf) + SB * (sizeof(float4) + 2 * sizeof(int));
+  // per-warp partial locals [P][3K] reuse the staging arrays after the last batch
+  static_assert(P * 3 * K <= SB * (MSTR + YSTR), "per-warp partials fit in the staging arrays");
 };
 
 template <int P, int SB>
@@ -295,9 +304,9 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
   int    *Src = reinterpret_cast<int *>(Off + SB);
   int    *Lvl = Src + SB;
   static_assert((SB * (sizeof(float4) + 2 * sizeof(int))) % 16 == 0, "keeps the complex arrays aligned");
-  zf *Ms  = reinterpret_cast<zf *>(Lvl + SB);
-  zf *Ys  = Ms + SB * MSTR;
-  zf *Lsm = Ys + SB * YSTR;
+  zf *Ms = reinterpret_cast<zf *>(Lvl + SB);
+  zf *Ys = Ms + SB * MSTR;
+  zf *Lw = Ms; // [P][3K] after the batches
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int4 me = lanes[n * 32 + lane];
   const int  j = me.x, k0 = me.y & 255, kb = me.y >> 8, rep = me.z, R = me.w & 255;
@@ -325,13 +334,14 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
                                        (float)iRs);
       }
       __syncthreads();
-      // stage multipoles: Mp32 * 2^{(lt - ls) n}
-      for (int e = threadIdx.x; e < nb * 3 * PP; e += nthreads) {
-        const int b = e / (3 * PP), r = e - b * (3 * PP);
+      // stage multipoles: Mp32 * 2^{(lt - ls) n}; each thread keeps its entries r
+      for (int r = threadIdx.x; r < 3 * PP; r += nthreads) {
         const int nn = (int)sqrtf((float)(r / 3)); // degree of entry n^2+n+m (exact for these small integers)
-        const float2 v  = a.Mp[(size_t)Src[b] * 3 * PP + r];
-        const int    sh = (lt - Lvl[b]) * nn;
-        Ms[b * MSTR + r] = {ldexpf(v.x, sh), ldexpf(v.y, sh)};
+        for (int b = 0; b < nb; b++) {
+          const float2 v  = a.Mp[(size_t)Src[b] * 3 * PP + r];
+          const int    sh = (lt - Lvl[b]) * nn;
+          Ms[b * MSTR + r] = {scale2f(v.x, sh), scale2f(v.y, sh)};
+        }
       }
       // stage singular harmonics at d / R_s, folded and scaled by 2^{(ls - lt) q} / R_s
       if (threadIdx.x < nb * P) {
@@ -339,16 +349,14 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
         const float4 o = Off[b];
         const float  dx = o.x, dy = o.y, dz = o.z;
         const float  r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.0f / r2, S00 = rsqrtf(r2);
-        zf           col[P];
-        singular_column<float, P>(m, dx, dy, dz, ir2, S00, col);
-        zf *Y = Ys + b * YSTR + M2L_YOFF;
-        for (int q = m; q < P; q++) {
-          const float f  = ldexpf(o.w, (ls - lt) * q);
-          const zf    v  = {col[q].r * f, col[q].i * f};
+        zf          *Y = Ys + b * YSTR + M2L_YOFF;
+        singular_column_emit<float, P>(m, dx, dy, dz, ir2, S00, [&](int q, zf c) {
+          const float f    = scale2f(o.w, (ls - lt) * q);
+          const zf    v    = {c.r * f, c.i * f};
           Y[q * q + q + m] = (m & 1) ? zf{-v.r, -v.i} : v;
           if (m > 0)
             Y[q * q + q - m] = conj(v);
-        }
+        });
       }
       __syncthreads();
       if (j >= 0) {
@@ -394,27 +402,23 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
           }
         }
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < 3 * K; e += nthreads)
-      Lsm[e] = {0.f, 0.f};
-    for (int w = 0; w < P; w++) {
-      __syncthreads();
-      if (n == w && j >= 0 && rep == 0) {
+    __syncthreads(); // staging arrays free: per-warp partials Lw[n] (each output of row j
+                     // is owned by one lane of each warp n <= P-1-j)
+    if (j >= 0 && rep == 0) {
 #pragma unroll
-        for (int kk = 0; kk < KB; kk++)
-          if (kk < kb)
+      for (int kk = 0; kk < KB; kk++)
+        if (kk < kb)
 #pragma unroll
-            for (int d = 0; d < 3; d++) {
-              zf &o = Lsm[tri(j, k0 + kk) * 3 + d];
-              o     = o + acc[kk][d];
-            }
-      }
+          for (int d = 0; d < 3; d++)
+            Lw[n * 3 * K + tri(j, k0 + kk) * 3 + d] = acc[kk][d];
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 3 * K; e += nthreads) {
       int jj, kk;
       jk_of_m(e / 3, jj, kk);
-      const zf     v = Lsm[e];
+      zf v = Lw[e];
+      for (int w = 1; w <= P - 1 - jj; w++)
+        v = v + Lw[w * 3 * K + e];
       const double s = ((jj & 1) ? -1.0 : 1.0) * cell_iRpow(a, lt, jj);
       a.L[(size_t)t * 3 * K + e] = make_double2(v.r * s, v.i * s);
     }
