@@ -311,7 +311,7 @@ void ensure_items(vfmm_handle h)
   VFMM_CUDA_TRY(cudaMemcpy(h->items32.p, tab32.data(), tab32.size() * sizeof(int4), cudaMemcpyHostToDevice));
   const char *sb = getenv("VFMM_M2L_BATCH");
   h->m2l_batch   = sb && (atoi(sb) == 8 || atoi(sb) == 32) ? atoi(sb) : 16;
-  auto lt32      = m2l_lane_table(h->cfg.p, h->cfg.p >= 15 ? 8 : 4, h->m2l_batch); // tile width and batch of k_m2l32v2
+  auto lt32      = m2l_lane_table(h->cfg.p, m2l_half_width(h->cfg.p), h->m2l_batch); // half-tile width and batch of k_m2l32v2
   h->lanes32.reserve(lt32.size());
   VFMM_CUDA_TRY(cudaMemcpy(h->lanes32.p, lt32.data(), lt32.size() * sizeof(int4), cudaMemcpyHostToDevice));
   h->items_P        = h->cfg.p;

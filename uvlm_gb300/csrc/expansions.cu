@@ -723,29 +723,33 @@ void downward_l2l(cudaStream_t s, const ExpArgs &e) { VFMM_DISPATCH(l2l_P, s, e)
 void l2p_p2p_pass(cudaStream_t s, const ExpArgs &e, double *out) { VFMM_DISPATCH(l2p_bodies_P, s, e, out) }
 void l2p_sensor_pass(cudaStream_t s, const ExpArgs &e, double *out) { VFMM_DISPATCH(l2p_sensors_P, s, e, out) }
 
-// Lane table of the lockstep M2L (k_m2l32v2): warp n (input degree n) splits
-// the output rows j <= P-1-n into tiles of kb columns; with T tiles, R =
-// min(32 / T, sb) replicas of them take turns over the batch's sources.
-// Entry [n * 32 + lane] = {j, k0 | kbn << 8, replica, R | T << 8}, j = -1 idle.
-std::vector<int4> m2l_lane_table(int P, int kb, int sb)
+// Lane table of the lockstep M2L (k_m2l32v2).  For degree n the outputs
+// (j, k), j <= P-1-n, 0 <= k <= j, are cut into half-tiles of kh consecutive
+// columns of one row; two half-tiles (any rows) form a lane tile, so short
+// rows waste few multiply-adds.  With T tiles, R = min(32 / T, sb) replicas
+// take turns over the batch's sources.  Entry [n * 32 + lane] =
+// {jA | k0A << 8 | kwA << 16, jB | k0B << 8 | kwB << 16, replica, R | T << 8};
+// a missing second half has kwB = 0 (and repeats the first's row/column);
+// x = -1 marks an idle lane.
+std::vector<int4> m2l_lane_table(int P, int kh, int sb)
 {
   std::vector<int4> tab((size_t)P * 32, make_int4(-1, 0, 0, 1));
   for (int n = 0; n < P; n++) {
-    std::vector<int4> tiles;
+    std::vector<int> halves;
     for (int j = 0; j <= P - 1 - n; j++)
-      for (int k0 = 0; k0 <= j; k0 += kb)
-        tiles.push_back(make_int4(j, k0 | (std::min(kb, j + 1 - k0) << 8), 0, 0));
+      for (int k0 = 0; k0 <= j; k0 += kh)
+        halves.push_back(j | (k0 << 8) | (std::min(kh, j + 1 - k0) << 16));
+    std::vector<int2> tiles;
+    for (size_t i = 0; i < halves.size(); i += 2)
+      tiles.push_back(make_int2(halves[i], i + 1 < halves.size() ? halves[i + 1] : (halves[i] & 0xffff)));
     const int T = (int)tiles.size();
     if (T > 32)
       throw Error(VFMM_ERR_UNSUPPORTED, "M2L lane table: more than 32 tiles for one degree");
     const int R = std::max(1, std::min(32 / T, sb));
     for (int l = 0; l < 32; l++) {
       int4 e = make_int4(-1, 0, 0, R | (T << 8));
-      if (l < T * R) {
-        e   = tiles[l % T];
-        e.z = l / T;
-        e.w = R | (T << 8);
-      }
+      if (l < T * R)
+        e = make_int4(tiles[l % T].x, tiles[l % T].y, l / T, R | (T << 8));
       tab[(size_t)n * 32 + l] = e;
     }
   }

@@ -265,15 +265,24 @@ __global__ void __launch_bounds__(128) k_l2l32(DevMixed a, const int *cells, int
 
 // M2L, lockstep form.  One block per target cell, one warp per input degree
 // n (P warps).  Within warp n every lane runs the same m-loop (-n..n), so
-// there is no divergence; a lane owns an output tile (row j, columns
-// k0..k0+3, all 3 components) and keeps a sliding register window over the
-// singular harmonics S'_{j+n}^{m-k}.  Warps whose degree has few tiles
-// replicate them over several sources of the batch.  The per-pair factor
-// (R_t/R_s)^j / R_s is split exactly into 2^{(lt-ls) n} on the staged
-// multipole and 2^{(ls-lt) q} / R_s on the staged harmonics (q = j + n).
-// Lane table entry: {j, k0 | kb << 8, replica, replicas | tiles << 8}; j < 0
-// marks an idle lane.
+// there is no divergence; a lane owns an output tile of two half-tiles (each
+// a row j and KH consecutive columns k, all 3 components) and keeps one
+// sliding register window per half over the singular harmonics
+// S'_{j+n}^{m-k}.  Warps whose degree has few tiles replicate them over
+// several sources of the batch.  The per-pair factor (R_t/R_s)^j / R_s is
+// split exactly into 2^{(lt-ls) n} on the staged multipole and
+// 2^{(ls-lt) q} / R_s on the staged harmonics (q = j + n).  Lane table: see
+// m2l_lane_table.
 constexpr int M2L_YOFF = 4; // leading pad of each staged harmonic table
+
+// Asynchronous 8-byte global -> shared copy (cp.async, sm_80+) and the wait
+// for all of this thread's copies.
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // v * 2^e, equal to ldexpf(v, e): a multiply by the exactly built power of
 // two inside the normal exponent range, ldexpf outside it.
@@ -284,7 +293,7 @@ __device__ __forceinline__ float scale2f(float v, int e)
 
 template <int P, int SB>
 struct M2LV2 {
-  static constexpr int KB = P >= 15 ? 8 : 4; // k columns per lane tile: at most 32 tiles per degree
+  static constexpr int KH = m2l_half_width(P); // k columns per half-tile
   static constexpr int K = nterms(P), PP = P * P;
   static constexpr int MSTR = 3 * PP + 1;            // complex stride of a staged multipole
   static constexpr int YSTR = PP + M2L_YOFF + 1;     // complex stride of a staged harmonic table
@@ -297,7 +306,7 @@ template <int P, int SB>
 __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__restrict__ lanes, int ncells)
 {
   using G = M2LV2<P, SB>;
-  constexpr int K = G::K, PP = G::PP, MSTR = G::MSTR, YSTR = G::YSTR, KB = G::KB;
+  constexpr int K = G::K, PP = G::PP, MSTR = G::MSTR, YSTR = G::YSTR, KH = G::KH;
   extern __shared__ float4 smem32[];
   // 16-byte-aligned fields first: per source (d / R_s, 1 / R_s), source index, level
   float4 *Off = smem32;
@@ -309,15 +318,18 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
   zf *Lw = Ms; // [P][3K] after the batches
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int4 me = lanes[n * 32 + lane];
-  const int  j = me.x, k0 = me.y & 255, kb = me.y >> 8, rep = me.z, R = me.w & 255;
+  const bool busy = me.x >= 0;
+  const int  jA = me.x & 255, k0A = (me.x >> 8) & 255, kwA = (me.x >> 16) & 255;
+  const int  jB = me.y & 255, k0B = (me.y >> 8) & 255, kwB = (me.y >> 16) & 255;
+  const int  rep = me.z, R = me.w & 255;
   const int  nthreads = P * 32;
   for (int t = blockIdx.x; t < ncells; t += gridDim.x) {
-    zf acc[KB][3];
+    zf accA[KH][3], accB[KH][3];
 #pragma unroll
-    for (int kk = 0; kk < KB; kk++)
+    for (int kk = 0; kk < KH; kk++)
 #pragma unroll
       for (int d = 0; d < 3; d++)
-        acc[kk][d] = {0.f, 0.f};
+        accA[kk][d] = accB[kk][d] = {0.f, 0.f};
     const int    q0 = a.m2l_start[t], q1 = a.m2l_start[t + 1];
     const double tx = a.cv.x[t], ty = a.cv.y[t], tz = a.cv.z[t];
     const int    lt = a.cv.level[t];
@@ -334,15 +346,12 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
                                        (float)iRs);
       }
       __syncthreads();
-      // stage multipoles: Mp32 * 2^{(lt - ls) n}; each thread keeps its entries r
-      for (int r = threadIdx.x; r < 3 * PP; r += nthreads) {
-        const int nn = (int)sqrtf((float)(r / 3)); // degree of entry n^2+n+m (exact for these small integers)
-        for (int b = 0; b < nb; b++) {
-          const float2 v  = a.Mp[(size_t)Src[b] * 3 * PP + r];
-          const int    sh = (lt - Lvl[b]) * nn;
-          Ms[b * MSTR + r] = {scale2f(v.x, sh), scale2f(v.y, sh)};
-        }
-      }
+      // stage multipoles: asynchronous copies of Mp32, all in flight at once
+      // while the harmonics are made; sources on another level than the
+      // target are scaled by 2^{(lt - ls) n} afterwards
+      for (int r = threadIdx.x; r < 3 * PP; r += nthreads)
+        for (int b = 0; b < nb; b++)
+          cp_async8(Ms + b * MSTR + r, a.Mp + (size_t)Src[b] * 3 * PP + r);
       // stage singular harmonics at d / R_s, folded and scaled by 2^{(ls - lt) q} / R_s
       if (threadIdx.x < nb * P) {
         const int    b = threadIdx.x / P, m = threadIdx.x - b * P, ls = Lvl[b];
@@ -358,30 +367,56 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
             Y[q * q + q - m] = conj(v);
         });
       }
+      cp_async_wait_all();
       __syncthreads();
-      if (j >= 0) {
-        const int q    = j + n;
-        const int base = M2L_YOFF + q * q + q - k0;
+      bool cross = false;
+      for (int b = 0; b < nb; b++)
+        cross |= Lvl[b] != lt;
+      if (cross) { // block-uniform
+        for (int r = threadIdx.x; r < 3 * PP; r += nthreads) {
+          const int nn = (int)sqrtf((float)(r / 3)); // degree of entry n^2+n+m (exact for these small integers)
+          for (int b = 0; b < nb; b++) {
+            const int sh = (lt - Lvl[b]) * nn;
+            if (sh != 0) {
+              zf &v = Ms[b * MSTR + r];
+              v     = {scale2f(v.r, sh), scale2f(v.i, sh)};
+            }
+          }
+        }
+        __syncthreads();
+      }
+      if (busy) {
+        const int qA = jA + n, qB = jB + n;
+        const int baseA = M2L_YOFF + qA * qA + qA - k0A, baseB = M2L_YOFF + qB * qB + qB - k0B;
         for (int b = rep; b < nb; b += R) {
-          const zf *Y  = Ys + b * YSTR + base;
+          const zf *YA = Ys + b * YSTR + baseA;
+          const zf *YB = Ys + b * YSTR + baseB;
           const zf *Mb = Ms + b * MSTR + (n * n + n) * 3;
-          zf        y[KB];
+          zf        ya[KH], yb[KH];
 #pragma unroll
-          for (int kk = 0; kk < KB; kk++)
-            y[kk] = Y[-n - kk];
+          for (int kk = 0; kk < KH; kk++) {
+            ya[kk] = YA[-n - kk];
+            yb[kk] = YB[-n - kk];
+          }
           for (int m = -n; m <= n; m++) {
             const zf m0 = Mb[m * 3 + 0], m1 = Mb[m * 3 + 1], m2 = Mb[m * 3 + 2];
 #pragma unroll
-            for (int kk = 0; kk < KB; kk++) {
-              cfma(acc[kk][0], m0, y[kk]);
-              cfma(acc[kk][1], m1, y[kk]);
-              cfma(acc[kk][2], m2, y[kk]);
+            for (int kk = 0; kk < KH; kk++) {
+              cfma(accA[kk][0], m0, ya[kk]);
+              cfma(accA[kk][1], m1, ya[kk]);
+              cfma(accA[kk][2], m2, ya[kk]);
+              cfma(accB[kk][0], m0, yb[kk]);
+              cfma(accB[kk][1], m1, yb[kk]);
+              cfma(accB[kk][2], m2, yb[kk]);
             }
             if (m < n) {
 #pragma unroll
-              for (int kk = KB - 1; kk > 0; kk--)
-                y[kk] = y[kk - 1];
-              y[0] = Y[m + 1];
+              for (int kk = KH - 1; kk > 0; kk--) {
+                ya[kk] = ya[kk - 1];
+                yb[kk] = yb[kk - 1];
+              }
+              ya[0] = YA[m + 1];
+              yb[0] = YB[m + 1];
             }
           }
         }
@@ -391,26 +426,33 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
     const int T = me.w >> 8;
     for (int st = 1; st < R; st <<= 1) {
 #pragma unroll
-      for (int kk = 0; kk < KB; kk++)
+      for (int kk = 0; kk < KH; kk++)
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-          const float vr = __shfl_down_sync(0xffffffffu, acc[kk][d].r, T * st);
-          const float vi = __shfl_down_sync(0xffffffffu, acc[kk][d].i, T * st);
-          if (j >= 0 && (rep % (2 * st)) == 0 && rep + st < R) {
-            acc[kk][d].r += vr;
-            acc[kk][d].i += vi;
+          const float ar = __shfl_down_sync(0xffffffffu, accA[kk][d].r, T * st);
+          const float ai = __shfl_down_sync(0xffffffffu, accA[kk][d].i, T * st);
+          const float br = __shfl_down_sync(0xffffffffu, accB[kk][d].r, T * st);
+          const float bi = __shfl_down_sync(0xffffffffu, accB[kk][d].i, T * st);
+          if (busy && (rep % (2 * st)) == 0 && rep + st < R) {
+            accA[kk][d].r += ar;
+            accA[kk][d].i += ai;
+            accB[kk][d].r += br;
+            accB[kk][d].i += bi;
           }
         }
     }
     __syncthreads(); // staging arrays free: per-warp partials Lw[n] (each output of row j
                      // is owned by one lane of each warp n <= P-1-j)
-    if (j >= 0 && rep == 0) {
+    if (busy && rep == 0) {
 #pragma unroll
-      for (int kk = 0; kk < KB; kk++)
-        if (kk < kb)
+      for (int kk = 0; kk < KH; kk++)
 #pragma unroll
-          for (int d = 0; d < 3; d++)
-            Lw[n * 3 * K + tri(j, k0 + kk) * 3 + d] = acc[kk][d];
+        for (int d = 0; d < 3; d++) {
+          if (kk < kwA)
+            Lw[n * 3 * K + tri(jA, k0A + kk) * 3 + d] = accA[kk][d];
+          if (kk < kwB)
+            Lw[n * 3 * K + tri(jB, k0B + kk) * 3 + d] = accB[kk][d];
+        }
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 3 * K; e += nthreads) {
@@ -540,9 +582,12 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
     __syncthreads();
 
     for (int tc = 0; tc < nb; tc += 128) {
+      // every thread works: the first `full` targets of the chunk have G members,
+      // the others G - 1; member g of target tt takes every Gt-th column / source
       const int  nt = min(128, nb - tc);
-      const int  G = 128 / nt, tt = threadIdx.x % nt, g = threadIdx.x / nt;
-      const bool active = g < G;
+      const int  G = (128 + nt - 1) / nt, full = 128 - (G - 1) * nt;
+      const int  tt = threadIdx.x % nt, g = threadIdx.x / nt, Gt = tt < full ? G : G - 1;
+      const bool active = g < Gt;
       float      hi[12], lo[12];
       for (int k = 0; k < 12; k++)
         hi[k] = lo[k] = 0.f;
@@ -561,7 +606,7 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
             const float sc = 1.f / float(2 * m);
             diag           = {(diag.r * x - diag.i * y) * sc, (diag.r * y + diag.i * x) * sc};
           }
-          if ((m - g) % G != 0)
+          if ((m - g) % Gt != 0)
             continue;
           const float w  = m == 0 ? 1.f : 2.f;
           zf          ya = diag, yb{0.f, 0.f};
@@ -622,12 +667,12 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
           }
           __syncthreads();
           if (active) {
-            for (int j0 = g; j0 < cnt; j0 += 16 * G) {
+            for (int j0 = g; j0 < cnt; j0 += 16 * Gt) {
               float sacc[12];
               for (int k = 0; k < 12; k++)
                 sacc[k] = 0.f;
-              const int jend = min(cnt, j0 + 16 * G);
-              for (int jb = j0; jb < jend; jb += G) {
+              const int jend = min(cnt, j0 + 16 * Gt);
+              for (int jb = j0; jb < jend; jb += Gt) {
                 const float4 ps = Sp[jb];
                 const float  dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
                 const float  R2 = dx * dx + dy * dy + dz * dz;
@@ -697,7 +742,8 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
         double    r[12];
         for (int k = 0; k < 12; k++) {
           float h = 0.f, l = 0.f;
-          for (int gg = 0; gg < G; gg++) {
+          const int Gm = t < full ? G : G - 1;
+          for (int gg = 0; gg < Gm; gg++) {
             two_sum_add(h, l, rhi[(gg * nt + t) * 12 + k]);
             l += rlo[(gg * nt + t) * 12 + k];
           }

@@ -211,7 +211,9 @@ struct MixedArgs {
   int           m2l_batch; // sources staged per batch in k_m2l32v2 (8, 16 or 32)
   double        R0;
 };
-std::vector<int4> m2l_lane_table(int P, int kb, int sb);
+// Columns per half-tile of the mixed M2L lane tiles: at most 32 tiles per degree.
+__host__ __device__ constexpr int m2l_half_width(int P) { return P >= 16 ? 4 : 2; }
+std::vector<int4> m2l_lane_table(int P, int kh, int sb);
 void p2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
 void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
 void m2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m); // FP32, scaled
