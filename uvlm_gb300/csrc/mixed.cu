@@ -502,6 +502,66 @@ struct L2P32Sizes {
   static_assert((size_t)CH * 2 * sizeof(float4) >= 2 * 128 * 12 * sizeof(float), "the staging buffer holds the reduction");
 };
 
+constexpr float kInv4pi = 0.0795774715459476679f;
+constexpr float kC2spi  = 1.12837916709551257f; // 2/sqrt(pi)
+constexpr float kKS     = 0.0317468755f;        // (2/sqrt(pi)) / (8 sqrt(2) pi)
+constexpr float kIsq2   = 0.707106781186547524f;
+
+// Weights of one pair of the regularised Biot-Savart kernel
+// (multipoleKernels.hpp:239-283) from R^2, w = 1/(2 sigma^2), is = 1/sigma:
+// velocity G = g(rho) / (4 pi R^3) and gradient A = (t2 / sigma^2 -
+// 3 g / R^2) / (4 pi R^3), rho = R / (sqrt(2) sigma), g = erf(rho) - t2,
+// t2 = (2/sqrt(pi)) rho e^(-rho^2).  For rho^2 < 0.25 the x^3-scaled series
+// replaces the cancelling difference; R^2 = 0 (the body itself) gives zero.
+__device__ __forceinline__ void p2p_weights(float R2, float w, float is, float &Gc, float &Ac)
+{
+  const float RS   = R2 * w; // rho^2
+  const float R2s  = R2 != 0.f ? R2 : 1.f;
+  const float rinv = rsqrtf(R2s);
+  const float xs   = R2s * rinv * is * kIsq2;
+  const float erfS = erff(xs);
+  const float t2   = kC2spi * xs * __expf(-RS);
+  const float c4   = kInv4pi * rinv * rinv * rinv;
+  const float gg   = erfS - t2;
+  Gc               = gg * c4;
+  Ac               = (t2 * 2.f * w - 3.f * gg * rinv * rinv) * c4;
+  if (RS < 0.25f) {
+    const float gpoly = ((((((1.f / 5400.f) * RS - 1.f / 780.f) * RS + 1.f / 132.f) * RS - 1.f / 27.f) * RS + 1.f / 7.f) * RS - 0.4f) * RS + 2.f / 3.f;
+    const float hpoly = ((((((-1.f / 6120.f) * RS + 1.f / 900.f) * RS - 1.f / 156.f) * RS + 1.f / 33.f) * RS - 1.f / 9.f) * RS + 2.f / 7.f) * RS - 0.4f;
+    const float is2 = is * is, is3 = is2 * is;
+    Gc              = gpoly * kKS * is3;
+    Ac              = hpoly * kKS * is3 * is2;
+  }
+  if (R2 == 0.f)
+    Gc = Ac = 0.f;
+}
+
+// sacc += the pair's velocity (0..2) and gradient (3..11, J[a][b] at 3+3a+b)
+// terms, offset d = x_target - x_source, strength al.
+__device__ __forceinline__ void p2p_accum(float dx, float dy, float dz, float4 al, float Gc, float Ac, float *sacc)
+{
+  const float cr0 = dy * al.z - dz * al.y, cr1 = dz * al.x - dx * al.z, cr2 = dx * al.y - dy * al.x;
+  sacc[0]         = fmaf(Gc, cr0, sacc[0]);
+  sacc[1]         = fmaf(Gc, cr1, sacc[1]);
+  sacc[2]         = fmaf(Gc, cr2, sacc[2]);
+  const float a0 = Ac * cr0, a1 = Ac * cr1, a2 = Ac * cr2;
+  sacc[3]        = fmaf(a0, dx, sacc[3]);
+  sacc[4]        = fmaf(a0, dy, sacc[4]);
+  sacc[5]        = fmaf(a0, dz, sacc[5]);
+  sacc[6]        = fmaf(a1, dx, sacc[6]);
+  sacc[7]        = fmaf(a1, dy, sacc[7]);
+  sacc[8]        = fmaf(a1, dz, sacc[8]);
+  sacc[9]        = fmaf(a2, dx, sacc[9]);
+  sacc[10]       = fmaf(a2, dy, sacc[10]);
+  sacc[11]       = fmaf(a2, dz, sacc[11]);
+  sacc[6]        = fmaf(-Gc, al.z, sacc[6]);
+  sacc[9]        = fmaf(Gc, al.y, sacc[9]);
+  sacc[4]        = fmaf(Gc, al.z, sacc[4]);
+  sacc[10]       = fmaf(-Gc, al.x, sacc[10]);
+  sacc[5]        = fmaf(-Gc, al.y, sacc[5]);
+  sacc[8]        = fmaf(Gc, al.x, sacc[8]);
+}
+
 // two-sum: hi + lo accumulates v without losing its low-order bits
 __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v)
 {
@@ -542,10 +602,7 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
   float  *rlo  = rhi + 128 * 12;                // [128][12] partial sums (lo)
   (void)K1;
   (void)K2;
-  const float inv4pi = 0.0795774715459476679f;
-  const float c2spi  = 1.12837916709551257f; // 2/sqrt(pi)
-  const float KS     = 0.0317468755f;        // (2/sqrt(pi)) / (8 sqrt(2) pi)
-  const float isq2   = 0.707106781186547524f;
+  const float inv4pi = kInv4pi;
 
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
     const int    c = a.leaf_cells[li];
@@ -672,57 +729,22 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
               for (int k = 0; k < 12; k++)
                 sacc[k] = 0.f;
               const int jend = min(cnt, j0 + 16 * Gt);
-              for (int jb = j0; jb < jend; jb += Gt) {
-                const float4 ps = Sp[jb];
+              // two sources per iteration, straight-line, accumulated in source order
+              for (int jb = j0; jb < jend; jb += 2 * Gt) {
+                const int    jb2 = jb + Gt;
+                const bool   two = jb2 < jend;
+                const float4 ps = Sp[jb], qs = Sp[two ? jb2 : jb];
+                const float4 al = Sa[jb], bl = Sa[two ? jb2 : jb];
                 const float  dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
-                const float  R2 = dx * dx + dy * dy + dz * dz;
-                if (R2 != 0.f) {
-                  const float4 al = Sa[jb];
-                  const float  RS = R2 * ps.w; // R^2 / (2 sigma^2)
-                  float        Gc, Ac;
-                  if (RS < 0.25f) {
-                    // x^3-scaled series of the regularised kernel: no cancellation for close pairs
-                    const float gpoly = ((((((1.f / 5400.f) * RS - 1.f / 780.f) * RS + 1.f / 132.f) * RS - 1.f / 27.f) * RS + 1.f / 7.f) * RS - 0.4f) *
-                                            RS +
-                                        2.f / 3.f;
-                    const float hpoly = ((((((-1.f / 6120.f) * RS + 1.f / 900.f) * RS - 1.f / 156.f) * RS + 1.f / 33.f) * RS - 1.f / 9.f) * RS +
-                                         2.f / 7.f) *
-                                            RS -
-                                        0.4f;
-                    const float is = al.w, is2 = is * is, is3 = is2 * is;
-                    Gc             = gpoly * KS * is3;
-                    Ac             = hpoly * KS * is3 * is2;
-                  } else {
-                    const float rinv = rsqrtf(R2);
-                    const float xs   = R2 * rinv * al.w * isq2; // R / (sqrt(2) sigma)
-                    const float erfS = erff(xs);
-                    const float t2   = c2spi * xs * __expf(-RS);
-                    const float c4   = inv4pi * rinv * rinv * rinv;
-                    const float gg   = erfS - t2;
-                    Gc               = gg * c4;
-                    Ac               = (t2 * 2.f * ps.w - 3.f * gg * rinv * rinv) * c4;
-                  }
-                  const float cr0 = dy * al.z - dz * al.y, cr1 = dz * al.x - dx * al.z, cr2 = dx * al.y - dy * al.x;
-                  sacc[0] = fmaf(Gc, cr0, sacc[0]);
-                  sacc[1] = fmaf(Gc, cr1, sacc[1]);
-                  sacc[2] = fmaf(Gc, cr2, sacc[2]);
-                  const float a0 = Ac * cr0, a1 = Ac * cr1, a2 = Ac * cr2;
-                  sacc[3]  = fmaf(a0, dx, sacc[3]);
-                  sacc[4]  = fmaf(a0, dy, sacc[4]);
-                  sacc[5]  = fmaf(a0, dz, sacc[5]);
-                  sacc[6]  = fmaf(a1, dx, sacc[6]);
-                  sacc[7]  = fmaf(a1, dy, sacc[7]);
-                  sacc[8]  = fmaf(a1, dz, sacc[8]);
-                  sacc[9]  = fmaf(a2, dx, sacc[9]);
-                  sacc[10] = fmaf(a2, dy, sacc[10]);
-                  sacc[11] = fmaf(a2, dz, sacc[11]);
-                  sacc[6]  = fmaf(-Gc, al.z, sacc[6]);
-                  sacc[9]  = fmaf(Gc, al.y, sacc[9]);
-                  sacc[4]  = fmaf(Gc, al.z, sacc[4]);
-                  sacc[10] = fmaf(-Gc, al.x, sacc[10]);
-                  sacc[5]  = fmaf(-Gc, al.y, sacc[5]);
-                  sacc[8]  = fmaf(Gc, al.x, sacc[8]);
-                }
+                const float  ex = pt.x - qs.x, ey = pt.y - qs.y, ez = pt.z - qs.z;
+                const float  R2 = dx * dx + dy * dy + dz * dz, R2b = ex * ex + ey * ey + ez * ez;
+                float        G1, A1, G2, A2;
+                p2p_weights(R2, ps.w, al.w, G1, A1);
+                p2p_weights(R2b, qs.w, bl.w, G2, A2);
+                if (!two)
+                  G2 = A2 = 0.f;
+                p2p_accum(dx, dy, dz, al, G1, A1, sacc);
+                p2p_accum(ex, ey, ez, bl, G2, A2, sacc);
               }
               for (int k = 0; k < 12; k++)
                 two_sum_add(hi[k], lo[k], -sacc[k]); // the near field enters with a minus sign
