@@ -259,7 +259,7 @@ void build_lists(cudaStream_t s, Tree &tt, Tree &st, double theta, DevInfo *info
     L.ls.front[1].reserve(L.cap_front);
     L.ls.p2p_raw.reserve(L.cap_p2p);
     L.ls.m2l_raw.reserve(L.cap_m2l);
-    traverse(s, tt.view(), st.view(), tt.ncells, tt.maxLevel, st.maxLevel, theta, info, L.ls, L.ls.front[0].cap, L.ls.p2p_raw.cap,
+    traverse(s, tt.view(), st.view(), tt.ncells, st.ncells, tt.maxLevel, st.maxLevel, theta, info, L.ls, L.ls.front[0].cap, L.ls.p2p_raw.cap,
              L.ls.m2l_raw.cap);
     read_info(s, info, hinfo);
     if (!hinfo->overflow)
@@ -700,14 +700,15 @@ int vfmm_get_lists(vfmm_handle h, uint64_t *p2p, size_t cap_p2p, size_t *n_p2p, 
       *n_p2p = (size_t)h->lists.n_p2p;
     if (n_m2l)
       *n_m2l = (size_t)h->lists.n_m2l;
-    auto fetch = [&](const unsigned long long *src, int cnt, uint64_t *dst, size_t cap) {
+    const int kb   = h->lists.ls.key_bits;
+    auto      fetch = [&](const unsigned long long *src, int cnt, uint64_t *dst, size_t cap) {
       if (!dst || cap < (size_t)cnt || cnt == 0)
         return;
       std::vector<unsigned long long> k(cnt);
       VFMM_CUDA_TRY(cudaMemcpy(k.data(), src, cnt * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
       for (int i = 0; i < cnt; i++) {
-        dst[2 * i]     = k[i] >> 32;
-        dst[2 * i + 1] = k[i] & 0xffffffffull;
+        dst[2 * i]     = k[i] >> kb;
+        dst[2 * i + 1] = k[i] & ((1ull << kb) - 1);
       }
     };
     VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));

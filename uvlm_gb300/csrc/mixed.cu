@@ -316,6 +316,8 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
   zf *Ms = reinterpret_cast<zf *>(Lvl + SB);
   zf *Ys = Ms + SB * MSTR;
   zf *Lw = Ms; // [P][3K] after the batches
+  __shared__ unsigned cross_mask; // batch sources on another level than the target
+  static_assert(SB <= 32, "one warp stages a batch");
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int4 me = lanes[n * 32 + lane];
   const bool busy = me.x >= 0;
@@ -336,14 +338,21 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
     for (int qb = q0; qb < q1; qb += SB) {
       const int nb = min(SB, q1 - qb);
       __syncthreads();
-      if (threadIdx.x < nb) {
-        const int    s   = a.m2l_src[qb + threadIdx.x];
-        const int    ls  = a.cv.level[s];
-        const double iRs = ldexp(a.iR0, ls);
-        Src[threadIdx.x] = s;
-        Lvl[threadIdx.x] = ls;
-        Off[threadIdx.x] = make_float4((float)((tx - a.cv.x[s]) * iRs), (float)((ty - a.cv.y[s]) * iRs), (float)((tz - a.cv.z[s]) * iRs),
-                                       (float)iRs);
+      if (threadIdx.x < 32) { // nb <= SB <= 32: warp 0 stages the batch's sources
+        bool cl = false;
+        if (threadIdx.x < nb) {
+          const int    s   = a.m2l_src[qb + threadIdx.x];
+          const int    ls  = a.cv.level[s];
+          const double iRs = ldexp(a.iR0, ls);
+          Src[threadIdx.x] = s;
+          Lvl[threadIdx.x] = ls;
+          Off[threadIdx.x] = make_float4((float)((tx - a.cv.x[s]) * iRs), (float)((ty - a.cv.y[s]) * iRs), (float)((tz - a.cv.z[s]) * iRs),
+                                         (float)iRs);
+          cl = ls != lt;
+        }
+        const unsigned msk = __ballot_sync(0xffffffffu, cl);
+        if (threadIdx.x == 0)
+          cross_mask = msk;
       }
       __syncthreads();
       // stage multipoles: asynchronous copies of Mp32, all in flight at once
@@ -369,18 +378,15 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
       }
       cp_async_wait_all();
       __syncthreads();
-      bool cross = false;
-      for (int b = 0; b < nb; b++)
-        cross |= Lvl[b] != lt;
-      if (cross) { // block-uniform
+      const unsigned cmask = cross_mask;
+      if (cmask) { // block-uniform: sources on another level than the target
         for (int r = threadIdx.x; r < 3 * PP; r += nthreads) {
           const int nn = (int)sqrtf((float)(r / 3)); // degree of entry n^2+n+m (exact for these small integers)
-          for (int b = 0; b < nb; b++) {
+          for (unsigned mk = cmask; mk; mk &= mk - 1) {
+            const int b  = __ffs(mk) - 1;
             const int sh = (lt - Lvl[b]) * nn;
-            if (sh != 0) {
-              zf &v = Ms[b * MSTR + r];
-              v     = {scale2f(v.r, sh), scale2f(v.i, sh)};
-            }
+            zf       &v  = Ms[b * MSTR + r];
+            v            = {scale2f(v.r, sh), scale2f(v.i, sh)};
           }
         }
         __syncthreads();

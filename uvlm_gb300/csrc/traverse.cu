@@ -9,6 +9,7 @@
 // with the reference's operation order and no contraction (traverse.hpp:
 // 52-57); near leaf pairs go to P2P, near others to the next frontier, far
 // pairs to M2L.  Pairs are then sorted by (target, source) into CSR rows.
+#include <algorithm>
 #include <cub/cub.cuh>
 #include "vfmm_internal.cuh"
 
@@ -23,6 +24,25 @@ __device__ __forceinline__ bool mac_near(const CellsView &a, int i, const CellsV
   const double R2  = __dmul_rn(__dmul_rn(nrm, theta), theta);
   const double s   = __dadd_rn(a.R[i], b.R[j]);
   return R2 < __dmul_rn(s, s);
+}
+
+// Warp-aggregated reservation in *ctr: every lane of the warp calls with its
+// count c (possibly 0) and receives its start offset; one atomic per warp.
+__device__ __forceinline__ int warp_reserve(int *ctr, int c)
+{
+  const int lane = threadIdx.x & 31;
+  int       incl = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o)
+      incl += v;
+  }
+  const int tot  = __shfl_sync(0xffffffffu, incl, 31);
+  int       base = 0;
+  if (lane == 31 && tot)
+    base = atomicAdd(ctr, tot);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  return base + incl - c;
 }
 
 __global__ void k_traverse_init(CellsView tc, CellsView sc, int2 *front, DevInfo *info, unsigned long long *p2p)
@@ -47,12 +67,15 @@ __global__ void k_traverse_step(CellsView tc, CellsView sc, const int2 *__restri
                                 int cell_bits, int *overflow)
 {
   const int n = *n_in;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int2 pr = fin[q];
+  // warp-uniform trip count (blockDim is a multiple of 32) for the aggregated reservations
+  for (int q0 = blockIdx.x * blockDim.x; q0 < n; q0 += gridDim.x * blockDim.x) {
+    const int  q     = q0 + threadIdx.x;
+    const bool valid = q < n;
+    const int2 pr    = valid ? fin[q] : make_int2(0, 0);
     const int  T = pr.x, S = pr.y;
     const bool splitT = sc.nchild[S] == 0 || (tc.R[T] >= sc.R[S] && tc.nchild[T] != 0);
     const int  c0 = splitT ? tc.child[T] : sc.child[S];
-    const int  nc = splitT ? tc.nchild[T] : sc.nchild[S];
+    const int  nc = valid ? (splitT ? tc.nchild[T] : sc.nchild[S]) : 0;
     unsigned   kind = 0; // 2 bits per child: 0 m2l, 1 p2p, 2 push
     int        cm = 0, cp = 0, cf = 0;
     for (int k = 0; k < nc; k++) {
@@ -67,9 +90,9 @@ __global__ void k_traverse_step(CellsView tc, CellsView sc, const int2 *__restri
       cp += kd == 1;
       cf += kd == 2;
     }
-    int bm = cm ? atomicAdd(nm2l, cm) : 0;
-    int bp = cp ? atomicAdd(np2p, cp) : 0;
-    int bf = cf ? atomicAdd(n_out, cf) : 0;
+    int bm = warp_reserve(nm2l, cm);
+    int bp = warp_reserve(np2p, cp);
+    int bf = warp_reserve(n_out, cf);
     if (bm + cm > cap_m2l || bp + cp > cap_p2p || bf + cf > cap_front) {
       atomicExch(overflow, 1);
       continue;
@@ -88,17 +111,18 @@ __global__ void k_traverse_step(CellsView tc, CellsView sc, const int2 *__restri
   }
 }
 
-void traverse(cudaStream_t s, CellsView tc, CellsView sc, int ntc, int maxLevelT, int maxLevelS, double theta, DevInfo *info, ListScratch &ls,
-              size_t cap_front, size_t cap_p2p, size_t cap_m2l)
+void traverse(cudaStream_t s, CellsView tc, CellsView sc, int ntc, int nsc, int maxLevelT, int maxLevelS, double theta, DevInfo *info,
+              ListScratch &ls, size_t cap_front, size_t cap_p2p, size_t cap_m2l)
 {
   ls.front[0].reserve(cap_front);
   ls.front[1].reserve(cap_front);
   ls.p2p_raw.reserve(cap_p2p);
   ls.m2l_raw.reserve(cap_m2l);
+  // pair keys (target << key_bits | source): the sort then covers 2 * key_bits bits
   int cell_bits = 1;
-  while ((1 << cell_bits) < ntc + 1)
+  while ((1ll << cell_bits) < (long long)std::max(ntc, nsc))
     cell_bits++;
-  (void)cell_bits;
+  ls.key_bits = cell_bits;
   k_traverse_init<<<1, 32, 0, s>>>(tc, sc, ls.front[0].p, info, ls.p2p_raw.p);
   count_launch();
   const int steps = maxLevelT + maxLevelS + 1;
@@ -107,25 +131,26 @@ void traverse(cudaStream_t s, CellsView tc, CellsView sc, int ntc, int maxLevelT
     VFMM_CUDA_TRY(cudaMemsetAsync(&info->front_n[b], 0, sizeof(int), s));
     k_traverse_step<<<152 * 8, 128, 0, s>>>(tc, sc, ls.front[a].p, &info->front_n[a], ls.front[b].p, &info->front_n[b], (int)ls.front[b].cap,
                                             ls.p2p_raw.p, ls.m2l_raw.p, &info->n_p2p, &info->n_m2l, (int)ls.p2p_raw.cap, (int)ls.m2l_raw.cap, theta,
-                                            32, &info->overflow);
+                                            cell_bits, &info->overflow);
     count_launch();
   }
   VFMM_LAUNCH_CHECK();
 }
 
-// CSR rows by target from sorted (target << 32 | source) keys; also counts
-// body-body P2P interactions (self pairs excluded).
-__global__ void k_csr(const unsigned long long *__restrict__ keys, int n, int ncells, int *start, int *src, const int *nbody,
+// CSR rows by target from sorted (target << kb | source) keys; also counts
+// body-body P2P interactions (self pairs excluded), one atomic per warp.
+__global__ void k_csr(const unsigned long long *__restrict__ keys, int n, int kb, int ncells, int *start, int *src, const int *nbody,
                       unsigned long long *interactions)
 {
-  unsigned long long local = 0;
+  const unsigned long long smask = (1ull << kb) - 1;
+  unsigned long long       local = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
-    const int t  = i < n ? (int)(keys[i] >> 32) : ncells;
-    const int tp = i > 0 ? (int)(keys[i - 1] >> 32) : -1;
+    const int t  = i < n ? (int)(keys[i] >> kb) : ncells;
+    const int tp = i > 0 ? (int)(keys[i - 1] >> kb) : -1;
     for (int r = tp + 1; r <= t; r++)
       start[r] = i;
     if (i < n) {
-      const int sidx = (int)(keys[i] & 0xffffffffull);
+      const int sidx = (int)(keys[i] & smask);
       src[i]         = sidx;
       if (nbody) {
         const unsigned long long a = (unsigned long long)nbody[t], b = (unsigned long long)nbody[sidx];
@@ -133,8 +158,12 @@ __global__ void k_csr(const unsigned long long *__restrict__ keys, int n, int nc
       }
     }
   }
-  if (interactions && local)
-    atomicAdd(interactions, local);
+  if (interactions) {
+    for (int o = 16; o > 0; o >>= 1)
+      local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local)
+      atomicAdd(interactions, local);
+  }
 }
 
 void lists_to_csr(cudaStream_t s, ListScratch &ls, int n_p2p, int n_m2l, int ncells_t, int cell_bits, int *p2p_start, int *p2p_src, int *m2l_start,
@@ -143,7 +172,7 @@ void lists_to_csr(cudaStream_t s, ListScratch &ls, int n_p2p, int n_m2l, int nce
   (void)cell_bits;
   ls.p2p_sorted.reserve(n_p2p + 1);
   ls.m2l_sorted.reserve(n_m2l + 1);
-  const int end_bit = 64;
+  const int end_bit = 2 * ls.key_bits;
   size_t    b1 = 0, b2 = 0;
   VFMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(nullptr, b1, ls.p2p_raw.p, ls.p2p_sorted.p, n_p2p, 0, end_bit, s));
   VFMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(nullptr, b2, ls.m2l_raw.p, ls.m2l_sorted.p, n_m2l, 0, end_bit, s));
@@ -156,9 +185,9 @@ void lists_to_csr(cudaStream_t s, ListScratch &ls, int n_p2p, int n_m2l, int nce
     VFMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(ls.cub_tmp.p, b2, ls.m2l_raw.p, ls.m2l_sorted.p, n_m2l, 0, end_bit, s));
     count_launch();
   }
-  k_csr<<<grid_for(n_p2p + 1, 256), 256, 0, s>>>(ls.p2p_sorted.p, n_p2p, ncells_t, p2p_start, p2p_src, nbody_t, interactions);
+  k_csr<<<grid_for(n_p2p + 1, 256), 256, 0, s>>>(ls.p2p_sorted.p, n_p2p, ls.key_bits, ncells_t, p2p_start, p2p_src, nbody_t, interactions);
   count_launch();
-  k_csr<<<grid_for(n_m2l + 1, 256), 256, 0, s>>>(ls.m2l_sorted.p, n_m2l, ncells_t, m2l_start, m2l_src, nullptr, nullptr);
+  k_csr<<<grid_for(n_m2l + 1, 256), 256, 0, s>>>(ls.m2l_sorted.p, n_m2l, ls.key_bits, ncells_t, m2l_start, m2l_src, nullptr, nullptr);
   count_launch();
   VFMM_LAUNCH_CHECK();
 }

@@ -140,9 +140,10 @@ struct ListScratch {
   DevBuf<unsigned long long> p2p_raw, m2l_raw, p2p_sorted, m2l_sorted;
   DevBuf<unsigned char>      cub_tmp;
   size_t                     cub_bytes = 0;
+  int                        key_bits  = 32; // pair key = target << key_bits | source
 };
-void traverse(cudaStream_t s, CellsView tc, CellsView sc, int ntc, int maxLevelT, int maxLevelS, double theta, DevInfo *info, ListScratch &ls,
-              size_t cap_front, size_t cap_p2p, size_t cap_m2l);
+void traverse(cudaStream_t s, CellsView tc, CellsView sc, int ntc, int nsc, int maxLevelT, int maxLevelS, double theta, DevInfo *info,
+              ListScratch &ls, size_t cap_front, size_t cap_p2p, size_t cap_m2l);
 void lists_to_csr(cudaStream_t s, ListScratch &ls, int n_p2p, int n_m2l, int ncells_t, int cell_bits, int *p2p_start, int *p2p_src, int *m2l_start,
                   int *m2l_src, const int *nbody_t, unsigned long long *interactions);
 
