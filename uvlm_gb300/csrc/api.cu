@@ -98,7 +98,7 @@ struct vfmm_handle_s {
   // expansions
   DevBuf<double2> M, L, Mprep;
   DevBuf<int4>    items, items32, lanes32;
-  int             m2l_batch = 16; // sources per mixed-M2L batch (32 for p <= 10); VFMM_M2L_BATCH = 8, 16 or 32 overrides
+  int             m2l_batch = 16; // sources per mixed-M2L batch (32 for p <= 10); VFMM_M2L_BATCH = 8, 16, 24 or 32 overrides
   int             items_P = 0, items_per_lane = 0;
   DevBuf<float2>  Mp32;
   DevBuf<float4>  pos32, alp32;
@@ -310,8 +310,9 @@ void ensure_items(vfmm_handle h)
   h->items32.reserve(tab32.size());
   VFMM_CUDA_TRY(cudaMemcpy(h->items32.p, tab32.data(), tab32.size() * sizeof(int4), cudaMemcpyHostToDevice));
   const char *sb = getenv("VFMM_M2L_BATCH");
-  // 32 sources per batch while two blocks still fit an SM's shared memory (p <= 10), else 16
-  h->m2l_batch = sb && (atoi(sb) == 8 || atoi(sb) == 16 || atoi(sb) == 32) ? atoi(sb) : (h->cfg.p <= 10 ? 32 : 16);
+  // sources per batch, measured best on GB300: 32 for p <= 10, 24 for p = 11-12, else 16
+  const int def  = h->cfg.p <= 10 ? 32 : (h->cfg.p <= 12 ? 24 : 16);
+  h->m2l_batch   = sb && (atoi(sb) == 8 || atoi(sb) == 16 || atoi(sb) == 24 || atoi(sb) == 32) ? atoi(sb) : def;
   auto lt32      = m2l_lane_table(h->cfg.p, m2l_half_width(h->cfg.p), h->m2l_batch); // half-tile width and batch of k_m2l32v2
   h->lanes32.reserve(lt32.size());
   VFMM_CUDA_TRY(cudaMemcpy(h->lanes32.p, lt32.data(), lt32.size() * sizeof(int4), cudaMemcpyHostToDevice));

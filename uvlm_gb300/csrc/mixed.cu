@@ -876,6 +876,8 @@ static void m2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   count_launch();
   if (m.m2l_batch == 32)
     m2l32_launch<P, 32>(s, d, e, m);
+  else if (m.m2l_batch == 24)
+    m2l32_launch<P, 24>(s, d, e, m);
   else if (m.m2l_batch == 8)
     m2l32_launch<P, 8>(s, d, e, m);
   else
