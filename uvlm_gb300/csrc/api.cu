@@ -98,7 +98,7 @@ struct vfmm_handle_s {
   // expansions
   DevBuf<double2> M, L, Mprep;
   DevBuf<int4>    items, items32, lanes32;
-  int             m2l_batch = 16; // sources per mixed-M2L batch (32 for p <= 10); VFMM_M2L_BATCH = 8, 16, 24 or 32 overrides
+  int             m2l_batch = 16; // sources per mixed-M2L batch (set per p); VFMM_M2L_BATCH = 8, 16, 24 or 32 overrides
   int             items_P = 0, items_per_lane = 0;
   DevBuf<float2>  Mp32;
   DevBuf<float4>  pos32, alp32;
