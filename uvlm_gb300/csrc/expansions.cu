@@ -14,6 +14,8 @@ namespace vfmm {
 
 typedef cx<double> zd;
 
+static __constant__ HarmRecip<double> kHarmRecipD = make_harm_recip<double>();
+
 __device__ __forceinline__ zd ldz(const double2 *p)
 {
   const double2 v = *p;
@@ -423,12 +425,13 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(DevExp a, double *out)
         zd diag{1.0, 0.0};
         for (int m = 0; m < D1; m++) {
           if (m > 0) {
-            const double s = 1.0 / double(2 * m);
+            const double s = kHarmRecipD.s[m];
             diag           = {(diag.r * x - diag.i * y) * s, (diag.r * y + diag.i * x) * s};
           }
           const double w  = m == 0 ? 1.0 : 2.0;
           zd           ya = diag, yb{0, 0};
-          for (int n = m; n < D1; n++) {
+          double       tn = double(2 * m + 1); // 2n + 1
+          for (int n = m; n < D1; n++, tn += 2.0) {
             const int t = tri(n, m);
             for (int ax = 0; ax < 3; ax++) {
               const zd u = U[t * 3 + ax];
@@ -439,8 +442,8 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(DevExp a, double *out)
                 const zd u = JJ[t * 9 + ae];
                 f[3 + ae] += w * (u.r * ya.r - u.i * ya.i);
               }
-            const double cc = -1.0 / double((n + m + 1) * (n - m + 1));
-            const double zz = double(2 * n + 1) * z;
+            const double cc = kHarmRecipD.c[t];
+            const double zz = tn * z;
             const zd     nx = {cc * (zz * ya.r + r2 * yb.r), cc * (zz * ya.i + r2 * yb.i)};
             yb              = ya;
             ya              = nx;

@@ -98,6 +98,26 @@ __device__ __forceinline__ void singular_column(int m, T x, T y, T z, T inv_r2, 
   singular_column_emit<T, NDEG>(m, x, y, z, inv_r2, S00, [&](int n, cx<T> v) { out[n] = v; });
 }
 
+// Reciprocals used by the regular-harmonic recurrence when it runs with
+// runtime indices: c[tri(n, m)] = -1 / ((n+m+1)(n-m+1)) and s[m] = 1 / (2m),
+// n < 16.  Correctly rounded like the divisions they replace.
+template <class T>
+struct HarmRecip {
+  T c[nterms(16)];
+  T s[17];
+};
+template <class T>
+constexpr HarmRecip<T> make_harm_recip()
+{
+  HarmRecip<T> r{};
+  for (int n = 0; n < 16; n++)
+    for (int m = 0; m <= n; m++)
+      r.c[tri(n, m)] = T(-1) / T((n + m + 1) * (n - m + 1));
+  for (int m = 1; m < 17; m++)
+    r.s[m] = T(1) / T(2 * m);
+  return r;
+}
+
 template <class T>
 __device__ __forceinline__ cx<T> neg_if(cx<T> v, bool neg) { return neg ? cx<T>{-v.r, -v.i} : v; }
 

@@ -26,6 +26,8 @@ namespace vfmm {
 typedef cx<float>  zf;
 typedef cx<double> zd;
 
+static __constant__ HarmRecip<float> kHarmRecipF = make_harm_recip<float>();
+
 struct DevMixed {
   CellsView     cv;
   const double *soa;
@@ -294,6 +296,7 @@ __device__ __forceinline__ float scale2f(float v, int e)
 template <int P, int SB>
 struct M2LV2 {
   static constexpr int KH = m2l_half_width(P); // k columns per half-tile
+  static_assert(KH >= 2, "the two-step window update assumes KH >= 2");
   static constexpr int K = nterms(P), PP = P * P;
   static constexpr int MSTR = 3 * PP + 1;            // complex stride of a staged multipole
   static constexpr int YSTR = PP + M2L_YOFF + 1;     // complex stride of a staged harmonic table
@@ -398,31 +401,52 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
           const zf *YA = Ys + b * YSTR + baseA;
           const zf *YB = Ys + b * YSTR + baseB;
           const zf *Mb = Ms + b * MSTR + (n * n + n) * 3;
-          zf        ya[KH], yb[KH];
+          // windows ya[kk] = YA[m - kk], yb[kk] = YB[m - kk] of the current m
+          zf ya[KH], yb[KH];
 #pragma unroll
           for (int kk = 0; kk < KH; kk++) {
             ya[kk] = YA[-n - kk];
             yb[kk] = YB[-n - kk];
           }
-          for (int m = -n; m <= n; m++) {
+          // one step: column kk of each half-tile takes M'_n^m S'_{q}^{m-k0-kk}
+          auto step = [&](int m, const zf (&wa)[KH], const zf (&wb)[KH]) {
             const zf m0 = Mb[m * 3 + 0], m1 = Mb[m * 3 + 1], m2 = Mb[m * 3 + 2];
 #pragma unroll
             for (int kk = 0; kk < KH; kk++) {
-              cfma(accA[kk][0], m0, ya[kk]);
-              cfma(accA[kk][1], m1, ya[kk]);
-              cfma(accA[kk][2], m2, ya[kk]);
-              cfma(accB[kk][0], m0, yb[kk]);
-              cfma(accB[kk][1], m1, yb[kk]);
-              cfma(accB[kk][2], m2, yb[kk]);
+              cfma(accA[kk][0], m0, wa[kk]);
+              cfma(accA[kk][1], m1, wa[kk]);
+              cfma(accA[kk][2], m2, wa[kk]);
+              cfma(accB[kk][0], m0, wb[kk]);
+              cfma(accB[kk][1], m1, wb[kk]);
+              cfma(accB[kk][2], m2, wb[kk]);
             }
-            if (m < n) {
+          };
+          step(-n, ya, yb);
+          // the remaining 2n steps two at a time (m + 1, m + 2)
+          for (int m = -n; m < n; m += 2) {
+            zf wa1[KH], wb1[KH], wa2[KH], wb2[KH];
+            wa1[0] = YA[m + 1];
+            wb1[0] = YB[m + 1];
+            wa2[0] = YA[m + 2];
+            wb2[0] = YB[m + 2];
+            wa2[1] = wa1[0];
+            wb2[1] = wb1[0];
 #pragma unroll
-              for (int kk = KH - 1; kk > 0; kk--) {
-                ya[kk] = ya[kk - 1];
-                yb[kk] = yb[kk - 1];
-              }
-              ya[0] = YA[m + 1];
-              yb[0] = YB[m + 1];
+            for (int kk = 1; kk < KH; kk++) {
+              wa1[kk] = ya[kk - 1];
+              wb1[kk] = yb[kk - 1];
+            }
+#pragma unroll
+            for (int kk = 2; kk < KH; kk++) {
+              wa2[kk] = ya[kk - 2];
+              wb2[kk] = yb[kk - 2];
+            }
+            step(m + 1, wa1, wb1);
+            step(m + 2, wa2, wb2);
+#pragma unroll
+            for (int kk = 0; kk < KH; kk++) {
+              ya[kk] = wa2[kk];
+              yb[kk] = wb2[kk];
             }
           }
         }
@@ -663,17 +687,20 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
         float       f[12];
         for (int k = 0; k < 12; k++)
           f[k] = 0.f;
-        zf diag{1.f, 0.f};
-        for (int m = 0; m < D1; m++) {
+        zf  diag{1.f, 0.f};
+        int turn = g; // this member evaluates the columns m with m = g (mod Gt)
+        for (int m = 0; m < D1; m++, turn--) {
           if (m > 0) {
-            const float sc = 1.f / float(2 * m);
+            const float sc = kHarmRecipF.s[m];
             diag           = {(diag.r * x - diag.i * y) * sc, (diag.r * y + diag.i * x) * sc};
           }
-          if ((m - g) % Gt != 0)
+          if (turn != 0)
             continue;
-          const float w  = m == 0 ? 1.f : 2.f;
+          turn          = Gt;
+          const float w = m == 0 ? 1.f : 2.f;
           zf          ya = diag, yb{0.f, 0.f};
-          for (int n = m; n < D1; n++) {
+          float       tn = float(2 * m + 1); // 2n + 1
+          for (int n = m; n < D1; n++, tn += 2.f) {
             const int t = tri(n, m);
             for (int ax = 0; ax < 3; ax++) {
               const zf u = U[t * 3 + ax];
@@ -684,8 +711,8 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
                 const zf u = JJ[t * 9 + ae];
                 f[3 + ae] += w * (u.r * ya.r - u.i * ya.i);
               }
-            const float cc = -1.f / float((n + m + 1) * (n - m + 1));
-            const float zz = float(2 * n + 1) * z;
+            const float cc = kHarmRecipF.c[t];
+            const float zz = tn * z;
             const zf    nx = {cc * (zz * ya.r + r2 * yb.r), cc * (zz * ya.i + r2 * yb.i)};
             yb             = ya;
             ya             = nx;
