@@ -43,7 +43,7 @@ def oracle() -> ctypes.CDLL:
         L.vo_build_tree.restype = _L
         L.vo_lists.argtypes = [_vp, _vp, _d, _vp, _L, _PL, _vp, _L, _PL]
         L.vo_calculate.argtypes = [_vp, _L, _i, _i, _d, _i, _i, _vp, _vp, _L, _PL]
-        L.vo_advance.argtypes = [_vp, _L, _i, _i, _d, _d, _i, _i, _i, _i, _d, _i]
+        L.vo_advance.argtypes = [_vp, _L, _i, _i, _d, _d, _i, _i, _i, _i, _d, _i, _i, _d]
         L.vo_sensors.argtypes = [_vp, _L, _vp, _L, _i, _i, _d]
         L.vo_direct.argtypes = [_vp, _L, _vp, _L]
         L.vo_direct.restype = None
@@ -70,6 +70,7 @@ def ref(P: int, ncrit: int, theta: float) -> ctypes.CDLL:
     L.ref_calculate.argtypes = [_vp, _L, _i, _i, _vp, _vp, _L, _PL]
     L.ref_advance.argtypes = [_vp, _L, _d, _i, _i, _i]
     L.ref_sensors.argtypes = [_vp, _L, _vp, _L]
+    L.ref_advance_viscous.argtypes = [_vp, _L, _d, _i, _i, _i, _d]
     L.ref_direct.argtypes = [_vp, _L, _vp, _L]
     L.ref_direct.restype = None
     return L
@@ -121,10 +122,11 @@ def calculate(bodies: np.ndarray, P: int, ncrit: int, theta: float, stretching: 
 
 
 def advance(bodies: np.ndarray, P: int, ncrit: int, theta: float, dt: float, steps: int, scheme: int,
-            stretching: int = 0, formulation: int = 0, relax: float = 0.0, rk4_fixed: int = 0) -> np.ndarray:
+            stretching: int = 0, formulation: int = 0, relax: float = 0.0, rk4_fixed: int = 0, viscous: int = 0,
+            nu: float = 0.0) -> np.ndarray:
     b = bodies.copy()
     rc = oracle().vo_advance(b.ctypes.data, b.size, P, ncrit, theta, dt, steps, scheme, stretching, formulation,
-                             relax, rk4_fixed)
+                             relax, rk4_fixed, viscous, nu)
     if rc != 0:
         raise RuntimeError(f"oracle advance failed ({rc})")
     return b

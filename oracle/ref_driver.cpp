@@ -167,6 +167,40 @@ int ref_advance(void *bodies, long n, double dt, int steps, int scheme, int stre
   return -1;
 }
 
+// FMMCalculator::advance with a viscous scheme (fmmCalculator.hpp:713-724,
+// called after every calculate): viscous 1 = Vortex::PSE (multipoleKernels.hpp:
+// 415-450), 2 = Vortex::CSM (fmmCalculator.hpp:334-337).  The reference never
+// sets its viscosity member _nu (fmmCalculator.hpp:56); it is set here.
+// Transposed stretching, cVPM.
+int ref_advance_viscous(void *bodies, long n, double dt, int steps, int scheme, int viscous, double nu)
+{
+  auto run = [&](auto tag_scheme, auto tag_visc) {
+    using S = decltype(tag_scheme);
+    using V = decltype(tag_visc);
+    Bodies b = load(bodies, n);
+    Vortex::FMMCalculator<Host, Device, S, V, Vortex::cVPM, Vortex::Transposed> calc;
+    calc._nu = nu;
+    for (int s = 0; s < steps; s++)
+      calc.advance(b, dt);
+    store(bodies, b);
+    return 0;
+  };
+  auto by_scheme = [&](auto tag_visc) {
+    switch (scheme) {
+    case 0: return run(Vortex::Euler{}, tag_visc);
+    case 1: return run(Vortex::RK2{}, tag_visc);
+    case 2: return run(Vortex::RK3{}, tag_visc);
+    case 3: return run(Vortex::RK4{}, tag_visc);
+    }
+    return -1;
+  };
+  if (viscous == 1)
+    return by_scheme(Vortex::PSE{});
+  if (viscous == 2)
+    return by_scheme(Vortex::CSM{});
+  return -1;
+}
+
 // init + calculate on the particles, then getSensorData (fmmCalculator.hpp:726-731).
 int ref_sensors(void *bodies, long n, void *sensors, long ns)
 {

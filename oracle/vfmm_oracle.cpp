@@ -374,6 +374,61 @@ struct FMM {
     L.assign(cells.size() * 3 * K, cd(0, 0));
   }
 
+  // calculateViscosity (fmmCalculator.hpp:713-724), after calculate.
+  // kind 1, PSE (multipoleKernels.hpp:415-450): over the P2P pairs, per target i
+  // and source leaf, sum (vol_i alpha_j - vol_j alpha_i) e^{-R^2/(2 s^2)} / s^5 with
+  // s^2 = sigma_i^2 + sigma_j^2 over R^2 != 0, and add it times
+  // nu / sqrt(2) / pi / sqrt(pi) to dadt_i.  kind 2, CSM (fmmCalculator.hpp:334-337):
+  // drdt += (sqrt(sigma^2 + 2 nu dt) - sigma) / dt.
+  void viscosity(Body *b, long n, int kind, double nu, double dt)
+  {
+    if (kind == 2) {
+#pragma omp parallel for
+      for (long i = 0; i < n; i++)
+        b[i].drdt += (std::sqrt((b[i].radius * b[i].radius) + (2.0 * nu * dt)) - b[i].radius) / dt;
+      return;
+    }
+    if (kind != 1)
+      return;
+    const long        nc = (long)cells.size();
+    std::vector<long> start(nc + 1, 0);
+    for (auto &pr : p2p)
+      start[pr.first + 1]++;
+    for (long c = 0; c < nc; c++)
+      start[c + 1] += start[c];
+    std::vector<long> src(p2p.size()), fill(start.begin(), start.end() - 1);
+    for (auto &pr : p2p)
+      src[fill[pr.first]++] = (long)pr.second;
+    const double sqrt2  = 1.41421356237309504880168872420969808;
+    const double pi     = 3.14159265358979323846264338327950288;
+    const double prefix = nu / sqrt2 * inv_pi * inv_sqrtpi;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long c = 0; c < nc; c++)
+      for (long q = start[c]; q < start[c + 1]; q++) {
+        const Cell &S = cells[src[q]];
+        for (uint64_t i = cells[c].BodyOffset; i < cells[c].BodyOffset + cells[c].NBODY; i++) {
+          double sum[3] = {0, 0, 0};
+          for (uint64_t j = S.BodyOffset; j < S.BodyOffset + S.NBODY; j++) {
+            double dX[3];
+            for (int d = 0; d < 3; d++)
+              dX[d] = b[i].X[d] - b[j].X[d];
+            const double R2 = dX[0] * dX[0] + dX[1] * dX[1] + dX[2] * dX[2];
+            if (R2 != 0) {
+              const double oo    = 1. / (b[i].radius * b[i].radius + b[j].radius * b[j].radius);
+              const double s5    = oo * oo * std::sqrt(oo);
+              const double vol_i = 4. / 3. * pi * b[i].radius * b[i].radius * b[i].radius;
+              const double vol_j = 4. / 3. * pi * b[j].radius * b[j].radius * b[j].radius;
+              const double e     = std::exp(-0.5 * R2 * oo);
+              for (int d = 0; d < 3; d++)
+                sum[d] += (vol_i * b[j].alpha[d] - vol_j * b[i].alpha[d]) * e * s5;
+            }
+          }
+          for (int d = 0; d < 3; d++)
+            b[i].dadt[d] += sum[d] * prefix;
+        }
+      }
+  }
+
   // P2M, multipoleKernels.hpp:452-477
   void P2M(long c, const Body *b)
   {
@@ -894,9 +949,10 @@ int vo_calculate(Body *bodies, long n, int P, int ncrit, double theta, int stret
 
 // FMMCalculator::advance (fmmCalculator.hpp:919-1005) `steps` times; scheme 0
 // Euler, 1 RK2, 2 RK3, 3 RK4; rk4_fixed=1 uses dt (not 0.5 dt) in RK4 stage 3;
-// relax_f > 0 applies relaxation after each step with the last stage's J.
+// relax_f > 0 applies relaxation after each step with the last stage's J;
+// viscous 1 PSE / 2 CSM with viscosity nu after every calculate.
 int vo_advance(Body *b, long n, int P, int ncrit, double theta, double dt, int steps, int scheme, int stretching, int formulation, double relax_f,
-               int rk4_fixed)
+               int rk4_fixed, int viscous, double nu)
 {
   FMM f(P, ncrit, theta);
   f.stretching  = stretching;
@@ -906,6 +962,7 @@ int vo_advance(Body *b, long n, int P, int ncrit, double theta, double dt, int s
     if (!f.ok)
       return false;
     f.calculate(b, n);
+    f.viscosity(b, n, viscous, nu, dt);
 #pragma omp parallel for
     for (long i = 0; i < n; i++)
       update(b[i]);
@@ -922,6 +979,7 @@ int vo_advance(Body *b, long n, int P, int ncrit, double theta, double dt, int s
       for (long i = 0; i < n; i++)
         storeInitialState(b[i]);
       f.calculate(b, n);
+      f.viscosity(b, n, viscous, nu, dt);
       for (long i = 0; i < n; i++)
         stepRK21(b[i], dt);
       ok = stage([&](Body &q) { stepRK22(q, dt); });
@@ -935,6 +993,7 @@ int vo_advance(Body *b, long n, int P, int ncrit, double theta, double dt, int s
       for (long i = 0; i < n; i++)
         storeInitialState(b[i]);
       f.calculate(b, n);
+      f.viscosity(b, n, viscous, nu, dt);
       for (long i = 0; i < n; i++)
         stepRK41(b[i], dt);
       ok = stage([&](Body &q) { stepRK4mid(q, dt, 0.5); }) && stage([&](Body &q) { stepRK4mid(q, dt, rk4_fixed ? 1.0 : 0.5); }) &&

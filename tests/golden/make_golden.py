@@ -10,7 +10,7 @@ committed and read by the tests everywhere.
 Each body carries its input index in `drdt_old`, a field the evaluation never
 touches, so the tree permutation can be read from the permuted output.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [viscous]   (viscous: only the viscous cases)
 """
 from __future__ import annotations
 
@@ -112,6 +112,23 @@ def advance_case(name, b, P, ncrit, theta, dt, steps, scheme, stretching=0):
          out_J=out["J"])
 
 
+def viscous_case(name, b, P, ncrit, theta, dt, steps, scheme, viscous, nu):
+    """advance with Vortex::PSE (viscous 1) or Vortex::CSM (2), viscosity nu."""
+    R = O.ref(P, ncrit, theta)
+    out = b.copy()
+    rc = R.ref_advance_viscous(out.ctypes.data, out.size, dt, steps, scheme, viscous, nu)
+    assert rc == 0
+    save(name, P=P, ncrit=ncrit, theta=theta, dt=dt, steps=steps, scheme=scheme, stretching=0, viscous=viscous, nu=nu,
+         **inputs_of(b), out_X=out["X"], out_alpha=out["alpha"], out_radius=out["radius"], out_velocity=out["velocity"],
+         out_J=out["J"])
+
+
+def viscous_cases():
+    viscous_case("advance_pse_cloud", workloads.cloud(700, seed=14), 6, 16, 0.5, 0.05, 2, 1, 1, 0.01)
+    viscous_case("advance_pse_rk3_ring", workloads.ring(8, seed=15), 6, 32, 0.5, 0.01, 1, 2, 1, 0.005)
+    viscous_case("advance_csm_cloud", workloads.cloud(600, seed=16), 6, 16, 0.5, 0.05, 2, 1, 2, 0.01)
+
+
 def sensor_case(name, b, s, P, ncrit, theta):
     R = O.ref(P, ncrit, theta)
     bb, ss = b.copy(), s.copy()
@@ -156,4 +173,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["viscous"]:
+        viscous_cases()
+    else:
+        main()
+        viscous_cases()

@@ -63,6 +63,17 @@ def test_advance(name):
         assert rel(out[f], d["out_" + f]) < 1e-11, f
 
 
+@pytest.mark.parametrize("name", ["advance_pse_cloud", "advance_pse_rk3_ring", "advance_csm_cloud"])
+def test_advance_viscous(name):
+    """PSE and CSM viscous schemes (calculateViscosity, fmmCalculator.hpp:713-724)."""
+    d = golden(name)
+    b = golden_bodies(d)
+    out = O.advance(b, int(d["P"]), int(d["ncrit"]), float(d["theta"]), float(d["dt"]), int(d["steps"]), int(d["scheme"]),
+                    viscous=int(d["viscous"]), nu=float(d["nu"]))
+    for f in ["X", "alpha", "radius", "velocity", "J"]:
+        assert rel(out[f], d["out_" + f]) < 1e-11, f
+
+
 def test_sensors():
     d = golden("sensors_p6")
     b = golden_bodies(d)
