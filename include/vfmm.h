@@ -47,6 +47,8 @@ enum { VFMM_EULER = 0, VFMM_RK2 = 1, VFMM_RK3 = 2, VFMM_RK4 = 3 };
 enum { VFMM_TRANSPOSED = 0, VFMM_CLASSIC = 1 };
 /* VPM formulation: Vortex::cVPM / rVPM (fmmCalculator.hpp:19-20). */
 enum { VFMM_CVPM = 0, VFMM_RVPM = 1 };
+/* Viscous scheme: Vortex::Inviscid / PSE / CSM (fmmCalculator.hpp:11-12, 713-724). */
+enum { VFMM_INVISCID = 0, VFMM_PSE = 1, VFMM_CSM = 2 };
 /* Arithmetic of the evaluation: FP64 throughout (the drop-in), or mixed
  * (FP32 P2P with compensated sums, FP32 P2M/M2M/M2L/L2L/L2P with per-cell
  * scaling, FP64 tree and FP64 expansion arrays between the kernels). */
@@ -63,7 +65,10 @@ typedef struct {
   double relax;       /* relaxation factor f in [0,1]; 0 = off (relaxation.hpp:8-19) */
   int    rk4_fixed;   /* 1: RK4 stage 3 uses dt; 0: 0.5*dt as the reference (fmmCalculator.hpp:683-689) */
   int    device;      /* CUDA device ordinal; -1 = the caller's current device */
-  int    reserved[6];
+  int    viscous;     /* VFMM_INVISCID, VFMM_PSE or VFMM_CSM, applied after every evaluation of a stage */
+  int    reserved0;
+  double nu;          /* kinematic viscosity for PSE/CSM (the reference leaves its _nu unset, fmmCalculator.hpp:56) */
+  int    reserved[2];
 } vfmm_config;
 
 /* exafmm::Body (exafmmTypes.hpp:18-32), 296 bytes. J[a][b] = du_a/dx_b. */

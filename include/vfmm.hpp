@@ -65,10 +65,10 @@ public:
 
 template <typename Host, typename Device, typename IntegrationScheme, typename ViscousScheme, typename Formulation, typename Stretching>
 struct FMMCalculator {
-  static_assert(std::is_same<ViscousScheme, Inviscid>::value, "vfmm implements the Inviscid scheme only");
-
+  // nu: the viscosity of the PSE/CSM schemes, which the reference declares
+  // (fmmCalculator.hpp:56) but never sets
   explicit FMMCalculator(int p = exafmm::P, int ncrit = exafmm::ncrit, double theta = exafmm::MAC_theta, int precision = VFMM_FP64,
-                         double relax = 0.0)
+                         double relax = 0.0, double nu = 0.0)
   {
     vfmm_config c;
     vfmm_default_config(&c);
@@ -83,6 +83,8 @@ struct FMMCalculator {
                                                                   : VFMM_RK4;
     c.stretching  = std::is_same<Stretching, Classic>::value ? VFMM_CLASSIC : VFMM_TRANSPOSED;
     c.formulation = std::is_same<Formulation, rVPM>::value ? VFMM_RVPM : VFMM_CVPM;
+    c.viscous     = std::is_same<ViscousScheme, PSE>::value ? VFMM_PSE : (std::is_same<ViscousScheme, CSM>::value ? VFMM_CSM : VFMM_INVISCID);
+    c.nu          = nu;
     check(vfmm_create(&c, &h_), "vfmm_create");
   }
   ~FMMCalculator()

@@ -184,3 +184,38 @@ def test_mixed_matches_fp64_fmm(vfmm_lib, kind, n, P, ncrit):
     ed = rel_l2(out["mixed"]["dadt"], out["fp64"]["dadt"])
     print(f"{kind} n={n} P={P}: velocity {ev:.3e}  J {eJ:.3e}  dadt {ed:.3e}")
     assert ev < 1e-6 and eJ < 1e-6 and ed < 1e-6, (ev, eJ, ed)
+
+
+VISC = {"advance_pse_cloud": "PSE", "advance_pse_rk3_ring": "PSE", "advance_csm_cloud": "CSM"}
+
+
+@pytest.mark.parametrize("name", list(VISC))
+def test_advance_viscous_matches_reference(vfmm_lib, name):
+    """PSE and CSM (calculateViscosity, fmmCalculator.hpp:713-724) against the
+    reference's own advance with the viscosity set."""
+    d = golden(name)
+    b = golden_bodies(d)
+    with calc_for(d, integration=SCHEMES[int(d["scheme"])], viscous=VISC[name], nu=float(d["nu"])) as c:
+        for _ in range(int(d["steps"])):
+            c.advance(b, float(d["dt"]))
+    for f in ["X", "alpha", "radius", "velocity", "J"]:
+        assert rel(b[f], d["out_" + f]) < TOL, f
+
+
+def test_pse_mixed_matches_fp64(vfmm_lib):
+    """The FP32 PSE of the mixed mode against the FP64 one: the viscous part of
+    the strengths after one Euler stage (PSE run minus inviscid run), relative L2."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(30000, seed=17)
+    da = {}
+    for prec in ["fp64", "mixed"]:
+        out = {}
+        for visc in ["Inviscid", "PSE"]:
+            with FMMCalculator(p=8, ncrit=32, theta=0.5, integration="Euler", precision=prec, viscous=visc, nu=0.01) as c:
+                bb = b.copy()
+                c.advance(bb, 0.01)
+                out[visc] = bb
+        assert (out["PSE"]["X"] == out["Inviscid"]["X"]).all()  # same tree order
+        da[prec] = out["PSE"]["alpha"] - out["Inviscid"]["alpha"]
+    assert np.abs(da["fp64"]).max() > 0
+    assert rel_l2(da["mixed"], da["fp64"]) < 1e-5

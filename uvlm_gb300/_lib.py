@@ -38,13 +38,15 @@ EULER, RK2, RK3, RK4 = 0, 1, 2, 3
 TRANSPOSED, CLASSIC = 0, 1
 CVPM, RVPM = 0, 1
 FP64, MIXED = 0, 1
+INVISCID, PSE, CSM = 0, 1, 2
 
 
 class vfmm_config(ctypes.Structure):
     _fields_ = [("p", ctypes.c_int), ("ncrit", ctypes.c_int), ("theta", ctypes.c_double),
                 ("precision", ctypes.c_int), ("integrator", ctypes.c_int), ("stretching", ctypes.c_int),
                 ("formulation", ctypes.c_int), ("relax", ctypes.c_double), ("rk4_fixed", ctypes.c_int),
-                ("device", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+                ("device", ctypes.c_int), ("viscous", ctypes.c_int), ("reserved0", ctypes.c_int),
+                ("nu", ctypes.c_double), ("reserved", ctypes.c_int * 2)]
 
 
 class VfmmError(RuntimeError):

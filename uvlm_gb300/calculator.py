@@ -23,14 +23,14 @@ _SCHEMES = {"Euler": _lib.EULER, "RK2": _lib.RK2, "RK3": _lib.RK3, "RK4": _lib.R
 _STRETCH = {"Transposed": _lib.TRANSPOSED, "Classic": _lib.CLASSIC}
 _FORM = {"cVPM": _lib.CVPM, "rVPM": _lib.RVPM}
 _PREC = {"fp64": _lib.FP64, "mixed": _lib.MIXED}
+_VISC = {"Inviscid": _lib.INVISCID, "PSE": _lib.PSE, "CSM": _lib.CSM}
 
 
 class FMMCalculator:
     def __init__(self, p: int = 4, ncrit: int = 128, theta: float = 0.3, integration: str = "RK3",
                  viscous: str = "Inviscid", formulation: str = "cVPM", stretching: str = "Transposed",
-                 precision: str = "fp64", relax: float = 0.0, rk4_fixed: bool = False, device: int = -1):
-        if viscous != "Inviscid":
-            raise NotImplementedError("only the Inviscid scheme is implemented (PSE/CSM are not on this path)")
+                 precision: str = "fp64", relax: float = 0.0, rk4_fixed: bool = False, device: int = -1,
+                 nu: float = 0.0):
         cfg = _lib.vfmm_config()
         lib().vfmm_default_config(ctypes.byref(cfg))
         cfg.p, cfg.ncrit, cfg.theta = int(p), int(ncrit), float(theta)
@@ -41,6 +41,8 @@ class FMMCalculator:
         cfg.relax = float(relax)
         cfg.rk4_fixed = int(bool(rk4_fixed))
         cfg.device = int(device)
+        cfg.viscous = _VISC[viscous]
+        cfg.nu = float(nu)
         h = ctypes.c_void_p()
         code = lib().vfmm_create(ctypes.byref(cfg), ctypes.byref(h))
         if code != 0:

@@ -165,6 +165,10 @@ void validate(const vfmm_config &c)
     throw Error(VFMM_ERR_INVALID, "unknown formulation");
   if (c.relax < 0 || c.relax > 1)
     throw Error(VFMM_ERR_INVALID, "relax must be in [0, 1]");
+  if (c.viscous != VFMM_INVISCID && c.viscous != VFMM_PSE && c.viscous != VFMM_CSM)
+    throw Error(VFMM_ERR_INVALID, "unknown viscous scheme");
+  if (!(c.nu >= 0) || !(c.nu < 1e300))
+    throw Error(VFMM_ERR_INVALID, "nu must be finite and >= 0");
 }
 
 void ensure_bodies(vfmm_handle h, size_t n)
@@ -467,6 +471,8 @@ void stage_update(vfmm_handle h, int stage, double dt)
   a.do_update     = 1;
   a.dt            = dt;
   a.relax         = (stage == stages_of(a.scheme) - 1) ? h->cfg.relax : 0.0;
+  a.csm           = h->cfg.viscous == VFMM_CSM;
+  a.nu            = h->cfg.nu;
   finish_and_update(h->stream, h->soa[h->cur].p, h->cap, h->n, a);
   VFMM_CUDA_TRY(cudaEventRecord(h->ph[6], h->stream));
   h->ph_valid = true;
@@ -476,6 +482,9 @@ void run_stage(vfmm_handle h, int stage, double dt)
 {
   build_tree_and_lists(h);
   calculate(h);
+  if (h->cfg.viscous == VFMM_PSE) // calculateViscosity after calculate (fmmCalculator.hpp:713-724)
+    pse_pass(h->stream, particle_args(h), h->cfg.precision == VFMM_MIXED ? h->pos32.p : nullptr,
+             h->cfg.precision == VFMM_MIXED ? h->alp32.p : nullptr, h->cfg.nu, h->soa[h->cur].p);
   stage_update(h, stage, dt);
 }
 

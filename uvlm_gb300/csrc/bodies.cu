@@ -132,6 +132,8 @@ __global__ void k_stage_update(double *soa, size_t cap, int n, StageArgs a)
   const double h = a.dt;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     BodyRef q{soa, cap, i};
+    if (a.csm) // core spreading, fmmCalculator.hpp:334-337
+      q(F_DRDT) += (sqrt((q(F_R) * q(F_R)) + (2.0 * a.nu * h)) - q(F_R)) / h;
     if (a.do_update) {
       if (a.store_initial) { // storeInitialState, fmmCalculator.hpp:493-509
         for (int d = 0; d < 3; d++) {

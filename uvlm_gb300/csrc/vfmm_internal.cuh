@@ -157,7 +157,8 @@ void reset_rates(cudaStream_t s, double *soa, size_t cap, int n);
 // fmmCalculator.hpp:493-711; stretching/formulation complete the rates first.
 struct StageArgs {
   int    scheme, stage, stretching, formulation, rk4_fixed, store_initial, do_update;
-  double dt, relax;
+  int    csm; // add the core-spreading rate before the update (fmmCalculator.hpp:334-337)
+  double dt, relax, nu;
 };
 void finish_and_update(cudaStream_t s, double *soa, size_t cap, int n, const StageArgs &a);
 void relax_bodies(cudaStream_t s, double *soa, size_t cap, int n, double f);
@@ -220,6 +221,10 @@ void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
 void m2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m); // FP32, scaled
 void l2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m); // FP32, scaled
 void l2p_p2p_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out);
+
+// ---- viscous.cu: PSE over the P2P lists, added to dadt in soa (FP64 from the
+// soa fields when pos32 is null, else FP32 from the mixed-mode body records)
+void pse_pass(cudaStream_t s, const ExpArgs &e, const float4 *pos32, const float4 *alp32, double nu, double *soa);
 
 // ---- direct.cu
 void direct_sum(cudaStream_t s, const double *tx, const double *ty, const double *tz, int nt, const double *src, size_t scap, int ns, double *out /*12*nt*/);
