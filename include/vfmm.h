@@ -142,6 +142,16 @@ int vfmm_advance(vfmm_handle h, vfmm_body *bodies, size_t n, double dt);
  * VFMM_ERR_STATE before the first calculate/advance. */
 int vfmm_get_sensor_data(vfmm_handle h, vfmm_body *sensors, size_t n);
 
+/* FMMCalculator::RBF (fmmCalculator.hpp:856-917): re-interpolates the
+ * particles' vorticity onto new points.  The particles are permuted into their
+ * tree order (as init does); points whose vorticity is below 1e-6 in all three
+ * components are dropped; the first *m_out entries of `points` then hold the
+ * kept points in their tree order with alpha = the strengths that reproduce the
+ * vorticity (conjugate gradients, at most 100 iterations, squared residual
+ * 1e-10; *iterations, if not null, gets the count).  FP64.  Leaves the handle
+ * with the particles' tree and no evaluation. */
+int vfmm_rbf(vfmm_handle h, vfmm_body *particles, size_t n, vfmm_body *points, size_t m, size_t *m_out, int *iterations);
+
 /* Relaxation (relaxation.hpp:8-19, written 0-based) of the device bodies with
  * factor f, using the J of the last evaluation. */
 int vfmm_relax(vfmm_handle h, double f);

@@ -105,6 +105,13 @@ struct FMMCalculator {
   void advance(exafmm::Bodies &bodies, double dt) { check(vfmm_advance(h_, bodies.data(), bodies.size(), dt), "advance"); }
   // fmmCalculator.hpp:726
   void getSensorData(exafmm::Bodies &sensors) { check(vfmm_get_sensor_data(h_, sensors.data(), sensors.size()), "getSensorData"); }
+  // fmmCalculator.hpp:856 — vorticity re-interpolation; newPoints shrinks to the kept points
+  void RBF(exafmm::Bodies &particles, exafmm::Bodies &newPoints)
+  {
+    size_t kept = 0;
+    check(vfmm_rbf(h_, particles.data(), particles.size(), newPoints.data(), newPoints.size(), &kept, nullptr), "RBF");
+    newPoints.resize(kept);
+  }
   // relaxation.hpp:8 (the reference leaves it unwired)
   void relaxation(double f) { check(vfmm_relax(h_, f), "relaxation"); }
 

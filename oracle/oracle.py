@@ -60,7 +60,7 @@ def ref_available() -> bool:
 def ref(P: int, ncrit: int, theta: float) -> ctypes.CDLL:
     """The reference compiled for (P, ncrit, theta); builds it on first use."""
     so = os.path.join(HERE, "_ref", f"libref_p{P}_c{ncrit}_t{theta}.so")
-    if not os.path.exists(so):
+    if not os.path.exists(so) or ref_available():  # make rebuilds it when the driver or the shim changed
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_P={P}", f"REF_NCRIT={ncrit}", f"REF_THETA={theta}"], check=True)
     L = ctypes.CDLL(so)
     L.ref_build_tree.argtypes = [_vp, _L, _vp, _L]
@@ -71,6 +71,7 @@ def ref(P: int, ncrit: int, theta: float) -> ctypes.CDLL:
     L.ref_advance.argtypes = [_vp, _L, _d, _i, _i, _i]
     L.ref_sensors.argtypes = [_vp, _L, _vp, _L]
     L.ref_advance_viscous.argtypes = [_vp, _L, _d, _i, _i, _i, _d]
+    L.ref_rbf.argtypes = [_vp, _L, _vp, _L, _PL]
     L.ref_direct.argtypes = [_vp, _L, _vp, _L]
     L.ref_direct.restype = None
     return L

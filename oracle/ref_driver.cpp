@@ -201,6 +201,22 @@ int ref_advance_viscous(void *bodies, long n, double dt, int steps, int scheme, 
   return -1;
 }
 
+// FMMCalculator::RBF (fmmCalculator.hpp:856-917): vorticity of the particles
+// at the new points, points with |omega| < 1e-6 removed, CG for the point
+// strengths.  particles and points are permuted as the reference leaves them;
+// *m_out = points kept.  The reference prints its CG residuals to stdout.
+int ref_rbf(void *particles, long n, void *points, long m, long *m_out)
+{
+  Bodies p = load(particles, n);
+  Bodies q = load(points, m);
+  Calc<Vortex::RK2, Vortex::Transposed, Vortex::cVPM> calc;
+  calc.RBF(p, q);
+  store(particles, p);
+  store(points, q);
+  *m_out = (long)q.size();
+  return 0;
+}
+
 // init + calculate on the particles, then getSensorData (fmmCalculator.hpp:726-731).
 int ref_sensors(void *bodies, long n, void *sensors, long ns)
 {

@@ -10,7 +10,7 @@ committed and read by the tests everywhere.
 Each body carries its input index in `drdt_old`, a field the evaluation never
 touches, so the tree permutation can be read from the permuted output.
 
-Usage:  python tests/golden/make_golden.py [viscous]   (viscous: only the viscous cases)
+Usage:  python tests/golden/make_golden.py [viscous|rbf]   (only those cases)
 """
 from __future__ import annotations
 
@@ -129,6 +129,26 @@ def viscous_cases():
     viscous_case("advance_csm_cloud", workloads.cloud(600, seed=16), 6, 16, 0.5, 0.05, 2, 1, 2, 0.01)
 
 
+def rbf_case(name, b, lo, hi, k, rfac, P, ncrit, theta):
+    """FMMCalculator::RBF of particles b onto a k^3 lattice over [lo, hi]^3
+    with point radius rfac * spacing."""
+    R = O.ref(P, ncrit, theta)
+    g = np.linspace(lo, hi, k)
+    pts = np.zeros(k ** 3, BODY_DTYPE)
+    pts["X"] = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    pts["radius"] = rfac * (g[1] - g[0])
+    bb, pp, m = b.copy(), pts.copy(), ctypes.c_long()
+    assert R.ref_rbf(bb.ctypes.data, bb.size, pp.ctypes.data, pp.size, ctypes.byref(m)) == 0
+    pp = pp[:m.value]
+    save(name, P=P, ncrit=ncrit, theta=theta, **inputs_of(b), points_X=pts["X"], points_radius=pts["radius"],
+         out_particles_X=bb["X"], out_X=pp["X"], out_alpha=pp["alpha"], out_vorticity=pp["velocity_old"])
+
+
+def rbf_cases():
+    rbf_case("rbf_cloud", workloads.cloud(800, seed=18), -1.8, 1.8, 14, 0.6, 6, 16, 0.5)
+    rbf_case("rbf_ring_c32", workloads.ring(6, seed=19), -1.4, 1.4, 16, 0.5, 6, 32, 0.5)
+
+
 def sensor_case(name, b, s, P, ncrit, theta):
     R = O.ref(P, ncrit, theta)
     bb, ss = b.copy(), s.copy()
@@ -175,6 +195,9 @@ def main():
 if __name__ == "__main__":
     if sys.argv[1:] == ["viscous"]:
         viscous_cases()
+    elif sys.argv[1:] == ["rbf"]:
+        rbf_cases()
     else:
         main()
         viscous_cases()
+        rbf_cases()

@@ -94,6 +94,15 @@ class FMMCalculator:
         s = _lib.as_bodies(sensors)
         self._check(lib().vfmm_get_sensor_data(self._h, s.ctypes.data, s.size))
 
+    def RBF(self, particles: np.ndarray, points: np.ndarray) -> tuple[np.ndarray, int]:
+        """FMMCalculator::RBF: permutes `particles` into tree order (in place)
+        and returns (kept points with their new strengths, CG iterations)."""
+        p = _lib.as_bodies(particles)
+        q = _lib.as_bodies(points).copy()
+        m, it = ctypes.c_size_t(), ctypes.c_int()
+        self._check(lib().vfmm_rbf(self._h, p.ctypes.data, p.size, q.ctypes.data, q.size, ctypes.byref(m), ctypes.byref(it)))
+        return q[:m.value], it.value
+
     def relax(self, f: float) -> None:
         self._check(lib().vfmm_relax(self._h, float(f)))
 

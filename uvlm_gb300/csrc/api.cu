@@ -6,6 +6,7 @@
 // All work runs on the handle's stream; the host synchronises twice per
 // tree build (node counts, pair counts) and at the end of each API call.
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <exception>
@@ -404,14 +405,11 @@ void calculate(vfmm_handle h)
 // of the last calculate, the velocity-only P2P against the particles as they
 // are now, then L2L and L2P down the sensor tree.  The sensors come back in
 // sensor-tree order.  FP64 in both precision modes.
-void sensor_data(vfmm_handle h, vfmm_body *sens, size_t n)
+// Point sets (sensors, re-interpolation points) in ssoa[scur].
+void load_points(vfmm_handle h, const vfmm_body *pts, size_t n)
 {
-  if (!h->has_eval)
-    throw Error(VFMM_ERR_STATE, "sensor data needs the particles' multipoles: call calculate or advance first");
-  if (n == 0)
-    throw Error(VFMM_ERR_INVALID, "no sensors");
   if (n > (size_t)0x7fffffff)
-    throw Error(VFMM_ERR_INVALID, "too many sensors");
+    throw Error(VFMM_ERR_INVALID, "too many points");
   cudaStream_t s = h->stream;
   if (n > h->scap) {
     const size_t cap = n + n / 8 + 256;
@@ -423,8 +421,27 @@ void sensor_data(vfmm_handle h, vfmm_body *sens, size_t n)
   }
   h->aos.reserve(std::max(n, (size_t)h->n) * NFIELD);
   h->ns = (int)n;
-  VFMM_CUDA_TRY(cudaMemcpyAsync(h->aos.p, sens, n * sizeof(vfmm_body), cudaMemcpyHostToDevice, s));
+  VFMM_CUDA_TRY(cudaMemcpyAsync(h->aos.p, pts, n * sizeof(vfmm_body), cudaMemcpyHostToDevice, s));
   aos_to_soa(s, h->aos.p, h->ssoa[h->scur].p, h->scap, (int)n);
+}
+
+void points_to_host(vfmm_handle h, vfmm_body *pts, size_t n)
+{
+  soa_to_aos(h->stream, h->ssoa[h->scur].p, h->scap, h->aos.p, (int)n);
+  VFMM_CUDA_TRY(cudaMemcpyAsync(pts, h->aos.p, n * sizeof(vfmm_body), cudaMemcpyDeviceToHost, h->stream));
+  VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
+}
+
+void sensor_data(vfmm_handle h, vfmm_body *sens, size_t n)
+{
+  if (!h->has_eval)
+    throw Error(VFMM_ERR_STATE, "sensor data needs the particles' multipoles: call calculate or advance first");
+  if (n == 0)
+    throw Error(VFMM_ERR_INVALID, "no sensors");
+  if (n > (size_t)0x7fffffff)
+    throw Error(VFMM_ERR_INVALID, "too many sensors");
+  cudaStream_t s = h->stream;
+  load_points(h, sens, n);
   build_tree(s, h->ssoa, h->scur, h->scap, (int)n, h->cfg.ncrit, h->sinfo, h->shinfo, h->ts, h->stree);
   build_lists(s, h->stree, h->tree, h->cfg.theta, h->sinfo, h->shinfo, h->slists, nullptr);
 
@@ -454,9 +471,84 @@ void sensor_data(vfmm_handle h, vfmm_body *sens, size_t n)
   m2l_sensor_pass(s, se);
   downward_l2l(s, se);
   l2p_sensor_pass(s, se, h->ssoa[h->scur].p);
-  soa_to_aos(s, h->ssoa[h->scur].p, h->scap, h->aos.p, (int)n);
-  VFMM_CUDA_TRY(cudaMemcpyAsync(sens, h->aos.p, n * sizeof(vfmm_body), cudaMemcpyDeviceToHost, s));
-  VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+  points_to_host(h, sens, n);
+}
+
+// FMMCalculator::RBF (fmmCalculator.hpp:856-917), FP64: the particles' tree
+// (init) and a tree of the points with their lists against the particles;
+// the particles' vorticity at the points; points whose three components are
+// all below 1e-6 are dropped (host side, as the reference does); a tree of the
+// rest with point-to-point lists; strengths alpha = vorticity * volume as the
+// start, then at most 100 iterations of three component-wise conjugate
+// gradients (stop when every squared residual is below 1e-10).  Returns the
+// kept points (their count in *m_out) in their tree order, alpha = solution.
+void rbf(vfmm_handle h, vfmm_body *particles, size_t n, vfmm_body *points, size_t m, size_t *m_out, int *iterations)
+{
+  cudaStream_t s = h->stream;
+  upload(h, particles, n);
+  build_tree_and_lists(h);
+  download(h, particles, n); // init permutes the particles (tree.hpp:101-113)
+  load_points(h, points, m);
+  build_tree(s, h->ssoa, h->scur, h->scap, (int)m, h->cfg.ncrit, h->sinfo, h->shinfo, h->ts, h->stree);
+  build_lists(s, h->stree, h->tree, h->cfg.theta, h->sinfo, h->shinfo, h->slists, nullptr);
+  rbf_vorticity(s, h->stree.view(), h->stree.leaf_cells.p, h->stree.nleaves, h->slists.p2p_start.p, h->slists.p2p_src.p, h->ssoa[h->scur].p,
+                h->scap, h->tree.view(), h->soa[h->cur].p, h->cap, h->ssoa[h->scur].p, F_VOLD, 0);
+  std::vector<vfmm_body> pts(m);
+  points_to_host(h, pts.data(), m);
+  std::vector<vfmm_body> kept;
+  kept.reserve(m);
+  for (const auto &p : pts)
+    if (!(std::abs(p.velocity_old[0]) < 1e-6 && std::abs(p.velocity_old[1]) < 1e-6 && std::abs(p.velocity_old[2]) < 1e-6))
+      kept.push_back(p);
+  const size_t mk = kept.size();
+  *m_out          = mk;
+  if (iterations)
+    *iterations = 0;
+  if (mk == 0)
+    return;
+  load_points(h, kept.data(), mk);
+  build_tree(s, h->ssoa, h->scur, h->scap, (int)mk, h->cfg.ncrit, h->sinfo, h->shinfo, h->ts, h->stree);
+  build_lists(s, h->stree, h->stree, h->cfg.theta, h->sinfo, h->shinfo, h->slists, nullptr);
+  h->dtmp.reserve(RBF_PARTIALS + 8);
+  double *scratch = h->dtmp.p, *dsum = scratch + RBF_PARTIALS;
+  double *soa     = h->ssoa[h->scur].p;
+  auto    reduce  = [&](int op, const double *c, double out[3]) {
+    rbf_op(s, op, soa, h->scap, (int)mk, c, scratch, dsum);
+    VFMM_CUDA_TRY(cudaMemcpyAsync(h->shinfo->X0, dsum, 3 * sizeof(double), cudaMemcpyDeviceToHost, s)); // pinned staging
+    VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int d = 0; d < 3; d++)
+      out[d] = h->shinfo->X0[d];
+  };
+  auto apply = [&]() { // A p: the vorticity of the points' current strengths at the points
+    rbf_vorticity(s, h->stree.view(), h->stree.leaf_cells.p, h->stree.nleaves, h->slists.p2p_start.p, h->slists.p2p_src.p, soa, h->scap,
+                  h->stree.view(), soa, h->scap, soa, F_U, 1);
+  };
+  const double eps = 2.220446049250313080847263336181640625e-16, tol = 1e-10;
+  rbf_op(s, RBF_INIT_ALPHA, soa, h->scap, (int)mk, nullptr, scratch, nullptr);
+  apply();
+  double res[3], resn[3], pAp[3], c[3];
+  reduce(RBF_INIT_RESIDUAL, nullptr, res);
+  int it = 0;
+  for (; it < 100; it++) {
+    apply();
+    reduce(RBF_PAP, nullptr, pAp);
+    for (int d = 0; d < 3; d++)
+      c[d] = (res[d] > eps && std::abs(pAp[d]) > eps) ? res[d] / pAp[d] : 0.0;
+    rbf_op(s, RBF_UPDATE, soa, h->scap, (int)mk, c, scratch, nullptr);
+    reduce(RBF_RES_NORM, nullptr, resn);
+    if (resn[0] < tol && resn[1] < tol && resn[2] < tol)
+      break;
+    for (int d = 0; d < 3; d++) {
+      c[d]   = (resn[d] > eps && res[d] > eps) ? resn[d] / res[d] : 0.0;
+      res[d] = resn[d];
+    }
+    rbf_op(s, RBF_UPDATE_P, soa, h->scap, (int)mk, c, scratch, nullptr);
+  }
+  if (iterations)
+    *iterations = it;
+  rbf_op(s, RBF_STORE, soa, h->scap, (int)mk, nullptr, scratch, nullptr);
+  points_to_host(h, points, mk);
+  h->has_eval = false; // the particle tree is current, its expansions are not
 }
 
 void stage_update(vfmm_handle h, int stage, double dt)
@@ -651,6 +743,17 @@ int vfmm_get_sensor_data(vfmm_handle h, vfmm_body *sensors, size_t n)
     if (!sensors)
       throw Error(VFMM_ERR_INVALID, "null sensors");
     sensor_data(h, sensors, n);
+  });
+}
+
+int vfmm_rbf(vfmm_handle h, vfmm_body *particles, size_t n, vfmm_body *points, size_t m, size_t *m_out, int *iterations)
+{
+  return guarded(h, [&] {
+    if (!particles || !points || !m_out)
+      throw Error(VFMM_ERR_INVALID, "null argument");
+    if (m == 0)
+      throw Error(VFMM_ERR_INVALID, "no points");
+    rbf(h, particles, n, points, m, m_out, iterations);
   });
 }
 

@@ -226,6 +226,15 @@ void l2p_p2p_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double 
 // soa fields when pos32 is null, else FP32 from the mixed-mode body records)
 void pse_pass(cudaStream_t s, const ExpArgs &e, const float4 *pos32, const float4 *alp32, double nu, double *soa);
 
+// ---- rbf.cu: vorticity re-interpolation (FMMCalculator::RBF)
+enum RbfOp { RBF_INIT_ALPHA, RBF_INIT_RESIDUAL, RBF_PAP, RBF_UPDATE, RBF_RES_NORM, RBF_UPDATE_P, RBF_STORE };
+constexpr int RBF_PARTIALS = 152 * 2 * 3; // doubles of reduction scratch
+// out[field..field+2] of the targets = -(Gaussian vorticity of the sources over the P2P lists)
+void rbf_vorticity(cudaStream_t s, CellsView tc, const int *leaf_cells, int nleaves, const int *p2p_start, const int *p2p_src, const double *tsoa,
+                   size_t tcap, CellsView sc, const double *ssoa, size_t scap, double *out, int field, int zero_dadt);
+// one elementwise step over n bodies; with sums != null also its three component sums (device)
+void rbf_op(cudaStream_t s, int op, double *soa, size_t cap, int n, const double c[3], double *scratch, double *sums);
+
 // ---- direct.cu
 void direct_sum(cudaStream_t s, const double *tx, const double *ty, const double *tz, int nt, const double *src, size_t scap, int ns, double *out /*12*nt*/);
 
