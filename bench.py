@@ -57,6 +57,8 @@ def parse(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--out", default=None, help="also write the JSON line to this file")
+    ap.add_argument("--workload", default="cloud", choices=["cloud", "rings64"],
+                    help="cloud: the headline N = 2^20 cloud; rings64: 64 independent rings, batched")
     return ap.parse_args(argv)
 
 
@@ -381,11 +383,52 @@ def measure_accuracy(args, calc) -> dict:
     return acc
 
 
+def run_rings64(args, dist: Dist) -> dict | None:
+    """64 independent vortex rings (N log-uniform in [2k, 60k], random radius,
+    core, circulation and orientation), p = 8, theta = 0.5, leaf 32, RK2, one
+    step = one advance of every ring, through vfmm_advance_batch on host
+    arrays (copies included); the same systems advanced one after another on
+    the same handles are timed beside it."""
+    from uvlm_gb300 import FMMCalculator, advance_batch, workloads
+    systems = workloads.ring_batch(64, seed=7 + dist.rank)
+    ntot = sum(b.size for b in systems)
+    kw = dict(p=8, ncrit=32, theta=0.5, integration="RK2", precision=args.precision, device=dist.local_rank)
+    calcs = [FMMCalculator(**kw) for _ in systems]
+    work = [b.copy() for b in systems]
+    for _ in range(args.warmup):
+        advance_batch(calcs, work, args.dt)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        advance_batch(calcs, work, args.dt)
+    tb = dist.max(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for c, b in zip(calcs, work):
+            c.advance(b, args.dt)
+    ts = dist.max(time.perf_counter() - t0)
+    for c in calcs:
+        c.close()
+    if dist.rank != 0:
+        return None
+    evals = dist.world * ntot * 2 * args.steps  # RK2: two evaluations per step
+    return {"metric": "particle-evals/sec, 64 independent rings, batched advance", "value": evals / tb, "unit": UNIT,
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tb / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic (seeded rings; no dataset)",
+            "config": {"workload": "64 rings, N log-uniform [2k, 60k], RK2 step per ring", "bodies_total": ntot, "p": 8,
+                       "theta": 0.5, "ncrit": 32, "precision": args.precision, "timing": "host wall clock, copies included"},
+            "sequential": {"value": evals / ts, "ms_per_step": 1e3 * ts / args.steps,
+                           "note": "the same systems advanced one vfmm_advance after another"}}
+
+
 def main(argv=None):
     args = parse(argv)
     dist = Dist()
     if args.impl == "reference":
         line = run_reference(args, dist)
+    elif args.workload == "rings64":
+        line = run_rings64(args, dist)
     else:
         from uvlm_gb300 import _build, _lib
         if not os.path.exists(_lib.LIB_PATH):

@@ -134,6 +134,15 @@ int vfmm_copy_bodies_to_host(vfmm_handle h, vfmm_body *bodies, size_t n);
  * evaluation).  With relax > 0, relaxation follows the step (using that J). */
 int vfmm_advance(vfmm_handle h, vfmm_body *bodies, size_t n, double dt);
 
+/* advance (fmmCalculator.hpp:919-1005) for `count` independent systems at
+ * once: system b is bodies[b][0 .. n[b]) on handles[b] (distinct handles, each
+ * with its own configuration and stream).  Every system's stages run as in
+ * vfmm_advance and give the same results; the work of all systems is
+ * interleaved on the GPU.  On an error every handle's vfmm_last_error holds
+ * the message and the systems' states are unspecified.  No counterpart in the
+ * reference, which advances one system per calculator. */
+int vfmm_advance_batch(vfmm_handle *handles, vfmm_body *const *bodies, const size_t *n, int count, double dt);
+
 /* FMMCalculator::getSensorData (fmmCalculator.hpp:726-731): velocity at probe
  * points from the particles (multipoles of the last calculate, near field
  * from the particles as they are now); velocity and dadt are overwritten, the

@@ -172,3 +172,20 @@ def direct(targets: np.ndarray, sources: np.ndarray) -> np.ndarray:
 
 def new_bodies(n: int) -> np.ndarray:
     return np.zeros(n, BODY_DTYPE)
+
+
+def advance_batch(calculators: list, bodies: list, dt: float) -> None:
+    """vfmm_advance_batch: advance independent systems, bodies[b] on
+    calculators[b] (distinct), each array overwritten as advance does."""
+    bs = [_lib.as_bodies(b) for b in bodies]
+    k = len(bs)
+    if k != len(calculators) or k == 0:
+        raise ValueError("one calculator per body array")
+    hs = (ctypes.c_void_p * k)(*[c.handle for c in calculators])
+    ps = (ctypes.c_void_p * k)(*[b.ctypes.data for b in bs])
+    ns = (ctypes.c_size_t * k)(*[b.size for b in bs])
+    code = lib().vfmm_advance_batch(hs, ps, ns, k, float(dt))
+    if code != 0:
+        raise _lib.VfmmError(code, lib().vfmm_last_error(calculators[0].handle).decode())
+    for c, b in zip(calculators, bs):
+        c.n = b.size

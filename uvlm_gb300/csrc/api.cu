@@ -217,8 +217,8 @@ void read_info(vfmm_handle h) { read_info(h->stream, h->info, h->hinfo); }
 // Tree of the n bodies in soa[cur] (field-major, capacity cap).  The bodies
 // are gathered into tree order in soa[cur ^ 1] and cur flips, as buildTree
 // permutes its bodies (tree.hpp:101-113).  One host sync (node counts).
-void build_tree(cudaStream_t s, DevBuf<double> *soa, int &cur, size_t cap, int n, int ncrit, DevInfo *info, DevInfo *hinfo, TreeScratch &ts,
-                Tree &t)
+void tree_enqueue(cudaStream_t s, DevBuf<double> *soa, int &cur, size_t cap, int n, int ncrit, DevInfo *info, DevInfo *hinfo, TreeScratch &ts,
+                  Tree &t)
 {
   VFMM_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(DevInfo), s));
   check_finite(s, soa[cur].p, cap, n, info);
@@ -234,7 +234,13 @@ void build_tree(cudaStream_t s, DevBuf<double> *soa, int &cur, size_t cap, int n
   t.level_start.reserve(MAXL + 2);
   tree_build_cells(s, n, ncrit, nncap, info, ts, t.view(), t.level_cells.p, t.level_start.p, t.leaf_cells.p);
   VFMM_CUDA_TRY(cudaMemcpyAsync(t.level_start_host, t.level_start.p, sizeof(int) * (MAXL + 2), cudaMemcpyDeviceToHost, s));
-  read_info(s, info, hinfo);
+  VFMM_CUDA_TRY(cudaMemcpyAsync(hinfo, info, sizeof(DevInfo), cudaMemcpyDeviceToHost, s));
+}
+
+// Second half of a tree build: wait for the node counts, check them.
+void tree_finish(cudaStream_t s, DevInfo *hinfo, Tree &t)
+{
+  VFMM_CUDA_TRY(cudaStreamSynchronize(s));
   if (hinfo->nonfinite)
     throw Error(VFMM_ERR_NONFINITE, "non-finite position, strength or radius");
   if (hinfo->err)
@@ -247,11 +253,19 @@ void build_tree(cudaStream_t s, DevBuf<double> *soa, int &cur, size_t cap, int n
   t.R0       = hinfo->R0;
 }
 
+void build_tree(cudaStream_t s, DevBuf<double> *soa, int &cur, size_t cap, int n, int ncrit, DevInfo *info, DevInfo *hinfo, TreeScratch &ts,
+                Tree &t)
+{
+  tree_enqueue(s, soa, cur, cap, n, ncrit, info, hinfo, ts, t);
+  tree_finish(s, hinfo, t);
+}
+
 // Lists of the traversal of targets tt against sources st (traverse.hpp:
 // 32-85), growing the capacities until nothing overflows (one host sync per
 // attempt), then sorted into CSR rows.  interactions (device counter, may be
 // null) receives the body-body P2P count of a self traversal.
-void build_lists(cudaStream_t s, Tree &tt, Tree &st, double theta, DevInfo *info, DevInfo *hinfo, Lists &L, unsigned long long *interactions)
+// First half of a traversal: enqueue it and the copy of its pair counts.
+void lists_enqueue(cudaStream_t s, Tree &tt, Tree &st, double theta, DevInfo *info, DevInfo *hinfo, Lists &L)
 {
   if (L.cap_front == 0) {
     const size_t nc = (size_t)std::max(tt.ncells, st.ncells), nl = (size_t)std::max(tt.nleaves, st.nleaves);
@@ -259,22 +273,26 @@ void build_lists(cudaStream_t s, Tree &tt, Tree &st, double theta, DevInfo *info
     L.cap_p2p       = std::max<size_t>(4096, nl * 48);
     L.cap_m2l       = std::max<size_t>(4096, nc * 240);
   }
-  for (int attempt = 0;; attempt++) {
-    L.ls.front[0].reserve(L.cap_front);
-    L.ls.front[1].reserve(L.cap_front);
-    L.ls.p2p_raw.reserve(L.cap_p2p);
-    L.ls.m2l_raw.reserve(L.cap_m2l);
-    traverse(s, tt.view(), st.view(), tt.ncells, st.ncells, tt.maxLevel, st.maxLevel, theta, info, L.ls, L.ls.front[0].cap, L.ls.p2p_raw.cap,
-             L.ls.m2l_raw.cap);
-    read_info(s, info, hinfo);
-    if (!hinfo->overflow)
-      break;
-    if (attempt > 8)
-      throw Error(VFMM_ERR_CAPACITY, "interaction lists keep overflowing");
+  L.ls.front[0].reserve(L.cap_front);
+  L.ls.front[1].reserve(L.cap_front);
+  L.ls.p2p_raw.reserve(L.cap_p2p);
+  L.ls.m2l_raw.reserve(L.cap_m2l);
+  traverse(s, tt.view(), st.view(), tt.ncells, st.ncells, tt.maxLevel, st.maxLevel, theta, info, L.ls, L.ls.front[0].cap, L.ls.p2p_raw.cap,
+           L.ls.m2l_raw.cap);
+  VFMM_CUDA_TRY(cudaMemcpyAsync(hinfo, info, sizeof(DevInfo), cudaMemcpyDeviceToHost, s));
+}
+
+// Second half: wait for the pair counts.  On overflow the capacities grow and
+// false is returned (enqueue again); else the CSR rows are enqueued.
+bool lists_finish(cudaStream_t s, Tree &tt, DevInfo *info, DevInfo *hinfo, Lists &L, unsigned long long *interactions)
+{
+  VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hinfo->overflow) {
     L.cap_front = std::max(L.cap_front * 2, L.ls.front[0].cap * 2);
     L.cap_p2p   = std::max(L.cap_p2p * 2, L.ls.p2p_raw.cap * 2);
     L.cap_m2l   = std::max(L.cap_m2l * 2, L.ls.m2l_raw.cap * 2);
     VFMM_CUDA_TRY(cudaMemsetAsync(&info->overflow, 0, sizeof(int), s));
+    return false;
   }
   L.n_p2p = hinfo->n_p2p;
   L.n_m2l = hinfo->n_m2l;
@@ -286,6 +304,18 @@ void build_lists(cudaStream_t s, Tree &tt, Tree &st, double theta, DevInfo *info
     VFMM_CUDA_TRY(cudaMemsetAsync(interactions, 0, sizeof(unsigned long long), s));
   lists_to_csr(s, L.ls, L.n_p2p, L.n_m2l, tt.ncells, 32, L.p2p_start.p, L.p2p_src.p, L.m2l_start.p, L.m2l_src.p,
                interactions ? tt.nbody.p : nullptr, interactions);
+  return true;
+}
+
+void build_lists(cudaStream_t s, Tree &tt, Tree &st, double theta, DevInfo *info, DevInfo *hinfo, Lists &L, unsigned long long *interactions)
+{
+  for (int attempt = 0;; attempt++) {
+    if (attempt > 9)
+      throw Error(VFMM_ERR_CAPACITY, "interaction lists keep overflowing");
+    lists_enqueue(s, tt, st, theta, info, hinfo, L);
+    if (lists_finish(s, tt, info, hinfo, L, interactions))
+      break;
+  }
 }
 
 // Tree and lists of the bodies in soa[cur]; bodies are reordered into tree order.
@@ -570,14 +600,92 @@ void stage_update(vfmm_handle h, int stage, double dt)
   h->ph_valid = true;
 }
 
-void run_stage(vfmm_handle h, int stage, double dt)
+// Evaluation, viscosity and the stage update of a stage whose tree and lists
+// are built; all enqueued on the handle's stream.
+void evaluate_and_update(vfmm_handle h, int stage, double dt)
 {
-  build_tree_and_lists(h);
   calculate(h);
   if (h->cfg.viscous == VFMM_PSE) // calculateViscosity after calculate (fmmCalculator.hpp:713-724)
     pse_pass(h->stream, particle_args(h), h->cfg.precision == VFMM_MIXED ? h->pos32.p : nullptr,
              h->cfg.precision == VFMM_MIXED ? h->alp32.p : nullptr, h->cfg.nu, h->soa[h->cur].p);
   stage_update(h, stage, dt);
+}
+
+void run_stage(vfmm_handle h, int stage, double dt)
+{
+  build_tree_and_lists(h);
+  evaluate_and_update(h, stage, dt);
+}
+
+// advance for several independent systems, each on its own handle and
+// stream, scheduled phase by phase: every system's tree is enqueued before
+// any node count is awaited, every traversal before any pair count, then
+// every evaluation and update, so that small systems overlap on the GPU and
+// each synchronisation point is met once per batch, not once per system.
+void advance_batch(vfmm_handle *hs, vfmm_body *const *bodies, const size_t *ns, int count, double dt)
+{
+  auto on = [&](int b) {
+    VFMM_CUDA_TRY(cudaSetDevice(hs[b]->device));
+    g_launch_counter = &hs[b]->launches;
+  };
+  int S = 0;
+  for (int b = 0; b < count; b++) {
+    on(b);
+    upload(hs[b], bodies[b], ns[b]);
+    S = std::max(S, stages_of(hs[b]->cfg.integrator));
+  }
+  for (int st = 0; st < S; st++) {
+    std::vector<int> act;
+    for (int b = 0; b < count; b++)
+      if (st < stages_of(hs[b]->cfg.integrator))
+        act.push_back(b);
+    for (int b : act) {
+      on(b);
+      vfmm_handle h = hs[b];
+      h->has_tree = h->has_eval = false;
+      VFMM_CUDA_TRY(cudaEventRecord(h->ph[0], h->stream));
+      tree_enqueue(h->stream, h->soa, h->cur, h->cap, h->n, h->cfg.ncrit, h->info, h->hinfo, h->ts, h->tree);
+    }
+    for (int b : act) {
+      on(b);
+      tree_finish(hs[b]->stream, hs[b]->hinfo, hs[b]->tree);
+    }
+    std::vector<int> pend = act;
+    for (int attempt = 0; !pend.empty(); attempt++) {
+      if (attempt > 9)
+        throw Error(VFMM_ERR_CAPACITY, "interaction lists keep overflowing");
+      for (int b : pend) {
+        on(b);
+        vfmm_handle h = hs[b];
+        lists_enqueue(h->stream, h->tree, h->tree, h->cfg.theta, h->info, h->hinfo, h->lists);
+      }
+      std::vector<int> next;
+      for (int b : pend) {
+        on(b);
+        vfmm_handle h = hs[b];
+        if (!lists_finish(h->stream, h->tree, h->info, h->hinfo, h->lists, &h->info->p2p_interactions))
+          next.push_back(b);
+      }
+      pend.swap(next);
+    }
+    for (int b : act) {
+      on(b);
+      vfmm_handle h = hs[b];
+      VFMM_CUDA_TRY(cudaEventRecord(h->ph[1], h->stream));
+      h->has_tree = true;
+      evaluate_and_update(h, st, dt);
+    }
+  }
+  for (int b = 0; b < count; b++) { // enqueue every copy back, then wait
+    on(b);
+    vfmm_handle h = hs[b];
+    soa_to_aos(h->stream, h->soa[h->cur].p, h->cap, h->aos.p, h->n);
+    VFMM_CUDA_TRY(cudaMemcpyAsync(bodies[b], h->aos.p, ns[b] * sizeof(vfmm_body), cudaMemcpyDeviceToHost, h->stream));
+  }
+  for (int b = 0; b < count; b++) {
+    on(b);
+    VFMM_CUDA_TRY(cudaStreamSynchronize(hs[b]->stream));
+  }
 }
 
 } // namespace
@@ -744,6 +852,35 @@ int vfmm_get_sensor_data(vfmm_handle h, vfmm_body *sensors, size_t n)
       throw Error(VFMM_ERR_INVALID, "null sensors");
     sensor_data(h, sensors, n);
   });
+}
+
+int vfmm_advance_batch(vfmm_handle *handles, vfmm_body *const *bodies, const size_t *n, int count, double dt)
+{
+  if (!handles || !bodies || !n || count <= 0)
+    return VFMM_ERR_INVALID;
+  for (int b = 0; b < count; b++) {
+    if (!handles[b] || !bodies[b])
+      return VFMM_ERR_INVALID;
+    for (int c = 0; c < b; c++)
+      if (handles[c] == handles[b])
+        return VFMM_ERR_INVALID;
+  }
+  unsigned long long *prev = g_launch_counter;
+  int                 code = VFMM_OK;
+  std::string         msg;
+  try {
+    advance_batch(handles, bodies, n, count, dt);
+  } catch (const Error &e) {
+    code = e.code;
+    msg  = e.msg;
+  } catch (const std::exception &e) {
+    code = VFMM_ERR_CUDA;
+    msg  = e.what();
+  }
+  g_launch_counter = prev;
+  for (int b = 0; b < count; b++)
+    handles[b]->err = msg;
+  return code;
 }
 
 int vfmm_rbf(vfmm_handle h, vfmm_body *particles, size_t n, vfmm_body *points, size_t m, size_t *m_out, int *iterations)

@@ -83,3 +83,19 @@ def leapfrog(stations: int = 512, seed: int = 0) -> np.ndarray:
     r1 = ring(stations, seed=seed, center=(0.0, 0.0, 0.0))
     r2 = ring(stations, seed=seed + 1, center=(0.0, 0.0, 0.5))
     return np.concatenate([r1, r2])
+
+
+def ring_batch(count: int = 64, seed: int = 0, n_min: int = 2000, n_max: int = 60000) -> list[np.ndarray]:
+    """Independent vortex rings for batched runs: N log-uniform in [n_min, n_max]
+    (rounded to whole 127-point stations), R ~ U[0.5, 2], a/R ~ U[0.05, 0.15],
+    Gamma ~ U[0.5, 2], random orientation and centre."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        stations = max(8, int(round(n / 127)))
+        R = rng.uniform(0.5, 2.0)
+        axis = rng.normal(size=3)
+        out.append(ring(stations, R=R, a=R * rng.uniform(0.05, 0.15), gamma=rng.uniform(0.5, 2.0), seed=seed * 1000 + k,
+                        center=tuple(rng.uniform(-1, 1, 3)), axis=tuple(axis / np.linalg.norm(axis))))
+    return out
