@@ -161,6 +161,12 @@ int vfmm_get_sensor_data(vfmm_handle h, vfmm_body *sensors, size_t n);
  * with the particles' tree and no evaluation. */
 int vfmm_rbf(vfmm_handle h, vfmm_body *particles, size_t n, vfmm_body *points, size_t m, size_t *m_out, int *iterations);
 
+/* Global invariants of the bodies on the device, FP64, reproducible:
+ * out[0..2] circulation sum alpha, out[3..5] linear impulse 1/2 sum x cross
+ * alpha, out[6..8] angular impulse 1/3 sum x cross (x cross alpha).  No
+ * counterpart in the reference. */
+int vfmm_diagnostics(vfmm_handle h, double *out);
+
 /* Relaxation (relaxation.hpp:8-19, written 0-based) of the device bodies with
  * factor f, using the J of the last evaluation. */
 int vfmm_relax(vfmm_handle h, double f);

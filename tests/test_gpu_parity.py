@@ -219,3 +219,23 @@ def test_pse_mixed_matches_fp64(vfmm_lib):
         da[prec] = out["PSE"]["alpha"] - out["Inviscid"]["alpha"]
     assert np.abs(da["fp64"]).max() > 0
     assert rel_l2(da["mixed"], da["fp64"]) < 1e-5
+
+
+def test_diagnostics_against_host(vfmm_lib):
+    """Circulation and impulses of the device bodies against a host FP64 sum,
+    before and after an advance (the ring's circulation is conserved)."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.ring(64, seed=2)
+    with FMMCalculator(p=8, ncrit=32, theta=0.5, integration="RK2") as c:
+        c.load(b)
+        for step in range(2):
+            d = c.diagnostics()
+            if step:
+                c.copyBodies2Host(b)
+            x, a = b["X"], b["alpha"]
+            xa = np.cross(x, a)
+            host = {"circulation": a.sum(0), "linear_impulse": 0.5 * xa.sum(0), "angular_impulse": np.cross(x, xa).sum(0) / 3}
+            for k, v in host.items():
+                assert np.allclose(d[k], v, rtol=1e-12, atol=1e-12 * np.abs(v).max()), k
+            c.advance(b, 0.01)
+            c.load(b)

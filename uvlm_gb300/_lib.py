@@ -69,6 +69,7 @@ _PROTOS = {
     "vfmm_advance": (_i, [_H, _vp, _sz, _d]),
     "vfmm_get_sensor_data": (_i, [_H, _vp, _sz]),
     "vfmm_relax": (_i, [_H, _d]),
+    "vfmm_diagnostics": (_i, [_H, ctypes.POINTER(_d)]),
     "vfmm_advance_batch": (_i, [ctypes.POINTER(_H), ctypes.POINTER(_vp), ctypes.POINTER(_sz), _i, _d]),
     "vfmm_rbf": (_i, [_H, _vp, _sz, _vp, _sz, ctypes.POINTER(_sz), ctypes.POINTER(ctypes.c_int)]),
     "vfmm_get_tree": (_i, [_H, _vp, _sz, ctypes.POINTER(_sz)]),

@@ -103,6 +103,13 @@ class FMMCalculator:
         self._check(lib().vfmm_rbf(self._h, p.ctypes.data, p.size, q.ctypes.data, q.size, ctypes.byref(m), ctypes.byref(it)))
         return q[:m.value], it.value
 
+    def diagnostics(self) -> dict:
+        """Circulation, linear and angular impulse of the bodies on the device (FP64)."""
+        out = (ctypes.c_double * 9)()
+        self._check(lib().vfmm_diagnostics(self._h, out))
+        v = np.array(out[:])
+        return {"circulation": v[0:3], "linear_impulse": v[3:6], "angular_impulse": v[6:9]}
+
     def relax(self, f: float) -> None:
         self._check(lib().vfmm_relax(self._h, float(f)))
 

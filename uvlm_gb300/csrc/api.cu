@@ -894,6 +894,20 @@ int vfmm_rbf(vfmm_handle h, vfmm_body *particles, size_t n, vfmm_body *points, s
   });
 }
 
+int vfmm_diagnostics(vfmm_handle h, double *out)
+{
+  return guarded(h, [&] {
+    if (!out)
+      throw Error(VFMM_ERR_INVALID, "null output");
+    if (h->n == 0)
+      throw Error(VFMM_ERR_STATE, "no bodies on the device");
+    h->dtmp.reserve(DIAG_SCRATCH + 16);
+    diagnostics(h->stream, h->soa[h->cur].p, h->cap, h->n, h->dtmp.p, h->dtmp.p + DIAG_SCRATCH);
+    VFMM_CUDA_TRY(cudaMemcpyAsync(out, h->dtmp.p + DIAG_SCRATCH, 9 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  });
+}
+
 int vfmm_relax(vfmm_handle h, double f)
 {
   return guarded(h, [&] {

@@ -298,4 +298,56 @@ double fma_probe(cudaStream_t s, bool fp64, void *scratch, int iters, float *ms_
   return 2.0 * 8.0 * iters * (double)blocks * threads;
 }
 
+// Global invariants of the particle field, FP64: circulation sum alpha,
+// linear impulse 1/2 sum x cross alpha, angular impulse 1/3 sum x cross (x cross
+// alpha).  Fixed partition (DIAG_BLOCKS blocks) and fixed summation order, so
+// the sums are reproducible.
+constexpr int DIAG_BLOCKS = 152 * 2, DIAG_THREADS = 256;
+__global__ void __launch_bounds__(DIAG_THREADS) k_diag(const double *soa, size_t cap, int n, double *partials)
+{
+  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double x[3] = {soa[F_X * cap + i], soa[(F_X + 1) * cap + i], soa[(F_X + 2) * cap + i]};
+    const double a[3] = {soa[F_A * cap + i], soa[(F_A + 1) * cap + i], soa[(F_A + 2) * cap + i]};
+    const double xa[3] = {x[1] * a[2] - x[2] * a[1], x[2] * a[0] - x[0] * a[2], x[0] * a[1] - x[1] * a[0]};
+    const double xxa[3] = {x[1] * xa[2] - x[2] * xa[1], x[2] * xa[0] - x[0] * xa[2], x[0] * xa[1] - x[1] * xa[0]};
+    for (int d = 0; d < 3; d++) {
+      acc[d] += a[d];
+      acc[3 + d] += 0.5 * xa[d];
+      acc[6 + d] += xxa[d] / 3.0;
+    }
+  }
+  __shared__ double red[9][DIAG_THREADS];
+  for (int k = 0; k < 9; k++)
+    red[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int st = DIAG_THREADS / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int k = 0; k < 9; k++)
+        red[k][threadIdx.x] += red[k][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x < 9)
+    partials[blockIdx.x * 9 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_diag_final(const double *partials, int nb, double *out)
+{
+  if (threadIdx.x < 9) {
+    double v = 0;
+    for (int b = 0; b < nb; b++)
+      v += partials[b * 9 + threadIdx.x];
+    out[threadIdx.x] = v;
+  }
+}
+
+void diagnostics(cudaStream_t s, const double *soa, size_t cap, int n, double *scratch, double *out)
+{
+  k_diag<<<DIAG_BLOCKS, DIAG_THREADS, 0, s>>>(soa, cap, n, scratch);
+  count_launch();
+  k_diag_final<<<1, 32, 0, s>>>(scratch, DIAG_BLOCKS, out);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
 } // namespace vfmm

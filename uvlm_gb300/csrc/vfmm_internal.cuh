@@ -163,6 +163,9 @@ struct StageArgs {
 void finish_and_update(cudaStream_t s, double *soa, size_t cap, int n, const StageArgs &a);
 void relax_bodies(cudaStream_t s, double *soa, size_t cap, int n, double f);
 void fill_bytes(cudaStream_t s, void *p, size_t bytes, int value);
+constexpr int DIAG_SCRATCH = 152 * 2 * 9; // doubles of partial sums for diagnostics()
+// out[9] (device) = circulation, linear impulse, angular impulse of the bodies
+void diagnostics(cudaStream_t s, const double *soa, size_t cap, int n, double *scratch, double *out);
 double fma_probe(cudaStream_t s, bool fp64, void *scratch, int iters, float *ms_out, cudaEvent_t e0, cudaEvent_t e1);
 
 // ---- expansions.cu (FP64 path)
