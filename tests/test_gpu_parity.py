@@ -223,7 +223,7 @@ def test_pse_mixed_matches_fp64(vfmm_lib):
 
 def test_diagnostics_against_host(vfmm_lib):
     """Circulation and impulses of the device bodies against a host FP64 sum,
-    before and after an advance (the ring's circulation is conserved)."""
+    before and after an advance."""
     from uvlm_gb300 import FMMCalculator, workloads
     b = workloads.ring(64, seed=2)
     with FMMCalculator(p=8, ncrit=32, theta=0.5, integration="RK2") as c:
@@ -234,8 +234,10 @@ def test_diagnostics_against_host(vfmm_lib):
                 c.copyBodies2Host(b)
             x, a = b["X"], b["alpha"]
             xa = np.cross(x, a)
-            host = {"circulation": a.sum(0), "linear_impulse": 0.5 * xa.sum(0), "angular_impulse": np.cross(x, xa).sum(0) / 3}
-            for k, v in host.items():
-                assert np.allclose(d[k], v, rtol=1e-12, atol=1e-12 * np.abs(v).max()), k
+            xxa = np.cross(x, xa)
+            host = {"circulation": (a.sum(0), np.abs(a).sum()), "linear_impulse": (0.5 * xa.sum(0), np.abs(xa).sum()),
+                    "angular_impulse": (xxa.sum(0) / 3, np.abs(xxa).sum())}
+            for k, (v, mag) in host.items():  # the sums may cancel: compare against the size of their terms
+                assert np.abs(d[k] - v).max() < 1e-13 * mag, k
             c.advance(b, 0.01)
             c.load(b)
