@@ -526,7 +526,7 @@ struct L2P32Sizes {
   static constexpr int    K  = nterms(P);
   static constexpr int    K1 = nterms(P - 1) > 0 ? nterms(P - 1) : 1;
   static constexpr int    K2 = nterms(P - 2) > 0 ? nterms(P - 2) : 1;
-  static constexpr int    CH = 1024; // near-field source bodies staged per chunk
+  static constexpr int    CH = 768; // near-field source bodies staged per chunk (measured best: 6 blocks per SM)
   static constexpr size_t bytes =
       (size_t)CH * 2 * sizeof(float4) + 128 * (sizeof(float4) + sizeof(int)) + (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zf);
   static_assert((size_t)CH * 2 * sizeof(float4) >= 2 * 128 * 12 * sizeof(float), "the staging buffer holds the reduction");
