@@ -61,13 +61,15 @@ __device__ __forceinline__ void jk_of_m(int jks, int &j, int &k)
 
 // ------------------------------------------------------------------ prep
 // Leaf-relative FP32 body data for the P2P sources and targets.
+// One warp per leaf (leaves hold ~ncrit/2 bodies).
 __global__ void k_prep_bodies(DevMixed a)
 {
-  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  for (int li = blockIdx.x * wpb + (threadIdx.x >> 5); li < a.nleaves; li += gridDim.x * wpb) {
     const int    c  = a.leaf_cells[li];
     const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
     const double cx_ = a.cv.x[c], cy_ = a.cv.y[c], cz_ = a.cv.z[c];
-    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+    for (int t = lane; t < nb; t += 32) {
       const int    b  = b0 + t;
       const double sg = a.soa[F_R * a.cap + b];
       float4       p, q;
@@ -871,7 +873,7 @@ static void p2m32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   DevMixed     d     = dev_mixed(e, m);
   const size_t bytes = (size_t)32 * nterms(P) * sizeof(zf) + 32 * 3 * sizeof(float);
   if (e.nleaves > 0) {
-    k_prep_bodies<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
+    k_prep_bodies<<<std::min((e.nleaves + 3) / 4, 152 * 16), 128, 0, s>>>(d);
     count_launch();
     k_p2m32<P><<<std::min(e.nleaves, 152 * 16), 64, bytes, s>>>(d);
     count_launch();

@@ -120,6 +120,18 @@ void tree_bounds(cudaStream_t s, const double *X, size_t cap, int n, DevInfo *in
 }
 
 // ------------------------------------------------------------ keys
+// a > b for finite doubles, on the integer pipe: the sign-magnitude bit
+// patterns, mapped to two's-complement order, compare as the doubles do;
+// +0 and -0 compare equal.
+__device__ __forceinline__ bool dgreater(double a, double b)
+{
+  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  if (((ia | ib) & 0x7fffffffffffffffll) == 0)
+    return false; // both zero
+  const long long ka = ia ^ ((ia >> 63) & 0x7fffffffffffffffll), kb = ib ^ ((ib >> 63) & 0x7fffffffffffffffll);
+  return ka > kb;
+}
+
 __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, int n, const DevInfo *info,
                        uint64_t *keys, uint32_t *idx)
 {
@@ -134,7 +146,7 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
     uint64_t     key  = 0;
 #pragma unroll 1
     for (int l = 0; l < MAXL; l++) {
-      const int b0 = p[0] > c[0], b1 = p[1] > c[1], b2 = p[2] > c[2];
+      const int b0 = dgreater(p[0], c[0]), b1 = dgreater(p[1], c[1]), b2 = dgreater(p[2], c[2]);
       key          = (key << 3) | (uint64_t)(b0 | (b1 << 1) | (b2 << 2));
       const double r = half[l];
       c[0]           = __dadd_rn(c[0], b0 ? r : -r);
