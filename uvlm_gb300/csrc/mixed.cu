@@ -51,6 +51,19 @@ struct DevMixed {
 __device__ __forceinline__ double cell_Rpow(const DevMixed &a, int level, int n) { return ldexp(a.R0pow[n], -level * n); }
 __device__ __forceinline__ double cell_iRpow(const DevMixed &a, int level, int n) { return ldexp(a.iR0pow[n], level * n); }
 
+// Store the scaled multipole Mt_n^m (m >= 0, component d) of cell c in the
+// folded FP32 form read by M2L, [cell][n^2+n+m][d]: M'_n^m = (-1)^m Mt_n^m and,
+// for m > 0, M'_n^{-m} = conj(Mt_n^m).  Written by P2M and M2M, which hold Mt
+// in FP32 already.
+__device__ __forceinline__ void store_mfold(const DevMixed &a, int PP, int c, int n, int m, int d, float re, float im)
+{
+  float2   *row = a.Mp + (size_t)c * 3 * PP;
+  const int nn  = n * n + n;
+  row[(nn + m) * 3 + d] = (m & 1) ? make_float2(-re, -im) : make_float2(re, im);
+  if (m > 0)
+    row[(nn - m) * 3 + d] = make_float2(re, -im);
+}
+
 __device__ __forceinline__ void jk_of_m(int jks, int &j, int &k)
 {
   j = 0;
@@ -141,39 +154,13 @@ __global__ void __launch_bounds__(64) k_p2m32(DevMixed a)
         jk_of_m(o / 3, n, m);
         const double s = cell_Rpow(a, lev, n);
         a.M[(size_t)c * 3 * K + o] = make_double2(acc[i].r * s, acc[i].i * s);
+        store_mfold(a, P * P, c, n, m, o % 3, acc[i].r, acc[i].i);
       }
     }
   }
 }
 
 // ------------------------------------------------------------------ M2L
-// Prepared scaled multipoles, sign- and conjugation-folded as in k_mprep:
-// Mp[cell][n^2+n+m][d] = ((-1)^m M_n^m (m>=0) | conj(M_n^|m|) (m<0)) / R_c^n.
-template <int P>
-__global__ void k_mprep32(DevMixed a, int ncells)
-{
-  constexpr int K = nterms(P), PP = P * P;
-  const long    total = (long)ncells * PP * 3;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(e / (PP * 3)), r = (int)(e % (PP * 3)), idx = r / 3, d = r % 3;
-    int       n = 0;
-    while ((n + 1) * (n + 1) <= idx)
-      n++;
-    const int     m = idx - n * n - n;
-    const double2 v = a.M[(size_t)c * 3 * K + tri(n, m >= 0 ? m : -m) * 3 + d];
-    const double  s = cell_iRpow(a, a.cv.level[c], n);
-    double        re = v.x * s, im = v.y * s;
-    if (m >= 0) {
-      if (m & 1) {
-        re = -re;
-        im = -im;
-      }
-    } else
-      im = -im;
-    a.Mp[e] = make_float2((float)re, (float)im);
-  }
-}
-
 // M2M and L2L in FP32 (multipoleKernels.hpp:479-516, :591-628) with every
 // operand scaled by the parent's half-width R_p: the child multipoles enter
 // as M_c / R_p^n and the parent's local expansion as L_p R_p^n, the offset
@@ -218,6 +205,7 @@ __global__ void __launch_bounds__(128) k_m2m32(DevMixed a, const int *cells, int
       double2     *q   = a.M + (size_t)c * 3 * K + o;
       const double2 old = *q;
       *q                = make_double2(old.x + (double)sum.r * s, old.y + (double)sum.i * s);
+      store_mfold(a, P * P, c, j, k, d, sum.r, sum.i);
     }
   }
 }
@@ -901,8 +889,7 @@ static void m2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
 {
   DevMixed  d  = dev_mixed(e, m);
   const int PP = P * P;
-  k_mprep32<P><<<grid_for((long)e.ncells * PP * 3, 256), 256, 0, s>>>(d, e.ncells);
-  count_launch();
+  (void)PP; // the folded FP32 multipoles were written by P2M and M2M
   if (m.m2l_batch == 32)
     m2l32_launch<P, 32>(s, d, e, m);
   else if (m.m2l_batch == 24)
