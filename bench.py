@@ -57,6 +57,8 @@ def parse(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--out", default=None, help="also write the JSON line to this file")
+    ap.add_argument("--autotune", action="store_true",
+                    help="also report the opt-in autotuner's choice (leaf size, M2L batch) and its stage time")
     ap.add_argument("--workload", default="cloud", choices=["cloud", "rings64"],
                     help="cloud: the headline N = 2^20 cloud; rings64: 64 independent rings, batched")
     return ap.parse_args(argv)
@@ -316,6 +318,12 @@ def run_ours(args, dist: Dist) -> dict | None:
     if fp64:
         line["fp64"] = fp64
         line["fp64"]["speedup_mixed_vs_fp64"] = fp64["ms_per_step"] / line["ms_per_step"]
+    if args.autotune:
+        with FMMCalculator(p=args.p, ncrit=args.ncrit, theta=args.theta, integration="RK2", precision=args.precision,
+                           device=dist.local_rank) as ct:
+            line["autotuned"] = ct.autotune(bodies, args.dt)
+            line["autotuned"]["note"] = ("opt-in: another leaf size builds another tree than the reference's ncrit; "
+                                         "stage times from the tuner's own CUDA-event timing, L2 not flushed")
     if not args.no_cpu_baseline and dist.world == 1:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(args).items() if k != "seconds"}
     return line

@@ -143,6 +143,26 @@ int vfmm_advance(vfmm_handle h, vfmm_body *bodies, size_t n, double dt);
  * reference, which advances one system per calculator. */
 int vfmm_advance_batch(vfmm_handle *handles, vfmm_body *const *bodies, const size_t *n, int count, double dt);
 
+/* Result of vfmm_autotune. */
+typedef struct {
+  int    ncrit;                /* chosen leaf size */
+  int    m2l_batch;            /* chosen M2L source batch (mixed mode) */
+  double ms_per_stage;         /* its measured stage time */
+  double default_ms_per_stage; /* the stage time with the configuration before tuning */
+  int    tried;                /* configurations timed */
+  int    reserved[3];
+} vfmm_tuning;
+
+/* Opt-in autotuner: times one stage (best of two after a warm-up) of `bodies`
+ * for leaf sizes 16..256 and, in mixed mode, M2L source batches 16/24/32, and
+ * keeps the fastest in the handle (vfmm_get_config shows the leaf size).  A
+ * leaf size other than the reference's compile-time ncrit (exafmmTypes.hpp:14)
+ * builds a different tree and lists, so results are no longer those of the
+ * reference at its ncrit.  The bodies on the device afterwards are a copy of
+ * `bodies` after one stage; call vfmm_init / vfmm_advance as usual.  No
+ * counterpart in the reference. */
+int vfmm_autotune(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, vfmm_tuning *out);
+
 /* FMMCalculator::getSensorData (fmmCalculator.hpp:726-731): velocity at probe
  * points from the particles (multipoles of the last calculate, near field
  * from the particles as they are now); velocity and dadt are overwritten, the

@@ -45,6 +45,8 @@ def test_struct_layouts():
     from uvlm_gb300._lib import BODY_DTYPE, CELL_DTYPE, vfmm_config
     assert BODY_DTYPE.itemsize == 296 and CELL_DTYPE.itemsize == 72
     assert ctypes.sizeof(vfmm_config) == 72  # static_assert'ed in api.cu
+    from uvlm_gb300._lib import vfmm_tuning
+    assert ctypes.sizeof(vfmm_tuning) == 40
 
 
 def test_null_arguments_are_rejected_without_a_gpu(vfmm_lib):

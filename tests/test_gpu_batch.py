@@ -55,3 +55,26 @@ def test_batch_rejects_repeated_handles(vfmm_lib):
     with FMMCalculator(p=4, ncrit=16, theta=0.5) as c:
         with pytest.raises(VfmmError):
             advance_batch([c, c], [workloads.cloud(100, seed=1), workloads.cloud(100, seed=2)], 0.01)
+
+
+def test_autotune(vfmm_lib):
+    """The opt-in tuner returns a timed leaf size and batch, keeps them, and the
+    tuned calculator still meets the mixed-mode bar against FP64 at that leaf size."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(60000, seed=21)
+    with FMMCalculator(p=8, ncrit=64, theta=0.5, integration="Euler", precision="mixed") as c:
+        t = c.autotune(b, 0.01)
+        assert t["tried"] == 27 and t["ncrit"] in (16, 24, 32, 48, 64, 96, 128, 192, 256) and t["m2l_batch"] in (16, 24, 32)
+        assert t["ms_per_stage"] <= t["default_ms_per_stage"]
+        bb = b.copy()
+        c.init(bb)
+        c.calculate()
+        c.copyBodies2Host(bb)
+    with FMMCalculator(p=8, ncrit=t["ncrit"], theta=0.5, precision="fp64") as c64:
+        ref = b.copy()
+        c64.init(ref)
+        c64.calculate()
+        c64.copyBodies2Host(ref)
+    assert (bb["X"] == ref["X"]).all()
+    err = np.linalg.norm(bb["velocity"] - ref["velocity"]) / np.linalg.norm(ref["velocity"])
+    assert err < 1e-6

@@ -1,0 +1,38 @@
+"""Interaction lists that outgrow their buffers: a handle whose list buffers
+were sized on a small body set meets a much larger one, overflows, grows its
+buffers and traverses again.  The lists and fields must equal those of a fresh
+handle sized for the large set."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_list_overflow_retry_matches_fresh_handle(vfmm_lib, precision):
+    from uvlm_gb300 import FMMCalculator, workloads
+    kw = dict(p=6, ncrit=16, theta=0.5, integration="Euler", precision=precision)
+    large = workloads.cloud(200000, seed=31)
+    with FMMCalculator(**kw) as c:
+        small = workloads.cloud(300, seed=30)
+        c.init(small)
+        c.calculate()
+        out = large.copy()
+        c.init(out)
+        c.calculate()
+        c.copyBodies2Host(out)
+        st = c.stats()
+        lists = c.lists()
+    # the first buffers hold a few thousand pairs: the large set overflowed them
+    assert st["m2l_pairs"] > 100000 and st["p2p_pairs"] > 10000
+    with FMMCalculator(**kw) as f:
+        ref = large.copy()
+        f.init(ref)
+        f.calculate()
+        f.copyBodies2Host(ref)
+        assert f.stats() == st
+        ref_lists = f.lists()
+    for a, b in zip(lists, ref_lists):
+        assert np.array_equal(a, b)
+    for fld in ["X", "velocity", "J", "dadt"]:
+        assert np.array_equal(out[fld], ref[fld]), fld

@@ -110,6 +110,16 @@ class FMMCalculator:
         v = np.array(out[:])
         return {"circulation": v[0:3], "linear_impulse": v[3:6], "angular_impulse": v[6:9]}
 
+    def autotune(self, bodies: np.ndarray, dt: float = 0.01) -> dict:
+        """vfmm_autotune: time leaf sizes (and M2L batches in mixed mode) on
+        these bodies and keep the fastest in this calculator (opt-in: another
+        leaf size than the reference's builds another tree)."""
+        b = _lib.as_bodies(bodies)
+        t = _lib.vfmm_tuning()
+        self._check(lib().vfmm_autotune(self._h, b.ctypes.data, b.size, float(dt), ctypes.byref(t)))
+        return {"ncrit": t.ncrit, "m2l_batch": t.m2l_batch, "ms_per_stage": t.ms_per_stage,
+                "default_ms_per_stage": t.default_ms_per_stage, "tried": t.tried}
+
     def relax(self, f: float) -> None:
         self._check(lib().vfmm_relax(self._h, float(f)))
 

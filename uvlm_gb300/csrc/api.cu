@@ -61,6 +61,7 @@ using namespace vfmm;
 static_assert(sizeof(vfmm_config) == 72, "vfmm_config layout");
 static_assert(sizeof(vfmm_body) == 296, "vfmm_body must match exafmm::Body");
 static_assert(sizeof(vfmm_cell) == 72, "vfmm_cell layout");
+static_assert(sizeof(vfmm_tuning) == 40, "vfmm_tuning layout");
 
 struct vfmm_handle_s {
   vfmm_config  cfg;
@@ -100,7 +101,8 @@ struct vfmm_handle_s {
   DevBuf<double2> M, L, Mprep;
   DevBuf<int4>    items, items32, lanes32;
   int             m2l_batch = 16; // sources per mixed-M2L batch (set per p); VFMM_M2L_BATCH = 8, 16, 24 or 32 overrides
-  int             items_P = 0, items_per_lane = 0;
+  int             items_P = 0, items_per_lane = 0, items_batch = 0;
+  int             m2l_batch_forced = 0; // set by vfmm_autotune
   DevBuf<float2>  Mp32;
   DevBuf<float4>  pos32, alp32;
 
@@ -334,7 +336,7 @@ void build_tree_and_lists(vfmm_handle h)
 
 void ensure_items(vfmm_handle h)
 {
-  if (h->items_P == h->cfg.p)
+  if (h->items_P == h->cfg.p && h->items_batch == h->m2l_batch_forced)
     return;
   int  per = 0;
   auto tab = m2l_schedule(h->cfg.p, 32, 2, 4, &per);
@@ -348,10 +350,13 @@ void ensure_items(vfmm_handle h)
   // sources per batch, measured best on GB300: 32 for p <= 10, 24 for p = 11-12, else 16
   const int def  = h->cfg.p <= 10 ? 32 : (h->cfg.p <= 12 ? 24 : 16);
   h->m2l_batch   = sb && (atoi(sb) == 8 || atoi(sb) == 16 || atoi(sb) == 24 || atoi(sb) == 32) ? atoi(sb) : def;
+  if (h->m2l_batch_forced)
+    h->m2l_batch = h->m2l_batch_forced;
   auto lt32      = m2l_lane_table(h->cfg.p, m2l_half_width(h->cfg.p), h->m2l_batch); // half-tile width and batch of k_m2l32v2
   h->lanes32.reserve(lt32.size());
   VFMM_CUDA_TRY(cudaMemcpy(h->lanes32.p, lt32.data(), lt32.size() * sizeof(int4), cudaMemcpyHostToDevice));
   h->items_P        = h->cfg.p;
+  h->items_batch    = h->m2l_batch_forced;
   h->items_per_lane = per;
 }
 
@@ -881,6 +886,62 @@ int vfmm_advance_batch(vfmm_handle *handles, vfmm_body *const *bodies, const siz
   for (int b = 0; b < count; b++)
     handles[b]->err = msg;
   return code;
+}
+
+int vfmm_autotune(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, vfmm_tuning *out)
+{
+  return guarded(h, [&] {
+    if (!bodies || !out)
+      throw Error(VFMM_ERR_INVALID, "null argument");
+    cudaStream_t s = h->stream;
+    // one stage of `bodies` with the handle's current leaf size and batch: best of two after a warm-up
+    auto time_stage = [&]() {
+      float best = 1e30f;
+      for (int r = 0; r < 3; r++) {
+        upload(h, bodies, n);
+        VFMM_CUDA_TRY(cudaEventRecord(h->ev[12], s));
+        run_stage(h, 0, dt);
+        VFMM_CUDA_TRY(cudaEventRecord(h->ev[13], s));
+        VFMM_CUDA_TRY(cudaEventSynchronize(h->ev[13]));
+        float ms = 0;
+        VFMM_CUDA_TRY(cudaEventElapsedTime(&ms, h->ev[12], h->ev[13]));
+        if (r > 0)
+          best = std::min(best, ms);
+      }
+      return best;
+    };
+    const int  ncrit0 = h->cfg.ncrit, forced0 = h->m2l_batch_forced;
+    const bool mixed  = h->cfg.precision == VFMM_MIXED;
+    std::memset(out, 0, sizeof(*out));
+    out->default_ms_per_stage = time_stage();
+    out->ncrit                = ncrit0;
+    out->m2l_batch            = h->m2l_batch;
+    out->ms_per_stage         = out->default_ms_per_stage;
+    const int leaf[] = {16, 24, 32, 48, 64, 96, 128, 192, 256};
+    const int bat[]  = {16, 24, 32};
+    try {
+      for (int nc : leaf)
+        for (int b = 0; b < (mixed ? 3 : 1); b++) {
+          h->cfg.ncrit         = nc;
+          h->m2l_batch_forced  = mixed ? bat[b] : 0;
+          const float ms       = time_stage();
+          out->tried++;
+          if (ms < out->ms_per_stage) {
+            out->ms_per_stage = ms;
+            out->ncrit        = nc;
+            out->m2l_batch    = h->m2l_batch;
+          }
+        }
+    } catch (...) {
+      h->cfg.ncrit        = ncrit0;
+      h->m2l_batch_forced = forced0;
+      throw;
+    }
+    h->cfg.ncrit        = out->ncrit;
+    h->m2l_batch_forced = mixed ? out->m2l_batch : 0;
+    h->has_tree = h->has_eval = false;
+    VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+  });
 }
 
 int vfmm_rbf(vfmm_handle h, vfmm_body *particles, size_t n, vfmm_body *points, size_t m, size_t *m_out, int *iterations)

@@ -62,11 +62,17 @@ __global__ void k_traverse_init(CellsView tc, CellsView sc, int2 *front, DevInfo
   }
 }
 
-__global__ void k_traverse_step(CellsView tc, CellsView sc, const int2 *__restrict__ fin, int *n_in, int2 *fout, int *n_out, int cap_front,
-                                unsigned long long *p2p, unsigned long long *m2l, int *np2p, int *nm2l, int cap_p2p, int cap_m2l, double theta,
-                                int cell_bits, int *overflow)
+__global__ void k_traverse_step(CellsView tc, CellsView sc, const int2 *__restrict__ fin, int *n_in, int cap_in, int2 *fout, int *n_out,
+                                int cap_front, unsigned long long *p2p, unsigned long long *m2l, int *np2p, int *nm2l, int cap_p2p, int cap_m2l,
+                                double theta, int cell_bits, int *overflow)
 {
-  const int n = *n_in;
+  // After an overflow the previous step's counter has run past its buffer and
+  // some of its slots were left unwritten: the lists are redone with larger
+  // buffers, so the remaining steps do nothing.  The clamp keeps every read of
+  // fin inside its buffer regardless.
+  if (*(volatile int *)overflow)
+    return;
+  const int n = min(*n_in, cap_in);
   // warp-uniform trip count (blockDim is a multiple of 32) for the aggregated reservations
   for (int q0 = blockIdx.x * blockDim.x; q0 < n; q0 += gridDim.x * blockDim.x) {
     const int  q     = q0 + threadIdx.x;
@@ -118,6 +124,10 @@ void traverse(cudaStream_t s, CellsView tc, CellsView sc, int ntc, int nsc, int 
   ls.front[1].reserve(cap_front);
   ls.p2p_raw.reserve(cap_p2p);
   ls.m2l_raw.reserve(cap_m2l);
+  // the kernel's counters and capacities are int
+  const size_t int_max = 0x7fffffff;
+  if (ls.front[0].cap > int_max || ls.front[1].cap > int_max || ls.p2p_raw.cap > int_max || ls.m2l_raw.cap > int_max)
+    throw Error(VFMM_ERR_CAPACITY, "interaction lists exceed 2^31 pairs");
   // pair keys (target << key_bits | source): the sort then covers 2 * key_bits bits
   int cell_bits = 1;
   while ((1ll << cell_bits) < (long long)std::max(ntc, nsc))
@@ -129,7 +139,8 @@ void traverse(cudaStream_t s, CellsView tc, CellsView sc, int ntc, int nsc, int 
   for (int it = 0; it < steps; it++) {
     const int a = it & 1, b = a ^ 1;
     VFMM_CUDA_TRY(cudaMemsetAsync(&info->front_n[b], 0, sizeof(int), s));
-    k_traverse_step<<<152 * 8, 128, 0, s>>>(tc, sc, ls.front[a].p, &info->front_n[a], ls.front[b].p, &info->front_n[b], (int)ls.front[b].cap,
+    k_traverse_step<<<152 * 8, 128, 0, s>>>(tc, sc, ls.front[a].p, &info->front_n[a], (int)ls.front[a].cap, ls.front[b].p, &info->front_n[b],
+                                            (int)ls.front[b].cap,
                                             ls.p2p_raw.p, ls.m2l_raw.p, &info->n_p2p, &info->n_m2l, (int)ls.p2p_raw.cap, (int)ls.m2l_raw.cap, theta,
                                             cell_bits, &info->overflow);
     count_launch();
