@@ -163,6 +163,37 @@ typedef struct {
  * counterpart in the reference. */
 int vfmm_autotune(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, vfmm_tuning *out);
 
+/* Objective of vfmm_adjoint, evaluated on the state after the last step:
+ *   energy * E + impulse . I + sum_i seed_x_i . x_i + seed_alpha_i . alpha_i,
+ * E = sum_i u_i . (x_i cross alpha_i) (the kinetic energy of an unbounded
+ * flow, u from an FP64 evaluation of that state) and I = 1/2 sum_i x_i cross
+ * alpha_i.  The seed arrays hold n x 3 doubles indexed like the `bodies`
+ * passed in (bodies move in memory as the trees reorder them; the adjoint
+ * tracks that), or are NULL. */
+typedef struct vfmm_objective {
+  double        energy;
+  double        impulse[3];
+  const double *seed_x;
+  const double *seed_alpha;
+} vfmm_objective;
+
+/* Reverse-mode gradient of the objective after `steps` steps of advance
+ * from `bodies` (not modified) with respect to their initial positions and
+ * strengths: grad_x and grad_alpha receive n x 3 doubles in the order of
+ * `bodies`.  The forward steps run in the handle's precision; the reverse
+ * sweep is the exact transpose of the FP64 evaluation (P2P pairs, transposed
+ * L2P, L2L, M2L, M2M, P2M, the bounding-box dependence of the cell centres)
+ * and of the stage updates, at the states of the forward trajectory.  States
+ * are kept every `checkpoint_every` steps and the steps in between are
+ * recomputed, so device memory holds ceil(steps / checkpoint_every) + stages
+ * x checkpoint_every body states.  With grad_x and grad_alpha both NULL only
+ * *value is computed.  Covers Euler, RK2 and RK3 with the cVPM formulation,
+ * no viscosity and no relaxation (VFMM_ERR_UNSUPPORTED otherwise).  The
+ * reference has no adjoint; its L2P takes one derivative by complex step
+ * (multipoleKernels.hpp:630-742, complexify.hpp). */
+int vfmm_adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int steps, int checkpoint_every, const vfmm_objective *objective,
+                 double *value, double *grad_x, double *grad_alpha);
+
 /* FMMCalculator::getSensorData (fmmCalculator.hpp:726-731): velocity at probe
  * points from the particles (multipoles of the last calculate, near field
  * from the particles as they are now); velocity and dadt are overwritten, the

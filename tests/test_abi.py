@@ -47,6 +47,8 @@ def test_struct_layouts():
     assert ctypes.sizeof(vfmm_config) == 72  # static_assert'ed in api.cu
     from uvlm_gb300._lib import vfmm_tuning
     assert ctypes.sizeof(vfmm_tuning) == 40
+    from uvlm_gb300._lib import vfmm_objective
+    assert ctypes.sizeof(vfmm_objective) == 48
 
 
 def test_null_arguments_are_rejected_without_a_gpu(vfmm_lib):

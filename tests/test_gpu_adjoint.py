@@ -1,0 +1,126 @@
+"""Reverse-mode gradients (vfmm_adjoint) against central finite differences of
+the same FP64 forward: directional derivatives of the objective along random
+directions of the initial positions and strengths, one evaluation alone and
+through Euler, RK2 and RK3 steps with checkpointing.
+
+The FMM is piecewise smooth: at theta = 0.5 cells two apart on the octree
+lattice sit exactly on the MAC boundary |dX| theta = R_i + R_j
+(traverse.hpp:52-57), so rounding decides them and any change of the
+bounding box can flip them, a jump that a finite difference sees.  The
+checks use theta = 0.47, where no exact ties exist, or at theta = 0.5 only
+directions that leave the bounding box (and so every cell centre) fixed."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6  # relative, directional derivative against central differences
+
+
+def fd_check(c, b, dt, steps, every=1, nd=3, h=1e-7, seed=0, parts=("x", "alpha"), interior=False, **obj):
+    val, gx, ga = c.adjoint(b, dt, steps, every, **obj)
+    rng = np.random.default_rng(seed)
+    amax = np.abs(b["alpha"]).max()
+    errs = []
+    for part in parts:
+        for _ in range(nd):
+            vx = rng.normal(size=gx.shape) if part == "x" else np.zeros(gx.shape)
+            va = rng.normal(size=ga.shape) * amax if part == "alpha" else np.zeros(ga.shape)
+            if interior:  # leave the bodies that set the bounding box in place
+                for d in range(3):
+                    vx[np.argmin(b["X"][:, d])] = vx[np.argmax(b["X"][:, d])] = 0
+            bp, bm = b.copy(), b.copy()
+            bp["X"] += h * vx
+            bp["alpha"] += h * va
+            bm["X"] -= h * vx
+            bm["alpha"] -= h * va
+            fp = c.adjoint(bp, dt, steps, every, gradient=False, **obj)
+            fm = c.adjoint(bm, dt, steps, every, gradient=False, **obj)
+            fd = (fp - fm) / (2 * h)
+            an = float((gx * vx).sum() + (ga * va).sum())
+            errs.append((part, abs(fd - an) / abs(an), fd, an))
+    return val, gx, ga, errs
+
+
+def worst(errs):
+    return max(e[1] for e in errs)
+
+
+def test_evaluation_gradient_single_leaf(vfmm_lib):
+    """All bodies in one leaf: the objective's evaluation is the P2P near field only."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(200, seed=1)
+    with FMMCalculator(p=6, ncrit=256, theta=0.5, integration="Euler") as c:
+        _, _, _, errs = fd_check(c, b, 0.01, 0)
+    assert worst(errs) < TOL, errs
+
+
+def test_evaluation_gradient_full_tree(vfmm_lib):
+    """A deep tree: P2M, M2M, M2L, L2L, L2P transposed, plus the bounding-box terms."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(4000, seed=2)
+    with FMMCalculator(p=8, ncrit=32, theta=0.47, integration="Euler") as c:
+        _, _, _, errs = fd_check(c, b, 0.01, 0)
+    assert worst(errs) < TOL, errs
+    with FMMCalculator(p=8, ncrit=32, theta=0.5, integration="Euler") as c:
+        _, _, _, errs = fd_check(c, b, 0.01, 0, interior=True, seed=1)
+    assert worst(errs) < TOL, errs
+
+
+@pytest.mark.parametrize("integration,stretching", [("Euler", "Transposed"), ("RK2", "Transposed"), ("RK3", "Transposed"),
+                                                    ("RK2", "Classic")])
+def test_step_gradients(vfmm_lib, integration, stretching):
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.ring(24, seed=3)
+    with FMMCalculator(p=8, ncrit=32, theta=0.47, integration=integration, stretching=stretching) as c:
+        _, _, _, errs = fd_check(c, b, 0.02, 2, every=1, nd=2, h=1e-8)
+    assert worst(errs) < 1e-5, errs  # h = 1e-8: rounding of the differences ~1e-7
+
+
+def test_checkpoint_spacing_does_not_change_the_gradient(vfmm_lib):
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.leapfrog(16, seed=4)
+    out = []
+    with FMMCalculator(p=8, ncrit=32, theta=0.5, integration="RK3") as c:
+        for every in (1, 2, 4):
+            out.append(c.adjoint(b, 0.01, 4, every))
+    for v, gx, ga in out[1:]:
+        assert v == out[0][0] and np.array_equal(gx, out[0][1]) and np.array_equal(ga, out[0][2])
+
+
+def test_seeds_follow_the_bodies(vfmm_lib):
+    """With only seeds on the final state and no steps, the gradient is the seed
+    itself, in the caller's order although the trees reorder the bodies."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(3000, seed=5)
+    rng = np.random.default_rng(6)
+    sx, sa = rng.normal(size=(b.size, 3)), rng.normal(size=(b.size, 3))
+    with FMMCalculator(p=6, ncrit=32, theta=0.47, integration="RK2") as c:
+        v, gx, ga = c.adjoint(b, 0.01, 0, energy=0.0, impulse=(0, 0, 0), seed_x=sx, seed_alpha=sa)
+        assert np.array_equal(gx, sx) and np.array_equal(ga, sa)
+        assert v == pytest.approx(float((sx * b["X"]).sum() + (sa * b["alpha"]).sum()), rel=1e-12)
+        _, _, _, errs = fd_check(c, b, 0.02, 1, energy=0.0, impulse=(0, 0, 0), seed_x=sx, seed_alpha=sa, nd=2)
+    assert worst(errs) < TOL, errs
+
+
+def test_mixed_forward_gradient_close_to_fp64(vfmm_lib):
+    """A mixed-precision forward sweep with the FP64 reverse sweep: the gradient
+    differs from the all-FP64 one by the trajectory's FP32 rounding."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.leapfrog(16, seed=7)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        with FMMCalculator(p=8, ncrit=32, theta=0.47, integration="RK3", precision=prec) as c:
+            res[prec] = c.adjoint(b, 0.01, 3, 2)
+    for k in (1, 2):
+        a, r = res["mixed"][k], res["fp64"][k]
+        assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-6
+
+
+def test_adjoint_rejects_what_it_does_not_cover(vfmm_lib):
+    from uvlm_gb300 import FMMCalculator, VfmmError, workloads
+    b = workloads.cloud(500, seed=8)
+    for kw in (dict(integration="RK4"), dict(formulation="rVPM"), dict(viscous="PSE", nu=0.01), dict(relax=0.3)):
+        with FMMCalculator(p=4, ncrit=32, theta=0.5, **kw) as c:
+            with pytest.raises(VfmmError):
+                c.adjoint(b, 0.01, 1)

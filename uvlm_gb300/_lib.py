@@ -46,6 +46,11 @@ class vfmm_tuning(ctypes.Structure):
                 ("default_ms_per_stage", ctypes.c_double), ("tried", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
+class vfmm_objective(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("impulse", ctypes.c_double * 3), ("seed_x", ctypes.c_void_p),
+                ("seed_alpha", ctypes.c_void_p)]
+
+
 class vfmm_config(ctypes.Structure):
     _fields_ = [("p", ctypes.c_int), ("ncrit", ctypes.c_int), ("theta", ctypes.c_double),
                 ("precision", ctypes.c_int), ("integrator", ctypes.c_int), ("stretching", ctypes.c_int),
@@ -75,6 +80,7 @@ _PROTOS = {
     "vfmm_get_sensor_data": (_i, [_H, _vp, _sz]),
     "vfmm_relax": (_i, [_H, _d]),
     "vfmm_autotune": (_i, [_H, _vp, _sz, _d, _vp]),
+    "vfmm_adjoint": (_i, [_H, _vp, _sz, _d, _i, _i, _vp, ctypes.POINTER(_d), _vp, _vp]),
     "vfmm_diagnostics": (_i, [_H, ctypes.POINTER(_d)]),
     "vfmm_advance_batch": (_i, [ctypes.POINTER(_H), ctypes.POINTER(_vp), ctypes.POINTER(_sz), _i, _d]),
     "vfmm_rbf": (_i, [_H, _vp, _sz, _vp, _sz, ctypes.POINTER(_sz), ctypes.POINTER(ctypes.c_int)]),

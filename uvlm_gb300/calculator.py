@@ -120,6 +120,34 @@ class FMMCalculator:
         return {"ncrit": t.ncrit, "m2l_batch": t.m2l_batch, "ms_per_stage": t.ms_per_stage,
                 "default_ms_per_stage": t.default_ms_per_stage, "tried": t.tried}
 
+    def adjoint(self, bodies: np.ndarray, dt: float, steps: int, checkpoint_every: int = 10, energy: float = 1.0,
+                impulse=(0.0, 0.0, 1.0), seed_x=None, seed_alpha=None, gradient: bool = True):
+        """vfmm_adjoint: the objective energy * E + impulse . I (+ seeds . final
+        x, alpha) after `steps` steps of advance from `bodies` (not modified),
+        and with gradient=True its gradients with respect to the initial
+        positions and strengths, as (value, grad_x, grad_alpha) with n x 3
+        arrays in the order of `bodies`."""
+        b = _lib.as_bodies(bodies)
+        n = b.size
+        obj = _lib.vfmm_objective()
+        obj.energy = float(energy)
+        for k in range(3):
+            obj.impulse[k] = float(impulse[k])
+        keep = []
+        for name, arr in (("seed_x", seed_x), ("seed_alpha", seed_alpha)):
+            if arr is not None:
+                a = np.ascontiguousarray(arr, dtype=np.float64).reshape(n, 3)
+                keep.append(a)
+                setattr(obj, name, a.ctypes.data)
+        value = ctypes.c_double()
+        gx = np.zeros((n, 3)) if gradient else None
+        ga = np.zeros((n, 3)) if gradient else None
+        self._check(lib().vfmm_adjoint(self._h, b.ctypes.data, n, float(dt), int(steps), int(checkpoint_every), ctypes.byref(obj),
+                                       ctypes.byref(value), gx.ctypes.data if gradient else None,
+                                       ga.ctypes.data if gradient else None))
+        del keep
+        return (value.value, gx, ga) if gradient else value.value
+
     def relax(self, f: float) -> None:
         self._check(lib().vfmm_relax(self._h, float(f)))
 

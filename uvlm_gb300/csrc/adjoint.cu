@@ -1,0 +1,1112 @@
+// Reverse mode of the FP64 evaluation and of the RK stage updates: the
+// building blocks of vfmm_adjoint, the adjoint of advance
+// (fmmCalculator.hpp:919-1005) for the inviscid cVPM path.
+//
+// One evaluation maps the bodies (x, alpha, sigma) to u and J through the
+// expansion passes P2M -> M2M -> M2L -> L2L -> L2P and the P2P near field
+// (multipoleKernels.hpp:223-742), then the stage adds the stretching term
+// dalpha/dt = J^T alpha (or J alpha, fmmCalculator.hpp:391-405).  Given the
+// adjoints (ubar, Jbar) of u and J, the passes run backwards as their exact
+// transposes: L2P^T leaf by leaf, L2L^T up the levels, M2L^T gathered per
+// source cell over the transposed lists, M2M^T down the levels, P2M^T leaf
+// by leaf, and the pair terms of P2P differentiated in closed form, once per
+// target and once per source, so every output has a single writer and the
+// sums run in a fixed order.
+//
+// The tree is a piecewise-constant function of the positions; the cell
+// centres are X0 + R0 o_c with X0, R0 the bounding box of getBounds
+// (tree.hpp:7-26).  Their derivatives follow from two exact invariances of
+// the evaluation: a common translation of bodies and X0 changes nothing, and
+// a dilation about X0 of bodies, R0 and sigma scales u by s^-2 and J by s^-3.
+// So, with xbar_far the far-field partial adjoints at fixed geometry,
+//   X0bar = -sum xbar_far,   R0 R0bar = sum(-2 ubar.u_far - 3 Jbar:J_far)
+//                                         - sum xbar_far . (x - X0),
+// passed to the bodies that set the bounding box.
+#include <algorithm>
+#include "harmonics.cuh"
+#include "vfmm_internal.cuh"
+
+namespace vfmm {
+
+namespace {
+
+typedef cx<double> zd;
+
+static __constant__ HarmRecip<double> kHR = make_harm_recip<double>();
+
+constexpr double kInvPi     = 0.318309886183790671537767526745028724;
+constexpr double kInvSqrtPi = 0.564189583547756286948079451560772586;
+
+__device__ __forceinline__ zd ldz(const double2 *p)
+{
+  const double2 v = *p;
+  return {v.x, v.y};
+}
+__device__ __forceinline__ void stz(double2 *p, zd v) { *p = make_double2(v.r, v.i); }
+__device__ __forceinline__ void cadd(zd &a, zd b)
+{
+  a.r += b.r;
+  a.i += b.i;
+}
+__device__ __forceinline__ void jk_of(int jks, int &j, int &k)
+{
+  j = 0;
+  while ((j + 1) * (j + 2) / 2 <= jks)
+    j++;
+  k = jks - j * (j + 1) / 2;
+}
+
+struct AdjDev {
+  CellsView     cv;
+  const double *soa; // bodies in tree order: X, A, R, and U, J of the FP64 evaluation
+  size_t        cap;
+  const double2 *L;  // local expansions of the evaluation
+  double2       *Lb, *Mb;
+  const int     *leaf_cells;
+  int            nleaves;
+  const int     *p2p_start, *p2p_src;   // P2P rows by target leaf
+  const int     *p2pT_start, *p2pT_tgt; // P2P rows by source leaf
+  const int     *m2lT_start, *m2lT_tgt; // M2L rows by source cell
+  double        *w;                     // work fields (AdjW), field-major, capacity cap
+};
+
+__device__ __forceinline__ double &W(const AdjDev &a, int f, int i) { return a.w[(size_t)f * a.cap + i]; }
+__device__ __forceinline__ double B(const AdjDev &a, int f, int i) { return a.soa[(size_t)f * a.cap + i]; }
+
+// ------------------------------------------------------------------ L2P^T
+// Far field of the forward pass at a body of leaf c:
+//   u_a = sum w_m Re(U_a[n,m] Y_n^m),  U = (1/4pi) curl of the local expansion,
+//   J_ae = sum w_m Re(JJ_ae[n,m] Y_n^m),  JJ_ae = D_e U_a.
+// Adjoint: Ubar[n,m] = sum_b w_m ubar_b conj(Y(x_b)), likewise JJbar, then the
+// transposed derivative operators give Lbar of the leaf.  The body's own
+// position adjoint is ubar . dU/dx + Jbar : dJ/dx, with dJ_ae/dx_g evaluated
+// from HH = D_g JJ_ae.
+template <int P>
+struct AdjL2PSizes {
+  static constexpr int    K  = nterms(P);
+  static constexpr int    N1 = nterms(P - 1);                  // degree <= P-2
+  static constexpr int    N2 = P >= 3 ? nterms(P - 2) : 0;     // degree <= P-3
+  static constexpr int    N3 = P >= 4 ? nterms(P - 3) : 0;     // degree <= P-4
+  static constexpr int    K1 = N1 > 0 ? N1 : 1, K2 = N2 > 0 ? N2 : 1, K3 = N3 > 0 ? N3 : 1;
+  static constexpr int    NB = 32; // bodies per staging chunk
+  static constexpr size_t zcount = 3 * K + 3 * K1 + 9 * K2 + 27 * K3 + 3 * K1 + 9 * K2 + 3 * K + NB * K1;
+  static constexpr size_t bytes  = zcount * sizeof(zd) + NB * 12 * sizeof(double);
+};
+
+template <int P>
+__global__ void __launch_bounds__(128) k_adj_l2p(AdjDev a)
+{
+  using S = AdjL2PSizes<P>;
+  constexpr int K = S::K, K1 = S::K1, K2 = S::K2, K3 = S::K3, N1 = S::N1, N2 = S::N2, N3 = S::N3, NB = S::NB;
+  constexpr int NO = (3 * N1 + 9 * N2 + 127) / 128;
+  extern __shared__ double2 smem_raw[];
+  zd     *Lc  = reinterpret_cast<zd *>(smem_raw);
+  zd     *U   = Lc + 3 * K;
+  zd     *JJ  = U + 3 * K1;
+  zd     *HH  = JJ + 9 * K2;
+  zd     *Ub  = HH + 27 * K3;
+  zd     *JJb = Ub + 3 * K1;
+  zd     *Lb  = JJb + 9 * K2;
+  zd     *Ys  = Lb + 3 * K;
+  double *Sd  = reinterpret_cast<double *>(Ys + NB * K1);
+  const double inv4pi = 0.25 * kInvPi;
+
+  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+    const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
+    const double cxx = a.cv.x[c], cyy = a.cv.y[c], czz = a.cv.z[c];
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * K; e += 128)
+      Lc[e] = ldz(a.L + (size_t)c * 3 * K + e);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * N1; e += 128) { // as the forward L2P
+      const int idx = e / 3, ax = e % 3;
+      int       n, mu;
+      jk_of(idx, n, mu);
+      const int b1 = (ax + 1) % 3, c1 = (ax + 2) % 3;
+      const zd  p = deriv_coef(Lc, n, mu, b1, 3, c1), q = deriv_coef(Lc, n, mu, c1, 3, b1);
+      U[idx * 3 + ax] = {inv4pi * (p.r - q.r), inv4pi * (p.i - q.i)};
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 9 * N2; e += 128) {
+      const int idx = e / 9, ae = e % 9;
+      int       n, mu;
+      jk_of(idx, n, mu);
+      JJ[idx * 9 + ae] = deriv_coef(U, n, mu, ae % 3, 3, ae / 3);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 27 * N3; e += 128) {
+      const int idx = e / 27, r = e % 27;
+      int       n, mu;
+      jk_of(idx, n, mu);
+      HH[idx * 27 + r] = deriv_coef(JJ, n, mu, r % 3, 9, r / 3); // D_g JJ_ae at ae * 3 + g
+    }
+    __syncthreads();
+
+    zd acc[NO > 0 ? NO : 1];
+#pragma unroll
+    for (int i = 0; i < (NO > 0 ? NO : 1); i++)
+      acc[i] = {0, 0};
+    for (int c0 = 0; c0 < nb; c0 += NB) {
+      const int nbc = min(NB, nb - c0);
+      if (threadIdx.x < nbc) {
+        const int t = threadIdx.x, b = b0 + c0 + t;
+        regular_harmonics<double, P - 1>(B(a, F_X, b) - cxx, B(a, F_X + 1, b) - cyy, B(a, F_X + 2, b) - czz, Ys + t * K1);
+        double sd[12];
+        for (int k = 0; k < 12; k++) {
+          sd[k]          = W(a, W_SU + k, b);
+          Sd[t * 12 + k] = sd[k];
+        }
+        double uf[3] = {0, 0, 0}, jf[9], hf[27];
+        for (int k = 0; k < 9; k++)
+          jf[k] = 0;
+        for (int k = 0; k < 27; k++)
+          hf[k] = 0;
+        for (int n = 0; n <= P - 2; n++)
+          for (int m = 0; m <= n; m++) {
+            const int    idx = tri(n, m);
+            const zd     y   = Ys[t * K1 + idx];
+            const double wm  = m == 0 ? 1.0 : 2.0;
+            for (int ax = 0; ax < 3; ax++)
+              uf[ax] += wm * (U[idx * 3 + ax].r * y.r - U[idx * 3 + ax].i * y.i);
+            if (idx < N2)
+              for (int ae = 0; ae < 9; ae++)
+                jf[ae] += wm * (JJ[idx * 9 + ae].r * y.r - JJ[idx * 9 + ae].i * y.i);
+            if (idx < N3)
+              for (int r = 0; r < 27; r++)
+                hf[r] += wm * (HH[idx * 27 + r].r * y.r - HH[idx * 27 + r].i * y.i);
+          }
+        double e = 0;
+        for (int ax = 0; ax < 3; ax++)
+          e -= 2.0 * sd[ax] * uf[ax];
+        for (int ae = 0; ae < 9; ae++)
+          e -= 3.0 * sd[3 + ae] * jf[ae];
+        for (int g = 0; g < 3; g++) {
+          double xb = 0;
+          for (int ax = 0; ax < 3; ax++)
+            xb += sd[ax] * jf[ax * 3 + g];
+          for (int ae = 0; ae < 9; ae++)
+            xb += sd[3 + ae] * hf[ae * 3 + g];
+          W(a, W_XF + g, b) = xb;
+        }
+        W(a, W_EF, b) = e;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < NO; i++) {
+        const int o = threadIdx.x + 128 * i;
+        if (o < 3 * N1) {
+          const int idx = o / 3, ax = o % 3;
+          int       n, m;
+          jk_of(idx, n, m);
+          const double wm = m == 0 ? 1.0 : 2.0;
+          for (int tt = 0; tt < nbc; tt++) {
+            const zd     y = Ys[tt * K1 + idx];
+            const double s = wm * Sd[tt * 12 + ax];
+            acc[i].r += s * y.r;
+            acc[i].i -= s * y.i;
+          }
+        } else if (o < 3 * N1 + 9 * N2) {
+          const int o2 = o - 3 * N1, idx = o2 / 9, ae = o2 % 9;
+          int       n, m;
+          jk_of(idx, n, m);
+          const double wm = m == 0 ? 1.0 : 2.0;
+          for (int tt = 0; tt < nbc; tt++) {
+            const zd     y = Ys[tt * K1 + idx];
+            const double s = wm * Sd[tt * 12 + 3 + ae];
+            acc[i].r += s * y.r;
+            acc[i].i -= s * y.i;
+          }
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < NO; i++) {
+      const int o = threadIdx.x + 128 * i;
+      if (o < 3 * N1)
+        Ub[o] = acc[i];
+      else if (o < 3 * N1 + 9 * N2)
+        JJb[o - 3 * N1] = acc[i];
+    }
+    for (int e = threadIdx.x; e < 3 * K; e += 128)
+      Lb[e] = {0, 0};
+    __syncthreads();
+    // JJ_ae = D_e U_a, transposed: one thread per component a (fixed order)
+    if (threadIdx.x < 3) {
+      const int ax = threadIdx.x;
+      for (int idx = 0; idx < N2; idx++) {
+        int n, mu;
+        jk_of(idx, n, mu);
+        for (int ex = 0; ex < 3; ex++)
+          deriv_coef_adj(Ub, n, mu, ex, 3, ax, JJb[idx * 9 + ax * 3 + ex]);
+      }
+    }
+    __syncthreads();
+    // U_a = (1/4pi)(D_{a+1} psi_{a+2} - D_{a+2} psi_{a+1}), transposed: one thread per psi component
+    if (threadIdx.x < 3) {
+      const int cc = threadIdx.x;
+      for (int idx = 0; idx < N1; idx++) {
+        int n, mu;
+        jk_of(idx, n, mu);
+        const zd u1 = Ub[idx * 3 + (cc + 1) % 3], u2 = Ub[idx * 3 + (cc + 2) % 3];
+        deriv_coef_adj(Lb, n, mu, (cc + 2) % 3, 3, cc, zd{inv4pi * u1.r, inv4pi * u1.i});
+        deriv_coef_adj(Lb, n, mu, (cc + 1) % 3, 3, cc, zd{-inv4pi * u2.r, -inv4pi * u2.i});
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * K; e += 128)
+      stz(a.Lb + (size_t)c * 3 * K + e, Lb[e]);
+  }
+}
+
+// ------------------------------------------------------------------ L2L^T
+// Forward (k_l2l): L_child[j,k] += terms in L_parent[n, +-m] and the regular
+// harmonics of X_child - X_parent.  Transposed, per parent coefficient
+// (n, mm): for every child and child coefficient (j <= n, k <= j),
+//   term A (mm >= 1, k + mm <= n - j): +-conj(Lbar_child[j,k] Y[n-j, k+mm]),
+//   term B (|mm - k| <= n - j):        +-Lbar_child[j,k] (conj Y[n-j, mm-k] | Y[n-j, k-mm]).
+template <int P>
+__global__ void __launch_bounds__(128) k_adj_l2l(AdjDev a, const int *cells, int count)
+{
+  constexpr int K = nterms(P);
+  extern __shared__ double2 smem_raw[];
+  zd *Lch = reinterpret_cast<zd *>(smem_raw); // [8][3K]
+  zd *Ys  = Lch + 8 * 3 * K;                  // [8][K]
+  for (int pi = blockIdx.x; pi < count; pi += gridDim.x) {
+    const int p = cells[pi], nch = a.cv.nchild[p], ch0 = a.cv.child[p];
+    if (nch == 0)
+      continue;
+    __syncthreads();
+    for (int e = threadIdx.x; e < nch * 3 * K; e += blockDim.x)
+      Lch[e] = ldz(a.Lb + (size_t)ch0 * 3 * K + e);
+    if (threadIdx.x < nch) {
+      const int ch = ch0 + threadIdx.x;
+      regular_harmonics<double, P>(a.cv.x[ch] - a.cv.x[p], a.cv.y[ch] - a.cv.y[p], a.cv.z[ch] - a.cv.z[p], Ys + threadIdx.x * K);
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < 3 * K; o += blockDim.x) {
+      const int idx = o / 3, d = o % 3;
+      int       n, mm;
+      jk_of(idx, n, mm);
+      zd acc{0, 0};
+      for (int ci = 0; ci < nch; ci++) {
+        const zd *Y = Ys + ci * K, *Lc = Lch + ci * 3 * K;
+        for (int j = 0; j <= n; j++) {
+          const int nj = n - j;
+          for (int k = 0; k <= j; k++) {
+            const zd l = Lc[tri(j, k) * 3 + d];
+            if (mm >= 1 && k + mm <= nj)
+              cadd(acc, neg_if(conj(l * Y[tri(nj, k + mm)]), (k & 1) != 0));
+            if (abs(mm - k) <= nj) {
+              const bool neg = mm < k && ((k - mm) & 1);
+              const zd   wc  = mm >= k ? conj(Y[tri(nj, mm - k)]) : Y[tri(nj, k - mm)];
+              cadd(acc, neg_if(l * wc, neg));
+            }
+          }
+        }
+      }
+      stz(a.Lb + (size_t)p * 3 * K + o, acc);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ M2L^T
+// Forward (k_m2l): L_t[j,k] = (-1)^j sum_s sum_{n <= P-1-j} sum_m M'_s[n,m] S'_ts[j+n, m-k]
+// with M' the sign-folded multipoles (k_mprep).  Transposed, per source s
+// over its targets t:  M'bar[n,m] = sum_t sum_{j <= P-1-n} sum_{k <= j}
+// (-1)^j Lbar_t[j,k] conj(S'_ts[j+n, m-k]), then
+// Mbar[n,m] = (-1)^m M'bar[n,m] + conj(M'bar[n,-m]) (m > 0).
+// One warp per source cell; lanes own outputs (n, m, d).
+template <int P>
+struct AdjM2LSizes {
+  static constexpr int    K = nterms(P), PP = P * P, NE = 3 * PP;
+  static constexpr int    WS = (3 * K + PP > NE) ? 3 * K + PP : NE; // per warp, zd
+  static constexpr size_t bytes = (size_t)4 * WS * sizeof(zd);
+};
+
+template <int P>
+__global__ void __launch_bounds__(128) k_adj_m2l(AdjDev a, int ncells)
+{
+  using S = AdjM2LSizes<P>;
+  constexpr int K = S::K, NE = S::NE, NA = (NE + 31) / 32, WS = S::WS;
+  extern __shared__ double2 smem_raw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  zd       *Lt = reinterpret_cast<zd *>(smem_raw) + w * WS;
+  zd       *Sp = Lt + 3 * K;
+  int       on[NA], om[NA];
+#pragma unroll
+  for (int i = 0; i < NA; i++) {
+    const int e = lane + 32 * i, idx = e / 3;
+    int       n = 0;
+    while ((n + 1) * (n + 1) <= idx)
+      n++;
+    on[i] = n;
+    om[i] = idx - n * n - n;
+  }
+  for (int s = blockIdx.x * 4 + w; s < ncells; s += gridDim.x * 4) {
+    zd acc[NA];
+#pragma unroll
+    for (int i = 0; i < NA; i++)
+      acc[i] = {0, 0};
+    const int    q0 = a.m2lT_start[s], q1 = a.m2lT_start[s + 1];
+    const double sx = a.cv.x[s], sy = a.cv.y[s], sz = a.cv.z[s];
+    for (int q = q0; q < q1; q++) {
+      const int t = a.m2lT_tgt[q];
+      __syncwarp();
+      for (int e = lane; e < 3 * K; e += 32) {
+        int j, k;
+        jk_of(e / 3, j, k);
+        const zd v = ldz(a.Lb + (size_t)t * 3 * K + e);
+        Lt[e]      = (j & 1) ? zd{-v.r, -v.i} : v;
+      }
+      if (lane < P) {
+        const double dx = a.cv.x[t] - sx, dy = a.cv.y[t] - sy, dz = a.cv.z[t] - sz;
+        const double r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.0 / r2, S00 = sqrt(ir2);
+        zd           col[P];
+        singular_column<double, P>(lane, dx, dy, dz, ir2, S00, col);
+        const int m = lane;
+        for (int n = m; n < P; n++) {
+          const zd v        = col[n];
+          Sp[n * n + n + m] = (m & 1) ? zd{-v.r, -v.i} : v;
+          if (m > 0)
+            Sp[n * n + n - m] = conj(v);
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < NA; i++) {
+        const int e = lane + 32 * i;
+        if (e < NE) {
+          const int d = e % 3, n = on[i], m = om[i];
+          for (int j = 0; j <= P - 1 - n; j++) {
+            const int qq = j + n, base = qq * qq + qq + m;
+            for (int k = 0; k <= j; k++)
+              cadd(acc[i], Lt[tri(j, k) * 3 + d] * conj(Sp[base - k]));
+          }
+        }
+      }
+    }
+    __syncwarp();
+    zd *Mpb = Lt; // [n^2+n+m][d]
+#pragma unroll
+    for (int i = 0; i < NA; i++) {
+      const int e = lane + 32 * i;
+      if (e < NE)
+        Mpb[e] = acc[i];
+    }
+    __syncwarp();
+    for (int e = lane; e < 3 * K; e += 32) {
+      const int d = e % 3;
+      int       n, mm;
+      jk_of(e / 3, n, mm);
+      zd v = Mpb[(n * n + n + mm) * 3 + d];
+      if (mm & 1)
+        v = {-v.r, -v.i};
+      if (mm > 0)
+        cadd(v, conj(Mpb[(n * n + n - mm) * 3 + d]));
+      stz(a.Mb + (size_t)s * 3 * K + e, v);
+    }
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------ M2M^T
+// Forward (m2m_term_sum): M_parent[j,k] += terms in M_child[j-n, .] and the
+// regular harmonics of X_parent - X_child.  Transposed, per child
+// coefficient (j', k'), over n <= P-1-j' and the parent's (j' + n, k):
+//   term 1 (k' >= 1, m = k - k', |m| <= n): +-Mbar_p[j,k] (Y[n,m] | conj Y[n,|m|]),
+//   term 2 (m = k + k' <= n):               +-conj(Mbar_p[j,k] Y[n,m]).
+template <int P>
+__global__ void __launch_bounds__(128) k_adj_m2m(AdjDev a, const int *cells, int count)
+{
+  constexpr int K = nterms(P);
+  extern __shared__ double2 smem_raw[];
+  zd *Mp = reinterpret_cast<zd *>(smem_raw); // [3K]
+  zd *Ys = Mp + 3 * K;                       // [8][K]
+  for (int pi = blockIdx.x; pi < count; pi += gridDim.x) {
+    const int c = cells[pi], nch = a.cv.nchild[c], ch0 = a.cv.child[c];
+    if (nch == 0)
+      continue;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * K; e += blockDim.x)
+      Mp[e] = ldz(a.Mb + (size_t)c * 3 * K + e);
+    if (threadIdx.x < nch) {
+      const int ch = ch0 + threadIdx.x;
+      regular_harmonics<double, P>(a.cv.x[c] - a.cv.x[ch], a.cv.y[c] - a.cv.y[ch], a.cv.z[c] - a.cv.z[ch], Ys + threadIdx.x * K);
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < nch * 3 * K; o += blockDim.x) {
+      const int ci = o / (3 * K), r = o % (3 * K), d = r % 3;
+      int       jp, kp;
+      jk_of(r / 3, jp, kp);
+      const zd *Y = Ys + ci * K;
+      zd        acc{0, 0};
+      for (int n = 0; n <= P - 1 - jp; n++) {
+        const int j = jp + n;
+        if (kp >= 1)
+          for (int k = max(0, kp - n); k <= min(j, kp + n); k++) {
+            const int  m   = k - kp;
+            const zd   y   = Y[tri(n, m > 0 ? m : -m)];
+            const bool neg = ((m < 0 ? (m & 1) : 0) ^ (n & 1)) != 0;
+            cadd(acc, neg_if(Mp[tri(j, k) * 3 + d] * (m > 0 ? y : conj(y)), neg));
+          }
+        for (int k = 0; k <= n - kp; k++) {
+          const int  m   = k + kp;
+          const bool neg = ((k + n + m) & 1) != 0;
+          cadd(acc, neg_if(conj(Mp[tri(j, k) * 3 + d] * Y[tri(n, m)]), neg));
+        }
+      }
+      double2 *q = a.Mb + (size_t)(ch0 + ci) * 3 * K + r;
+      stz(q, ldz(q) + acc);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ P2M^T
+// Forward (k_p2m): M_d[n,m] = sum_b alpha_bd conj(Y_n^m(x_b - X_c)).
+//   alphabar_bd = sum Re(Mbar_d[n,m] Y_n^m(x_b - X_c)),
+//   xbar_b = sum_d alpha_bd grad phi_d,  phi_d(x) = sum Re(Mbar_d[n,m] Y_n^m(x)),
+// the gradient from the derivative operators applied to Mbar_d written as a
+// full-range real expansion (m > 0 terms halved).
+template <int P>
+struct AdjP2MSizes {
+  static constexpr int    K = nterms(P), N1 = nterms(P - 1);
+  static constexpr size_t bytes = (size_t)(6 * K + 9 * N1) * sizeof(zd);
+};
+
+template <int P>
+__global__ void __launch_bounds__(128) k_adj_p2m(AdjDev a)
+{
+  constexpr int K = nterms(P), N1 = nterms(P - 1);
+  extern __shared__ double2 smem_raw[];
+  zd *Mb = reinterpret_cast<zd *>(smem_raw); // [K][3]
+  zd *Cn = Mb + 3 * K;                       // [K][3]
+  zd *DM = Cn + 3 * K;                       // [N1][9]: D_ax of component d at ax * 3 + d
+  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+    const int c = a.leaf_cells[li];
+    if (a.cv.level[c] == 0)
+      continue; // the forward P2M skips level 0
+    const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
+    const double cxx = a.cv.x[c], cyy = a.cv.y[c], czz = a.cv.z[c];
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * K; e += blockDim.x) {
+      int n, m;
+      jk_of(e / 3, n, m);
+      const zd v = ldz(a.Mb + (size_t)c * 3 * K + e);
+      Mb[e]      = v;
+      Cn[e]      = m == 0 ? v : zd{0.5 * v.r, 0.5 * v.i};
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 9 * N1; e += blockDim.x) {
+      const int idx = e / 9, r = e % 9;
+      int       n, mu;
+      jk_of(idx, n, mu);
+      DM[idx * 9 + r] = deriv_coef(Cn, n, mu, r / 3, 3, r % 3);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+      const int    b = b0 + t;
+      const double x = B(a, F_X, b) - cxx, y = B(a, F_X + 1, b) - cyy, z = B(a, F_X + 2, b) - czz;
+      const double al[3] = {B(a, F_A, b), B(a, F_A + 1, b), B(a, F_A + 2, b)};
+      const double r2    = x * x + y * y + z * z;
+      double       ab[3] = {0, 0, 0}, F[9];
+      for (int k = 0; k < 9; k++)
+        F[k] = 0;
+      zd diag{1.0, 0.0};
+      for (int m = 0; m < P; m++) {
+        if (m > 0) {
+          const double s = kHR.s[m];
+          diag           = {(diag.r * x - diag.i * y) * s, (diag.r * y + diag.i * x) * s};
+        }
+        const double wm = m == 0 ? 1.0 : 2.0;
+        zd           ya = diag, yb{0, 0};
+        double       tn = double(2 * m + 1);
+        for (int n = m; n < P; n++, tn += 2.0) {
+          const int ti = tri(n, m);
+          for (int d = 0; d < 3; d++)
+            ab[d] += Mb[ti * 3 + d].r * ya.r - Mb[ti * 3 + d].i * ya.i;
+          if (n <= P - 2)
+            for (int k = 0; k < 9; k++)
+              F[k] += wm * (DM[ti * 9 + k].r * ya.r - DM[ti * 9 + k].i * ya.i);
+          if (n + 1 < P) {
+            const double cc = kHR.c[ti], zz = tn * z;
+            const zd     nx = {cc * (zz * ya.r + r2 * yb.r), cc * (zz * ya.i + r2 * yb.i)};
+            yb              = ya;
+            ya              = nx;
+          }
+        }
+      }
+      for (int d = 0; d < 3; d++)
+        W(a, W_AP2M + d, b) = ab[d];
+      for (int ax = 0; ax < 3; ax++)
+        W(a, W_XF + ax, b) += al[0] * F[ax * 3] + al[1] * F[ax * 3 + 1] + al[2] * F[ax * 3 + 2];
+    }
+  }
+}
+
+// ------------------------------------------------------------------ P2P^T
+// One pair of the forward near field (target i, source j, d = x_i - x_j,
+// sigma = sigma_j, R^2 != 0): u_i -= q (d x alpha_j), J_i -= grad_d(q (d x alpha_j)),
+// q = g / (4 pi r^3), g = erf(sqrt(RS)) - (2/sqrt(pi)) sqrt(RS) e^-RS,
+// RS = r^2 / (2 sigma^2).  Its part of S = ubar.u + Jbar:J is
+//   s = -q (A + C) - h B,  A = alpha.(ubar x d), B = alpha.((Jbar d) x d),
+//   C = alpha.ct,  ct_c = eps_abc Jbar_ab,  h = q'(r)/r,
+// and the derivatives below follow with q_{r^2} = h/2 and
+//   h_{r^2} = c4 (-2.5 t2/(sigma^2 r^2) - 0.5 t2/sigma^4 + 7.5 g/r^4),
+// t2 = (2/sqrt(pi)) sqrt(RS) e^-RS, c4 = 1/(4 pi r^3).
+// gd = ds/dd (to x_i; minus to x_j), wa = ds/dalpha_j.
+__device__ __forceinline__ void pair_adj(double dx, double dy, double dz, const double *al, double sg, const double *ub, const double *Jb,
+                                         const double *ct, double *gd, double *wa)
+{
+  const double R2 = dx * dx + dy * dy + dz * dz;
+  const double S2 = sg * sg, RS = R2 / S2 / 2.0, sqrtRS = sqrt(RS);
+  const double erfS = erf(sqrtRS), expm = exp(-RS), invR = 1.0 / sqrt(R2);
+  const double t2 = 2.0 * kInvSqrtPi * sqrtRS * expm, c4 = 0.25 * kInvPi / R2 * invR, g = erfS - t2;
+  const double q   = g * c4;
+  const double h   = c4 * (t2 / S2 - 3.0 * g / R2);
+  const double hR2 = c4 * (-2.5 * t2 / (S2 * R2) - 0.5 * t2 / (S2 * S2) + 7.5 * g / (R2 * R2));
+  const double d[3] = {dx, dy, dz};
+  double       m[3];
+  for (int r = 0; r < 3; r++)
+    m[r] = Jb[3 * r] * dx + Jb[3 * r + 1] * dy + Jb[3 * r + 2] * dz;
+  const double uxd[3] = {ub[1] * dz - ub[2] * dy, ub[2] * dx - ub[0] * dz, ub[0] * dy - ub[1] * dx};
+  const double mxd[3] = {m[1] * dz - m[2] * dy, m[2] * dx - m[0] * dz, m[0] * dy - m[1] * dx};
+  const double A = al[0] * uxd[0] + al[1] * uxd[1] + al[2] * uxd[2];
+  const double Bv = al[0] * mxd[0] + al[1] * mxd[1] + al[2] * mxd[2];
+  const double C = al[0] * ct[0] + al[1] * ct[1] + al[2] * ct[2];
+  const double dxa[3] = {dy * al[2] - dz * al[1], dz * al[0] - dx * al[2], dx * al[1] - dy * al[0]};
+  const double axu[3] = {al[1] * ub[2] - al[2] * ub[1], al[2] * ub[0] - al[0] * ub[2], al[0] * ub[1] - al[1] * ub[0]};
+  const double axm[3] = {al[1] * m[2] - al[2] * m[1], al[2] * m[0] - al[0] * m[2], al[0] * m[1] - al[1] * m[0]};
+  const double fq = -h * (A + C) - 2.0 * hR2 * Bv; // -2 q_{r^2} (A + C) - 2 h_{r^2} B
+  for (int k = 0; k < 3; k++) {
+    const double jtd = Jb[k] * dxa[0] + Jb[3 + k] * dxa[1] + Jb[6 + k] * dxa[2];
+    gd[k]            = fq * d[k] - q * axu[k] - h * (jtd + axm[k]);
+    wa[k]            = -q * uxd[k] - h * mxd[k] - q * ct[k];
+  }
+}
+
+__device__ __forceinline__ void load_seeds(const AdjDev &a, int i, double *ub, double *Jb, double *ct)
+{
+  for (int k = 0; k < 3; k++)
+    ub[k] = W(a, W_SU + k, i);
+  for (int k = 0; k < 9; k++)
+    Jb[k] = W(a, W_SJ + k, i);
+  ct[0] = Jb[5] - Jb[7];
+  ct[1] = Jb[6] - Jb[2];
+  ct[2] = Jb[1] - Jb[3];
+}
+
+// Per target: xbar_i += sum over its near sources of ds/dd.
+__global__ void __launch_bounds__(128) k_adj_p2p_tgt(AdjDev a)
+{
+  __shared__ double red[128 * 3];
+  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+    const int c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
+    const int q0 = a.p2p_start[c], q1 = a.p2p_start[c + 1];
+    for (int tc = 0; tc < nb; tc += 128) {
+      const int nbc = min(128, nb - tc);
+      const int TG = nbc <= 32 ? 32 : (nbc <= 64 ? 64 : 128), G = 128 / TG;
+      const int tt = threadIdx.x % TG, g = threadIdx.x / TG;
+      double    s[3] = {0, 0, 0};
+      if (tt < nbc) {
+        const int    i  = b0 + tc + tt;
+        const double xi = B(a, F_X, i), yi = B(a, F_X + 1, i), zi = B(a, F_X + 2, i);
+        double       ub[3], Jb[9], ct[3];
+        load_seeds(a, i, ub, Jb, ct);
+        for (int q = q0 + g; q < q1; q += G) {
+          const int sc = a.p2p_src[q], sb = a.cv.body[sc], sn = a.cv.nbody[sc];
+          for (int j = sb; j < sb + sn; j++) {
+            const double dx = xi - B(a, F_X, j), dy = yi - B(a, F_X + 1, j), dz = zi - B(a, F_X + 2, j);
+            if (dx * dx + dy * dy + dz * dz != 0) {
+              const double al[3] = {B(a, F_A, j), B(a, F_A + 1, j), B(a, F_A + 2, j)};
+              double       gd[3], wa[3];
+              pair_adj(dx, dy, dz, al, B(a, F_R, j), ub, Jb, ct, gd, wa);
+              for (int k = 0; k < 3; k++)
+                s[k] += gd[k];
+            }
+          }
+        }
+      }
+      __syncthreads();
+      for (int k = 0; k < 3; k++)
+        red[threadIdx.x * 3 + k] = s[k];
+      __syncthreads();
+      if (threadIdx.x < nbc) {
+        const int i = b0 + tc + threadIdx.x;
+        for (int k = 0; k < 3; k++) {
+          double v = 0;
+          for (int gg = 0; gg < G; gg++)
+            v += red[(gg * TG + threadIdx.x) * 3 + k];
+          W(a, W_XNT + k, i) = v;
+        }
+      }
+    }
+  }
+}
+
+// Per source: xbar_j -= sum over its near targets of ds/dd, alphabar_j += ds/dalpha_j.
+__global__ void __launch_bounds__(128) k_adj_p2p_src(AdjDev a)
+{
+  __shared__ double red[128 * 6];
+  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+    const int c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
+    const int q0 = a.p2pT_start[c], q1 = a.p2pT_start[c + 1];
+    for (int tc = 0; tc < nb; tc += 128) {
+      const int nbc = min(128, nb - tc);
+      const int TG = nbc <= 32 ? 32 : (nbc <= 64 ? 64 : 128), G = 128 / TG;
+      const int tt = threadIdx.x % TG, g = threadIdx.x / TG;
+      double    s[6] = {0, 0, 0, 0, 0, 0};
+      if (tt < nbc) {
+        const int    j  = b0 + tc + tt;
+        const double xj = B(a, F_X, j), yj = B(a, F_X + 1, j), zj = B(a, F_X + 2, j);
+        const double al[3] = {B(a, F_A, j), B(a, F_A + 1, j), B(a, F_A + 2, j)};
+        const double sg    = B(a, F_R, j);
+        for (int q = q0 + g; q < q1; q += G) {
+          const int tcell = a.p2pT_tgt[q], tb = a.cv.body[tcell], tn = a.cv.nbody[tcell];
+          for (int i = tb; i < tb + tn; i++) {
+            const double dx = B(a, F_X, i) - xj, dy = B(a, F_X + 1, i) - yj, dz = B(a, F_X + 2, i) - zj;
+            if (dx * dx + dy * dy + dz * dz != 0) {
+              double ub[3], Jb[9], ct[3], gd[3], wa[3];
+              load_seeds(a, i, ub, Jb, ct);
+              pair_adj(dx, dy, dz, al, sg, ub, Jb, ct, gd, wa);
+              for (int k = 0; k < 3; k++) {
+                s[k] -= gd[k];
+                s[3 + k] += wa[k];
+              }
+            }
+          }
+        }
+      }
+      __syncthreads();
+      for (int k = 0; k < 6; k++)
+        red[threadIdx.x * 6 + k] = s[k];
+      __syncthreads();
+      if (threadIdx.x < nbc) {
+        const int j = b0 + tc + threadIdx.x;
+        for (int k = 0; k < 6; k++) {
+          double v = 0;
+          for (int gg = 0; gg < G; gg++)
+            v += red[(gg * TG + threadIdx.x) * 6 + k];
+          W(a, k < 3 ? W_XNS + k : W_ANS + k - 3, j) = v;
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ bodies
+// Seeds of an evaluation from the stage cotangent (cu, ca) of (u, dalpha/dt):
+// ubar = cu and, for dalpha/dt = J^T alpha (transposed) or J alpha
+// (classic), Jbar and the direct alphabar.
+__global__ void k_adj_seeds(const double *soa, double *w, size_t cap, int n, int stretching)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    auto         S  = [&](int f) -> double & { return w[(size_t)f * cap + i]; };
+    auto         Bf = [&](int f) { return soa[(size_t)f * cap + i]; };
+    const double ca[3] = {S(W_COT + 3), S(W_COT + 4), S(W_COT + 5)};
+    const double al[3] = {Bf(F_A), Bf(F_A + 1), Bf(F_A + 2)};
+    for (int k = 0; k < 3; k++)
+      S(W_SU + k) = S(W_COT + k);
+    for (int r = 0; r < 3; r++)
+      for (int cc = 0; cc < 3; cc++) {
+        // transposed: dadt_c' = sum_r J[r][c'] alpha_r -> Jbar[r][c'] = alpha_r ca_c'
+        // classic:    dadt_r  = sum_c J[r][c] alpha_c  -> Jbar[r][c]  = ca_r alpha_c
+        S(W_SJ + 3 * r + cc) = stretching == VFMM_TRANSPOSED ? al[r] * ca[cc] : ca[r] * al[cc];
+      }
+    for (int cc = 0; cc < 3; cc++) {
+      double v = 0;
+      for (int r = 0; r < 3; r++)
+        v += (stretching == VFMM_TRANSPOSED ? Bf(F_J + 3 * cc + r) : Bf(F_J + 3 * r + cc)) * ca[r];
+      S(W_ASTR + cc) = v;
+    }
+  }
+}
+
+// The transposed stage update (bodies.cu k_stage_update) in the tree order
+// of the stage: the stage's cotangent of (u, dalpha/dt) into W_COT, the
+// adjoint state g updated except for the evaluation's own contribution.
+__global__ void k_adj_stage_pre(double *g, double *w, size_t cap, int n, int scheme, int stage, double h)
+{
+  const double A  = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
+  const double Bc = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    auto G  = [&](int f) -> double & { return g[(size_t)f * cap + i]; };
+    auto Wc = [&](int f) -> double & { return w[(size_t)(W_COT + f) * cap + i]; };
+    for (int k = 0; k < 3; k++) {
+      double *xb = &G(G_XB + k), *ab = &G(G_AB + k), *vb = &G(G_VB + k), *db = &G(G_DB + k), *xob = &G(G_XOB + k), *aob = &G(G_AOB + k);
+      if (scheme == VFMM_EULER) { // x' = x + h f
+        Wc(k)     = h * *xb;
+        Wc(3 + k) = h * *ab;
+      } else if (scheme == VFMM_RK2 && stage == 0) { // xold = x; v = f; x' = x + h v
+        const double vt = *vb + h * *xb, dt_ = *db + h * *ab;
+        Wc(k)           = vt;
+        Wc(3 + k)       = dt_;
+        *xb += *xob;
+        *ab += *aob;
+        *vb = *db = *xob = *aob = 0;
+      } else if (scheme == VFMM_RK2) { // v' = f/2 + v/2; x' = xold + h v'
+        const double vt = *vb + h * *xb, dt_ = *db + h * *ab;
+        Wc(k)           = 0.5 * vt;
+        Wc(3 + k)       = 0.5 * dt_;
+        *xob += *xb;
+        *aob += *ab;
+        *xb = *ab = 0;
+        *vb       = 0.5 * vt;
+        *db       = 0.5 * dt_;
+      } else { // RK3: Q' = A Q + h f; x' = x + B Q'
+        const double qx = *vb + Bc * *xb, qa = *db + Bc * *ab;
+        Wc(k)           = h * qx;
+        Wc(3 + k)       = h * qa;
+        *vb             = A * qx;
+        *db             = A * qa;
+      }
+    }
+  }
+}
+
+// g[XB] += the evaluation's position adjoints, g[AB] += its strength adjoints.
+__global__ void k_adj_combine(double *g, const double *w, size_t cap, int n)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int k = 0; k < 3; k++) {
+      const size_t o = (size_t)k * cap + i;
+      g[(size_t)G_XB * cap + o] += w[(size_t)W_XF * cap + o] + w[(size_t)W_XNT * cap + o] + w[(size_t)W_XNS * cap + o];
+      g[(size_t)G_AB * cap + o] += w[(size_t)W_ASTR * cap + o] + w[(size_t)W_AP2M * cap + o] + w[(size_t)W_ANS * cap + o];
+    }
+}
+
+// Bounding-box terms.  Per block: sum xbar_far (3), sum e (1),
+// sum xbar_far.(x - X0) (1), then per axis (min, argmin, max, argmax).
+constexpr int GEO_BLOCKS = 152 * 2, GEO_THREADS = 256, GEO_FIELDS = 17;
+__global__ void __launch_bounds__(GEO_THREADS) k_adj_geom_partial(const double *soa, const double *w, size_t cap, int n, const DevInfo *info,
+                                                                   double *part)
+{
+  __shared__ double red[GEO_THREADS][GEO_FIELDS];
+  double            v[GEO_FIELDS];
+  for (int k = 0; k < 5; k++)
+    v[k] = 0;
+  for (int d = 0; d < 3; d++) {
+    v[5 + 4 * d] = INFINITY;
+    v[6 + 4 * d] = -1;
+    v[7 + 4 * d] = -INFINITY;
+    v[8 + 4 * d] = -1;
+  }
+  const double X0[3] = {info->X0[0], info->X0[1], info->X0[2]};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int d = 0; d < 3; d++) {
+      const double xf = w[(size_t)(W_XF + d) * cap + i], x = soa[(size_t)(F_X + d) * cap + i];
+      v[d] += xf;
+      v[4] += xf * (x - X0[d]);
+      if (x < v[5 + 4 * d]) {
+        v[5 + 4 * d] = x;
+        v[6 + 4 * d] = i;
+      }
+      if (x > v[7 + 4 * d]) {
+        v[7 + 4 * d] = x;
+        v[8 + 4 * d] = i;
+      }
+    }
+    v[3] += w[(size_t)W_EF * cap + i];
+  }
+  for (int k = 0; k < GEO_FIELDS; k++)
+    red[threadIdx.x][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int t = 1; t < GEO_THREADS; t++) {
+      for (int k = 0; k < 5; k++)
+        v[k] += red[t][k];
+      for (int d = 0; d < 3; d++) {
+        const double *r = red[t];
+        if (r[5 + 4 * d] < v[5 + 4 * d] || (r[5 + 4 * d] == v[5 + 4 * d] && r[6 + 4 * d] >= 0 && r[6 + 4 * d] < v[6 + 4 * d])) {
+          v[5 + 4 * d] = r[5 + 4 * d];
+          v[6 + 4 * d] = r[6 + 4 * d];
+        }
+        if (r[7 + 4 * d] > v[7 + 4 * d] || (r[7 + 4 * d] == v[7 + 4 * d] && r[8 + 4 * d] >= 0 && r[8 + 4 * d] < v[8 + 4 * d])) {
+          v[7 + 4 * d] = r[7 + 4 * d];
+          v[8 + 4 * d] = r[8 + 4 * d];
+        }
+      }
+    }
+    for (int k = 0; k < GEO_FIELDS; k++)
+      part[blockIdx.x * GEO_FIELDS + k] = v[k];
+  }
+}
+
+__global__ void k_adj_geom_final(const double *part, int nb, const DevInfo *info, double *g, size_t cap)
+{
+  if (threadIdx.x || blockIdx.x)
+    return;
+  double v[GEO_FIELDS];
+  for (int k = 0; k < GEO_FIELDS; k++)
+    v[k] = part[k];
+  for (int b = 1; b < nb; b++) {
+    const double *r = part + b * GEO_FIELDS;
+    for (int k = 0; k < 5; k++)
+      v[k] += r[k];
+    for (int d = 0; d < 3; d++) {
+      if (r[5 + 4 * d] < v[5 + 4 * d] || (r[5 + 4 * d] == v[5 + 4 * d] && r[6 + 4 * d] >= 0 && r[6 + 4 * d] < v[6 + 4 * d])) {
+        v[5 + 4 * d] = r[5 + 4 * d];
+        v[6 + 4 * d] = r[6 + 4 * d];
+      }
+      if (r[7 + 4 * d] > v[7 + 4 * d] || (r[7 + 4 * d] == v[7 + 4 * d] && r[8 + 4 * d] >= 0 && r[8 + 4 * d] < v[8 + 4 * d])) {
+        v[7 + 4 * d] = r[7 + 4 * d];
+        v[8 + 4 * d] = r[8 + 4 * d];
+      }
+    }
+  }
+  const double R0 = info->R0;
+  if (!(R0 > 0))
+    return;
+  const double R0b = (v[3] - v[4]) / R0;
+  int          ds  = 0;
+  for (int d = 1; d < 3; d++)
+    if (v[7 + 4 * d] - v[5 + 4 * d] > v[7 + 4 * ds] - v[5 + 4 * ds])
+      ds = d;
+  for (int d = 0; d < 3; d++) {
+    const int    imn = (int)v[6 + 4 * d], imx = (int)v[8 + 4 * d];
+    const double X0b = -v[d];
+    double       gmn = 0.5 * X0b, gmx = 0.5 * X0b;
+    if (d == ds) { // R0 = 1.00001 (max - min) / 2 along the widest axis
+      gmx += 0.5 * 1.00001 * R0b;
+      gmn -= 0.5 * 1.00001 * R0b;
+    }
+    if (imn >= 0)
+      g[(size_t)(G_XB + d) * cap + imn] += gmn;
+    if (imx >= 0)
+      g[(size_t)(G_XB + d) * cap + imx] += gmx;
+  }
+}
+
+// out[f][perm[p]] = in[f][p] for the NG adjoint-state fields.
+__global__ void k_adj_scatter(const double *__restrict__ in, double *__restrict__ out, size_t cap, int n, const uint32_t *__restrict__ perm)
+{
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const uint32_t q = perm[p];
+    for (int f = 0; f < NG; f++)
+      out[(size_t)f * cap + q] = in[(size_t)f * cap + p];
+  }
+}
+
+__global__ void k_orig_update(const int *__restrict__ in, int *__restrict__ out, const uint32_t *__restrict__ perm, int n)
+{
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+    out[p] = in[perm[p]];
+}
+
+__global__ void k_iota_int(int *a, int n)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    a[i] = i;
+}
+
+// Objective at the final state (bodies in the order of their last tree, u
+// from an FP64 evaluation; orig = index of each body in the caller's array):
+//   value = wE sum u.(x cross alpha) + 1/2 wI.sum x cross alpha + seeds.(x, alpha),
+// its direct derivatives into g, the seed of u into W_SU (Jbar = 0).
+constexpr int OBJ_BLOCKS = 152 * 2, OBJ_THREADS = 256;
+__global__ void __launch_bounds__(OBJ_THREADS) k_adj_objective(const double *soa, size_t cap, int n, const int *orig, const double *seed_x,
+                                                                const double *seed_a, double wE, double wI0, double wI1, double wI2, double *g,
+                                                                double *w, double *part)
+{
+  __shared__ double red[OBJ_THREADS];
+  const double      wI[3] = {wI0, wI1, wI2};
+  double            acc   = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    auto         Bf = [&](int f) { return soa[(size_t)f * cap + i]; };
+    const double x[3] = {Bf(F_X), Bf(F_X + 1), Bf(F_X + 2)}, al[3] = {Bf(F_A), Bf(F_A + 1), Bf(F_A + 2)},
+                 u[3] = {Bf(F_U), Bf(F_U + 1), Bf(F_U + 2)};
+    const double xa[3] = {x[1] * al[2] - x[2] * al[1], x[2] * al[0] - x[0] * al[2], x[0] * al[1] - x[1] * al[0]};
+    const double au[3] = {al[1] * u[2] - al[2] * u[1], al[2] * u[0] - al[0] * u[2], al[0] * u[1] - al[1] * u[0]};
+    const double ux[3] = {u[1] * x[2] - u[2] * x[1], u[2] * x[0] - u[0] * x[2], u[0] * x[1] - u[1] * x[0]};
+    const double aw[3] = {al[1] * wI[2] - al[2] * wI[1], al[2] * wI[0] - al[0] * wI[2], al[0] * wI[1] - al[1] * wI[0]};
+    const double wx[3] = {wI[1] * x[2] - wI[2] * x[1], wI[2] * x[0] - wI[0] * x[2], wI[0] * x[1] - wI[1] * x[0]};
+    const int    o     = orig[i];
+    for (int k = 0; k < 3; k++) {
+      const double sx = seed_x ? seed_x[3 * (size_t)o + k] : 0.0, sa = seed_a ? seed_a[3 * (size_t)o + k] : 0.0;
+      acc += wE * u[k] * xa[k] + 0.5 * wI[k] * xa[k] + sx * x[k] + sa * al[k];
+      g[(size_t)(G_XB + k) * cap + i]  = wE * au[k] + 0.5 * aw[k] + sx;
+      g[(size_t)(G_AB + k) * cap + i]  = wE * ux[k] + 0.5 * wx[k] + sa;
+      g[(size_t)(G_VB + k) * cap + i]  = 0;
+      g[(size_t)(G_DB + k) * cap + i]  = 0;
+      g[(size_t)(G_XOB + k) * cap + i] = 0;
+      g[(size_t)(G_AOB + k) * cap + i] = 0;
+      w[(size_t)(W_SU + k) * cap + i]   = wE * xa[k];
+      w[(size_t)(W_ASTR + k) * cap + i] = 0;
+    }
+    for (int k = 0; k < 9; k++)
+      w[(size_t)(W_SJ + k) * cap + i] = 0;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int st = OBJ_THREADS / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    part[blockIdx.x] = red[0];
+}
+
+__global__ void k_sum_final(const double *part, int nb, double *out)
+{
+  if (threadIdx.x || blockIdx.x)
+    return;
+  double v = 0;
+  for (int b = 0; b < nb; b++)
+    v += part[b];
+  *out = v;
+}
+
+__global__ void k_adj_rows(const double *g, size_t cap, int n, int field, double *rows)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int k = 0; k < 3; k++)
+      rows[3 * (size_t)i + k] = g[(size_t)(field + k) * cap + i];
+}
+
+// ------------------------------------------------------------------ host side
+template <class KernelT>
+void set_smem(KernelT k, size_t bytes, bool &once)
+{
+  if (!once) {
+    VFMM_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    once = true;
+  }
+}
+
+template <int P>
+void eval_adjoint_P(cudaStream_t s, const ExpArgs &e, const AdjDev &d)
+{
+  constexpr int K = nterms(P);
+  static bool   o1 = false, o2 = false, o3 = false, o4 = false, o5 = false;
+  if (e.nleaves > 0) {
+    set_smem(k_adj_l2p<P>, AdjL2PSizes<P>::bytes, o1);
+    k_adj_l2p<P><<<std::min(e.nleaves, 152 * 8), 128, AdjL2PSizes<P>::bytes, s>>>(d);
+    count_launch();
+  }
+  const size_t bl2l = (size_t)(8 * 3 * K + 8 * K) * sizeof(zd);
+  set_smem(k_adj_l2l<P>, bl2l, o2);
+  for (int l = e.maxLevel - 1; l >= 0; l--) { // forward L2L runs parents at levels 0 .. maxLevel-1
+    const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
+    if (n1 > n0) {
+      k_adj_l2l<P><<<std::min(n1 - n0, 152 * 16), 128, bl2l, s>>>(d, e.level_cells + n0, n1 - n0);
+      count_launch();
+    }
+  }
+  set_smem(k_adj_m2l<P>, AdjM2LSizes<P>::bytes, o3);
+  k_adj_m2l<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2LSizes<P>::bytes, s>>>(d, e.ncells);
+  count_launch();
+  const size_t bm2m = (size_t)(3 * K + 8 * K) * sizeof(zd);
+  set_smem(k_adj_m2m<P>, bm2m, o4);
+  for (int l = 1; l <= e.maxLevel - 1; l++) { // forward M2M runs parents at levels maxLevel-1 .. 1
+    const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
+    if (n1 > n0) {
+      k_adj_m2m<P><<<std::min(n1 - n0, 152 * 16), 128, bm2m, s>>>(d, e.level_cells + n0, n1 - n0);
+      count_launch();
+    }
+  }
+  if (e.nleaves > 0) {
+    set_smem(k_adj_p2m<P>, AdjP2MSizes<P>::bytes, o5);
+    k_adj_p2m<P><<<std::min(e.nleaves, 152 * 8), 128, AdjP2MSizes<P>::bytes, s>>>(d);
+    count_launch();
+    k_adj_p2p_tgt<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
+    count_launch();
+    k_adj_p2p_src<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
+    count_launch();
+  }
+  VFMM_LAUNCH_CHECK();
+}
+
+} // namespace
+
+void adjoint_eval(cudaStream_t s, const ExpArgs &e, const AdjBufs &b, const DevInfo *info)
+{
+  AdjDev d{};
+  d.cv         = e.cells;
+  d.soa        = e.soa;
+  d.cap        = e.cap;
+  d.L          = e.L;
+  d.Lb         = b.Lb;
+  d.Mb         = b.Mb;
+  d.leaf_cells = e.leaf_cells;
+  d.nleaves    = e.nleaves;
+  d.p2p_start  = e.p2p_start;
+  d.p2p_src    = e.p2p_src;
+  d.p2pT_start = b.p2pT_start;
+  d.p2pT_tgt   = b.p2pT_tgt;
+  d.m2lT_start = b.m2lT_start;
+  d.m2lT_tgt   = b.m2lT_tgt;
+  d.w          = b.w;
+  const int n  = b.n;
+  VFMM_CUDA_TRY(cudaMemsetAsync(b.w + (size_t)W_AP2M * e.cap, 0, 3 * e.cap * sizeof(double), s));
+  switch (e.P) {
+#define VFMM_ADJ_CASE(PP)                                                                                                                 \
+  case PP: eval_adjoint_P<PP>(s, e, d); break;
+    VFMM_ADJ_CASE(2) VFMM_ADJ_CASE(3) VFMM_ADJ_CASE(4) VFMM_ADJ_CASE(5) VFMM_ADJ_CASE(6) VFMM_ADJ_CASE(7) VFMM_ADJ_CASE(8)
+    VFMM_ADJ_CASE(9) VFMM_ADJ_CASE(10) VFMM_ADJ_CASE(11) VFMM_ADJ_CASE(12) VFMM_ADJ_CASE(13) VFMM_ADJ_CASE(14) VFMM_ADJ_CASE(15)
+    VFMM_ADJ_CASE(16)
+#undef VFMM_ADJ_CASE
+  default: throw Error(VFMM_ERR_UNSUPPORTED, "expansion order p must be in 2..16");
+  }
+  k_adj_combine<<<grid_for(n, 256), 256, 0, s>>>(b.g, b.w, e.cap, n);
+  count_launch();
+  k_adj_geom_partial<<<GEO_BLOCKS, GEO_THREADS, 0, s>>>(e.soa, b.w, e.cap, n, info, b.part);
+  count_launch();
+  k_adj_geom_final<<<1, 32, 0, s>>>(b.part, GEO_BLOCKS, info, b.g, e.cap);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+void adjoint_seeds(cudaStream_t s, const double *soa, double *w, size_t cap, int n, int stretching)
+{
+  k_adj_seeds<<<grid_for(n, 256), 256, 0, s>>>(soa, w, cap, n, stretching);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+void adjoint_stage_pre(cudaStream_t s, double *g, double *w, size_t cap, int n, int scheme, int stage, double dt)
+{
+  k_adj_stage_pre<<<grid_for(n, 256), 256, 0, s>>>(g, w, cap, n, scheme, stage, dt);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+void adjoint_objective(cudaStream_t s, const double *soa, size_t cap, int n, const int *orig, const double *seed_x, const double *seed_a, double wE,
+                       const double wI[3], double *g, double *w, double *part, double *value)
+{
+  k_adj_objective<<<OBJ_BLOCKS, OBJ_THREADS, 0, s>>>(soa, cap, n, orig, seed_x, seed_a, wE, wI[0], wI[1], wI[2], g, w, part);
+  count_launch();
+  k_sum_final<<<1, 32, 0, s>>>(part, OBJ_BLOCKS, value);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+void adjoint_scatter(cudaStream_t s, const double *in, double *out, size_t cap, int n, const uint32_t *perm)
+{
+  k_adj_scatter<<<grid_for(n, 256), 256, 0, s>>>(in, out, cap, n, perm);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+void orig_update(cudaStream_t s, const int *in, int *out, const uint32_t *perm, int n)
+{
+  k_orig_update<<<grid_for(n, 256), 256, 0, s>>>(in, out, perm, n);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+void iota_int(cudaStream_t s, int *a, int n)
+{
+  k_iota_int<<<grid_for(n, 256), 256, 0, s>>>(a, n);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+void adjoint_rows(cudaStream_t s, const double *g, size_t cap, int n, int field, double *rows)
+{
+  k_adj_rows<<<grid_for(n, 256), 256, 0, s>>>(g, cap, n, field, rows);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+} // namespace vfmm

@@ -62,6 +62,7 @@ static_assert(sizeof(vfmm_config) == 72, "vfmm_config layout");
 static_assert(sizeof(vfmm_body) == 296, "vfmm_body must match exafmm::Body");
 static_assert(sizeof(vfmm_cell) == 72, "vfmm_cell layout");
 static_assert(sizeof(vfmm_tuning) == 40, "vfmm_tuning layout");
+static_assert(sizeof(vfmm_objective) == 48, "vfmm_objective layout");
 
 struct vfmm_handle_s {
   vfmm_config  cfg;
@@ -109,6 +110,16 @@ struct vfmm_handle_s {
   DevBuf<unsigned char> flushbuf;
   DevBuf<double>        dtmp;
   bool                  has_tree = false, has_eval = false;
+
+  // reverse mode (vfmm_adjoint): adjoint state (ping-pong for the reorders),
+  // work fields, adjoint expansions, lists by source, checkpoints, the states
+  // of one recomputed segment, caller index of each body, seeds
+  struct {
+    DevBuf<double>             g[2], w, ckpt, tape, seedx, seeda, part, rows, value;
+    DevBuf<double2>            Mb, Lb;
+    DevBuf<int>                p2pT_start, p2pT_tgt, m2lT_start, m2lT_tgt, orig[2];
+    DevBuf<unsigned long long> tkeys, tsorted;
+  } adj;
 };
 
 namespace {
@@ -942,6 +953,183 @@ int vfmm_autotune(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, v
     h->has_tree = h->has_eval = false;
     VFMM_CUDA_TRY(cudaStreamSynchronize(s));
   });
+}
+
+// ---- reverse mode
+namespace {
+
+// Positions, strengths and radii (fields F_X..F_A+2 are contiguous) of the
+// bodies in soa[cur], to or from 7 * cap doubles at p.
+void save_state(vfmm_handle h, double *p)
+{
+  const double *q = h->soa[h->cur].p;
+  VFMM_CUDA_TRY(cudaMemcpyAsync(p, q + (size_t)F_X * h->cap, 6 * h->cap * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  VFMM_CUDA_TRY(cudaMemcpyAsync(p + 6 * h->cap, q + (size_t)F_R * h->cap, h->cap * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+}
+void load_state(vfmm_handle h, const double *p)
+{
+  double *q = h->soa[h->cur].p;
+  VFMM_CUDA_TRY(cudaMemcpyAsync(q + (size_t)F_X * h->cap, p, 6 * h->cap * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  VFMM_CUDA_TRY(cudaMemcpyAsync(q + (size_t)F_R * h->cap, p + 6 * h->cap, h->cap * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+}
+
+// The FP64 evaluation whatever the handle's precision (the reverse sweep
+// differentiates the FP64 expansions).
+void calculate_fp64(vfmm_handle h)
+{
+  const int prec     = h->cfg.precision;
+  h->cfg.precision   = VFMM_FP64;
+  try {
+    calculate(h);
+  } catch (...) {
+    h->cfg.precision = prec;
+    throw;
+  }
+  h->cfg.precision = prec;
+}
+
+void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int steps, int every, const vfmm_objective *obj, double *value,
+             double *gx, double *ga)
+{
+  const vfmm_config &c = h->cfg;
+  if (c.integrator != VFMM_EULER && c.integrator != VFMM_RK2 && c.integrator != VFMM_RK3)
+    throw Error(VFMM_ERR_UNSUPPORTED, "the adjoint covers Euler, RK2 and RK3");
+  if (c.formulation != VFMM_CVPM || c.viscous != VFMM_INVISCID || c.relax != 0)
+    throw Error(VFMM_ERR_UNSUPPORTED, "the adjoint covers the inviscid cVPM path without relaxation");
+  if (!bodies || !obj || !value)
+    throw Error(VFMM_ERR_INVALID, "null argument");
+  if (steps < 0 || every < 1)
+    throw Error(VFMM_ERR_INVALID, "steps must be >= 0 and checkpoint_every >= 1");
+  cudaStream_t s    = h->stream;
+  auto        &A    = h->adj;
+  const int    S    = stages_of(c.integrator);
+  const bool   grad = gx || ga;
+  upload(h, bodies, n);
+  const int    N   = h->n;
+  const size_t cap = h->cap, slot = 7 * cap;
+  A.orig[0].reserve(N);
+  A.orig[1].reserve(N);
+  int oc = 0;
+  iota_int(s, A.orig[0].p, N);
+  auto track = [&]() {
+    orig_update(s, A.orig[oc].p, A.orig[oc ^ 1].p, h->ts.perm.p, N);
+    oc ^= 1;
+  };
+  const double *dsx = nullptr, *dsa = nullptr;
+  if (obj->seed_x) {
+    A.seedx.reserve(3 * (size_t)N);
+    VFMM_CUDA_TRY(cudaMemcpyAsync(A.seedx.p, obj->seed_x, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, s));
+    dsx = A.seedx.p;
+  }
+  if (obj->seed_alpha) {
+    A.seeda.reserve(3 * (size_t)N);
+    VFMM_CUDA_TRY(cudaMemcpyAsync(A.seeda.p, obj->seed_alpha, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, s));
+    dsa = A.seeda.p;
+  }
+  const int nck = grad ? (steps + every - 1) / every : 0;
+  if (nck > 0)
+    A.ckpt.reserve((size_t)nck * slot);
+  // forward sweep, keeping the state at the start of every checkpoint_every-th step
+  for (int st = 0; st < steps; st++) {
+    if (grad && st % every == 0)
+      save_state(h, A.ckpt.p + (size_t)(st / every) * slot);
+    for (int k = 0; k < S; k++) {
+      build_tree_and_lists(h);
+      track();
+      evaluate_and_update(h, k, dt);
+    }
+  }
+  // the objective on the final state
+  build_tree_and_lists(h);
+  track();
+  calculate_fp64(h);
+  for (auto *b : {&A.g[0], &A.g[1]})
+    b->reserve((size_t)NG * cap);
+  A.w.reserve((size_t)NW * cap);
+  A.part.reserve(ADJ_PARTIALS);
+  A.value.reserve(1);
+  int          gc    = 0;
+  const double wI[3] = {obj->impulse[0], obj->impulse[1], obj->impulse[2]};
+  adjoint_objective(s, h->soa[h->cur].p, cap, N, A.orig[oc].p, dsx, dsa, obj->energy, wI, A.g[gc].p, A.w.p, A.part.p, A.value.p);
+  double v = 0;
+  VFMM_CUDA_TRY(cudaMemcpyAsync(&v, A.value.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+  *value = v;
+  h->has_tree = h->has_eval = false;
+  if (!grad)
+    return;
+  // vjp of the evaluation just made (tree, lists, FP64 expansions current;
+  // seeds in A.w; adjoint state in tree order), then back to the order the
+  // bodies had before this tree
+  auto vjp = [&]() {
+    const int    np = h->lists.n_p2p, nm = h->lists.n_m2l, nc = h->tree.ncells;
+    const size_t K3 = 3 * (size_t)(c.p * (c.p + 1) / 2);
+    A.p2pT_start.reserve(nc + 1);
+    A.m2lT_start.reserve(nc + 1);
+    A.p2pT_tgt.reserve(np + 1);
+    A.m2lT_tgt.reserve(nm + 1);
+    A.tkeys.reserve(std::max(np, nm) + 1);
+    A.tsorted.reserve(std::max(np, nm) + 1);
+    A.Mb.reserve(nc * K3);
+    A.Lb.reserve(nc * K3);
+    lists_transpose(s, h->lists.ls, np, nm, nc, A.tkeys.p, A.tsorted.p, A.p2pT_start.p, A.p2pT_tgt.p, A.m2lT_start.p, A.m2lT_tgt.p);
+    AdjBufs b{};
+    b.g          = A.g[gc].p;
+    b.w          = A.w.p;
+    b.n          = N;
+    b.Mb         = A.Mb.p;
+    b.Lb         = A.Lb.p;
+    b.p2pT_start = A.p2pT_start.p;
+    b.p2pT_tgt   = A.p2pT_tgt.p;
+    b.m2lT_start = A.m2lT_start.p;
+    b.m2lT_tgt   = A.m2lT_tgt.p;
+    b.part       = A.part.p;
+    adjoint_eval(s, particle_args(h), b, h->info);
+    adjoint_scatter(s, A.g[gc].p, A.g[gc ^ 1].p, cap, N, h->ts.perm.p);
+    gc ^= 1;
+  };
+  vjp();
+  // reverse sweep: per segment, recompute its steps from the checkpoint
+  // keeping every stage's input state, then run the stages backwards
+  A.tape.reserve((size_t)every * S * slot);
+  for (int seg = nck - 1; seg >= 0; seg--) {
+    const int st0 = seg * every, st1 = std::min(steps, st0 + every);
+    load_state(h, A.ckpt.p + (size_t)seg * slot);
+    for (int st = st0; st < st1; st++)
+      for (int k = 0; k < S; k++) {
+        save_state(h, A.tape.p + (size_t)((st - st0) * S + k) * slot);
+        run_stage(h, k, dt);
+      }
+    for (int st = st1 - 1; st >= st0; st--)
+      for (int k = S - 1; k >= 0; k--) {
+        load_state(h, A.tape.p + (size_t)((st - st0) * S + k) * slot);
+        build_tree_and_lists(h);
+        calculate_fp64(h);
+        adjoint_stage_pre(s, A.g[gc].p, A.w.p, cap, N, c.integrator, k, dt);
+        adjoint_seeds(s, h->soa[h->cur].p, A.w.p, cap, N, c.stretching);
+        vjp();
+      }
+  }
+  A.rows.reserve(3 * (size_t)N);
+  if (gx) {
+    adjoint_rows(s, A.g[gc].p, cap, N, G_XB, A.rows.p);
+    VFMM_CUDA_TRY(cudaMemcpyAsync(gx, A.rows.p, 3 * (size_t)N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  if (ga) {
+    adjoint_rows(s, A.g[gc].p, cap, N, G_AB, A.rows.p);
+    VFMM_CUDA_TRY(cudaMemcpyAsync(ga, A.rows.p, 3 * (size_t)N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  h->has_tree = h->has_eval = false;
+}
+
+} // namespace
+
+int vfmm_adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int steps, int checkpoint_every, const vfmm_objective *objective,
+                 double *value, double *grad_x, double *grad_alpha)
+{
+  return guarded(h, [&] { adjoint(h, bodies, n, dt, steps, checkpoint_every, objective, value, grad_x, grad_alpha); });
 }
 
 int vfmm_rbf(vfmm_handle h, vfmm_body *particles, size_t n, vfmm_body *points, size_t m, size_t *m_out, int *iterations)

@@ -326,32 +326,6 @@ __global__ void __launch_bounds__(128) k_l2l(DevExp a, const int *cells, int cou
 // Then the stretching term (fmmCalculator.hpp:391-405) and rVPM terms
 // (:407-418) from the complete u and J.
 
-// full-range coefficient c_n^m of a real expansion stored for m >= 0
-__device__ __forceinline__ zd coef_full(const zd *c, int n, int m, int stride, int comp)
-{
-  if (m > 0)
-    return c[tri(n, m) * stride + comp];
-  if (m == 0)
-    return {c[tri(n, 0) * stride + comp].r, 0.0};
-  return conj(c[tri(n, -m) * stride + comp]);
-}
-// coefficient (n, mu >= 0) of D_axis applied to expansion c (degree n+1 source)
-__device__ __forceinline__ zd deriv_coef(const zd *c, int n, int mu, int axis, int stride, int comp)
-{
-  if (axis == 2) {
-    zd v = coef_full(c, n + 1, mu, stride, comp);
-    return {-v.r, -v.i};
-  }
-  const double s = (mu - 1 >= 0) ? -1.0 : 1.0;
-  const double t = (mu + 1 >= 1) ? 1.0 : -1.0;
-  const zd     A = s * coef_full(c, n + 1, mu - 1, stride, comp);
-  const zd     B = t * coef_full(c, n + 1, mu + 1, stride, comp);
-  if (axis == 0)
-    return {0.5 * (A.r + B.r), 0.5 * (A.i + B.i)};
-  // -(i/2)(A - B)
-  return {0.5 * (A.i - B.i), -0.5 * (A.r - B.r)};
-}
-
 template <int P>
 struct L2PSizes {
   static constexpr int K  = nterms(P);

@@ -121,6 +121,78 @@ constexpr HarmRecip<T> make_harm_recip()
 template <class T>
 __device__ __forceinline__ cx<T> neg_if(cx<T> v, bool neg) { return neg ? cx<T>{-v.r, -v.i} : v; }
 
+// Full-range coefficient c_n^m of a real expansion stored for m >= 0:
+// c_n^{-m} = conj(c_n^m), and c_n^0 is taken as real.
+template <class T>
+__device__ __forceinline__ cx<T> coef_full(const cx<T> *c, int n, int m, int stride, int comp)
+{
+  if (m > 0)
+    return c[tri(n, m) * stride + comp];
+  if (m == 0)
+    return {c[tri(n, 0) * stride + comp].r, T(0)};
+  return conj(c[tri(n, -m) * stride + comp]);
+}
+// Coefficient (n, mu >= 0) of D_axis applied to the expansion c (whose degree
+// n + 1 terms are read), from the derivative rules above.
+template <class T>
+__device__ __forceinline__ cx<T> deriv_coef(const cx<T> *c, int n, int mu, int axis, int stride, int comp)
+{
+  if (axis == 2) {
+    const cx<T> v = coef_full(c, n + 1, mu, stride, comp);
+    return {-v.r, -v.i};
+  }
+  const T     s = (mu - 1 >= 0) ? T(-1) : T(1);
+  const T     t = (mu + 1 >= 1) ? T(1) : T(-1);
+  const cx<T> A = s * coef_full(c, n + 1, mu - 1, stride, comp);
+  const cx<T> B = t * coef_full(c, n + 1, mu + 1, stride, comp);
+  if (axis == 0)
+    return {T(0.5) * (A.r + B.r), T(0.5) * (A.i + B.i)};
+  // -(i/2)(A - B)
+  return {T(0.5) * (A.i - B.i), T(-0.5) * (A.r - B.r)};
+}
+
+// Transposes for reverse mode.  A complex variable's adjoint is
+// dS/dRe + i dS/dIm of the scalar S being differentiated; with that
+// convention z = w c (c constant) gives wbar += zbar conj(c), and
+// z = conj(w) gives wbar += conj(zbar).
+template <class T>
+__device__ __forceinline__ void coef_full_adj(cx<T> *cb, int n, int m, int stride, int comp, cx<T> g)
+{
+  if (m > 0) {
+    cx<T> &o = cb[tri(n, m) * stride + comp];
+    o.r += g.r;
+    o.i += g.i;
+  } else if (m == 0)
+    cb[tri(n, 0) * stride + comp].r += g.r;
+  else {
+    cx<T> &o = cb[tri(n, -m) * stride + comp];
+    o.r += g.r;
+    o.i -= g.i;
+  }
+}
+// Adds to cb the adjoint of deriv_coef(c, n, mu, axis, stride, comp) whose
+// result has adjoint vb.
+template <class T>
+__device__ __forceinline__ void deriv_coef_adj(cx<T> *cb, int n, int mu, int axis, int stride, int comp, cx<T> vb)
+{
+  if (axis == 2) {
+    coef_full_adj(cb, n + 1, mu, stride, comp, cx<T>{-vb.r, -vb.i});
+    return;
+  }
+  const T s = (mu - 1 >= 0) ? T(-1) : T(1);
+  const T t = (mu + 1 >= 1) ? T(1) : T(-1);
+  cx<T>   Ab, Bb;
+  if (axis == 0) {
+    Ab = {T(0.5) * vb.r, T(0.5) * vb.i};
+    Bb = Ab;
+  } else { // v = (-i/2) A + (i/2) B
+    Ab = {T(-0.5) * vb.i, T(0.5) * vb.r};
+    Bb = {T(0.5) * vb.i, T(-0.5) * vb.r};
+  }
+  coef_full_adj(cb, n + 1, mu - 1, stride, comp, cx<T>{s * Ab.r, s * Ab.i});
+  coef_full_adj(cb, n + 1, mu + 1, stride, comp, cx<T>{t * Bb.r, t * Bb.i});
+}
+
 // One output (j, k, d) of M2M for NC children at once (children t0..t0+NC-1
 // that exist): the index arithmetic is shared and the NC accumulators are
 // independent, which keeps the arithmetic pipe fed.  M2M of

@@ -203,4 +203,43 @@ void lists_to_csr(cudaStream_t s, ListScratch &ls, int n_p2p, int n_m2l, int nce
   VFMM_LAUNCH_CHECK();
 }
 
+// (target << kb | source) -> (source << kb | target)
+__global__ void k_swap_keys(const unsigned long long *__restrict__ in, unsigned long long *__restrict__ out, int n, int kb)
+{
+  const unsigned long long mask = (1ull << kb) - 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long k = in[i];
+    out[i]                     = ((k & mask) << kb) | (k >> kb);
+  }
+}
+
+// Rows by source cell of the sorted pair lists in ls (for the reverse-mode
+// passes, which gather per source): targets of source s at
+// tgt[start[s] .. start[s+1]).  keys and sorted hold max(n_p2p, n_m2l) keys.
+void lists_transpose(cudaStream_t s, ListScratch &ls, int n_p2p, int n_m2l, int ncells_s, unsigned long long *keys, unsigned long long *sorted,
+                     int *p2p_start, int *p2p_tgt, int *m2l_start, int *m2l_tgt)
+{
+  const int end_bit = 2 * ls.key_bits;
+  size_t    b1 = 0, b2 = 0;
+  VFMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(nullptr, b1, keys, sorted, n_p2p, 0, end_bit, s));
+  VFMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(nullptr, b2, keys, sorted, n_m2l, 0, end_bit, s));
+  ls.cub_tmp.reserve(std::max(b1, b2));
+  const unsigned long long *src[2] = {ls.p2p_sorted.p, ls.m2l_sorted.p};
+  const int                 cnt[2] = {n_p2p, n_m2l};
+  int                      *st[2] = {p2p_start, m2l_start}, *tg[2] = {p2p_tgt, m2l_tgt};
+  for (int l = 0; l < 2; l++) {
+    const int n = cnt[l];
+    if (n > 0) {
+      k_swap_keys<<<grid_for(n, 256), 256, 0, s>>>(src[l], keys, n, ls.key_bits);
+      count_launch();
+      size_t bytes = std::max(b1, b2);
+      VFMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(ls.cub_tmp.p, bytes, keys, sorted, n, 0, end_bit, s));
+      count_launch();
+    }
+    k_csr<<<grid_for(n + 1, 256), 256, 0, s>>>(sorted, n, ls.key_bits, ncells_s, st[l], tg[l], nullptr, nullptr);
+    count_launch();
+  }
+  VFMM_LAUNCH_CHECK();
+}
+
 } // namespace vfmm

@@ -146,6 +146,8 @@ void traverse(cudaStream_t s, CellsView tc, CellsView sc, int ntc, int nsc, int 
               ListScratch &ls, size_t cap_front, size_t cap_p2p, size_t cap_m2l);
 void lists_to_csr(cudaStream_t s, ListScratch &ls, int n_p2p, int n_m2l, int ncells_t, int cell_bits, int *p2p_start, int *p2p_src, int *m2l_start,
                   int *m2l_src, const int *nbody_t, unsigned long long *interactions);
+void lists_transpose(cudaStream_t s, ListScratch &ls, int n_p2p, int n_m2l, int ncells_s, unsigned long long *keys, unsigned long long *sorted,
+                     int *p2p_start, int *p2p_tgt, int *m2l_start, int *m2l_tgt);
 
 // ---- bodies.cu
 void aos_to_soa(cudaStream_t s, const double *aos, double *soa, size_t cap, int n);
@@ -237,6 +239,36 @@ void rbf_vorticity(cudaStream_t s, CellsView tc, const int *leaf_cells, int nlea
                    size_t tcap, CellsView sc, const double *ssoa, size_t scap, double *out, int field, int zero_dadt);
 // one elementwise step over n bodies; with sums != null also its three component sums (device)
 void rbf_op(cudaStream_t s, int op, double *soa, size_t cap, int n, const double c[3], double *scratch, double *sums);
+
+// ---- adjoint.cu: reverse mode of the FP64 evaluation and of the stage updates
+// Adjoint state of the bodies, permuted with them between stages: positions,
+// strengths and the RK registers (VOLD/DOLD, XOLD/AOLD).
+enum AdjG { G_XB = 0, G_AB = 3, G_VB = 6, G_DB = 9, G_XOB = 12, G_AOB = 15, NG = 18 };
+// Work fields of one evaluation's adjoint: seeds of u and J, far-field
+// position adjoints and dilation terms, near-field position and strength
+// adjoints (per target / per source), P2M^T and stretching strength
+// adjoints, and the stage cotangent of (u, dalpha/dt).
+enum AdjW { W_SU = 0, W_SJ = 3, W_XF = 12, W_EF = 15, W_XNT = 16, W_XNS = 19, W_ANS = 22, W_AP2M = 25, W_ASTR = 28, W_COT = 31, NW = 37 };
+struct AdjBufs {
+  double    *g; // adjoint state, NG fields
+  double    *w; // work, NW fields
+  int        n;
+  double2   *Mb, *Lb; // adjoint expansions [cell][3K]
+  const int *p2pT_start, *p2pT_tgt, *m2lT_start, *m2lT_tgt;
+  double    *part; // ADJ_PARTIALS doubles
+};
+constexpr int ADJ_PARTIALS = 152 * 2 * 17;
+// vjp of the evaluation whose tree, lists and FP64 expansions are in e, with
+// the seeds in b.w (W_SU, W_SJ, W_ASTR): adds to g[G_XB], g[G_AB].
+void adjoint_eval(cudaStream_t s, const ExpArgs &e, const AdjBufs &b, const DevInfo *info);
+void adjoint_seeds(cudaStream_t s, const double *soa, double *w, size_t cap, int n, int stretching);
+void adjoint_stage_pre(cudaStream_t s, double *g, double *w, size_t cap, int n, int scheme, int stage, double dt);
+void adjoint_objective(cudaStream_t s, const double *soa, size_t cap, int n, const int *orig, const double *seed_x, const double *seed_a, double wE,
+                       const double wI[3], double *g, double *w, double *part, double *value);
+void adjoint_scatter(cudaStream_t s, const double *in, double *out, size_t cap, int n, const uint32_t *perm);
+void orig_update(cudaStream_t s, const int *in, int *out, const uint32_t *perm, int n);
+void iota_int(cudaStream_t s, int *a, int n);
+void adjoint_rows(cudaStream_t s, const double *g, size_t cap, int n, int field, double *rows);
 
 // ---- direct.cu
 void direct_sum(cudaStream_t s, const double *tx, const double *ty, const double *tz, int nt, const double *src, size_t scap, int ns, double *out /*12*nt*/);
