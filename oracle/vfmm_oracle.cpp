@@ -1122,3 +1122,5 @@ void vo_l2p_body(int P, const double *Lc, const double *C, const double *X, doub
     out[3 + k] = b.J[k / 3][k % 3];
 }
 }
+
+#include "complex_step.hpp"

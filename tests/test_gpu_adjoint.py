@@ -124,3 +124,37 @@ def test_adjoint_rejects_what_it_does_not_cover(vfmm_lib):
         with FMMCalculator(p=4, ncrit=32, theta=0.5, **kw) as c:
             with pytest.raises(VfmmError):
                 c.adjoint(b, 0.01, 1)
+
+
+def _complex_step(b, P, ncrit, theta, scheme, dt, steps, dirs_x, dirs_a, energy=1.0, impulse=(0.0, 0.0, 1.0)):
+    import ctypes
+    from oracle.oracle import oracle
+    L = oracle()
+    n, nd = b.size, dirs_x.shape[0]
+    wI = np.array(impulse, float)
+    val, der = ctypes.c_double(), np.zeros(nd)
+    dx, da = np.ascontiguousarray(dirs_x), np.ascontiguousarray(dirs_a)
+    assert L.vo_cs_objective(b.ctypes.data, n, P, ncrit, theta, scheme, 0, dt, steps, energy, wI.ctypes.data, dx.ctypes.data,
+                             da.ctypes.data, nd, ctypes.byref(val), der.ctypes.data) == 0
+    return val.value, der
+
+
+@pytest.mark.parametrize("theta,steps", [(0.5, 0), (0.47, 2)])
+def test_gradient_matches_complex_step(vfmm_lib, theta, steps):
+    """Directional derivatives from the adjoint against the oracle's whole-step
+    complex step (real parts, trees and lists untouched by the step).  Multi-step
+    runs use theta = 0.47: CPU and GPU trajectories differ by rounding, and only
+    without exact MAC ties do both runs take the same branch at every stage."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.ring(16, seed=3)
+    rng = np.random.default_rng(11)
+    nd = 3
+    dx = rng.normal(size=(nd, b.size, 3))
+    da = rng.normal(size=(nd, b.size, 3)) * np.abs(b["alpha"]).max()
+    with FMMCalculator(p=8, ncrit=32, theta=theta, integration="RK3") as c:
+        v, gx, ga = c.adjoint(b, 0.02, steps, 1)
+    vc, der = _complex_step(b, 8, 32, theta, 2, 0.02, steps, dx, da)
+    assert abs(v - vc) <= 1e-10 * abs(vc)
+    for k in range(nd):
+        an = float((gx * dx[k]).sum() + (ga * da[k]).sum())
+        assert abs(an - der[k]) <= 1e-8 * abs(der[k]), (k, an, der[k])
