@@ -59,8 +59,11 @@ def parse(argv=None):
     ap.add_argument("--out", default=None, help="also write the JSON line to this file")
     ap.add_argument("--autotune", action="store_true",
                     help="also report the opt-in autotuner's choice (leaf size, M2L batch) and its stage time")
-    ap.add_argument("--workload", default="cloud", choices=["cloud", "rings64"],
-                    help="cloud: the headline N = 2^20 cloud; rings64: 64 independent rings, batched")
+    ap.add_argument("--workload", default="cloud", choices=["cloud", "rings64", "adjoint"],
+                    help="cloud: the headline N = 2^20 cloud; rings64: 64 independent rings, batched; "
+                         "adjoint: reverse-mode gradient of the leapfrogging rings")
+    ap.add_argument("--adj-steps", type=int, default=50, help="adjoint workload: RK3 steps")
+    ap.add_argument("--cs-dirs", type=int, default=2, help="adjoint workload: complex-step check directions (0 = none)")
     return ap.parse_args(argv)
 
 
@@ -430,6 +433,64 @@ def run_rings64(args, dist: Dist) -> dict | None:
                            "note": "the same systems advanced one vfmm_advance after another"}}
 
 
+def run_adjoint(args, dist: Dist) -> dict | None:
+    """Reverse-mode gradient of the leapfrogging-ring objective: two coaxial
+    rings of 512 stations x 127 points (130,048 bodies) at z = 0 and 0.5,
+    p = 8, theta = 0.5, leaf 32, 50 RK3 steps of dt = 0.01 with a checkpoint
+    every 10 steps; objective = kinetic energy sum u.(x cross alpha) + z-impulse
+    at the final state; gradient with respect to all initial positions and
+    strengths.  Timed on the host around vfmm_adjoint (copies included), beside
+    the forward sweep alone.  The check leg compares the FP64 gradient of the
+    8,128-body sub-case (32 stations) with the oracle's whole-step complex step
+    along random directions (theta = 0.47: CPU and GPU trajectories agree in
+    every tree and list decision only without exact MAC ties)."""
+    import ctypes
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.leapfrog(512, seed=dist.rank)
+    kw = dict(p=8, ncrit=32, theta=0.5, integration="RK3", precision=args.precision, device=dist.local_rank)
+    steps, every = args.adj_steps, 10
+    with FMMCalculator(**kw) as c:
+        c.adjoint(b, args.dt, 1, 1)  # warm-up: buffers and kernels
+        dist.barrier()
+        t0 = time.perf_counter()
+        c.adjoint(b, args.dt, steps, every, gradient=False)
+        tf = dist.max(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        v, gx, ga = c.adjoint(b, args.dt, steps, every)
+        tg = dist.max(time.perf_counter() - t0)
+    check = None
+    if dist.rank == 0 and args.cs_dirs > 0:
+        from oracle.oracle import oracle
+        b8 = workloads.leapfrog(32, seed=0)
+        n8 = b8.size
+        with FMMCalculator(p=8, ncrit=32, theta=0.47, integration="RK3", precision="fp64", device=dist.local_rank) as c:
+            v8, gx8, ga8 = c.adjoint(b8, args.dt, steps, every)
+        rng = np.random.default_rng(2024)
+        nd = args.cs_dirs
+        dx = rng.normal(size=(nd, n8, 3))
+        da = rng.normal(size=(nd, n8, 3)) * np.abs(b8["alpha"]).max()
+        wI = np.array([0.0, 0.0, 1.0])
+        val, der = ctypes.c_double(), np.zeros(nd)
+        t0 = time.perf_counter()
+        oracle().vo_cs_objective(b8.ctypes.data, n8, 8, 32, 0.47, 2, 0, args.dt, steps, 1.0, wI.ctypes.data, dx.ctypes.data,
+                                 da.ctypes.data, nd, ctypes.byref(val), der.ctypes.data)
+        tcs = time.perf_counter() - t0
+        an = np.einsum("kij,ij->k", dx, gx8) + np.einsum("kij,ij->k", da, ga8)
+        check = {"case": "2 rings x 32 stations x 127 (8,128 bodies), FP64, theta 0.47, 50 RK3 steps", "directions": nd,
+                 "max_rel_err_vs_complex_step": float(np.max(np.abs(an - der) / np.abs(der))),
+                 "value_rel_diff": abs(v8 - val.value) / abs(val.value), "complex_step_seconds": tcs}
+    if dist.rank != 0:
+        return None
+    return {"metric": "reverse-mode gradient wall time, 2 leapfrogging rings (130,048 bodies), 50 RK3 steps", "value": tg, "unit": "s",
+            "n_gpus": dist.world, "steps": steps, "warmup": 1, "ms_per_step": 1e3 * tg / steps, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+            "data": "synthetic (seeded rings; no dataset)",
+            "config": {"workload": "leapfrogging rings 2 x 512 x 127, KE + z-impulse objective", "bodies": int(b.size), "p": 8,
+                       "theta": 0.5, "ncrit": 32, "checkpoint_every": every, "precision": args.precision,
+                       "timing": "host wall clock around vfmm_adjoint, copies included"},
+            "forward_seconds": tf, "gradient_over_forward": tg / tf, "objective": v, "complex_step_check": check}
+
+
 def main(argv=None):
     args = parse(argv)
     dist = Dist()
@@ -437,6 +498,8 @@ def main(argv=None):
         line = run_reference(args, dist)
     elif args.workload == "rings64":
         line = run_rings64(args, dist)
+    elif args.workload == "adjoint":
+        line = run_adjoint(args, dist)
     else:
         from uvlm_gb300 import _build, _lib
         if not os.path.exists(_lib.LIB_PATH):

@@ -180,10 +180,12 @@ typedef struct vfmm_objective {
 /* Reverse-mode gradient of the objective after `steps` steps of advance
  * from `bodies` (not modified) with respect to their initial positions and
  * strengths: grad_x and grad_alpha receive n x 3 doubles in the order of
- * `bodies`.  The forward steps run in the handle's precision; the reverse
- * sweep is the exact transpose of the FP64 evaluation (P2P pairs, transposed
- * L2P, L2L, M2L, M2M, P2M, the bounding-box dependence of the cell centres)
- * and of the stage updates, at the states of the forward trajectory.  States
+ * `bodies`.  The reverse sweep is the transpose of the evaluation (P2P
+ * pairs, transposed L2P, L2L, M2L, M2M, P2M, the bounding-box dependence of
+ * the cell centres) and of the stage updates, at the states of the forward
+ * trajectory, all in the handle's precision: FP64 (the exact derivative of
+ * the FP64 step) or mixed (the forward kernels, P2P^T and M2L^T in FP32, the
+ * other transposes in FP64).  States
  * are kept every `checkpoint_every` steps and the steps in between are
  * recomputed, so device memory holds ceil(steps / checkpoint_every) + stages
  * x checkpoint_every body states.  With grad_x and grad_alpha both NULL only

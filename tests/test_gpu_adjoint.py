@@ -103,9 +103,10 @@ def test_seeds_follow_the_bodies(vfmm_lib):
     assert worst(errs) < TOL, errs
 
 
-def test_mixed_forward_gradient_close_to_fp64(vfmm_lib):
-    """A mixed-precision forward sweep with the FP64 reverse sweep: the gradient
-    differs from the all-FP64 one by the trajectory's FP32 rounding."""
+def test_mixed_gradient_close_to_fp64(vfmm_lib):
+    """Mixed precision (FP32 forward kernels, FP32 P2P^T and M2L^T in the
+    reverse sweep): the gradient differs from the all-FP64 one by FP32
+    rounding of the trajectory and of the transposed passes."""
     from uvlm_gb300 import FMMCalculator, workloads
     b = workloads.leapfrog(16, seed=7)
     res = {}
@@ -114,7 +115,7 @@ def test_mixed_forward_gradient_close_to_fp64(vfmm_lib):
             res[prec] = c.adjoint(b, 0.01, 3, 2)
     for k in (1, 2):
         a, r = res["mixed"][k], res["fp64"][k]
-        assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-6
+        assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-5
 
 
 def test_adjoint_rejects_what_it_does_not_cover(vfmm_lib):
@@ -158,3 +159,17 @@ def test_gradient_matches_complex_step(vfmm_lib, theta, steps):
     for k in range(nd):
         an = float((gx * dx[k]).sum() + (ga * da[k]).sum())
         assert abs(an - der[k]) <= 1e-8 * abs(der[k]), (k, an, der[k])
+
+
+def test_mixed_evaluation_gradient_close_to_fp64(vfmm_lib):
+    """One evaluation (steps = 0) of a cloud at high order: the FP32 transposes
+    against the FP64 ones."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(20000, seed=12)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        with FMMCalculator(p=12, ncrit=64, theta=0.5, integration="Euler", precision=prec) as c:
+            res[prec] = c.adjoint(b, 0.01, 0)
+    for k in (1, 2):
+        a, r = res["mixed"][k], res["fp64"][k]
+        assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-5

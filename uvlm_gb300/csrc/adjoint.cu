@@ -68,6 +68,11 @@ struct AdjDev {
   const int     *p2pT_start, *p2pT_tgt; // P2P rows by source leaf
   const int     *m2lT_start, *m2lT_tgt; // M2L rows by source cell
   double        *w;                     // work fields (AdjW), field-major, capacity cap
+  // mixed mode: FP32 body records of the evaluation and the seeds in FP32
+  const float4  *pos32, *alp32;         // (x - X_leaf, 1/(2 sigma^2)), (alpha, 1/sigma)
+  float4        *seeds32;               // per body 4 x float4: ubar, ct, Jbar (see k_adj_seeds32)
+  double         R0;
+  double         R0pow[PMAX + 2], iR0pow[PMAX + 2];
 };
 
 __device__ __forceinline__ double &W(const AdjDev &a, int f, int i) { return a.w[(size_t)f * a.cap + i]; }
@@ -964,6 +969,337 @@ __global__ void k_adj_rows(const double *g, size_t cap, int n, int field, double
       rows[3 * (size_t)i + k] = g[(size_t)(field + k) * cap + i];
 }
 
+// ------------------------------------------------------------------ FP32 reverse passes
+// Mixed mode runs the two dominant transposes, P2P^T and M2L^T, in FP32.
+//
+// P2P^T: the radial functions of one pair are written through
+//   F(s) = g(s) s^{-3/2},  s = r^2 / (2 sigma^2),
+// so that q = c F, h = c F' / sigma^2, h_{r^2} = c F'' / (2 sigma^4) with
+// c = 1 / (4 pi 2^{3/2} sigma^3); F and its derivatives come from the series
+// F = (2/sqrt(pi)) sum_k (-1)^k s^k / (k! (k + 3/2)) for s < 2 (g' = (2/sqrt(pi))
+// sqrt(s) e^-s integrated termwise; no cancellation at small r) and from the
+// closed forms in g, g', g'' above.  Positions are the evaluation's
+// leaf-relative FP32 records; partial sums per leaf are folded into a
+// float-float (two-sum) accumulator.
+struct SeriesF {
+  float a[17]; // (2/sqrt(pi)) (-1)^k / (k! (k + 3/2))
+};
+constexpr SeriesF make_series_f()
+{
+  SeriesF r{};
+  double  f = 1.0;
+  for (int k = 0; k < 17; k++) {
+    if (k > 0)
+      f *= k;
+    r.a[k] = (float)(1.128379167095512573896158903121545172 * ((k & 1) ? -1.0 : 1.0) / (f * (k + 1.5)));
+  }
+  return r;
+}
+static __constant__ SeriesF kSeriesF = make_series_f();
+
+__device__ __forceinline__ void radial_F(float s, float &F, float &F1, float &F2)
+{
+  if (s < 2.0f) {
+    float p = kSeriesF.a[16], p1 = 0.f, p2 = 0.f;
+#pragma unroll
+    for (int k = 15; k >= 0; k--) {
+      p2 = fmaf(p2, s, p1);
+      p1 = fmaf(p1, s, p);
+      p  = fmaf(p, s, kSeriesF.a[k]);
+    }
+    F  = p;
+    F1 = p1;
+    F2 = 2.f * p2;
+  } else {
+    const float tsp = 1.1283791670955126f; // 2 / sqrt(pi)
+    const float rs = sqrtf(s), e = expf(-s), is = 1.f / s, is15 = is / rs;
+    const float g1 = tsp * rs * e, g = erff(rs) - g1, g2 = tsp * e * (0.5f / rs - rs);
+    F  = g * is15;
+    F1 = (g1 - 1.5f * g * is) * is15;
+    F2 = (g2 - 3.f * g1 * is + 3.75f * g * is * is) * is15;
+  }
+}
+
+// ds/dd and ds/dalpha of one pair in FP32 (the algebra of pair_adj).
+__device__ __forceinline__ void pair_adj32(float dx, float dy, float dz, float ax, float ay, float az, float isg, float w2, const float *ub,
+                                           const float *Jb, const float *ct, float *gd, float *wa)
+{
+  const float R2 = dx * dx + dy * dy + dz * dz;
+  float       F, F1, F2;
+  radial_F(R2 * w2, F, F1, F2);
+  const float is2 = isg * isg, c = is2 * isg * 0.028134884879909f; // 1 / (4 pi 2^{3/2})
+  const float q = c * F, h = c * F1 * is2, hR2 = 0.5f * c * F2 * is2 * is2;
+  const float m0 = Jb[0] * dx + Jb[1] * dy + Jb[2] * dz, m1 = Jb[3] * dx + Jb[4] * dy + Jb[5] * dz, m2 = Jb[6] * dx + Jb[7] * dy + Jb[8] * dz;
+  const float uxd0 = ub[1] * dz - ub[2] * dy, uxd1 = ub[2] * dx - ub[0] * dz, uxd2 = ub[0] * dy - ub[1] * dx;
+  const float mxd0 = m1 * dz - m2 * dy, mxd1 = m2 * dx - m0 * dz, mxd2 = m0 * dy - m1 * dx;
+  const float A = ax * uxd0 + ay * uxd1 + az * uxd2, Bv = ax * mxd0 + ay * mxd1 + az * mxd2, C = ax * ct[0] + ay * ct[1] + az * ct[2];
+  const float dxa0 = dy * az - dz * ay, dxa1 = dz * ax - dx * az, dxa2 = dx * ay - dy * ax;
+  const float axu0 = ay * ub[2] - az * ub[1], axu1 = az * ub[0] - ax * ub[2], axu2 = ax * ub[1] - ay * ub[0];
+  const float axm0 = ay * m2 - az * m1, axm1 = az * m0 - ax * m2, axm2 = ax * m1 - ay * m0;
+  const float fq = -h * (A + C) - 2.f * hR2 * Bv;
+  gd[0] = fq * dx - q * axu0 - h * (Jb[0] * dxa0 + Jb[3] * dxa1 + Jb[6] * dxa2 + axm0);
+  gd[1] = fq * dy - q * axu1 - h * (Jb[1] * dxa0 + Jb[4] * dxa1 + Jb[7] * dxa2 + axm1);
+  gd[2] = fq * dz - q * axu2 - h * (Jb[2] * dxa0 + Jb[5] * dxa1 + Jb[8] * dxa2 + axm2);
+  wa[0] = -q * uxd0 - h * mxd0 - q * ct[0];
+  wa[1] = -q * uxd1 - h * mxd1 - q * ct[1];
+  wa[2] = -q * uxd2 - h * mxd2 - q * ct[2];
+}
+
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float v)
+{
+  const float t  = hi + v;
+  const float bb = t - hi;
+  lo += (hi - (t - bb)) + (v - bb);
+  hi = t;
+}
+
+// Seeds in FP32: [ubar0..2, ct0], [ct1, ct2, Jbar0, Jbar1], [Jbar2..5], [Jbar6..8, 0].
+__global__ void k_adj_seeds32(AdjDev a, int n)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double ub[3], Jb[9], ct[3];
+    load_seeds(a, i, ub, Jb, ct);
+    float4 *o = a.seeds32 + 4 * (size_t)i;
+    o[0]      = make_float4((float)ub[0], (float)ub[1], (float)ub[2], (float)ct[0]);
+    o[1]      = make_float4((float)ct[1], (float)ct[2], (float)Jb[0], (float)Jb[1]);
+    o[2]      = make_float4((float)Jb[2], (float)Jb[3], (float)Jb[4], (float)Jb[5]);
+    o[3]      = make_float4((float)Jb[6], (float)Jb[7], (float)Jb[8], 0.f);
+  }
+}
+__device__ __forceinline__ void load_seeds32(const AdjDev &a, int i, float *ub, float *Jb, float *ct)
+{
+  const float4 s0 = a.seeds32[4 * (size_t)i], s1 = a.seeds32[4 * (size_t)i + 1], s2 = a.seeds32[4 * (size_t)i + 2],
+               s3 = a.seeds32[4 * (size_t)i + 3];
+  ub[0] = s0.x, ub[1] = s0.y, ub[2] = s0.z, ct[0] = s0.w;
+  ct[1] = s1.x, ct[2] = s1.y, Jb[0] = s1.z, Jb[1] = s1.w;
+  Jb[2] = s2.x, Jb[3] = s2.y, Jb[4] = s2.z, Jb[5] = s2.w;
+  Jb[6] = s3.x, Jb[7] = s3.y, Jb[8] = s3.z;
+}
+
+// Per target: xbar_i += sum of ds/dd (FP32, leaf-relative).
+__global__ void __launch_bounds__(128) k_adj_p2p32_tgt(AdjDev a)
+{
+  __shared__ float red[2][128 * 3];
+  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+    const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
+    const int    q0 = a.p2p_start[c], q1 = a.p2p_start[c + 1];
+    const double cx = a.cv.x[c], cy = a.cv.y[c], cz = a.cv.z[c];
+    for (int tc = 0; tc < nb; tc += 128) {
+      const int nbc = min(128, nb - tc);
+      const int TG = nbc <= 32 ? 32 : (nbc <= 64 ? 64 : 128), G = 128 / TG;
+      const int tt = threadIdx.x % TG, g = threadIdx.x / TG;
+      float     hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
+      if (tt < nbc) {
+        const int    i  = b0 + tc + tt;
+        const float4 pi = a.pos32[i];
+        float        ub[3], Jb[9], ct[3];
+        load_seeds32(a, i, ub, Jb, ct);
+        for (int q = q0 + g; q < q1; q += G) {
+          const int   sc = a.p2p_src[q], sb = a.cv.body[sc], sn = a.cv.nbody[sc];
+          const float ox = (float)(a.cv.x[sc] - cx), oy = (float)(a.cv.y[sc] - cy), oz = (float)(a.cv.z[sc] - cz);
+          float       s[3] = {0.f, 0.f, 0.f};
+          for (int j = sb; j < sb + sn; j++) {
+            const float4 pj = a.pos32[j], aj = a.alp32[j];
+            const float  dx = pi.x - (pj.x + ox), dy = pi.y - (pj.y + oy), dz = pi.z - (pj.z + oz);
+            if (dx * dx + dy * dy + dz * dz != 0.f) {
+              float gd[3], wa[3];
+              pair_adj32(dx, dy, dz, aj.x, aj.y, aj.z, aj.w, pj.w, ub, Jb, ct, gd, wa);
+              s[0] += gd[0];
+              s[1] += gd[1];
+              s[2] += gd[2];
+            }
+          }
+          for (int k = 0; k < 3; k++)
+            two_sum_acc(hi[k], lo[k], s[k]);
+        }
+      }
+      __syncthreads();
+      for (int k = 0; k < 3; k++) {
+        red[0][threadIdx.x * 3 + k] = hi[k];
+        red[1][threadIdx.x * 3 + k] = lo[k];
+      }
+      __syncthreads();
+      if (threadIdx.x < nbc) {
+        const int i = b0 + tc + threadIdx.x;
+        for (int k = 0; k < 3; k++) {
+          float h = 0.f, l = 0.f;
+          for (int gg = 0; gg < G; gg++) {
+            two_sum_acc(h, l, red[0][(gg * TG + threadIdx.x) * 3 + k]);
+            l += red[1][(gg * TG + threadIdx.x) * 3 + k];
+          }
+          W(a, W_XNT + k, i) = (double)h + (double)l;
+        }
+      }
+    }
+  }
+}
+
+// Per source: xbar_j -= sum of ds/dd, alphabar_j += sum of ds/dalpha_j (FP32).
+__global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
+{
+  __shared__ float red[2][128 * 6];
+  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+    const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
+    const int    q0 = a.p2pT_start[c], q1 = a.p2pT_start[c + 1];
+    const double cx = a.cv.x[c], cy = a.cv.y[c], cz = a.cv.z[c];
+    for (int tc = 0; tc < nb; tc += 128) {
+      const int nbc = min(128, nb - tc);
+      const int TG = nbc <= 32 ? 32 : (nbc <= 64 ? 64 : 128), G = 128 / TG;
+      const int tt = threadIdx.x % TG, g = threadIdx.x / TG;
+      float     hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (tt < nbc) {
+        const int    j  = b0 + tc + tt;
+        const float4 pj = a.pos32[j], aj = a.alp32[j];
+        for (int q = q0 + g; q < q1; q += G) {
+          const int   tcell = a.p2pT_tgt[q], tb = a.cv.body[tcell], tn = a.cv.nbody[tcell];
+          const float ox = (float)(a.cv.x[tcell] - cx), oy = (float)(a.cv.y[tcell] - cy), oz = (float)(a.cv.z[tcell] - cz);
+          float       s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+          for (int i = tb; i < tb + tn; i++) {
+            const float4 pi = a.pos32[i];
+            const float  dx = (pi.x + ox) - pj.x, dy = (pi.y + oy) - pj.y, dz = (pi.z + oz) - pj.z;
+            if (dx * dx + dy * dy + dz * dz != 0.f) {
+              float ub[3], Jb[9], ct[3], gd[3], wa[3];
+              load_seeds32(a, i, ub, Jb, ct);
+              pair_adj32(dx, dy, dz, aj.x, aj.y, aj.z, aj.w, pj.w, ub, Jb, ct, gd, wa);
+              for (int k = 0; k < 3; k++) {
+                s[k] -= gd[k];
+                s[3 + k] += wa[k];
+              }
+            }
+          }
+          for (int k = 0; k < 6; k++)
+            two_sum_acc(hi[k], lo[k], s[k]);
+        }
+      }
+      __syncthreads();
+      for (int k = 0; k < 6; k++) {
+        red[0][threadIdx.x * 6 + k] = hi[k];
+        red[1][threadIdx.x * 6 + k] = lo[k];
+      }
+      __syncthreads();
+      if (threadIdx.x < nbc) {
+        const int j = b0 + tc + threadIdx.x;
+        for (int k = 0; k < 6; k++) {
+          float h = 0.f, l = 0.f;
+          for (int gg = 0; gg < G; gg++) {
+            two_sum_acc(h, l, red[0][(gg * TG + threadIdx.x) * 6 + k]);
+            l += red[1][(gg * TG + threadIdx.x) * 6 + k];
+          }
+          W(a, k < 3 ? W_XNS + k : W_ANS + k - 3, j) = (double)h + (double)l;
+        }
+      }
+    }
+  }
+}
+
+// M2L^T in FP32 with the mixed forward's scaling (R_s = the source cell's
+// half-width): with S'(d) = R_s^{-(q+1)} S'(d / R_s),
+//   Mbar_s[n] = R_s^{-n} sum_t sum_j Ltil_t[j] conj(S'_{j+n}(d / R_s)),
+//   Ltil_t[j,k] = (-1)^j Lbar_t[j,k] R_s^{-(j+1)},
+// the scaled operands formed in FP64 and rounded once.
+template <int P>
+struct AdjM2L32Sizes {
+  static constexpr int    K = nterms(P), PP = P * P, NE = 3 * PP;
+  static constexpr int    WS = (3 * K + PP > NE) ? 3 * K + PP : NE;
+  static constexpr size_t bytes = (size_t)4 * WS * sizeof(cx<float>);
+};
+
+template <int P>
+__global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells)
+{
+  using S = AdjM2L32Sizes<P>;
+  typedef cx<float> zf;
+  constexpr int K = S::K, NE = S::NE, NA = (NE + 31) / 32, WS = S::WS;
+  extern __shared__ double2 smem_raw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  zf       *Lt = reinterpret_cast<zf *>(smem_raw) + w * WS;
+  zf       *Sp = Lt + 3 * K;
+  int       on[NA], om[NA];
+#pragma unroll
+  for (int i = 0; i < NA; i++) {
+    const int e = lane + 32 * i, idx = e / 3;
+    int       n = 0;
+    while ((n + 1) * (n + 1) <= idx)
+      n++;
+    on[i] = n;
+    om[i] = idx - n * n - n;
+  }
+  for (int s = blockIdx.x * 4 + w; s < ncells; s += gridDim.x * 4) {
+    zf acc[NA];
+#pragma unroll
+    for (int i = 0; i < NA; i++)
+      acc[i] = {0.f, 0.f};
+    const int    q0 = a.m2lT_start[s], q1 = a.m2lT_start[s + 1];
+    const double sx = a.cv.x[s], sy = a.cv.y[s], sz = a.cv.z[s];
+    const int    ls = a.cv.level[s];
+    const double iRs = ldexp(1.0 / a.R0, ls); // 1 / R_s
+    for (int q = q0; q < q1; q++) {
+      const int t = a.m2lT_tgt[q];
+      __syncwarp();
+      for (int e = lane; e < 3 * K; e += 32) {
+        int j, k;
+        jk_of(e / 3, j, k);
+        const double2 v  = a.Lb[(size_t)t * 3 * K + e];
+        const double  sc = ((j & 1) ? -1.0 : 1.0) * ldexp(a.iR0pow[j + 1], ls * (j + 1)); // (-1)^j R_s^{-(j+1)}
+        Lt[e]            = {(float)(v.x * sc), (float)(v.y * sc)};
+      }
+      if (lane < P) {
+        const float dx = (float)((a.cv.x[t] - sx) * iRs), dy = (float)((a.cv.y[t] - sy) * iRs), dz = (float)((a.cv.z[t] - sz) * iRs);
+        const float r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.f / r2, S00 = sqrtf(ir2);
+        zf          col[P];
+        singular_column<float, P>(lane, dx, dy, dz, ir2, S00, col);
+        const int m = lane;
+        for (int n = m; n < P; n++) {
+          const zf v        = col[n];
+          Sp[n * n + n + m] = (m & 1) ? zf{-v.r, -v.i} : v;
+          if (m > 0)
+            Sp[n * n + n - m] = conj(v);
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < NA; i++) {
+        const int e = lane + 32 * i;
+        if (e < NE) {
+          const int d = e % 3, n = on[i], m = om[i];
+          for (int j = 0; j <= P - 1 - n; j++) {
+            const int qq = j + n, base = qq * qq + qq + m;
+            for (int k = 0; k <= j; k++) {
+              const zf l = Lt[tri(j, k) * 3 + d], y = Sp[base - k];
+              acc[i].r   = fmaf(l.r, y.r, fmaf(l.i, y.i, acc[i].r)); // l conj(y)
+              acc[i].i   = fmaf(l.i, y.r, fmaf(-l.r, y.i, acc[i].i));
+            }
+          }
+        }
+      }
+    }
+    __syncwarp();
+    zf *Mpb = Lt;
+#pragma unroll
+    for (int i = 0; i < NA; i++) {
+      const int e = lane + 32 * i;
+      if (e < NE)
+        Mpb[e] = acc[i];
+    }
+    __syncwarp();
+    for (int e = lane; e < 3 * K; e += 32) {
+      const int d = e % 3;
+      int       n, mm;
+      jk_of(e / 3, n, mm);
+      const zf v0 = Mpb[(n * n + n + mm) * 3 + d];
+      double   vr = (mm & 1) ? -(double)v0.r : (double)v0.r, vi = (mm & 1) ? -(double)v0.i : (double)v0.i;
+      if (mm > 0) {
+        const zf v1 = Mpb[(n * n + n - mm) * 3 + d];
+        vr += v1.r;
+        vi -= v1.i;
+      }
+      const double sc = ldexp(a.iR0pow[n], ls * n); // R_s^{-n}
+      a.Mb[(size_t)s * 3 * K + e] = make_double2(vr * sc, vi * sc);
+    }
+    __syncwarp();
+  }
+}
+
 // ------------------------------------------------------------------ host side
 template <class KernelT>
 void set_smem(KernelT k, size_t bytes, bool &once)
@@ -993,8 +1329,14 @@ void eval_adjoint_P(cudaStream_t s, const ExpArgs &e, const AdjDev &d)
       count_launch();
     }
   }
-  set_smem(k_adj_m2l<P>, AdjM2LSizes<P>::bytes, o3);
-  k_adj_m2l<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2LSizes<P>::bytes, s>>>(d, e.ncells);
+  if (d.pos32) {
+    static bool o6 = false;
+    set_smem(k_adj_m2l32<P>, AdjM2L32Sizes<P>::bytes, o6);
+    k_adj_m2l32<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2L32Sizes<P>::bytes, s>>>(d, e.ncells);
+  } else {
+    set_smem(k_adj_m2l<P>, AdjM2LSizes<P>::bytes, o3);
+    k_adj_m2l<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2LSizes<P>::bytes, s>>>(d, e.ncells);
+  }
   count_launch();
   const size_t bm2m = (size_t)(3 * K + 8 * K) * sizeof(zd);
   set_smem(k_adj_m2m<P>, bm2m, o4);
@@ -1009,10 +1351,17 @@ void eval_adjoint_P(cudaStream_t s, const ExpArgs &e, const AdjDev &d)
     set_smem(k_adj_p2m<P>, AdjP2MSizes<P>::bytes, o5);
     k_adj_p2m<P><<<std::min(e.nleaves, 152 * 8), 128, AdjP2MSizes<P>::bytes, s>>>(d);
     count_launch();
-    k_adj_p2p_tgt<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
-    count_launch();
-    k_adj_p2p_src<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
-    count_launch();
+    if (d.pos32) {
+      k_adj_p2p32_tgt<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
+      count_launch();
+      k_adj_p2p32_src<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
+      count_launch();
+    } else {
+      k_adj_p2p_tgt<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
+      count_launch();
+      k_adj_p2p_src<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
+      count_launch();
+    }
   }
   VFMM_LAUNCH_CHECK();
 }
@@ -1037,8 +1386,25 @@ void adjoint_eval(cudaStream_t s, const ExpArgs &e, const AdjBufs &b, const DevI
   d.m2lT_start = b.m2lT_start;
   d.m2lT_tgt   = b.m2lT_tgt;
   d.w          = b.w;
+  d.pos32      = b.pos32;
+  d.alp32      = b.alp32;
+  d.seeds32    = b.seeds32;
+  d.R0         = b.R0;
+  if (b.pos32) {
+    double p = 1.0, ip = 1.0;
+    for (int k = 0; k <= PMAX + 1; k++) {
+      d.R0pow[k]  = p;
+      d.iR0pow[k] = ip;
+      p *= b.R0;
+      ip /= b.R0;
+    }
+  }
   const int n  = b.n;
   VFMM_CUDA_TRY(cudaMemsetAsync(b.w + (size_t)W_AP2M * e.cap, 0, 3 * e.cap * sizeof(double), s));
+  if (b.pos32) {
+    k_adj_seeds32<<<grid_for(n, 256), 256, 0, s>>>(d, n);
+    count_launch();
+  }
   switch (e.P) {
 #define VFMM_ADJ_CASE(PP)                                                                                                                 \
   case PP: eval_adjoint_P<PP>(s, e, d); break;

@@ -119,6 +119,7 @@ struct vfmm_handle_s {
     DevBuf<double2>            Mb, Lb;
     DevBuf<int>                p2pT_start, p2pT_tgt, m2lT_start, m2lT_tgt, orig[2];
     DevBuf<unsigned long long> tkeys, tsorted;
+    DevBuf<float4>             seeds32;
   } adj;
 };
 
@@ -973,21 +974,6 @@ void load_state(vfmm_handle h, const double *p)
   VFMM_CUDA_TRY(cudaMemcpyAsync(q + (size_t)F_R * h->cap, p + 6 * h->cap, h->cap * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
 }
 
-// The FP64 evaluation whatever the handle's precision (the reverse sweep
-// differentiates the FP64 expansions).
-void calculate_fp64(vfmm_handle h)
-{
-  const int prec     = h->cfg.precision;
-  h->cfg.precision   = VFMM_FP64;
-  try {
-    calculate(h);
-  } catch (...) {
-    h->cfg.precision = prec;
-    throw;
-  }
-  h->cfg.precision = prec;
-}
-
 void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int steps, int every, const vfmm_objective *obj, double *value,
              double *gx, double *ga)
 {
@@ -1039,10 +1025,12 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
       evaluate_and_update(h, k, dt);
     }
   }
-  // the objective on the final state
+  // the objective on the final state; evaluations of the reverse sweep run in
+  // the handle's precision (mixed: FP32 P2P^T and M2L^T, the rest FP64)
+  const bool mixed = c.precision == VFMM_MIXED;
   build_tree_and_lists(h);
   track();
-  calculate_fp64(h);
+  calculate(h);
   for (auto *b : {&A.g[0], &A.g[1]})
     b->reserve((size_t)NG * cap);
   A.w.reserve((size_t)NW * cap);
@@ -1084,6 +1072,13 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
     b.m2lT_start = A.m2lT_start.p;
     b.m2lT_tgt   = A.m2lT_tgt.p;
     b.part       = A.part.p;
+    if (mixed) {
+      A.seeds32.reserve(4 * (size_t)N);
+      b.pos32   = h->pos32.p;
+      b.alp32   = h->alp32.p;
+      b.seeds32 = A.seeds32.p;
+      b.R0      = h->tree.R0;
+    }
     adjoint_eval(s, particle_args(h), b, h->info);
     adjoint_scatter(s, A.g[gc].p, A.g[gc ^ 1].p, cap, N, h->ts.perm.p);
     gc ^= 1;
@@ -1104,7 +1099,7 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
       for (int k = S - 1; k >= 0; k--) {
         load_state(h, A.tape.p + (size_t)((st - st0) * S + k) * slot);
         build_tree_and_lists(h);
-        calculate_fp64(h);
+        calculate(h);
         adjoint_stage_pre(s, A.g[gc].p, A.w.p, cap, N, c.integrator, k, dt);
         adjoint_seeds(s, h->soa[h->cur].p, A.w.p, cap, N, c.stretching);
         vjp();

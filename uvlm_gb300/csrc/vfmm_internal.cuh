@@ -256,6 +256,11 @@ struct AdjBufs {
   double2   *Mb, *Lb; // adjoint expansions [cell][3K]
   const int *p2pT_start, *p2pT_tgt, *m2lT_start, *m2lT_tgt;
   double    *part; // ADJ_PARTIALS doubles
+  // mixed mode (else null): the evaluation's FP32 body records, FP32 seed
+  // scratch (4 float4 per body), the tree's R0; P2P^T and M2L^T then run in FP32
+  const float4 *pos32, *alp32;
+  float4       *seeds32;
+  double        R0;
 };
 constexpr int ADJ_PARTIALS = 152 * 2 * 17;
 // vjp of the evaluation whose tree, lists and FP64 expansions are in e, with
