@@ -1301,27 +1301,17 @@ __global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells)
 }
 
 // ------------------------------------------------------------------ host side
-template <class KernelT>
-void set_smem(KernelT k, size_t bytes, bool &once)
-{
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
-}
-
 template <int P>
 void eval_adjoint_P(cudaStream_t s, const ExpArgs &e, const AdjDev &d)
 {
   constexpr int K = nterms(P);
-  static bool   o1 = false, o2 = false, o3 = false, o4 = false, o5 = false;
   if (e.nleaves > 0) {
-    set_smem(k_adj_l2p<P>, AdjL2PSizes<P>::bytes, o1);
+    VFMM_SMEM_ONCE(AdjL2PSizes<P>::bytes, k_adj_l2p<P>);
     k_adj_l2p<P><<<std::min(e.nleaves, 152 * 8), 128, AdjL2PSizes<P>::bytes, s>>>(d);
     count_launch();
   }
   const size_t bl2l = (size_t)(8 * 3 * K + 8 * K) * sizeof(zd);
-  set_smem(k_adj_l2l<P>, bl2l, o2);
+  VFMM_SMEM_ONCE(bl2l, k_adj_l2l<P>);
   for (int l = e.maxLevel - 1; l >= 0; l--) { // forward L2L runs parents at levels 0 .. maxLevel-1
     const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
     if (n1 > n0) {
@@ -1330,16 +1320,15 @@ void eval_adjoint_P(cudaStream_t s, const ExpArgs &e, const AdjDev &d)
     }
   }
   if (d.pos32) {
-    static bool o6 = false;
-    set_smem(k_adj_m2l32<P>, AdjM2L32Sizes<P>::bytes, o6);
+    VFMM_SMEM_ONCE(AdjM2L32Sizes<P>::bytes, k_adj_m2l32<P>);
     k_adj_m2l32<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2L32Sizes<P>::bytes, s>>>(d, e.ncells);
   } else {
-    set_smem(k_adj_m2l<P>, AdjM2LSizes<P>::bytes, o3);
+    VFMM_SMEM_ONCE(AdjM2LSizes<P>::bytes, k_adj_m2l<P>);
     k_adj_m2l<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2LSizes<P>::bytes, s>>>(d, e.ncells);
   }
   count_launch();
   const size_t bm2m = (size_t)(3 * K + 8 * K) * sizeof(zd);
-  set_smem(k_adj_m2m<P>, bm2m, o4);
+  VFMM_SMEM_ONCE(bm2m, k_adj_m2m<P>);
   for (int l = 1; l <= e.maxLevel - 1; l++) { // forward M2M runs parents at levels maxLevel-1 .. 1
     const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
     if (n1 > n0) {
@@ -1348,7 +1337,7 @@ void eval_adjoint_P(cudaStream_t s, const ExpArgs &e, const AdjDev &d)
     }
   }
   if (e.nleaves > 0) {
-    set_smem(k_adj_p2m<P>, AdjP2MSizes<P>::bytes, o5);
+    VFMM_SMEM_ONCE(AdjP2MSizes<P>::bytes, k_adj_p2m<P>);
     k_adj_p2m<P><<<std::min(e.nleaves, 152 * 8), 128, AdjP2MSizes<P>::bytes, s>>>(d);
     count_launch();
     if (d.pos32) {

@@ -6,6 +6,8 @@
 // All work runs on the handle's stream; the host synchronises twice per
 // tree build (node counts, pair counts) and at the end of each API call.
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -635,74 +637,52 @@ void run_stage(vfmm_handle h, int stage, double dt)
 }
 
 // advance for several independent systems, each on its own handle and
-// stream, scheduled phase by phase: every system's tree is enqueued before
-// any node count is awaited, every traversal before any pair count, then
-// every evaluation and update, so that small systems overlap on the GPU and
-// each synchronisation point is met once per batch, not once per system.
+// stream.  The systems are shared out to a pool of host threads (the host's
+// hardware threads, at most 16); each thread runs whole systems one after
+// another through vfmm_advance's code path, so the kernel launches and the two
+// host synchronisation points of every stage proceed for many systems at once
+// and their kernels overlap on the GPU.  Each system's results are those of
+// vfmm_advance on its own.
 void advance_batch(vfmm_handle *hs, vfmm_body *const *bodies, const size_t *ns, int count, double dt)
 {
-  auto on = [&](int b) {
-    VFMM_CUDA_TRY(cudaSetDevice(hs[b]->device));
-    g_launch_counter = &hs[b]->launches;
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int      T  = std::max(1, std::min({count, hw ? (int)hw : 1, 16}));
+  std::atomic<int>         next{0};
+  std::vector<int>         codes(count, VFMM_OK);
+  std::vector<std::string> msgs(count);
+  auto                     work = [&]() {
+    for (int b; (b = next.fetch_add(1)) < count;) {
+      vfmm_handle h = hs[b];
+      try {
+        VFMM_CUDA_TRY(cudaSetDevice(h->device));
+        g_launch_counter = &h->launches;
+        upload(h, bodies[b], ns[b]);
+        const int S = stages_of(h->cfg.integrator);
+        for (int st = 0; st < S; st++)
+          run_stage(h, st, dt);
+        download(h, bodies[b], ns[b]);
+      } catch (const Error &e) {
+        codes[b] = e.code;
+        msgs[b]  = e.msg;
+      } catch (const std::exception &e) {
+        codes[b] = VFMM_ERR_CUDA;
+        msgs[b]  = e.what();
+      }
+    }
+    g_launch_counter = nullptr;
   };
-  int S = 0;
-  for (int b = 0; b < count; b++) {
-    on(b);
-    upload(hs[b], bodies[b], ns[b]);
-    S = std::max(S, stages_of(hs[b]->cfg.integrator));
+  if (T == 1)
+    work();
+  else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < T; t++)
+      pool.emplace_back(work);
+    for (auto &t : pool)
+      t.join();
   }
-  for (int st = 0; st < S; st++) {
-    std::vector<int> act;
-    for (int b = 0; b < count; b++)
-      if (st < stages_of(hs[b]->cfg.integrator))
-        act.push_back(b);
-    for (int b : act) {
-      on(b);
-      vfmm_handle h = hs[b];
-      h->has_tree = h->has_eval = false;
-      VFMM_CUDA_TRY(cudaEventRecord(h->ph[0], h->stream));
-      tree_enqueue(h->stream, h->soa, h->cur, h->cap, h->n, h->cfg.ncrit, h->info, h->hinfo, h->ts, h->tree);
-    }
-    for (int b : act) {
-      on(b);
-      tree_finish(hs[b]->stream, hs[b]->hinfo, hs[b]->tree);
-    }
-    std::vector<int> pend = act;
-    for (int attempt = 0; !pend.empty(); attempt++) {
-      if (attempt > 9)
-        throw Error(VFMM_ERR_CAPACITY, "interaction lists keep overflowing");
-      for (int b : pend) {
-        on(b);
-        vfmm_handle h = hs[b];
-        lists_enqueue(h->stream, h->tree, h->tree, h->cfg.theta, h->info, h->hinfo, h->lists);
-      }
-      std::vector<int> next;
-      for (int b : pend) {
-        on(b);
-        vfmm_handle h = hs[b];
-        if (!lists_finish(h->stream, h->tree, h->info, h->hinfo, h->lists, &h->info->p2p_interactions))
-          next.push_back(b);
-      }
-      pend.swap(next);
-    }
-    for (int b : act) {
-      on(b);
-      vfmm_handle h = hs[b];
-      VFMM_CUDA_TRY(cudaEventRecord(h->ph[1], h->stream));
-      h->has_tree = true;
-      evaluate_and_update(h, st, dt);
-    }
-  }
-  for (int b = 0; b < count; b++) { // enqueue every copy back, then wait
-    on(b);
-    vfmm_handle h = hs[b];
-    soa_to_aos(h->stream, h->soa[h->cur].p, h->cap, h->aos.p, h->n);
-    VFMM_CUDA_TRY(cudaMemcpyAsync(bodies[b], h->aos.p, ns[b] * sizeof(vfmm_body), cudaMemcpyDeviceToHost, h->stream));
-  }
-  for (int b = 0; b < count; b++) {
-    on(b);
-    VFMM_CUDA_TRY(cudaStreamSynchronize(hs[b]->stream));
-  }
+  for (int b = 0; b < count; b++)
+    if (codes[b] != VFMM_OK)
+      throw Error(codes[b], msgs[b]);
 }
 
 } // namespace

@@ -561,11 +561,7 @@ template <int P>
 static void m2m_levels(cudaStream_t s, const ExpArgs &e, const DevExp &d)
 {
   const size_t bytes = (size_t)(8 * 3 + 8) * nterms(P) * sizeof(zd);
-  static bool  once  = false;
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2m<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
+  VFMM_SMEM_ONCE(bytes, k_m2m<P>);
   for (int l = e.maxLevel - 1; l >= 1; l--) {
     const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
     if (n1 > n0) {
@@ -581,11 +577,7 @@ static void upward_P(cudaStream_t s, const ExpArgs &e)
 {
   DevExp       d     = dev_args(e);
   const size_t bytes = (size_t)32 * nterms(P) * sizeof(zd) + 32 * 3 * sizeof(double);
-  static bool  once  = false;
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_p2m<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
+  VFMM_SMEM_ONCE(bytes, k_p2m<P>);
   if (e.nleaves > 0) {
     k_p2m<P><<<std::min(e.nleaves, 152 * 16), 64, bytes, s>>>(d);
     count_launch();
@@ -618,11 +610,7 @@ static void m2l_P(cudaStream_t s, const ExpArgs &e, bool prep)
   if (prep)
     mprep_P<P>(s, e);
   const size_t bytes = (size_t)4 * 4 * PP * sizeof(zd);
-  static bool  once  = false;
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2l<P, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
+  VFMM_SMEM_ONCE(bytes, k_m2l<P, 2, 4>);
   k_m2l<P, 2, 4><<<grid_for(e.ncells, 4, 152 * 32), 128, bytes, s>>>(d, e.ncells);
   count_launch();
   VFMM_LAUNCH_CHECK();
@@ -634,11 +622,7 @@ static void l2l_P(cudaStream_t s, const ExpArgs &e)
 {
   DevExp       d     = dev_args(e);
   const size_t bytes = (size_t)(3 + 8) * nterms(P) * sizeof(zd);
-  static bool  once  = false;
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_l2l<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
+  VFMM_SMEM_ONCE(bytes, k_l2l<P>);
   for (int l = 0; l < e.maxLevel; l++) {
     const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
     if (n1 > n0) {
@@ -654,11 +638,7 @@ static void l2p_P(cudaStream_t s, const ExpArgs &e, double *out)
 {
   DevExp       d     = dev_args(e);
   const size_t bytes = L2PSizes<P>::bytes;
-  static bool  once  = false;
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_l2p_p2p<P, SENS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
+  VFMM_SMEM_ONCE(bytes, k_l2p_p2p<P, SENS>);
   if (e.nleaves > 0) {
     k_l2p_p2p<P, SENS><<<std::min(e.nleaves, 152 * 16), 128, bytes, s>>>(d, out);
     count_launch();

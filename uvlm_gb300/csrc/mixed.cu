@@ -873,11 +873,7 @@ template <int P, int SB>
 static void m2l32_launch(cudaStream_t s, const DevMixed &d, const ExpArgs &e, const MixedArgs &m)
 {
   const size_t bytes = M2LV2<P, SB>::bytes;
-  static bool  once  = false;
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2l32v2<P, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
+  VFMM_SMEM_ONCE(bytes, k_m2l32v2<P, SB>);
   if (e.ncells > 0) {
     k_m2l32v2<P, SB><<<std::min(e.ncells, 152 * 8), P * 32, bytes, s>>>(d, m.lanes32, e.ncells);
     count_launch();
@@ -906,11 +902,7 @@ static void l2p32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double
 {
   DevMixed     d     = dev_mixed(e, m);
   const size_t bytes = L2P32Sizes<P>::bytes;
-  static bool  once  = false;
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_l2p_p2p32<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
+  VFMM_SMEM_ONCE(bytes, k_l2p_p2p32<P>);
   if (e.nleaves > 0) {
     k_l2p_p2p32<P><<<std::min(e.nleaves, 152 * 16), 128, bytes, s>>>(d, out);
     count_launch();
@@ -926,11 +918,7 @@ static void m2m32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
 {
   const DevMixed d     = dev_mixed(e, m);
   const size_t   bytes = (size_t)(8 * 3 + 8) * nterms(P) * sizeof(zf);
-  static bool    once  = false;
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_m2m32<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
+  VFMM_SMEM_ONCE(bytes, k_m2m32<P>);
   for (int l = e.maxLevel - 1; l >= 1; l--) {
     const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
     if (n1 > n0) {
@@ -946,11 +934,7 @@ static void l2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
 {
   const DevMixed d     = dev_mixed(e, m);
   const size_t   bytes = (size_t)(3 + 8) * nterms(P) * sizeof(zf);
-  static bool    once  = false;
-  if (!once) {
-    VFMM_CUDA_TRY(cudaFuncSetAttribute(k_l2l32<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    once = true;
-  }
+  VFMM_SMEM_ONCE(bytes, k_l2l32<P>);
   for (int l = 0; l < e.maxLevel; l++) {
     const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
     if (n1 > n0) {

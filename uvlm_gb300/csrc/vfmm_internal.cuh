@@ -76,6 +76,16 @@ inline void count_launch()
 
 #define VFMM_LAUNCH_CHECK() VFMM_CUDA_TRY(cudaGetLastError())
 
+// Raise a kernel's dynamic shared-memory limit once per process.  A
+// function-local static is initialised exactly once even when several host
+// threads launch (vfmm_advance_batch runs systems on a thread pool).
+// The kernel comes last so that template arguments may contain commas.
+#define VFMM_SMEM_ONCE(bytes, ...)                                                                                                      \
+  do {                                                                                                                                  \
+    static const cudaError_t vfmm_attr_ = cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bytes)); \
+    VFMM_CUDA_TRY(vfmm_attr_);                                                                                                          \
+  } while (0)
+
 struct Error {
   int         code;
   std::string msg;
