@@ -404,7 +404,25 @@ def run_rings64(args, dist: Dist) -> dict | None:
     systems = workloads.ring_batch(64, seed=7 + dist.rank)
     ntot = sum(b.size for b in systems)
     kw = dict(p=8, ncrit=32, theta=0.5, integration="RK2", precision=args.precision, device=dist.local_rank)
-    calcs = [FMMCalculator(**kw) for _ in systems]
+    tuned = None
+    if args.autotune:
+        # leaf size and M2L batch tuned per size bucket (N within a factor of 2)
+        # on the bucket's median system, then used by every handle of the bucket
+        buckets = {}
+        for i, b in enumerate(systems):
+            buckets.setdefault(int(np.log2(b.size)), []).append(i)
+        tuned = {}
+        for key, idx in sorted(buckets.items()):
+            med = sorted(idx, key=lambda i: systems[i].size)[len(idx) // 2]
+            with FMMCalculator(**kw) as c:
+                t = c.autotune(systems[med], args.dt)
+            tuned[key] = {"systems": len(idx), "ncrit": t["ncrit"], "m2l_batch": t["m2l_batch"],
+                          "ms_per_stage": t["ms_per_stage"], "default_ms_per_stage": t["default_ms_per_stage"]}
+        calcs = [FMMCalculator(**dict(kw, ncrit=tuned[int(np.log2(b.size))]["ncrit"],
+                                      m2l_batch=tuned[int(np.log2(b.size))]["m2l_batch"] if args.precision == "mixed" else 0))
+                 for b in systems]
+    else:
+        calcs = [FMMCalculator(**kw) for _ in systems]
     work = [b.copy() for b in systems]
     for _ in range(args.warmup):
         advance_batch(calcs, work, args.dt)
@@ -430,7 +448,8 @@ def run_rings64(args, dist: Dist) -> dict | None:
             "config": {"workload": "64 rings, N log-uniform [2k, 60k], RK2 step per ring", "bodies_total": ntot, "p": 8,
                        "theta": 0.5, "ncrit": 32, "precision": args.precision, "timing": "host wall clock, copies included"},
             "sequential": {"value": evals / ts, "ms_per_step": 1e3 * ts / args.steps,
-                           "note": "the same systems advanced one vfmm_advance after another"}}
+                           "note": "the same systems advanced one vfmm_advance after another"},
+            "autotuned_buckets": tuned}
 
 
 def run_adjoint(args, dist: Dist) -> dict | None:

@@ -78,3 +78,25 @@ def test_autotune(vfmm_lib):
     assert (bb["X"] == ref["X"]).all()
     err = np.linalg.norm(bb["velocity"] - ref["velocity"]) / np.linalg.norm(ref["velocity"])
     assert err < 1e-6
+
+
+def test_m2l_batch_config(vfmm_lib):
+    """vfmm_config.m2l_batch selects the mixed M2L source batch (what the tuner
+    sets); any allowed value stays within the mixed-mode bar, others are refused."""
+    from uvlm_gb300 import FMMCalculator, VfmmError, workloads
+    b = workloads.cloud(30000, seed=31)
+    out = {}
+    for prec, mb in (("fp64", 0), ("mixed", 16), ("mixed", 24), ("mixed", 32)):
+        with FMMCalculator(p=10, ncrit=64, theta=0.5, precision=prec, m2l_batch=mb) as c:
+            assert c.config.m2l_batch == mb
+            bb = b.copy()
+            c.init(bb)
+            c.calculate()
+            c.copyBodies2Host(bb)
+            out[mb] = bb
+    for mb in (16, 24, 32):
+        assert np.array_equal(out[mb]["X"], out[0]["X"])
+        err = np.linalg.norm(out[mb]["velocity"] - out[0]["velocity"]) / np.linalg.norm(out[0]["velocity"])
+        assert err < 1e-6
+    with pytest.raises(VfmmError):
+        FMMCalculator(p=10, ncrit=64, theta=0.5, precision="mixed", m2l_batch=12)

@@ -55,7 +55,7 @@ class vfmm_config(ctypes.Structure):
     _fields_ = [("p", ctypes.c_int), ("ncrit", ctypes.c_int), ("theta", ctypes.c_double),
                 ("precision", ctypes.c_int), ("integrator", ctypes.c_int), ("stretching", ctypes.c_int),
                 ("formulation", ctypes.c_int), ("relax", ctypes.c_double), ("rk4_fixed", ctypes.c_int),
-                ("device", ctypes.c_int), ("viscous", ctypes.c_int), ("reserved0", ctypes.c_int),
+                ("device", ctypes.c_int), ("viscous", ctypes.c_int), ("m2l_batch", ctypes.c_int),
                 ("nu", ctypes.c_double), ("reserved", ctypes.c_int * 2)]
 
 

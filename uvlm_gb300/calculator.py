@@ -30,7 +30,7 @@ class FMMCalculator:
     def __init__(self, p: int = 4, ncrit: int = 128, theta: float = 0.3, integration: str = "RK3",
                  viscous: str = "Inviscid", formulation: str = "cVPM", stretching: str = "Transposed",
                  precision: str = "fp64", relax: float = 0.0, rk4_fixed: bool = False, device: int = -1,
-                 nu: float = 0.0):
+                 nu: float = 0.0, m2l_batch: int = 0):
         cfg = _lib.vfmm_config()
         lib().vfmm_default_config(ctypes.byref(cfg))
         cfg.p, cfg.ncrit, cfg.theta = int(p), int(ncrit), float(theta)
@@ -43,6 +43,7 @@ class FMMCalculator:
         cfg.device = int(device)
         cfg.viscous = _VISC[viscous]
         cfg.nu = float(nu)
+        cfg.m2l_batch = int(m2l_batch)
         h = ctypes.c_void_p()
         code = lib().vfmm_create(ctypes.byref(cfg), ctypes.byref(h))
         if code != 0:

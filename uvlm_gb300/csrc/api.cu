@@ -105,7 +105,6 @@ struct vfmm_handle_s {
   DevBuf<int4>    items, items32, lanes32;
   int             m2l_batch = 16; // sources per mixed-M2L batch (set per p); VFMM_M2L_BATCH = 8, 16, 24 or 32 overrides
   int             items_P = 0, items_per_lane = 0, items_batch = 0;
-  int             m2l_batch_forced = 0; // set by vfmm_autotune
   DevBuf<float2>  Mp32;
   DevBuf<float4>  pos32, alp32;
 
@@ -182,6 +181,8 @@ void validate(const vfmm_config &c)
     throw Error(VFMM_ERR_INVALID, "unknown formulation");
   if (c.relax < 0 || c.relax > 1)
     throw Error(VFMM_ERR_INVALID, "relax must be in [0, 1]");
+  if (c.m2l_batch != 0 && c.m2l_batch != 8 && c.m2l_batch != 16 && c.m2l_batch != 24 && c.m2l_batch != 32)
+    throw Error(VFMM_ERR_INVALID, "m2l_batch must be 0, 8, 16, 24 or 32");
   if (c.viscous != VFMM_INVISCID && c.viscous != VFMM_PSE && c.viscous != VFMM_CSM)
     throw Error(VFMM_ERR_INVALID, "unknown viscous scheme");
   if (!(c.nu >= 0) || !(c.nu < 1e300))
@@ -350,7 +351,7 @@ void build_tree_and_lists(vfmm_handle h)
 
 void ensure_items(vfmm_handle h)
 {
-  if (h->items_P == h->cfg.p && h->items_batch == h->m2l_batch_forced)
+  if (h->items_P == h->cfg.p && h->items_batch == h->cfg.m2l_batch)
     return;
   int  per = 0;
   auto tab = m2l_schedule(h->cfg.p, 32, 2, 4, &per);
@@ -364,13 +365,13 @@ void ensure_items(vfmm_handle h)
   // sources per batch, measured best on GB300: 32 for p <= 10, 24 for p = 11-12, else 16
   const int def  = h->cfg.p <= 10 ? 32 : (h->cfg.p <= 12 ? 24 : 16);
   h->m2l_batch   = sb && (atoi(sb) == 8 || atoi(sb) == 16 || atoi(sb) == 24 || atoi(sb) == 32) ? atoi(sb) : def;
-  if (h->m2l_batch_forced)
-    h->m2l_batch = h->m2l_batch_forced;
+  if (h->cfg.m2l_batch)
+    h->m2l_batch = h->cfg.m2l_batch;
   auto lt32      = m2l_lane_table(h->cfg.p, m2l_half_width(h->cfg.p), h->m2l_batch); // half-tile width and batch of k_m2l32v2
   h->lanes32.reserve(lt32.size());
   VFMM_CUDA_TRY(cudaMemcpy(h->lanes32.p, lt32.data(), lt32.size() * sizeof(int4), cudaMemcpyHostToDevice));
   h->items_P        = h->cfg.p;
-  h->items_batch    = h->m2l_batch_forced;
+  h->items_batch    = h->cfg.m2l_batch;
   h->items_per_lane = per;
 }
 
@@ -902,7 +903,7 @@ int vfmm_autotune(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, v
       }
       return best;
     };
-    const int  ncrit0 = h->cfg.ncrit, forced0 = h->m2l_batch_forced;
+    const int  ncrit0 = h->cfg.ncrit, forced0 = h->cfg.m2l_batch;
     const bool mixed  = h->cfg.precision == VFMM_MIXED;
     std::memset(out, 0, sizeof(*out));
     out->default_ms_per_stage = time_stage();
@@ -914,9 +915,9 @@ int vfmm_autotune(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, v
     try {
       for (int nc : leaf)
         for (int b = 0; b < (mixed ? 3 : 1); b++) {
-          h->cfg.ncrit         = nc;
-          h->m2l_batch_forced  = mixed ? bat[b] : 0;
-          const float ms       = time_stage();
+          h->cfg.ncrit     = nc;
+          h->cfg.m2l_batch = mixed ? bat[b] : 0;
+          const float ms   = time_stage();
           out->tried++;
           if (ms < out->ms_per_stage) {
             out->ms_per_stage = ms;
@@ -925,12 +926,12 @@ int vfmm_autotune(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, v
           }
         }
     } catch (...) {
-      h->cfg.ncrit        = ncrit0;
-      h->m2l_batch_forced = forced0;
+      h->cfg.ncrit     = ncrit0;
+      h->cfg.m2l_batch = forced0;
       throw;
     }
-    h->cfg.ncrit        = out->ncrit;
-    h->m2l_batch_forced = mixed ? out->m2l_batch : 0;
+    h->cfg.ncrit     = out->ncrit;
+    h->cfg.m2l_batch = mixed ? out->m2l_batch : 0;
     h->has_tree = h->has_eval = false;
     VFMM_CUDA_TRY(cudaStreamSynchronize(s));
   });
