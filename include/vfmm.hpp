@@ -115,6 +115,24 @@ struct FMMCalculator {
   // relaxation.hpp:8 (the reference leaves it unwired)
   void relaxation(double f) { check(vfmm_relax(h_, f), "relaxation"); }
 
+  // Gradient of energy * E + impulse . I at the state `steps` steps after
+  // `bodies` with respect to their initial positions and strengths (no
+  // counterpart in the reference; see vfmm_adjoint).  Returns the objective;
+  // gradX and gradAlpha get 3 doubles per body in the order of `bodies`.
+  double adjoint(const exafmm::Bodies &bodies, double dt, int steps, int checkpointEvery, double energy, const double impulse[3],
+                 std::vector<double> &gradX, std::vector<double> &gradAlpha)
+  {
+    vfmm_objective o{};
+    o.energy = energy;
+    for (int d = 0; d < 3; d++)
+      o.impulse[d] = impulse[d];
+    gradX.resize(3 * bodies.size());
+    gradAlpha.resize(3 * bodies.size());
+    double v = 0;
+    check(vfmm_adjoint(h_, bodies.data(), bodies.size(), dt, steps, checkpointEvery, &o, &v, gradX.data(), gradAlpha.data()), "adjoint");
+    return v;
+  }
+
   vfmm_handle handle() const { return h_; }
 
 private:

@@ -24,9 +24,13 @@ int main()
     b.radius        = 3 * ds;
     particles.push_back(b);
   }
-  exafmm::Bodies sensors(1);
+  exafmm::Bodies      sensors(1);
+  std::vector<double> gx, ga;
+  double              energy = 0;
   try {
     FMMCalculator calc(8, 32, 0.5);
+    const double  wI[3] = {0.0, 0.0, 1.0};
+    energy              = calc.adjoint(particles, 0.01, 1, 1, 1.0, wI, gx, ga); // before advance reorders the bodies
     calc.advance(particles, 0.01);
     calc.getSensorData(sensors);
   } catch (const Vortex::Error &e) {
@@ -37,6 +41,9 @@ int main()
   for (const auto &b : particles)
     uz += b.velocity[2];
   const double uc = sensors[0].velocity[2];
-  std::printf("mean uz %.6e centre uz %.6e\n", uz / n, uc);
-  return std::isfinite(uz) && std::fabs(uc - 0.5) < 0.01 ? 0 : 2;
+  double gn = 0;
+  for (double g : gx)
+    gn += g * g;
+  std::printf("mean uz %.6e centre uz %.6e objective %.6e |grad_x| %.6e\n", uz / n, uc, energy, std::sqrt(gn));
+  return std::isfinite(uz) && std::fabs(uc - 0.5) < 0.01 && std::isfinite(gn) && gx.size() == 3 * (size_t)n ? 0 : 2;
 }
