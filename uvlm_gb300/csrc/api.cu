@@ -639,15 +639,17 @@ void run_stage(vfmm_handle h, int stage, double dt)
 
 // advance for several independent systems, each on its own handle and
 // stream.  The systems are shared out to a pool of host threads (the host's
-// hardware threads, at most 16); each thread runs whole systems one after
+// hardware threads, at most 16, or VFMM_BATCH_THREADS up to 64); each thread runs whole systems one after
 // another through vfmm_advance's code path, so the kernel launches and the two
 // host synchronisation points of every stage proceed for many systems at once
 // and their kernels overlap on the GPU.  Each system's results are those of
 // vfmm_advance on its own.
 void advance_batch(vfmm_handle *hs, vfmm_body *const *bodies, const size_t *ns, int count, double dt)
 {
-  const unsigned hw = std::thread::hardware_concurrency();
-  const int      T  = std::max(1, std::min({count, hw ? (int)hw : 1, 16}));
+  const unsigned hw  = std::thread::hardware_concurrency();
+  const char    *env = getenv("VFMM_BATCH_THREADS");
+  const int      cap = env && atoi(env) > 0 ? std::min(atoi(env), 64) : 16;
+  const int      T   = std::max(1, std::min({count, hw ? (int)hw : 1, cap}));
   std::atomic<int>         next{0};
   std::vector<int>         codes(count, VFMM_OK);
   std::vector<std::string> msgs(count);
