@@ -95,7 +95,7 @@ struct AdjL2PSizes {
   static constexpr int    K1 = N1 > 0 ? N1 : 1, K2 = N2 > 0 ? N2 : 1, K3 = N3 > 0 ? N3 : 1;
   static constexpr int    NB = 32; // bodies per staging chunk
   static constexpr size_t zcount = 3 * K + 3 * K1 + 9 * K2 + 27 * K3 + 3 * K1 + 9 * K2 + 3 * K + NB * K1;
-  static constexpr size_t bytes  = zcount * sizeof(zd) + NB * 12 * sizeof(double);
+  static constexpr size_t bytes  = zcount * sizeof(zd) + (NB * 12 + K1) * sizeof(double);
 };
 
 template <int P>
@@ -114,7 +114,13 @@ __global__ void __launch_bounds__(128) k_adj_l2p(AdjDev a)
   zd     *Lb  = JJb + 9 * K2;
   zd     *Ys  = Lb + 3 * K;
   double *Sd  = reinterpret_cast<double *>(Ys + NB * K1);
+  double *Wt  = Sd + NB * 12; // w_m of term tri(n, m): 1 for m = 0, else 2
   const double inv4pi = 0.25 * kInvPi;
+  for (int idx = threadIdx.x; idx < N1; idx += 128) {
+    int n, m;
+    jk_of(idx, n, m);
+    Wt[idx] = m == 0 ? 1.0 : 2.0;
+  }
 
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
     const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
@@ -156,44 +162,57 @@ __global__ void __launch_bounds__(128) k_adj_l2p(AdjDev a)
       if (threadIdx.x < nbc) {
         const int t = threadIdx.x, b = b0 + c0 + t;
         regular_harmonics<double, P - 1>(B(a, F_X, b) - cxx, B(a, F_X + 1, b) - cyy, B(a, F_X + 2, b) - czz, Ys + t * K1);
-        double sd[12];
-        for (int k = 0; k < 12; k++) {
-          sd[k]          = W(a, W_SU + k, b);
-          Sd[t * 12 + k] = sd[k];
-        }
-        double uf[3] = {0, 0, 0}, jf[9], hf[27];
-        for (int k = 0; k < 9; k++)
-          jf[k] = 0;
-        for (int k = 0; k < 27; k++)
-          hf[k] = 0;
-        for (int n = 0; n <= P - 2; n++)
-          for (int m = 0; m <= n; m++) {
-            const int    idx = tri(n, m);
-            const zd     y   = Ys[t * K1 + idx];
-            const double wm  = m == 0 ? 1.0 : 2.0;
+        for (int k = 0; k < 12; k++)
+          Sd[t * 12 + k] = W(a, W_SU + k, b);
+      }
+      __syncthreads();
+      // far field and its derivatives at each body: four threads per body
+      // (adjacent lanes), each summing every fourth term, combined by shuffles
+      {
+        const int t = threadIdx.x >> 2, part = threadIdx.x & 3;
+        double    f[39]; // u (3), J (9), dJ/dx (27)
+#pragma unroll
+        for (int k = 0; k < 39; k++)
+          f[k] = 0;
+        if (t < nbc)
+          for (int idx = part; idx < N1; idx += 4) {
+            const zd     y  = Ys[t * K1 + idx];
+            const double wm = Wt[idx];
+#pragma unroll
             for (int ax = 0; ax < 3; ax++)
-              uf[ax] += wm * (U[idx * 3 + ax].r * y.r - U[idx * 3 + ax].i * y.i);
+              f[ax] += wm * (U[idx * 3 + ax].r * y.r - U[idx * 3 + ax].i * y.i);
             if (idx < N2)
+#pragma unroll
               for (int ae = 0; ae < 9; ae++)
-                jf[ae] += wm * (JJ[idx * 9 + ae].r * y.r - JJ[idx * 9 + ae].i * y.i);
+                f[3 + ae] += wm * (JJ[idx * 9 + ae].r * y.r - JJ[idx * 9 + ae].i * y.i);
             if (idx < N3)
+#pragma unroll
               for (int r = 0; r < 27; r++)
-                hf[r] += wm * (HH[idx * 27 + r].r * y.r - HH[idx * 27 + r].i * y.i);
+                f[12 + r] += wm * (HH[idx * 27 + r].r * y.r - HH[idx * 27 + r].i * y.i);
           }
-        double e = 0;
-        for (int ax = 0; ax < 3; ax++)
-          e -= 2.0 * sd[ax] * uf[ax];
-        for (int ae = 0; ae < 9; ae++)
-          e -= 3.0 * sd[3 + ae] * jf[ae];
-        for (int g = 0; g < 3; g++) {
-          double xb = 0;
-          for (int ax = 0; ax < 3; ax++)
-            xb += sd[ax] * jf[ax * 3 + g];
-          for (int ae = 0; ae < 9; ae++)
-            xb += sd[3 + ae] * hf[ae * 3 + g];
-          W(a, W_XF + g, b) = xb;
+#pragma unroll
+        for (int k = 0; k < 39; k++) {
+          f[k] += __shfl_xor_sync(0xffffffffu, f[k], 1);
+          f[k] += __shfl_xor_sync(0xffffffffu, f[k], 2);
         }
-        W(a, W_EF, b) = e;
+        if (t < nbc && part == 0) {
+          const int     b  = b0 + c0 + t;
+          const double *sd = Sd + t * 12;
+          double        e  = 0;
+          for (int ax = 0; ax < 3; ax++)
+            e -= 2.0 * sd[ax] * f[ax];
+          for (int ae = 0; ae < 9; ae++)
+            e -= 3.0 * sd[3 + ae] * f[3 + ae];
+          for (int g = 0; g < 3; g++) {
+            double xb = 0;
+            for (int ax = 0; ax < 3; ax++)
+              xb += sd[ax] * f[3 + ax * 3 + g];
+            for (int ae = 0; ae < 9; ae++)
+              xb += sd[3 + ae] * f[12 + ae * 3 + g];
+            W(a, W_XF + g, b) = xb;
+          }
+          W(a, W_EF, b) = e;
+        }
       }
       __syncthreads();
 #pragma unroll
@@ -837,28 +856,46 @@ __global__ void __launch_bounds__(GEO_THREADS) k_adj_geom_partial(const double *
   }
 }
 
+// Combines the block partials: one warp, lane l over blocks l, l+32, ...,
+// then a fixed-order combine across lanes in lane 0.
 __global__ void k_adj_geom_final(const double *part, int nb, const DevInfo *info, double *g, size_t cap)
 {
-  if (threadIdx.x || blockIdx.x)
+  __shared__ double red[32][GEO_FIELDS];
+  const int         l = threadIdx.x;
+  if (blockIdx.x || l >= 32)
     return;
-  double v[GEO_FIELDS];
-  for (int k = 0; k < GEO_FIELDS; k++)
-    v[k] = part[k];
-  for (int b = 1; b < nb; b++) {
-    const double *r = part + b * GEO_FIELDS;
+  auto merge = [](double *v, const double *r) {
     for (int k = 0; k < 5; k++)
       v[k] += r[k];
     for (int d = 0; d < 3; d++) {
-      if (r[5 + 4 * d] < v[5 + 4 * d] || (r[5 + 4 * d] == v[5 + 4 * d] && r[6 + 4 * d] >= 0 && r[6 + 4 * d] < v[6 + 4 * d])) {
+      if (r[5 + 4 * d] < v[5 + 4 * d] || (r[5 + 4 * d] == v[5 + 4 * d] && r[6 + 4 * d] >= 0 && (v[6 + 4 * d] < 0 || r[6 + 4 * d] < v[6 + 4 * d]))) {
         v[5 + 4 * d] = r[5 + 4 * d];
         v[6 + 4 * d] = r[6 + 4 * d];
       }
-      if (r[7 + 4 * d] > v[7 + 4 * d] || (r[7 + 4 * d] == v[7 + 4 * d] && r[8 + 4 * d] >= 0 && r[8 + 4 * d] < v[8 + 4 * d])) {
+      if (r[7 + 4 * d] > v[7 + 4 * d] || (r[7 + 4 * d] == v[7 + 4 * d] && r[8 + 4 * d] >= 0 && (v[8 + 4 * d] < 0 || r[8 + 4 * d] < v[8 + 4 * d]))) {
         v[7 + 4 * d] = r[7 + 4 * d];
         v[8 + 4 * d] = r[8 + 4 * d];
       }
     }
+  };
+  double v[GEO_FIELDS];
+  for (int k = 0; k < 5; k++)
+    v[k] = 0;
+  for (int d = 0; d < 3; d++) {
+    v[5 + 4 * d] = INFINITY;
+    v[6 + 4 * d] = -1;
+    v[7 + 4 * d] = -INFINITY;
+    v[8 + 4 * d] = -1;
   }
+  for (int b = l; b < nb; b += 32)
+    merge(v, part + b * GEO_FIELDS);
+  for (int k = 0; k < GEO_FIELDS; k++)
+    red[l][k] = v[k];
+  __syncwarp();
+  if (l != 0)
+    return;
+  for (int t = 1; t < 32; t++)
+    merge(v, red[t]);
   const double R0 = info->R0;
   if (!(R0 > 0))
     return;
@@ -1209,26 +1246,29 @@ __global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells)
 {
   using S = AdjM2L32Sizes<P>;
   typedef cx<float> zf;
-  constexpr int K = S::K, NE = S::NE, NA = (NE + 31) / 32, WS = S::WS;
+  constexpr int K = S::K, PP = S::PP, NA = (PP + 31) / 32, WS = S::WS;
   extern __shared__ double2 smem_raw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   zf       *Lt = reinterpret_cast<zf *>(smem_raw) + w * WS;
   zf       *Sp = Lt + 3 * K;
-  int       on[NA], om[NA];
+  // a lane owns outputs (n, m) = n^2 + n + m = lane + 32 i, all three components
+  int on[NA], om[NA];
 #pragma unroll
   for (int i = 0; i < NA; i++) {
-    const int e = lane + 32 * i, idx = e / 3;
-    int       n = 0;
+    const int idx = lane + 32 * i;
+    int       n   = 0;
     while ((n + 1) * (n + 1) <= idx)
       n++;
     on[i] = n;
     om[i] = idx - n * n - n;
   }
   for (int s = blockIdx.x * 4 + w; s < ncells; s += gridDim.x * 4) {
-    zf acc[NA];
+    zf acc[NA][3];
 #pragma unroll
     for (int i = 0; i < NA; i++)
-      acc[i] = {0.f, 0.f};
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+        acc[i][d] = {0.f, 0.f};
     const int    q0 = a.m2lT_start[s], q1 = a.m2lT_start[s + 1];
     const double sx = a.cv.x[s], sy = a.cv.y[s], sz = a.cv.z[s];
     const int    ls = a.cv.level[s];
@@ -1259,28 +1299,32 @@ __global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells)
       __syncwarp();
 #pragma unroll
       for (int i = 0; i < NA; i++) {
-        const int e = lane + 32 * i;
-        if (e < NE) {
-          const int d = e % 3, n = on[i], m = om[i];
+        if (lane + 32 * i < PP) {
+          const int n = on[i], m = om[i];
           for (int j = 0; j <= P - 1 - n; j++) {
             const int qq = j + n, base = qq * qq + qq + m;
             for (int k = 0; k <= j; k++) {
-              const zf l = Lt[tri(j, k) * 3 + d], y = Sp[base - k];
-              acc[i].r   = fmaf(l.r, y.r, fmaf(l.i, y.i, acc[i].r)); // l conj(y)
-              acc[i].i   = fmaf(l.i, y.r, fmaf(-l.r, y.i, acc[i].i));
+              const zf  y  = Sp[base - k];
+              const zf *lp = Lt + tri(j, k) * 3;
+#pragma unroll
+              for (int d = 0; d < 3; d++) {
+                const zf l  = lp[d];
+                acc[i][d].r = fmaf(l.r, y.r, fmaf(l.i, y.i, acc[i][d].r)); // l conj(y)
+                acc[i][d].i = fmaf(l.i, y.r, fmaf(-l.r, y.i, acc[i][d].i));
+              }
             }
           }
         }
       }
     }
     __syncwarp();
-    zf *Mpb = Lt;
+    zf *Mpb = Lt; // [n^2+n+m][d]
 #pragma unroll
-    for (int i = 0; i < NA; i++) {
-      const int e = lane + 32 * i;
-      if (e < NE)
-        Mpb[e] = acc[i];
-    }
+    for (int i = 0; i < NA; i++)
+      if (lane + 32 * i < PP)
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+          Mpb[(lane + 32 * i) * 3 + d] = acc[i][d];
     __syncwarp();
     for (int e = lane; e < 3 * K; e += 32) {
       const int d = e % 3;
