@@ -23,6 +23,7 @@
 //                                         - sum xbar_far . (x - X0),
 // passed to the bodies that set the bounding box.
 #include <algorithm>
+#include <vector>
 #include "harmonics.cuh"
 #include "vfmm_internal.cuh"
 
@@ -32,7 +33,11 @@ namespace {
 
 typedef cx<double> zd;
 
-static __constant__ HarmRecip<double> kHR = make_harm_recip<double>();
+static __constant__ HarmRecip<double> kHR  = make_harm_recip<double>();
+static __constant__ HarmRecip<float>  kHRf = make_harm_recip<float>();
+template <class T> __device__ __forceinline__ const HarmRecip<T> &harm_recip();
+template <> __device__ __forceinline__ const HarmRecip<double> &harm_recip<double>() { return kHR; }
+template <> __device__ __forceinline__ const HarmRecip<float> &harm_recip<float>() { return kHRf; }
 
 constexpr double kInvPi     = 0.318309886183790671537767526745028724;
 constexpr double kInvSqrtPi = 0.564189583547756286948079451560772586;
@@ -43,7 +48,8 @@ __device__ __forceinline__ zd ldz(const double2 *p)
   return {v.x, v.y};
 }
 __device__ __forceinline__ void stz(double2 *p, zd v) { *p = make_double2(v.r, v.i); }
-__device__ __forceinline__ void cadd(zd &a, zd b)
+template <class T>
+__device__ __forceinline__ void cadd(cx<T> &a, cx<T> b)
 {
   a.r += b.r;
   a.i += b.i;
@@ -71,6 +77,7 @@ struct AdjDev {
   // mixed mode: FP32 body records of the evaluation and the seeds in FP32
   const float4  *pos32, *alp32;         // (x - X_leaf, 1/(2 sigma^2)), (alpha, 1/sigma)
   float4        *seeds32;               // per body 4 x float4: ubar, ct, Jbar (see k_adj_seeds32)
+  float2        *Lhat32;                // per cell 3K: scaled adjoint locals for M2L^T (k_adj_lhat32)
   double         R0;
   double         R0pow[PMAX + 2], iR0pow[PMAX + 2];
 };
@@ -283,53 +290,289 @@ __global__ void __launch_bounds__(128) k_adj_l2p(AdjDev a)
   }
 }
 
+// L2P^T for mixed mode: the per-leaf derivative operators and their
+// transposes stay FP64 (as k_adj_l2p); the per-body work runs in FP32 at the
+// leaf-relative position y = (x - X_c) / R_c, with the coefficients of degree
+// n multiplied by R_c^n (sum c_n Y_n(x - X_c) = sum (c_n R_c^n) Y_n(y)), so
+// the far-field values and their derivatives come out unscaled, and the
+// per-body sums Ubar = sum w ubar conj(Y(x - X_c)) as R_c^n times the FP32
+// sums over Y(y).
+__device__ __forceinline__ void load_seeds32(const AdjDev &a, int i, float *ub, float *Jb, float *ct); // FP32 seeds, below
+
+template <int P>
+struct AdjL2P32Sizes {
+  using S                          = AdjL2PSizes<P>;
+  static constexpr int    K        = S::K, K1 = S::K1, K2 = S::K2, K3 = S::K3, NB = S::NB;
+  static constexpr size_t zd_count = 3 * K + 3 * K1 + 9 * K2 + 3 * K1 + 9 * K2 + 3 * K;       // Lc, U, JJ, Ub, JJb, Lb
+  static constexpr size_t zf_count = 3 * K1 + 9 * K2 + 27 * K3 + NB * K1;                   // U32, JJ32, HH32, Ys
+  static constexpr size_t bytes    = zd_count * sizeof(zd) + zf_count * sizeof(cx<float>) + (NB * 12 + K1) * sizeof(float);
+};
+
+template <int P>
+__global__ void __launch_bounds__(128) k_adj_l2p32(AdjDev a)
+{
+  using S = AdjL2PSizes<P>;
+  typedef cx<float> zf;
+  constexpr int K = S::K, K1 = S::K1, K2 = S::K2, K3 = S::K3, N1 = S::N1, N2 = S::N2, N3 = S::N3, NB = S::NB;
+  constexpr int NO = (3 * N1 + 9 * N2 + 127) / 128;
+  extern __shared__ double2 smem_raw[];
+  zd    *Lc   = reinterpret_cast<zd *>(smem_raw);
+  zd    *U    = Lc + 3 * K;
+  zd    *JJ   = U + 3 * K1;
+  zd    *Ub   = JJ + 9 * K2;
+  zd    *JJb  = Ub + 3 * K1;
+  zd    *Lb   = JJb + 9 * K2;
+  zf    *U32  = reinterpret_cast<zf *>(Lb + 3 * K);
+  zf    *JJ32 = U32 + 3 * K1;
+  zf    *HH32 = JJ32 + 9 * K2;
+  zf    *Ys   = HH32 + 27 * K3;
+  float *Sd   = reinterpret_cast<float *>(Ys + NB * K1);
+  float *Wt   = Sd + NB * 12;
+  const double inv4pi = 0.25 * kInvPi;
+  for (int idx = threadIdx.x; idx < N1; idx += 128) {
+    int n, m;
+    jk_of(idx, n, m);
+    Wt[idx] = m == 0 ? 1.f : 2.f;
+  }
+  for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
+    const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c], lev = a.cv.level[c];
+    const double cxx = a.cv.x[c], cyy = a.cv.y[c], czz = a.cv.z[c];
+    const double iR  = ldexp(1.0 / a.R0, lev);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * K; e += 128)
+      Lc[e] = ldz(a.L + (size_t)c * 3 * K + e);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * N1; e += 128) {
+      const int idx = e / 3, ax = e % 3;
+      int       n, mu;
+      jk_of(idx, n, mu);
+      const int b1 = (ax + 1) % 3, c1 = (ax + 2) % 3;
+      const zd  p = deriv_coef(Lc, n, mu, b1, 3, c1), q = deriv_coef(Lc, n, mu, c1, 3, b1);
+      const zd  u = {inv4pi * (p.r - q.r), inv4pi * (p.i - q.i)};
+      U[idx * 3 + ax]   = u;
+      const double sc   = ldexp(a.R0pow[n], -lev * n);
+      U32[idx * 3 + ax] = {(float)(u.r * sc), (float)(u.i * sc)};
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 9 * N2; e += 128) {
+      const int idx = e / 9, ae = e % 9;
+      int       n, mu;
+      jk_of(idx, n, mu);
+      const zd v         = deriv_coef(U, n, mu, ae % 3, 3, ae / 3);
+      JJ[idx * 9 + ae]   = v;
+      const double sc    = ldexp(a.R0pow[n], -lev * n);
+      JJ32[idx * 9 + ae] = {(float)(v.r * sc), (float)(v.i * sc)};
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 27 * N3; e += 128) {
+      const int idx = e / 27, r = e % 27;
+      int       n, mu;
+      jk_of(idx, n, mu);
+      const zd     v  = deriv_coef(JJ, n, mu, r % 3, 9, r / 3);
+      const double sc = ldexp(a.R0pow[n], -lev * n);
+      HH32[idx * 27 + r] = {(float)(v.r * sc), (float)(v.i * sc)};
+    }
+    __syncthreads();
+
+    zf acc[NO > 0 ? NO : 1];
+#pragma unroll
+    for (int i = 0; i < (NO > 0 ? NO : 1); i++)
+      acc[i] = {0.f, 0.f};
+    for (int c0 = 0; c0 < nb; c0 += NB) {
+      const int nbc = min(NB, nb - c0);
+      if (threadIdx.x < nbc) {
+        const int t = threadIdx.x, b = b0 + c0 + t;
+        regular_harmonics<float, P - 1>((float)((B(a, F_X, b) - cxx) * iR), (float)((B(a, F_X + 1, b) - cyy) * iR),
+                                        (float)((B(a, F_X + 2, b) - czz) * iR), Ys + t * K1);
+        float ub[3], Jb[9], ct[3];
+        load_seeds32(a, b, ub, Jb, ct);
+        for (int k = 0; k < 3; k++)
+          Sd[t * 12 + k] = ub[k];
+        for (int k = 0; k < 9; k++)
+          Sd[t * 12 + 3 + k] = Jb[k];
+      }
+      __syncthreads();
+      {
+        const int t = threadIdx.x >> 2, part = threadIdx.x & 3;
+        float     f[39];
+#pragma unroll
+        for (int k = 0; k < 39; k++)
+          f[k] = 0.f;
+        if (t < nbc)
+          for (int idx = part; idx < N1; idx += 4) {
+            const zf    y  = Ys[t * K1 + idx];
+            const float wm = Wt[idx];
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++)
+              f[ax] = fmaf(wm, U32[idx * 3 + ax].r * y.r - U32[idx * 3 + ax].i * y.i, f[ax]);
+            if (idx < N2)
+#pragma unroll
+              for (int ae = 0; ae < 9; ae++)
+                f[3 + ae] = fmaf(wm, JJ32[idx * 9 + ae].r * y.r - JJ32[idx * 9 + ae].i * y.i, f[3 + ae]);
+            if (idx < N3)
+#pragma unroll
+              for (int r = 0; r < 27; r++)
+                f[12 + r] = fmaf(wm, HH32[idx * 27 + r].r * y.r - HH32[idx * 27 + r].i * y.i, f[12 + r]);
+          }
+#pragma unroll
+        for (int k = 0; k < 39; k++) {
+          f[k] += __shfl_xor_sync(0xffffffffu, f[k], 1);
+          f[k] += __shfl_xor_sync(0xffffffffu, f[k], 2);
+        }
+        if (t < nbc && part == 0) {
+          const int    b  = b0 + c0 + t;
+          const float *sd = Sd + t * 12;
+          double       e  = 0;
+          for (int ax = 0; ax < 3; ax++)
+            e -= 2.0 * sd[ax] * f[ax];
+          for (int ae = 0; ae < 9; ae++)
+            e -= 3.0 * sd[3 + ae] * f[3 + ae];
+          for (int g = 0; g < 3; g++) {
+            double xb = 0;
+            for (int ax = 0; ax < 3; ax++)
+              xb += (double)sd[ax] * f[3 + ax * 3 + g];
+            for (int ae = 0; ae < 9; ae++)
+              xb += (double)sd[3 + ae] * f[12 + ae * 3 + g];
+            W(a, W_XF + g, b) = xb;
+          }
+          W(a, W_EF, b) = e;
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < NO; i++) {
+        const int o = threadIdx.x + 128 * i;
+        if (o < 3 * N1) {
+          const int   idx = o / 3, ax = o % 3;
+          const float wm  = Wt[idx];
+          for (int tt = 0; tt < nbc; tt++) {
+            const zf    y  = Ys[tt * K1 + idx];
+            const float sv = wm * Sd[tt * 12 + ax];
+            acc[i].r       = fmaf(sv, y.r, acc[i].r);
+            acc[i].i       = fmaf(-sv, y.i, acc[i].i);
+          }
+        } else if (o < 3 * N1 + 9 * N2) {
+          const int   o2 = o - 3 * N1, idx = o2 / 9, ae = o2 % 9;
+          const float wm = Wt[idx];
+          for (int tt = 0; tt < nbc; tt++) {
+            const zf    y  = Ys[tt * K1 + idx];
+            const float sv = wm * Sd[tt * 12 + 3 + ae];
+            acc[i].r       = fmaf(sv, y.r, acc[i].r);
+            acc[i].i       = fmaf(-sv, y.i, acc[i].i);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // Ubar, JJbar = R_c^n times the FP32 sums (FP64 from here on)
+#pragma unroll
+    for (int i = 0; i < NO; i++) {
+      const int o = threadIdx.x + 128 * i;
+      if (o < 3 * N1 + 9 * N2) {
+        const int idx = o < 3 * N1 ? o / 3 : (o - 3 * N1) / 9;
+        int       n, m;
+        jk_of(idx, n, m);
+        const double sc = ldexp(a.R0pow[n], -lev * n);
+        const zd     v  = {(double)acc[i].r * sc, (double)acc[i].i * sc};
+        if (o < 3 * N1)
+          Ub[o] = v;
+        else
+          JJb[o - 3 * N1] = v;
+      }
+    }
+    for (int e = threadIdx.x; e < 3 * K; e += 128)
+      Lb[e] = {0, 0};
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      const int ax = threadIdx.x;
+      for (int idx = 0; idx < N2; idx++) {
+        int n, mu;
+        jk_of(idx, n, mu);
+        for (int ex = 0; ex < 3; ex++)
+          deriv_coef_adj(Ub, n, mu, ex, 3, ax, JJb[idx * 9 + ax * 3 + ex]);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      const int cc = threadIdx.x;
+      for (int idx = 0; idx < N1; idx++) {
+        int n, mu;
+        jk_of(idx, n, mu);
+        const zd u1 = Ub[idx * 3 + (cc + 1) % 3], u2 = Ub[idx * 3 + (cc + 2) % 3];
+        deriv_coef_adj(Lb, n, mu, (cc + 2) % 3, 3, cc, zd{inv4pi * u1.r, inv4pi * u1.i});
+        deriv_coef_adj(Lb, n, mu, (cc + 1) % 3, 3, cc, zd{-inv4pi * u2.r, -inv4pi * u2.i});
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * K; e += 128)
+      stz(a.Lb + (size_t)c * 3 * K + e, Lb[e]);
+  }
+}
+
 // ------------------------------------------------------------------ L2L^T
 // Forward (k_l2l): L_child[j,k] += terms in L_parent[n, +-m] and the regular
 // harmonics of X_child - X_parent.  Transposed, per parent coefficient
 // (n, mm): for every child and child coefficient (j <= n, k <= j),
 //   term A (mm >= 1, k + mm <= n - j): +-conj(Lbar_child[j,k] Y[n-j, k+mm]),
 //   term B (|mm - k| <= n - j):        +-Lbar_child[j,k] (conj Y[n-j, mm-k] | Y[n-j, k-mm]).
-template <int P>
+// T = float (mixed mode) works in the forward's scaled variables, scaled by
+// the parent's half-width R_p: Lbar_child[j] / R_p^j in, harmonics at
+// (X_child - X_parent) / R_p, Lbar_parent[n] = R_p^n times the FP32 sum.
+template <int P, class T>
 __global__ void __launch_bounds__(128) k_adj_l2l(AdjDev a, const int *cells, int count)
 {
-  constexpr int K = nterms(P);
+  typedef cx<T> zt;
+  constexpr bool MIX = sizeof(T) == 4;
+  constexpr int  K   = nterms(P);
   extern __shared__ double2 smem_raw[];
-  zd *Lch = reinterpret_cast<zd *>(smem_raw); // [8][3K]
-  zd *Ys  = Lch + 8 * 3 * K;                  // [8][K]
+  zt *Lch = reinterpret_cast<zt *>(smem_raw); // [8][3K]
+  zt *Ys  = Lch + 8 * 3 * K;                  // [8][K]
   for (int pi = blockIdx.x; pi < count; pi += gridDim.x) {
     const int p = cells[pi], nch = a.cv.nchild[p], ch0 = a.cv.child[p];
     if (nch == 0)
       continue;
+    const int    lev = a.cv.level[p];
+    const double iRp = MIX ? ldexp(1.0 / a.R0, lev) : 1.0;
     __syncthreads();
-    for (int e = threadIdx.x; e < nch * 3 * K; e += blockDim.x)
-      Lch[e] = ldz(a.Lb + (size_t)ch0 * 3 * K + e);
+    for (int e = threadIdx.x; e < nch * 3 * K; e += blockDim.x) {
+      const double2 v = a.Lb[(size_t)ch0 * 3 * K + e];
+      double        sc = 1.0;
+      if (MIX) {
+        int j, k;
+        jk_of((e % (3 * K)) / 3, j, k);
+        sc = ldexp(a.iR0pow[j], lev * j); // R_p^{-j}
+      }
+      Lch[e] = {(T)(v.x * sc), (T)(v.y * sc)};
+    }
     if (threadIdx.x < nch) {
       const int ch = ch0 + threadIdx.x;
-      regular_harmonics<double, P>(a.cv.x[ch] - a.cv.x[p], a.cv.y[ch] - a.cv.y[p], a.cv.z[ch] - a.cv.z[p], Ys + threadIdx.x * K);
+      regular_harmonics<T, P>((T)((a.cv.x[ch] - a.cv.x[p]) * iRp), (T)((a.cv.y[ch] - a.cv.y[p]) * iRp), (T)((a.cv.z[ch] - a.cv.z[p]) * iRp),
+                              Ys + threadIdx.x * K);
     }
     __syncthreads();
     for (int o = threadIdx.x; o < 3 * K; o += blockDim.x) {
       const int idx = o / 3, d = o % 3;
       int       n, mm;
       jk_of(idx, n, mm);
-      zd acc{0, 0};
+      zt acc{T(0), T(0)};
       for (int ci = 0; ci < nch; ci++) {
-        const zd *Y = Ys + ci * K, *Lc = Lch + ci * 3 * K;
+        const zt *Y = Ys + ci * K, *Lc = Lch + ci * 3 * K;
         for (int j = 0; j <= n; j++) {
           const int nj = n - j;
           for (int k = 0; k <= j; k++) {
-            const zd l = Lc[tri(j, k) * 3 + d];
+            const zt l = Lc[tri(j, k) * 3 + d];
             if (mm >= 1 && k + mm <= nj)
               cadd(acc, neg_if(conj(l * Y[tri(nj, k + mm)]), (k & 1) != 0));
             if (abs(mm - k) <= nj) {
               const bool neg = mm < k && ((k - mm) & 1);
-              const zd   wc  = mm >= k ? conj(Y[tri(nj, mm - k)]) : Y[tri(nj, k - mm)];
+              const zt   wc  = mm >= k ? conj(Y[tri(nj, mm - k)]) : Y[tri(nj, k - mm)];
               cadd(acc, neg_if(l * wc, neg));
             }
           }
         }
       }
-      stz(a.Lb + (size_t)p * 3 * K + o, acc);
+      const double sc = MIX ? ldexp(a.R0pow[n], -lev * n) : 1.0; // R_p^n
+      a.Lb[(size_t)p * 3 * K + o] = make_double2((double)acc.r * sc, (double)acc.i * sc);
     }
   }
 }
@@ -440,37 +683,52 @@ __global__ void __launch_bounds__(128) k_adj_m2l(AdjDev a, int ncells)
 // coefficient (j', k'), over n <= P-1-j' and the parent's (j' + n, k):
 //   term 1 (k' >= 1, m = k - k', |m| <= n): +-Mbar_p[j,k] (Y[n,m] | conj Y[n,|m|]),
 //   term 2 (m = k + k' <= n):               +-conj(Mbar_p[j,k] Y[n,m]).
-template <int P>
+// T = float: Mbar_parent[j] R_p^j in, harmonics at (X_parent - X_child) / R_p,
+// Mbar_child[j'] += the FP32 sum / R_p^{j'} (the forward's k_m2m32 scaling).
+template <int P, class T>
 __global__ void __launch_bounds__(128) k_adj_m2m(AdjDev a, const int *cells, int count)
 {
-  constexpr int K = nterms(P);
+  typedef cx<T> zt;
+  constexpr bool MIX = sizeof(T) == 4;
+  constexpr int  K   = nterms(P);
   extern __shared__ double2 smem_raw[];
-  zd *Mp = reinterpret_cast<zd *>(smem_raw); // [3K]
-  zd *Ys = Mp + 3 * K;                       // [8][K]
+  zt *Mp = reinterpret_cast<zt *>(smem_raw); // [3K]
+  zt *Ys = Mp + 3 * K;                       // [8][K]
   for (int pi = blockIdx.x; pi < count; pi += gridDim.x) {
     const int c = cells[pi], nch = a.cv.nchild[c], ch0 = a.cv.child[c];
     if (nch == 0)
       continue;
+    const int    lev = a.cv.level[c];
+    const double iRp = MIX ? ldexp(1.0 / a.R0, lev) : 1.0;
     __syncthreads();
-    for (int e = threadIdx.x; e < 3 * K; e += blockDim.x)
-      Mp[e] = ldz(a.Mb + (size_t)c * 3 * K + e);
+    for (int e = threadIdx.x; e < 3 * K; e += blockDim.x) {
+      const double2 v  = a.Mb[(size_t)c * 3 * K + e];
+      double        sc = 1.0;
+      if (MIX) {
+        int j, k;
+        jk_of(e / 3, j, k);
+        sc = ldexp(a.R0pow[j], -lev * j); // R_p^j
+      }
+      Mp[e] = {(T)(v.x * sc), (T)(v.y * sc)};
+    }
     if (threadIdx.x < nch) {
       const int ch = ch0 + threadIdx.x;
-      regular_harmonics<double, P>(a.cv.x[c] - a.cv.x[ch], a.cv.y[c] - a.cv.y[ch], a.cv.z[c] - a.cv.z[ch], Ys + threadIdx.x * K);
+      regular_harmonics<T, P>((T)((a.cv.x[c] - a.cv.x[ch]) * iRp), (T)((a.cv.y[c] - a.cv.y[ch]) * iRp), (T)((a.cv.z[c] - a.cv.z[ch]) * iRp),
+                              Ys + threadIdx.x * K);
     }
     __syncthreads();
     for (int o = threadIdx.x; o < nch * 3 * K; o += blockDim.x) {
       const int ci = o / (3 * K), r = o % (3 * K), d = r % 3;
       int       jp, kp;
       jk_of(r / 3, jp, kp);
-      const zd *Y = Ys + ci * K;
-      zd        acc{0, 0};
+      const zt *Y = Ys + ci * K;
+      zt        acc{T(0), T(0)};
       for (int n = 0; n <= P - 1 - jp; n++) {
         const int j = jp + n;
         if (kp >= 1)
           for (int k = max(0, kp - n); k <= min(j, kp + n); k++) {
             const int  m   = k - kp;
-            const zd   y   = Y[tri(n, m > 0 ? m : -m)];
+            const zt   y   = Y[tri(n, m > 0 ? m : -m)];
             const bool neg = ((m < 0 ? (m & 1) : 0) ^ (n & 1)) != 0;
             cadd(acc, neg_if(Mp[tri(j, k) * 3 + d] * (m > 0 ? y : conj(y)), neg));
           }
@@ -480,8 +738,9 @@ __global__ void __launch_bounds__(128) k_adj_m2m(AdjDev a, const int *cells, int
           cadd(acc, neg_if(conj(Mp[tri(j, k) * 3 + d] * Y[tri(n, m)]), neg));
         }
       }
-      double2 *q = a.Mb + (size_t)(ch0 + ci) * 3 * K + r;
-      stz(q, ldz(q) + acc);
+      const double sc = MIX ? ldexp(a.iR0pow[jp], lev * jp) : 1.0; // R_p^{-j'}
+      double2     *q  = a.Mb + (size_t)(ch0 + ci) * 3 * K + r;
+      *q              = make_double2(q->x + (double)acc.r * sc, q->y + (double)acc.i * sc);
     }
   }
 }
@@ -492,33 +751,41 @@ __global__ void __launch_bounds__(128) k_adj_m2m(AdjDev a, const int *cells, int
 //   xbar_b = sum_d alpha_bd grad phi_d,  phi_d(x) = sum Re(Mbar_d[n,m] Y_n^m(x)),
 // the gradient from the derivative operators applied to Mbar_d written as a
 // full-range real expansion (m > 0 terms halved).
-template <int P>
+// T = float: at y = (x - X_c) / R_c with Mbar_d[n] R_c^n (the forward's
+// k_p2m32 scaling); the position adjoint is the y-gradient over R_c.
+template <int P, class T>
 struct AdjP2MSizes {
   static constexpr int    K = nterms(P), N1 = nterms(P - 1);
-  static constexpr size_t bytes = (size_t)(6 * K + 9 * N1) * sizeof(zd);
+  static constexpr size_t bytes = (size_t)(6 * K + 9 * N1) * sizeof(cx<T>);
 };
 
-template <int P>
+template <int P, class T>
 __global__ void __launch_bounds__(128) k_adj_p2m(AdjDev a)
 {
-  constexpr int K = nterms(P), N1 = nterms(P - 1);
+  typedef cx<T> zt;
+  constexpr bool MIX = sizeof(T) == 4;
+  constexpr int  K = nterms(P), N1 = nterms(P - 1);
   extern __shared__ double2 smem_raw[];
-  zd *Mb = reinterpret_cast<zd *>(smem_raw); // [K][3]
-  zd *Cn = Mb + 3 * K;                       // [K][3]
-  zd *DM = Cn + 3 * K;                       // [N1][9]: D_ax of component d at ax * 3 + d
+  zt                 *Mb = reinterpret_cast<zt *>(smem_raw); // [K][3]
+  zt                 *Cn = Mb + 3 * K;                       // [K][3]
+  zt                 *DM = Cn + 3 * K;                       // [N1][9]: D_ax of component d at ax * 3 + d
+  const HarmRecip<T> &hr = harm_recip<T>();
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
     const int c = a.leaf_cells[li];
     if (a.cv.level[c] == 0)
       continue; // the forward P2M skips level 0
-    const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
+    const int    b0 = a.cv.body[c], nb = a.cv.nbody[c], lev = a.cv.level[c];
     const double cxx = a.cv.x[c], cyy = a.cv.y[c], czz = a.cv.z[c];
+    const double iRc = MIX ? ldexp(1.0 / a.R0, lev) : 1.0;
     __syncthreads();
     for (int e = threadIdx.x; e < 3 * K; e += blockDim.x) {
       int n, m;
       jk_of(e / 3, n, m);
-      const zd v = ldz(a.Mb + (size_t)c * 3 * K + e);
-      Mb[e]      = v;
-      Cn[e]      = m == 0 ? v : zd{0.5 * v.r, 0.5 * v.i};
+      const double2 v  = a.Mb[(size_t)c * 3 * K + e];
+      const double  sc = MIX ? ldexp(a.R0pow[n], -lev * n) : 1.0; // R_c^n
+      const zt      w  = {(T)(v.x * sc), (T)(v.y * sc)};
+      Mb[e]            = w;
+      Cn[e]            = m == 0 ? w : zt{T(0.5) * w.r, T(0.5) * w.i};
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 9 * N1; e += blockDim.x) {
@@ -530,22 +797,22 @@ __global__ void __launch_bounds__(128) k_adj_p2m(AdjDev a)
     __syncthreads();
     for (int t = threadIdx.x; t < nb; t += blockDim.x) {
       const int    b = b0 + t;
-      const double x = B(a, F_X, b) - cxx, y = B(a, F_X + 1, b) - cyy, z = B(a, F_X + 2, b) - czz;
+      const T      x = (T)((B(a, F_X, b) - cxx) * iRc), y = (T)((B(a, F_X + 1, b) - cyy) * iRc), z = (T)((B(a, F_X + 2, b) - czz) * iRc);
       const double al[3] = {B(a, F_A, b), B(a, F_A + 1, b), B(a, F_A + 2, b)};
-      const double r2    = x * x + y * y + z * z;
-      double       ab[3] = {0, 0, 0}, F[9];
+      const T      r2    = x * x + y * y + z * z;
+      T            ab[3] = {T(0), T(0), T(0)}, F[9];
       for (int k = 0; k < 9; k++)
-        F[k] = 0;
-      zd diag{1.0, 0.0};
+        F[k] = T(0);
+      zt diag{T(1), T(0)};
       for (int m = 0; m < P; m++) {
         if (m > 0) {
-          const double s = kHR.s[m];
-          diag           = {(diag.r * x - diag.i * y) * s, (diag.r * y + diag.i * x) * s};
+          const T s = hr.s[m];
+          diag      = {(diag.r * x - diag.i * y) * s, (diag.r * y + diag.i * x) * s};
         }
-        const double wm = m == 0 ? 1.0 : 2.0;
-        zd           ya = diag, yb{0, 0};
-        double       tn = double(2 * m + 1);
-        for (int n = m; n < P; n++, tn += 2.0) {
+        const T wm = m == 0 ? T(1) : T(2);
+        zt      ya = diag, yb{T(0), T(0)};
+        T       tn = T(2 * m + 1);
+        for (int n = m; n < P; n++, tn += T(2)) {
           const int ti = tri(n, m);
           for (int d = 0; d < 3; d++)
             ab[d] += Mb[ti * 3 + d].r * ya.r - Mb[ti * 3 + d].i * ya.i;
@@ -553,17 +820,17 @@ __global__ void __launch_bounds__(128) k_adj_p2m(AdjDev a)
             for (int k = 0; k < 9; k++)
               F[k] += wm * (DM[ti * 9 + k].r * ya.r - DM[ti * 9 + k].i * ya.i);
           if (n + 1 < P) {
-            const double cc = kHR.c[ti], zz = tn * z;
-            const zd     nx = {cc * (zz * ya.r + r2 * yb.r), cc * (zz * ya.i + r2 * yb.i)};
-            yb              = ya;
-            ya              = nx;
+            const T  cc = hr.c[ti], zz = tn * z;
+            const zt nx = {cc * (zz * ya.r + r2 * yb.r), cc * (zz * ya.i + r2 * yb.i)};
+            yb          = ya;
+            ya          = nx;
           }
         }
       }
       for (int d = 0; d < 3; d++)
-        W(a, W_AP2M + d, b) = ab[d];
+        W(a, W_AP2M + d, b) = (double)ab[d];
       for (int ax = 0; ax < 3; ax++)
-        W(a, W_XF + ax, b) += al[0] * F[ax * 3] + al[1] * F[ax * 3 + 1] + al[2] * F[ax * 3 + 2];
+        W(a, W_XF + ax, b) += (al[0] * F[ax * 3] + al[1] * F[ax * 3 + 1] + al[2] * F[ax * 3 + 2]) * iRc;
     }
   }
 }
@@ -1232,59 +1499,82 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
 // M2L^T in FP32 with the mixed forward's scaling (R_s = the source cell's
 // half-width): with S'(d) = R_s^{-(q+1)} S'(d / R_s),
 //   Mbar_s[n] = R_s^{-n} sum_t sum_j Ltil_t[j] conj(S'_{j+n}(d / R_s)),
-//   Ltil_t[j,k] = (-1)^j Lbar_t[j,k] R_s^{-(j+1)},
-// the scaled operands formed in FP64 and rounded once.
+//   Ltil_t[j,k] = (-1)^j Lbar_t[j,k] R_s^{-(j+1)} = Lhat_t[j,k] 2^{-(l_t - l_s)(j+1)},
+//   Lhat_t[j,k] = (-1)^j Lbar_t[j,k] R_t^{-(j+1)},
+// Lhat made once per cell (k_adj_lhat32).  When the target is coarser
+// (l_t < l_s) the factor 2^{-(l_t - l_s)(j+1)} would grow past FP32's range,
+// so that pair uses harmonics at d / R_t instead, with
+//   R_s^{-n} conj(...)  ->  R_s^{-n} 2^{(l_t - l_s) n} sum_j Lhat_t[j] conj(S'_{j+n}(d / R_t)):
+// every rescaling is then by 2^{-k}, k >= 0, exact or a negligible underflow
+// (the MAC keeps |d| >= 2 max(R_s, R_t)).  One warp per source cell.  The outputs (n, m), all three components,
+// are packed onto the lanes by term count ((P-n)(P-n+1)/2 terms each) so that
+// every lane has nearly the same work; a lane walks its outputs' terms in one
+// flattened loop of `iters` steps and adds each finished output into a
+// per-warp accumulator in shared memory, which only it writes.
+__global__ void k_adj_lhat32(const double2 *__restrict__ Lb, float2 *__restrict__ Lh, const int *__restrict__ level, int ncells, int K,
+                             double R0)
+{
+  const long total = (long)ncells * 3 * K;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(e / (3 * K)), r = (int)(e % (3 * K));
+    int       j, k;
+    jk_of(r / 3, j, k);
+    const double  sc = ((j & 1) ? -1.0 : 1.0) * pow(ldexp(R0, -level[c]), -(double)(j + 1)); // (-1)^j R_t^{-(j+1)}
+    const double2 v  = Lb[e];
+    Lh[e]            = make_float2((float)(v.x * sc), (float)(v.y * sc));
+  }
+}
+
 template <int P>
 struct AdjM2L32Sizes {
-  static constexpr int    K = nterms(P), PP = P * P, NE = 3 * PP;
-  static constexpr int    WS = (3 * K + PP > NE) ? 3 * K + PP : NE;
-  static constexpr size_t bytes = (size_t)4 * WS * sizeof(cx<float>);
+  static constexpr int    K = nterms(P), PP = P * P;
+  static constexpr int    WS = 3 * K + PP + 3 * PP; // Lt, S', accumulators (per warp, cx<float>)
+  static constexpr size_t bytes = (size_t)4 * WS * sizeof(cx<float>) + (size_t)3 * K;
 };
 
 template <int P>
-__global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells)
+__global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells, const int2 *__restrict__ table, int nslot, int iters)
 {
   using S = AdjM2L32Sizes<P>;
   typedef cx<float> zf;
-  constexpr int K = S::K, PP = S::PP, NA = (PP + 31) / 32, WS = S::WS;
+  constexpr int K = S::K, PP = S::PP, WS = S::WS;
   extern __shared__ double2 smem_raw[];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  zf       *Lt = reinterpret_cast<zf *>(smem_raw) + w * WS;
-  zf       *Sp = Lt + 3 * K;
-  // a lane owns outputs (n, m) = n^2 + n + m = lane + 32 i, all three components
-  int on[NA], om[NA];
-#pragma unroll
-  for (int i = 0; i < NA; i++) {
-    const int idx = lane + 32 * i;
-    int       n   = 0;
-    while ((n + 1) * (n + 1) <= idx)
-      n++;
-    on[i] = n;
-    om[i] = idx - n * n - n;
+  const int          w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  zf                *Lt   = reinterpret_cast<zf *>(smem_raw) + w * WS;
+  zf                *Sp   = Lt + 3 * K;
+  zf                *Acc  = Sp + PP; // [n^2+n+m][d]
+  unsigned char     *jtab = reinterpret_cast<unsigned char *>(reinterpret_cast<zf *>(smem_raw) + 4 * WS); // degree j of element e
+  for (int e = threadIdx.x; e < 3 * K; e += blockDim.x) {
+    int j, k;
+    jk_of(e / 3, j, k);
+    jtab[e] = (unsigned char)j;
   }
+  __syncthreads();
   for (int s = blockIdx.x * 4 + w; s < ncells; s += gridDim.x * 4) {
-    zf acc[NA][3];
-#pragma unroll
-    for (int i = 0; i < NA; i++)
-#pragma unroll
-      for (int d = 0; d < 3; d++)
-        acc[i][d] = {0.f, 0.f};
+    for (int e = lane; e < 3 * PP; e += 32)
+      Acc[e] = {0.f, 0.f};
     const int    q0 = a.m2lT_start[s], q1 = a.m2lT_start[s + 1];
     const double sx = a.cv.x[s], sy = a.cv.y[s], sz = a.cv.z[s];
     const int    ls = a.cv.level[s];
     const double iRs = ldexp(1.0 / a.R0, ls); // 1 / R_s
     for (int q = q0; q < q1; q++) {
-      const int t = a.m2lT_tgt[q];
+      const int t = a.m2lT_tgt[q], dl = a.cv.level[t] - ls;
       __syncwarp();
-      for (int e = lane; e < 3 * K; e += 32) {
-        int j, k;
-        jk_of(e / 3, j, k);
-        const double2 v  = a.Lb[(size_t)t * 3 * K + e];
-        const double  sc = ((j & 1) ? -1.0 : 1.0) * ldexp(a.iR0pow[j + 1], ls * (j + 1)); // (-1)^j R_s^{-(j+1)}
-        Lt[e]            = {(float)(v.x * sc), (float)(v.y * sc)};
-      }
+      const float2 *src = a.Lhat32 + (size_t)t * 3 * K;
+      if (dl <= 0)
+        for (int e = lane; e < 3 * K; e += 32) {
+          const float2 v = src[e];
+          Lt[e]          = {v.x, v.y};
+        }
+      else
+        for (int e = lane; e < 3 * K; e += 32) {
+          const float2 v  = src[e];
+          const float  sc = ldexpf(1.f, -dl * (jtab[e] + 1));
+          Lt[e]           = {v.x * sc, v.y * sc};
+        }
       if (lane < P) {
-        const float dx = (float)((a.cv.x[t] - sx) * iRs), dy = (float)((a.cv.y[t] - sy) * iRs), dz = (float)((a.cv.z[t] - sz) * iRs);
+        const double iRh = dl < 0 ? ldexp(iRs, dl) : iRs; // 1/R_t for a coarser target, else 1/R_s
+        const float  dx = (float)((a.cv.x[t] - sx) * iRh), dy = (float)((a.cv.y[t] - sy) * iRh), dz = (float)((a.cv.z[t] - sz) * iRh);
         const float r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.f / r2, S00 = sqrtf(ir2);
         zf          col[P];
         singular_column<float, P>(lane, dx, dy, dz, ir2, S00, col);
@@ -1297,43 +1587,54 @@ __global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells)
         }
       }
       __syncwarp();
+      int2 o      = table[lane * nslot];
+      int  n      = o.x, m = o.y, slot = 0, j = 0, k = 0;
+      bool active = n >= 0;
+      zf   acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      for (int it = 0; it < iters; it++) {
+        if (active) {
+          const int qq = j + n;
+          const zf  y  = Sp[qq * qq + qq + m - k];
+          const zf *lp = Lt + tri(j, k) * 3;
 #pragma unroll
-      for (int i = 0; i < NA; i++) {
-        if (lane + 32 * i < PP) {
-          const int n = on[i], m = om[i];
-          for (int j = 0; j <= P - 1 - n; j++) {
-            const int qq = j + n, base = qq * qq + qq + m;
-            for (int k = 0; k <= j; k++) {
-              const zf  y  = Sp[base - k];
-              const zf *lp = Lt + tri(j, k) * 3;
+          for (int d = 0; d < 3; d++) {
+            const zf l = lp[d];
+            acc[d].r   = fmaf(l.r, y.r, fmaf(l.i, y.i, acc[d].r)); // l conj(y)
+            acc[d].i   = fmaf(l.i, y.r, fmaf(-l.r, y.i, acc[d].i));
+          }
+          if (++k > j) {
+            k = 0;
+            if (++j > P - 1 - n) { // output (n, m) complete for this target
+              zf         *ap = Acc + (n * n + n + m) * 3;
+              const float sc = dl < 0 ? ldexpf(1.f, dl * n) : 1.f;
 #pragma unroll
               for (int d = 0; d < 3; d++) {
-                const zf l  = lp[d];
-                acc[i][d].r = fmaf(l.r, y.r, fmaf(l.i, y.i, acc[i][d].r)); // l conj(y)
-                acc[i][d].i = fmaf(l.i, y.r, fmaf(-l.r, y.i, acc[i][d].i));
+                ap[d].r = fmaf(sc, acc[d].r, ap[d].r);
+                ap[d].i = fmaf(sc, acc[d].i, ap[d].i);
+                acc[d]  = {0.f, 0.f};
               }
+              j = 0;
+              if (++slot < nslot) {
+                o      = table[lane * nslot + slot];
+                n      = o.x;
+                m      = o.y;
+                active = n >= 0;
+              } else
+                active = false;
             }
           }
         }
       }
     }
     __syncwarp();
-    zf *Mpb = Lt; // [n^2+n+m][d]
-#pragma unroll
-    for (int i = 0; i < NA; i++)
-      if (lane + 32 * i < PP)
-#pragma unroll
-        for (int d = 0; d < 3; d++)
-          Mpb[(lane + 32 * i) * 3 + d] = acc[i][d];
-    __syncwarp();
     for (int e = lane; e < 3 * K; e += 32) {
       const int d = e % 3;
       int       n, mm;
       jk_of(e / 3, n, mm);
-      const zf v0 = Mpb[(n * n + n + mm) * 3 + d];
+      const zf v0 = Acc[(n * n + n + mm) * 3 + d];
       double   vr = (mm & 1) ? -(double)v0.r : (double)v0.r, vi = (mm & 1) ? -(double)v0.i : (double)v0.i;
       if (mm > 0) {
-        const zf v1 = Mpb[(n * n + n - mm) * 3 + d];
+        const zf v1 = Acc[(n * n + n - mm) * 3 + d];
         vr += v1.r;
         vi -= v1.i;
       }
@@ -1344,45 +1645,117 @@ __global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells)
   }
 }
 
+// Packing of the M2L^T outputs (n, m), n < P, |m| <= n, onto 32 lanes by their
+// term counts (greedy: largest first onto the least loaded lane).  Entry
+// [lane * nslot + slot] = (n, m), or (-1, 0) past the lane's list; iters = the
+// largest lane total.  Made once per order and process on the current device.
+struct M2LTSchedule {
+  int2 *table;
+  int   nslot, iters;
+};
+template <int P>
+const M2LTSchedule &m2lt_schedule()
+{
+  static const M2LTSchedule sched = [] {
+    struct Out {
+      int n, m, cost;
+    };
+    std::vector<Out> outs;
+    for (int n = 0; n < P; n++)
+      for (int m = -n; m <= n; m++)
+        outs.push_back({n, m, (P - n) * (P - n + 1) / 2});
+    std::stable_sort(outs.begin(), outs.end(), [](const Out &x, const Out &y) { return x.cost > y.cost; });
+    std::vector<std::vector<int2>> lanes(32);
+    std::vector<int>               tot(32, 0);
+    for (const Out &o : outs) {
+      int l = 0;
+      for (int i = 1; i < 32; i++)
+        if (tot[i] < tot[l])
+          l = i;
+      lanes[l].push_back(make_int2(o.n, o.m));
+      tot[l] += o.cost;
+    }
+    M2LTSchedule r{};
+    for (int l = 0; l < 32; l++) {
+      r.nslot = std::max(r.nslot, (int)lanes[l].size());
+      r.iters = std::max(r.iters, tot[l]);
+    }
+    std::vector<int2> host(32 * r.nslot, make_int2(-1, 0));
+    for (int l = 0; l < 32; l++)
+      for (size_t i = 0; i < lanes[l].size(); i++)
+        host[l * r.nslot + i] = lanes[l][i];
+    VFMM_CUDA_TRY(cudaMalloc((void **)&r.table, host.size() * sizeof(int2)));
+    VFMM_CUDA_TRY(cudaMemcpy(r.table, host.data(), host.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    return r;
+  }();
+  return sched;
+}
+
 // ------------------------------------------------------------------ host side
 template <int P>
 void eval_adjoint_P(cudaStream_t s, const ExpArgs &e, const AdjDev &d)
 {
   constexpr int K = nterms(P);
   if (e.nleaves > 0) {
-    VFMM_SMEM_ONCE(AdjL2PSizes<P>::bytes, k_adj_l2p<P>);
-    k_adj_l2p<P><<<std::min(e.nleaves, 152 * 8), 128, AdjL2PSizes<P>::bytes, s>>>(d);
+    if (d.pos32) {
+      VFMM_SMEM_ONCE(AdjL2P32Sizes<P>::bytes, k_adj_l2p32<P>);
+      k_adj_l2p32<P><<<std::min(e.nleaves, 152 * 8), 128, AdjL2P32Sizes<P>::bytes, s>>>(d);
+    } else {
+      VFMM_SMEM_ONCE(AdjL2PSizes<P>::bytes, k_adj_l2p<P>);
+      k_adj_l2p<P><<<std::min(e.nleaves, 152 * 8), 128, AdjL2PSizes<P>::bytes, s>>>(d);
+    }
     count_launch();
   }
-  const size_t bl2l = (size_t)(8 * 3 * K + 8 * K) * sizeof(zd);
-  VFMM_SMEM_ONCE(bl2l, k_adj_l2l<P>);
+  const bool   mix  = d.pos32 != nullptr;
+  const size_t bl2l = (size_t)(8 * 3 * K + 8 * K) * (mix ? sizeof(cx<float>) : sizeof(zd));
+  if (mix)
+    VFMM_SMEM_ONCE(bl2l, k_adj_l2l<P, float>);
+  else
+    VFMM_SMEM_ONCE(bl2l, k_adj_l2l<P, double>);
   for (int l = e.maxLevel - 1; l >= 0; l--) { // forward L2L runs parents at levels 0 .. maxLevel-1
     const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
     if (n1 > n0) {
-      k_adj_l2l<P><<<std::min(n1 - n0, 152 * 16), 128, bl2l, s>>>(d, e.level_cells + n0, n1 - n0);
+      if (mix)
+        k_adj_l2l<P, float><<<std::min(n1 - n0, 152 * 16), 128, bl2l, s>>>(d, e.level_cells + n0, n1 - n0);
+      else
+        k_adj_l2l<P, double><<<std::min(n1 - n0, 152 * 16), 128, bl2l, s>>>(d, e.level_cells + n0, n1 - n0);
       count_launch();
     }
   }
   if (d.pos32) {
+    const M2LTSchedule &sc = m2lt_schedule<P>();
+    k_adj_lhat32<<<grid_for((long)e.ncells * 3 * K, 256), 256, 0, s>>>(d.Lb, d.Lhat32, e.cells.level, e.ncells, K, d.R0);
+    count_launch();
     VFMM_SMEM_ONCE(AdjM2L32Sizes<P>::bytes, k_adj_m2l32<P>);
-    k_adj_m2l32<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2L32Sizes<P>::bytes, s>>>(d, e.ncells);
+    k_adj_m2l32<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2L32Sizes<P>::bytes, s>>>(d, e.ncells, sc.table, sc.nslot, sc.iters);
   } else {
     VFMM_SMEM_ONCE(AdjM2LSizes<P>::bytes, k_adj_m2l<P>);
     k_adj_m2l<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2LSizes<P>::bytes, s>>>(d, e.ncells);
   }
   count_launch();
-  const size_t bm2m = (size_t)(3 * K + 8 * K) * sizeof(zd);
-  VFMM_SMEM_ONCE(bm2m, k_adj_m2m<P>);
+  const size_t bm2m = (size_t)(3 * K + 8 * K) * (mix ? sizeof(cx<float>) : sizeof(zd));
+  if (mix)
+    VFMM_SMEM_ONCE(bm2m, k_adj_m2m<P, float>);
+  else
+    VFMM_SMEM_ONCE(bm2m, k_adj_m2m<P, double>);
   for (int l = 1; l <= e.maxLevel - 1; l++) { // forward M2M runs parents at levels maxLevel-1 .. 1
     const int n0 = e.level_start_host[l], n1 = e.level_start_host[l + 1];
     if (n1 > n0) {
-      k_adj_m2m<P><<<std::min(n1 - n0, 152 * 16), 128, bm2m, s>>>(d, e.level_cells + n0, n1 - n0);
+      if (mix)
+        k_adj_m2m<P, float><<<std::min(n1 - n0, 152 * 16), 128, bm2m, s>>>(d, e.level_cells + n0, n1 - n0);
+      else
+        k_adj_m2m<P, double><<<std::min(n1 - n0, 152 * 16), 128, bm2m, s>>>(d, e.level_cells + n0, n1 - n0);
       count_launch();
     }
   }
   if (e.nleaves > 0) {
-    VFMM_SMEM_ONCE(AdjP2MSizes<P>::bytes, k_adj_p2m<P>);
-    k_adj_p2m<P><<<std::min(e.nleaves, 152 * 8), 128, AdjP2MSizes<P>::bytes, s>>>(d);
+    if (mix) {
+      VFMM_SMEM_ONCE((AdjP2MSizes<P, float>::bytes), k_adj_p2m<P, float>);
+      k_adj_p2m<P, float><<<std::min(e.nleaves, 152 * 8), 128, AdjP2MSizes<P, float>::bytes, s>>>(d);
+    } else {
+      VFMM_SMEM_ONCE((AdjP2MSizes<P, double>::bytes), k_adj_p2m<P, double>);
+      k_adj_p2m<P, double><<<std::min(e.nleaves, 152 * 8), 128, AdjP2MSizes<P, double>::bytes, s>>>(d);
+    }
     count_launch();
     if (d.pos32) {
       k_adj_p2p32_tgt<<<std::min(e.nleaves, 152 * 16), 128, 0, s>>>(d);
@@ -1422,6 +1795,7 @@ void adjoint_eval(cudaStream_t s, const ExpArgs &e, const AdjBufs &b, const DevI
   d.pos32      = b.pos32;
   d.alp32      = b.alp32;
   d.seeds32    = b.seeds32;
+  d.Lhat32     = b.Lhat32;
   d.R0         = b.R0;
   if (b.pos32) {
     double p = 1.0, ip = 1.0;

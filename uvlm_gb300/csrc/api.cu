@@ -121,6 +121,7 @@ struct vfmm_handle_s {
     DevBuf<int>                p2pT_start, p2pT_tgt, m2lT_start, m2lT_tgt, orig[2];
     DevBuf<unsigned long long> tkeys, tsorted;
     DevBuf<float4>             seeds32;
+    DevBuf<float2>             Lhat32;
   } adj;
 };
 
@@ -1057,6 +1058,8 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
     b.part       = A.part.p;
     if (mixed) {
       A.seeds32.reserve(4 * (size_t)N);
+      A.Lhat32.reserve(nc * K3);
+      b.Lhat32  = A.Lhat32.p;
       b.pos32   = h->pos32.p;
       b.alp32   = h->alp32.p;
       b.seeds32 = A.seeds32.p;

@@ -270,6 +270,7 @@ struct AdjBufs {
   // scratch (4 float4 per body), the tree's R0; P2P^T and M2L^T then run in FP32
   const float4 *pos32, *alp32;
   float4       *seeds32;
+  float2       *Lhat32; // ncells * 3K
   double        R0;
 };
 constexpr int ADJ_PARTIALS = 152 * 2 * 17;
