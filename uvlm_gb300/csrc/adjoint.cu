@@ -290,22 +290,22 @@ __global__ void __launch_bounds__(128) k_adj_l2p(AdjDev a)
   }
 }
 
-// L2P^T for mixed mode: the per-leaf derivative operators and their
-// transposes stay FP64 (as k_adj_l2p); the per-body work runs in FP32 at the
-// leaf-relative position y = (x - X_c) / R_c, with the coefficients of degree
-// n multiplied by R_c^n (sum c_n Y_n(x - X_c) = sum (c_n R_c^n) Y_n(y)), so
-// the far-field values and their derivatives come out unscaled, and the
-// per-body sums Ubar = sum w ubar conj(Y(x - X_c)) as R_c^n times the FP32
-// sums over Y(y).
+// L2P^T for mixed mode, in FP32 throughout on the leaf-scaled expansion
+// Lhat[j] = L[j] R_c^j: a derivative operator lowers the degree by one, so
+// with coefficients of degree n carried as c_n R_c^n each D becomes D / R_c,
+//   U32 = (1/4pi) curl D(Lhat) / R_c,  JJ32 = D(U32) / R_c,  HH32 = D(JJ32) / R_c,
+// and sum c_n Y_n(x - X_c) = sum (c_n R_c^n) Y_n(y), y = (x - X_c) / R_c, gives the
+// far field and its derivatives unscaled.  Backwards the same holds for the
+// adjoints (Ubar32 = Ubar / R_c^n is the FP32 sum over Y(y)), and only the
+// final Lbar = R_c^j Lhatbar is formed in FP64.
 __device__ __forceinline__ void load_seeds32(const AdjDev &a, int i, float *ub, float *Jb, float *ct); // FP32 seeds, below
 
 template <int P>
 struct AdjL2P32Sizes {
   using S                          = AdjL2PSizes<P>;
   static constexpr int    K        = S::K, K1 = S::K1, K2 = S::K2, K3 = S::K3, NB = S::NB;
-  static constexpr size_t zd_count = 3 * K + 3 * K1 + 9 * K2 + 3 * K1 + 9 * K2 + 3 * K;       // Lc, U, JJ, Ub, JJb, Lb
-  static constexpr size_t zf_count = 3 * K1 + 9 * K2 + 27 * K3 + NB * K1;                   // U32, JJ32, HH32, Ys
-  static constexpr size_t bytes    = zd_count * sizeof(zd) + zf_count * sizeof(cx<float>) + (NB * 12 + K1) * sizeof(float);
+  static constexpr size_t zf_count = 3 * K + 3 * K1 + 9 * K2 + 27 * K3 + 3 * K1 + 9 * K2 + 3 * K + NB * K1; // Lh, U, JJ, HH, Ub, JJb, Lb, Ys
+  static constexpr size_t bytes    = zf_count * sizeof(cx<float>) + (NB * 12 + K1) * sizeof(float);
 };
 
 template <int P>
@@ -316,19 +316,17 @@ __global__ void __launch_bounds__(128) k_adj_l2p32(AdjDev a)
   constexpr int K = S::K, K1 = S::K1, K2 = S::K2, K3 = S::K3, N1 = S::N1, N2 = S::N2, N3 = S::N3, NB = S::NB;
   constexpr int NO = (3 * N1 + 9 * N2 + 127) / 128;
   extern __shared__ double2 smem_raw[];
-  zd    *Lc   = reinterpret_cast<zd *>(smem_raw);
-  zd    *U    = Lc + 3 * K;
-  zd    *JJ   = U + 3 * K1;
-  zd    *Ub   = JJ + 9 * K2;
-  zd    *JJb  = Ub + 3 * K1;
-  zd    *Lb   = JJb + 9 * K2;
-  zf    *U32  = reinterpret_cast<zf *>(Lb + 3 * K);
-  zf    *JJ32 = U32 + 3 * K1;
-  zf    *HH32 = JJ32 + 9 * K2;
-  zf    *Ys   = HH32 + 27 * K3;
-  float *Sd   = reinterpret_cast<float *>(Ys + NB * K1);
-  float *Wt   = Sd + NB * 12;
-  const double inv4pi = 0.25 * kInvPi;
+  zf    *Lh  = reinterpret_cast<zf *>(smem_raw);
+  zf    *U   = Lh + 3 * K;
+  zf    *JJ  = U + 3 * K1;
+  zf    *HH  = JJ + 9 * K2;
+  zf    *Ub  = HH + 27 * K3;
+  zf    *JJb = Ub + 3 * K1;
+  zf    *Lb  = JJb + 9 * K2;
+  zf    *Ys  = Lb + 3 * K;
+  float *Sd  = reinterpret_cast<float *>(Ys + NB * K1);
+  float *Wt  = Sd + NB * 12;
+  const float inv4pi = (float)(0.25 * kInvPi);
   for (int idx = threadIdx.x; idx < N1; idx += 128) {
     int n, m;
     jk_of(idx, n, m);
@@ -338,39 +336,40 @@ __global__ void __launch_bounds__(128) k_adj_l2p32(AdjDev a)
     const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c], lev = a.cv.level[c];
     const double cxx = a.cv.x[c], cyy = a.cv.y[c], czz = a.cv.z[c];
     const double iR  = ldexp(1.0 / a.R0, lev);
+    const float  iRf = (float)iR;
     __syncthreads();
-    for (int e = threadIdx.x; e < 3 * K; e += 128)
-      Lc[e] = ldz(a.L + (size_t)c * 3 * K + e);
+    for (int e = threadIdx.x; e < 3 * K; e += 128) {
+      int j, k;
+      jk_of(e / 3, j, k);
+      const double2 v  = a.L[(size_t)c * 3 * K + e];
+      const double  sc = ldexp(a.R0pow[j], -lev * j); // R_c^j
+      Lh[e]            = {(float)(v.x * sc), (float)(v.y * sc)};
+    }
     __syncthreads();
     for (int e = threadIdx.x; e < 3 * N1; e += 128) {
       const int idx = e / 3, ax = e % 3;
       int       n, mu;
       jk_of(idx, n, mu);
       const int b1 = (ax + 1) % 3, c1 = (ax + 2) % 3;
-      const zd  p = deriv_coef(Lc, n, mu, b1, 3, c1), q = deriv_coef(Lc, n, mu, c1, 3, b1);
-      const zd  u = {inv4pi * (p.r - q.r), inv4pi * (p.i - q.i)};
-      U[idx * 3 + ax]   = u;
-      const double sc   = ldexp(a.R0pow[n], -lev * n);
-      U32[idx * 3 + ax] = {(float)(u.r * sc), (float)(u.i * sc)};
+      const zf  p = deriv_coef(Lh, n, mu, b1, 3, c1), q = deriv_coef(Lh, n, mu, c1, 3, b1);
+      const float sc = inv4pi * iRf;
+      U[idx * 3 + ax] = {sc * (p.r - q.r), sc * (p.i - q.i)};
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 9 * N2; e += 128) {
       const int idx = e / 9, ae = e % 9;
       int       n, mu;
       jk_of(idx, n, mu);
-      const zd v         = deriv_coef(U, n, mu, ae % 3, 3, ae / 3);
-      JJ[idx * 9 + ae]   = v;
-      const double sc    = ldexp(a.R0pow[n], -lev * n);
-      JJ32[idx * 9 + ae] = {(float)(v.r * sc), (float)(v.i * sc)};
+      const zf v       = deriv_coef(U, n, mu, ae % 3, 3, ae / 3);
+      JJ[idx * 9 + ae] = {v.r * iRf, v.i * iRf};
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 27 * N3; e += 128) {
       const int idx = e / 27, r = e % 27;
       int       n, mu;
       jk_of(idx, n, mu);
-      const zd     v  = deriv_coef(JJ, n, mu, r % 3, 9, r / 3);
-      const double sc = ldexp(a.R0pow[n], -lev * n);
-      HH32[idx * 27 + r] = {(float)(v.r * sc), (float)(v.i * sc)};
+      const zf v       = deriv_coef(JJ, n, mu, r % 3, 9, r / 3);
+      HH[idx * 27 + r] = {v.r * iRf, v.i * iRf};
     }
     __syncthreads();
 
@@ -404,15 +403,15 @@ __global__ void __launch_bounds__(128) k_adj_l2p32(AdjDev a)
             const float wm = Wt[idx];
 #pragma unroll
             for (int ax = 0; ax < 3; ax++)
-              f[ax] = fmaf(wm, U32[idx * 3 + ax].r * y.r - U32[idx * 3 + ax].i * y.i, f[ax]);
+              f[ax] = fmaf(wm, U[idx * 3 + ax].r * y.r - U[idx * 3 + ax].i * y.i, f[ax]);
             if (idx < N2)
 #pragma unroll
               for (int ae = 0; ae < 9; ae++)
-                f[3 + ae] = fmaf(wm, JJ32[idx * 9 + ae].r * y.r - JJ32[idx * 9 + ae].i * y.i, f[3 + ae]);
+                f[3 + ae] = fmaf(wm, JJ[idx * 9 + ae].r * y.r - JJ[idx * 9 + ae].i * y.i, f[3 + ae]);
             if (idx < N3)
 #pragma unroll
               for (int r = 0; r < 27; r++)
-                f[12 + r] = fmaf(wm, HH32[idx * 27 + r].r * y.r - HH32[idx * 27 + r].i * y.i, f[12 + r]);
+                f[12 + r] = fmaf(wm, HH[idx * 27 + r].r * y.r - HH[idx * 27 + r].i * y.i, f[12 + r]);
           }
 #pragma unroll
         for (int k = 0; k < 39; k++) {
@@ -422,17 +421,17 @@ __global__ void __launch_bounds__(128) k_adj_l2p32(AdjDev a)
         if (t < nbc && part == 0) {
           const int    b  = b0 + c0 + t;
           const float *sd = Sd + t * 12;
-          double       e  = 0;
+          float        e  = 0.f;
           for (int ax = 0; ax < 3; ax++)
-            e -= 2.0 * sd[ax] * f[ax];
+            e -= 2.f * sd[ax] * f[ax];
           for (int ae = 0; ae < 9; ae++)
-            e -= 3.0 * sd[3 + ae] * f[3 + ae];
+            e -= 3.f * sd[3 + ae] * f[3 + ae];
           for (int g = 0; g < 3; g++) {
-            double xb = 0;
+            float xb = 0.f;
             for (int ax = 0; ax < 3; ax++)
-              xb += (double)sd[ax] * f[3 + ax * 3 + g];
+              xb = fmaf(sd[ax], f[3 + ax * 3 + g], xb);
             for (int ae = 0; ae < 9; ae++)
-              xb += (double)sd[3 + ae] * f[12 + ae * 3 + g];
+              xb = fmaf(sd[3 + ae], f[12 + ae * 3 + g], xb);
             W(a, W_XF + g, b) = xb;
           }
           W(a, W_EF, b) = e;
@@ -464,48 +463,48 @@ __global__ void __launch_bounds__(128) k_adj_l2p32(AdjDev a)
       }
       __syncthreads();
     }
-    // Ubar, JJbar = R_c^n times the FP32 sums (FP64 from here on)
 #pragma unroll
     for (int i = 0; i < NO; i++) {
       const int o = threadIdx.x + 128 * i;
-      if (o < 3 * N1 + 9 * N2) {
-        const int idx = o < 3 * N1 ? o / 3 : (o - 3 * N1) / 9;
-        int       n, m;
-        jk_of(idx, n, m);
-        const double sc = ldexp(a.R0pow[n], -lev * n);
-        const zd     v  = {(double)acc[i].r * sc, (double)acc[i].i * sc};
-        if (o < 3 * N1)
-          Ub[o] = v;
-        else
-          JJb[o - 3 * N1] = v;
-      }
+      if (o < 3 * N1)
+        Ub[o] = acc[i];
+      else if (o < 3 * N1 + 9 * N2)
+        JJb[o - 3 * N1] = acc[i];
     }
     for (int e = threadIdx.x; e < 3 * K; e += 128)
-      Lb[e] = {0, 0};
+      Lb[e] = {0.f, 0.f};
     __syncthreads();
+    // JJ32 = D(U32) / R_c, transposed: one thread per component (fixed order)
     if (threadIdx.x < 3) {
       const int ax = threadIdx.x;
       for (int idx = 0; idx < N2; idx++) {
         int n, mu;
         jk_of(idx, n, mu);
-        for (int ex = 0; ex < 3; ex++)
-          deriv_coef_adj(Ub, n, mu, ex, 3, ax, JJb[idx * 9 + ax * 3 + ex]);
+        for (int ex = 0; ex < 3; ex++) {
+          const zf v = JJb[idx * 9 + ax * 3 + ex];
+          deriv_coef_adj(Ub, n, mu, ex, 3, ax, zf{v.r * iRf, v.i * iRf});
+        }
       }
     }
     __syncthreads();
     if (threadIdx.x < 3) {
-      const int cc = threadIdx.x;
+      const int   cc = threadIdx.x;
+      const float sc = inv4pi * iRf;
       for (int idx = 0; idx < N1; idx++) {
         int n, mu;
         jk_of(idx, n, mu);
-        const zd u1 = Ub[idx * 3 + (cc + 1) % 3], u2 = Ub[idx * 3 + (cc + 2) % 3];
-        deriv_coef_adj(Lb, n, mu, (cc + 2) % 3, 3, cc, zd{inv4pi * u1.r, inv4pi * u1.i});
-        deriv_coef_adj(Lb, n, mu, (cc + 1) % 3, 3, cc, zd{-inv4pi * u2.r, -inv4pi * u2.i});
+        const zf u1 = Ub[idx * 3 + (cc + 1) % 3], u2 = Ub[idx * 3 + (cc + 2) % 3];
+        deriv_coef_adj(Lb, n, mu, (cc + 2) % 3, 3, cc, zf{sc * u1.r, sc * u1.i});
+        deriv_coef_adj(Lb, n, mu, (cc + 1) % 3, 3, cc, zf{-sc * u2.r, -sc * u2.i});
       }
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < 3 * K; e += 128)
-      stz(a.Lb + (size_t)c * 3 * K + e, Lb[e]);
+    for (int e = threadIdx.x; e < 3 * K; e += 128) {
+      int j, k;
+      jk_of(e / 3, j, k);
+      const double sc = ldexp(a.R0pow[j], -lev * j); // Lbar = R_c^j Lhatbar
+      a.Lb[(size_t)c * 3 * K + e] = make_double2((double)Lb[e].r * sc, (double)Lb[e].i * sc);
+    }
   }
 }
 
@@ -1525,25 +1524,103 @@ __global__ void k_adj_lhat32(const double2 *__restrict__ Lb, float2 *__restrict_
   }
 }
 
+// Pieces of the M2L^T work, one schedule per order P and process: output
+// (n, m) has (P-n)(P-n+1)/2 terms (j <= P-1-n, k <= j, in that order); an
+// output longer than the mean lane load is cut into near-equal runs, and the
+// pieces are packed largest first onto the least loaded of 32 lanes.
+// table[lane * nslot + slot] = {n | (m + 16) << 8, j0 | k0 << 8, length,
+// piece id} (length 0 past a lane's list); the pieces of output
+// o = n^2 + n + m have ids pstart[o] .. pstart[o + 1] - 1; iters = the largest
+// lane load.  Made on the device current at first use.
+struct M2LTSchedule {
+  int4 *table;
+  int  *pstart;
+  int   nslot, iters, npieces;
+};
+template <int P>
+const M2LTSchedule &m2lt_schedule()
+{
+  static const M2LTSchedule sched = [] {
+    struct Piece {
+      int n, m, j0, k0, len, id;
+    };
+    int total = 0;
+    for (int n = 0; n < P; n++)
+      total += (2 * n + 1) * (P - n) * (P - n + 1) / 2;
+    const int          target = (total + 31) / 32;
+    std::vector<Piece> pieces;
+    std::vector<int>   pstart(P * P + 1, 0);
+    for (int n = 0; n < P; n++)
+      for (int m = -n; m <= n; m++) {
+        const int T  = (P - n) * (P - n + 1) / 2;
+        const int np = (T + target - 1) / target;
+        pstart[n * n + n + m] = (int)pieces.size();
+        int f = 0;
+        for (int q = 0; q < np; q++) {
+          const int len = T / np + (q < T % np ? 1 : 0);
+          int       j = 0, k = f;
+          while (k > j) { // flattened index f -> (j, k)
+            k -= j + 1;
+            j++;
+          }
+          pieces.push_back({n, m, j, k, len, (int)pieces.size()});
+          f += len;
+        }
+      }
+    pstart[P * P] = (int)pieces.size();
+    std::vector<Piece> order = pieces;
+    std::stable_sort(order.begin(), order.end(), [](const Piece &x, const Piece &y) { return x.len > y.len; });
+    std::vector<std::vector<Piece>> lanes(32);
+    std::vector<int>                load(32, 0);
+    for (const Piece &pc : order) {
+      int l = 0;
+      for (int i = 1; i < 32; i++)
+        if (load[i] < load[l])
+          l = i;
+      lanes[l].push_back(pc);
+      load[l] += pc.len;
+    }
+    M2LTSchedule r{};
+    r.npieces = (int)pieces.size();
+    for (int l = 0; l < 32; l++) {
+      r.nslot = std::max(r.nslot, (int)lanes[l].size());
+      r.iters = std::max(r.iters, load[l]);
+    }
+    std::vector<int4> host(32 * r.nslot, make_int4(0, 0, 0, 0));
+    for (int l = 0; l < 32; l++)
+      for (size_t i = 0; i < lanes[l].size(); i++) {
+        const Piece &pc       = lanes[l][i];
+        host[l * r.nslot + i] = make_int4(pc.n | ((pc.m + 16) << 8), pc.j0 | (pc.k0 << 8), pc.len, pc.id);
+      }
+    VFMM_CUDA_TRY(cudaMalloc((void **)&r.table, host.size() * sizeof(int4)));
+    VFMM_CUDA_TRY(cudaMemcpy(r.table, host.data(), host.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    VFMM_CUDA_TRY(cudaMalloc((void **)&r.pstart, pstart.size() * sizeof(int)));
+    VFMM_CUDA_TRY(cudaMemcpy(r.pstart, pstart.data(), pstart.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return r;
+  }();
+  return sched;
+}
+
 template <int P>
 struct AdjM2L32Sizes {
-  static constexpr int    K = nterms(P), PP = P * P;
-  static constexpr int    WS = 3 * K + PP + 3 * PP; // Lt, S', accumulators (per warp, cx<float>)
-  static constexpr size_t bytes = (size_t)4 * WS * sizeof(cx<float>) + (size_t)3 * K;
+  static constexpr int K = nterms(P), PP = P * P;
+  // per warp: Lt (3K), S' (PP), piece accumulators (3 per piece); plus the degree table
+  static size_t bytes(int npieces) { return (size_t)4 * (3 * K + PP + 3 * npieces) * sizeof(cx<float>) + (size_t)3 * K; }
 };
 
 template <int P>
-__global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells, const int2 *__restrict__ table, int nslot, int iters)
+__global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells, const int4 *__restrict__ table, const int *__restrict__ pstart, int nslot,
+                                                  int iters, int npieces)
 {
-  using S = AdjM2L32Sizes<P>;
   typedef cx<float> zf;
-  constexpr int K = S::K, PP = S::PP, WS = S::WS;
+  constexpr int K = nterms(P), PP = P * P;
   extern __shared__ double2 smem_raw[];
-  const int          w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  zf                *Lt   = reinterpret_cast<zf *>(smem_raw) + w * WS;
-  zf                *Sp   = Lt + 3 * K;
-  zf                *Acc  = Sp + PP; // [n^2+n+m][d]
-  unsigned char     *jtab = reinterpret_cast<unsigned char *>(reinterpret_cast<zf *>(smem_raw) + 4 * WS); // degree j of element e
+  const int      WS   = 3 * K + PP + 3 * npieces;
+  const int      w    = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  zf            *Lt   = reinterpret_cast<zf *>(smem_raw) + w * WS;
+  zf            *Sp   = Lt + 3 * K;
+  zf            *Pa   = Sp + PP; // [piece][d]
+  unsigned char *jtab = reinterpret_cast<unsigned char *>(reinterpret_cast<zf *>(smem_raw) + 4 * WS); // degree j of element e
   for (int e = threadIdx.x; e < 3 * K; e += blockDim.x) {
     int j, k;
     jk_of(e / 3, j, k);
@@ -1551,8 +1628,8 @@ __global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells, const i
   }
   __syncthreads();
   for (int s = blockIdx.x * 4 + w; s < ncells; s += gridDim.x * 4) {
-    for (int e = lane; e < 3 * PP; e += 32)
-      Acc[e] = {0.f, 0.f};
+    for (int e = lane; e < 3 * npieces; e += 32)
+      Pa[e] = {0.f, 0.f};
     const int    q0 = a.m2lT_start[s], q1 = a.m2lT_start[s + 1];
     const double sx = a.cv.x[s], sy = a.cv.y[s], sz = a.cv.z[s];
     const int    ls = a.cv.level[s];
@@ -1575,8 +1652,8 @@ __global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells, const i
       if (lane < P) {
         const double iRh = dl < 0 ? ldexp(iRs, dl) : iRs; // 1/R_t for a coarser target, else 1/R_s
         const float  dx = (float)((a.cv.x[t] - sx) * iRh), dy = (float)((a.cv.y[t] - sy) * iRh), dz = (float)((a.cv.z[t] - sz) * iRh);
-        const float r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.f / r2, S00 = sqrtf(ir2);
-        zf          col[P];
+        const float  r2 = dx * dx + dy * dy + dz * dz, ir2 = 1.f / r2, S00 = sqrtf(ir2);
+        zf           col[P];
         singular_column<float, P>(lane, dx, dy, dz, ir2, S00, col);
         const int m = lane;
         for (int n = m; n < P; n++) {
@@ -1587,12 +1664,12 @@ __global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells, const i
         }
       }
       __syncwarp();
-      int2 o      = table[lane * nslot];
-      int  n      = o.x, m = o.y, slot = 0, j = 0, k = 0;
-      bool active = n >= 0;
+      int  slot = 0;
+      int4 pc   = table[lane * nslot];
+      int  n = pc.x & 255, m = (pc.x >> 8) - 16, j = pc.y & 255, k = pc.y >> 8, left = pc.z;
       zf   acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
       for (int it = 0; it < iters; it++) {
-        if (active) {
+        if (left > 0) {
           const int qq = j + n;
           const zf  y  = Sp[qq * qq + qq + m - k];
           const zf *lp = Lt + tri(j, k) * 3;
@@ -1604,23 +1681,24 @@ __global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells, const i
           }
           if (++k > j) {
             k = 0;
-            if (++j > P - 1 - n) { // output (n, m) complete for this target
-              zf         *ap = Acc + (n * n + n + m) * 3;
-              const float sc = dl < 0 ? ldexpf(1.f, dl * n) : 1.f;
+            j++;
+          }
+          if (--left == 0) { // piece complete for this target
+            zf         *ap = Pa + pc.w * 3;
+            const float sc = dl < 0 ? ldexpf(1.f, dl * n) : 1.f;
 #pragma unroll
-              for (int d = 0; d < 3; d++) {
-                ap[d].r = fmaf(sc, acc[d].r, ap[d].r);
-                ap[d].i = fmaf(sc, acc[d].i, ap[d].i);
-                acc[d]  = {0.f, 0.f};
-              }
-              j = 0;
-              if (++slot < nslot) {
-                o      = table[lane * nslot + slot];
-                n      = o.x;
-                m      = o.y;
-                active = n >= 0;
-              } else
-                active = false;
+            for (int d = 0; d < 3; d++) {
+              ap[d].r = fmaf(sc, acc[d].r, ap[d].r);
+              ap[d].i = fmaf(sc, acc[d].i, ap[d].i);
+              acc[d]  = {0.f, 0.f};
+            }
+            if (++slot < nslot) {
+              pc   = table[lane * nslot + slot];
+              n    = pc.x & 255;
+              m    = (pc.x >> 8) - 16;
+              j    = pc.y & 255;
+              k    = pc.y >> 8;
+              left = pc.z;
             }
           }
         }
@@ -1631,64 +1709,26 @@ __global__ void __launch_bounds__(128) k_adj_m2l32(AdjDev a, int ncells, const i
       const int d = e % 3;
       int       n, mm;
       jk_of(e / 3, n, mm);
-      const zf v0 = Acc[(n * n + n + mm) * 3 + d];
-      double   vr = (mm & 1) ? -(double)v0.r : (double)v0.r, vi = (mm & 1) ? -(double)v0.i : (double)v0.i;
+      const int o0 = n * n + n + mm, o1 = n * n + n - mm;
+      float     ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
+      for (int pid = pstart[o0]; pid < pstart[o0 + 1]; pid++) {
+        ar += Pa[pid * 3 + d].r;
+        ai += Pa[pid * 3 + d].i;
+      }
+      double vr = (mm & 1) ? -(double)ar : (double)ar, vi = (mm & 1) ? -(double)ai : (double)ai;
       if (mm > 0) {
-        const zf v1 = Acc[(n * n + n - mm) * 3 + d];
-        vr += v1.r;
-        vi -= v1.i;
+        for (int pid = pstart[o1]; pid < pstart[o1 + 1]; pid++) {
+          br += Pa[pid * 3 + d].r;
+          bi += Pa[pid * 3 + d].i;
+        }
+        vr += br;
+        vi -= bi;
       }
       const double sc = ldexp(a.iR0pow[n], ls * n); // R_s^{-n}
       a.Mb[(size_t)s * 3 * K + e] = make_double2(vr * sc, vi * sc);
     }
     __syncwarp();
   }
-}
-
-// Packing of the M2L^T outputs (n, m), n < P, |m| <= n, onto 32 lanes by their
-// term counts (greedy: largest first onto the least loaded lane).  Entry
-// [lane * nslot + slot] = (n, m), or (-1, 0) past the lane's list; iters = the
-// largest lane total.  Made once per order and process on the current device.
-struct M2LTSchedule {
-  int2 *table;
-  int   nslot, iters;
-};
-template <int P>
-const M2LTSchedule &m2lt_schedule()
-{
-  static const M2LTSchedule sched = [] {
-    struct Out {
-      int n, m, cost;
-    };
-    std::vector<Out> outs;
-    for (int n = 0; n < P; n++)
-      for (int m = -n; m <= n; m++)
-        outs.push_back({n, m, (P - n) * (P - n + 1) / 2});
-    std::stable_sort(outs.begin(), outs.end(), [](const Out &x, const Out &y) { return x.cost > y.cost; });
-    std::vector<std::vector<int2>> lanes(32);
-    std::vector<int>               tot(32, 0);
-    for (const Out &o : outs) {
-      int l = 0;
-      for (int i = 1; i < 32; i++)
-        if (tot[i] < tot[l])
-          l = i;
-      lanes[l].push_back(make_int2(o.n, o.m));
-      tot[l] += o.cost;
-    }
-    M2LTSchedule r{};
-    for (int l = 0; l < 32; l++) {
-      r.nslot = std::max(r.nslot, (int)lanes[l].size());
-      r.iters = std::max(r.iters, tot[l]);
-    }
-    std::vector<int2> host(32 * r.nslot, make_int2(-1, 0));
-    for (int l = 0; l < 32; l++)
-      for (size_t i = 0; i < lanes[l].size(); i++)
-        host[l * r.nslot + i] = lanes[l][i];
-    VFMM_CUDA_TRY(cudaMalloc((void **)&r.table, host.size() * sizeof(int2)));
-    VFMM_CUDA_TRY(cudaMemcpy(r.table, host.data(), host.size() * sizeof(int2), cudaMemcpyHostToDevice));
-    return r;
-  }();
-  return sched;
 }
 
 // ------------------------------------------------------------------ host side
@@ -1723,11 +1763,12 @@ void eval_adjoint_P(cudaStream_t s, const ExpArgs &e, const AdjDev &d)
     }
   }
   if (d.pos32) {
-    const M2LTSchedule &sc = m2lt_schedule<P>();
+    const M2LTSchedule &sc    = m2lt_schedule<P>();
+    const size_t        bytes = AdjM2L32Sizes<P>::bytes(sc.npieces);
     k_adj_lhat32<<<grid_for((long)e.ncells * 3 * K, 256), 256, 0, s>>>(d.Lb, d.Lhat32, e.cells.level, e.ncells, K, d.R0);
     count_launch();
-    VFMM_SMEM_ONCE(AdjM2L32Sizes<P>::bytes, k_adj_m2l32<P>);
-    k_adj_m2l32<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2L32Sizes<P>::bytes, s>>>(d, e.ncells, sc.table, sc.nslot, sc.iters);
+    VFMM_SMEM_ONCE(bytes, k_adj_m2l32<P>);
+    k_adj_m2l32<P><<<grid_for(e.ncells, 4, 152 * 16), 128, bytes, s>>>(d, e.ncells, sc.table, sc.pstart, sc.nslot, sc.iters, sc.npieces);
   } else {
     VFMM_SMEM_ONCE(AdjM2LSizes<P>::bytes, k_adj_m2l<P>);
     k_adj_m2l<P><<<grid_for(e.ncells, 4, 152 * 16), 128, AdjM2LSizes<P>::bytes, s>>>(d, e.ncells);
