@@ -173,3 +173,29 @@ def test_mixed_evaluation_gradient_close_to_fp64(vfmm_lib):
     for k in (1, 2):
         a, r = res["mixed"][k], res["fp64"][k]
         assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_adjoint_edge_cases(vfmm_lib, precision):
+    """One body (no pairs, a root leaf), two bodies, and a cloud with coincident
+    bodies (pairs at zero distance are skipped, as in the forward)."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    one = workloads.cloud(1, seed=40)
+    two = workloads.cloud(2, seed=41)
+    dup = workloads.cloud(600, seed=42)
+    dup[300:]["X"] = dup[:300]["X"]
+    for b in (one, two, dup):
+        with FMMCalculator(p=6, ncrit=16, theta=0.47, integration="RK2", precision=precision) as c:
+            v, gx, ga = c.adjoint(b, 0.01, 2, 1)
+            assert np.isfinite(v) and np.isfinite(gx).all() and np.isfinite(ga).all()
+            if b.size == 1:
+                # one body: u = 0, so only the impulse term 1/2 (x cross alpha)_z acts and nothing moves
+                x, al = b["X"][0], b["alpha"][0]
+                assert v == pytest.approx(0.5 * (x[0] * al[1] - x[1] * al[0]), rel=1e-14)
+                assert np.allclose(gx[0], [0.5 * al[1], -0.5 * al[0], 0.0], rtol=1e-14, atol=0)
+                assert np.allclose(ga[0], [-0.5 * x[1], 0.5 * x[0], 0.0], rtol=1e-14, atol=0)
+            elif precision == "fp64" and b.size == 2:
+                # (coincident bodies are a jump of the forward map itself: a pair's J term
+                # tends to a nonzero limit as the distance goes to 0 but is skipped at 0)
+                _, _, _, errs = fd_check(c, b, 0.01, 2, nd=2, h=1e-7, seed=3)
+                assert worst(errs) < 1e-5, errs

@@ -36,3 +36,19 @@ def test_list_overflow_retry_matches_fresh_handle(vfmm_lib, precision):
         assert np.array_equal(a, b)
     for fld in ["X", "velocity", "J", "dadt"]:
         assert np.array_equal(out[fld], ref[fld]), fld
+
+
+def test_mixed_mode_degenerate_bounding_box(vfmm_lib):
+    """One body, or every body at one point: the bounding box has R0 = 0 and the
+    tree is a single root leaf.  The mixed kernels' scaling length must stay
+    positive (it once became 1/0); the step leaves the bodies where they are."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    for n in (1, 5):
+        b = workloads.cloud(n, seed=50)
+        b["X"] = b["X"][0]
+        for prec in ("fp64", "mixed"):
+            bb = b.copy()
+            with FMMCalculator(p=8, ncrit=16, theta=0.5, integration="RK2", precision=prec) as c:
+                c.advance(bb, 0.01)
+            assert np.isfinite(bb["velocity"]).all() and np.isfinite(bb["J"]).all()
+            assert np.array_equal(bb["X"], b["X"]) and np.array_equal(bb["alpha"], b["alpha"])

@@ -427,7 +427,9 @@ void calculate(vfmm_handle h)
     m.items32 = h->items32.p;
     m.lanes32   = h->lanes32.p;
     m.m2l_batch = h->m2l_batch;
-    m.R0      = h->tree.R0;
+    // the FP32 kernels' scaling length: any positive value is exact; R0 = 0
+    // (every body at one point, a single root leaf without far field) uses 1
+    m.R0      = h->tree.R0 > 0 ? h->tree.R0 : 1.0;
     p2m_mixed(s, e, m);
     m2m_mixed(s, e, m);
     VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
@@ -1063,7 +1065,7 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
       b.pos32   = h->pos32.p;
       b.alp32   = h->alp32.p;
       b.seeds32 = A.seeds32.p;
-      b.R0      = h->tree.R0;
+      b.R0      = h->tree.R0 > 0 ? h->tree.R0 : 1.0; // as calculate's scaling length
     }
     adjoint_eval(s, particle_args(h), b, h->info);
     adjoint_scatter(s, A.g[gc].p, A.g[gc ^ 1].p, cap, N, h->ts.perm.p);
