@@ -184,11 +184,13 @@ typedef struct vfmm_objective {
  * pairs, transposed L2P, L2L, M2L, M2M, P2M, the bounding-box dependence of
  * the cell centres) and of the stage updates, at the states of the forward
  * trajectory, all in the handle's precision: FP64 (the exact derivative of
- * the FP64 step) or mixed (the forward kernels, P2P^T and M2L^T in FP32, the
- * other transposes in FP64).  States
- * are kept every `checkpoint_every` steps and the steps in between are
- * recomputed, so device memory holds ceil(steps / checkpoint_every) + stages
- * x checkpoint_every body states.  With grad_x and grad_alpha both NULL only
+ * the FP64 step) or mixed (the forward kernels and the transposes in FP32
+ * with per-cell scaling).  States are kept every `checkpoint_every` steps;
+ * each segment between them is recomputed once, keeping every stage's
+ * evaluation (tree, lists, local expansions, body fields: roughly 450 bytes
+ * per body at p = 8), and then run backwards, so device memory holds
+ * ceil(steps / checkpoint_every) body states plus stages x checkpoint_every
+ * stage evaluations.  With grad_x and grad_alpha both NULL only
  * *value is computed.  Covers Euler, RK2 and RK3 with the cVPM formulation,
  * no viscosity and no relaxation (VFMM_ERR_UNSUPPORTED otherwise).  The
  * reference has no adjoint; its L2P takes one derivative by complex step

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <atomic>
 #include <thread>
+#include <type_traits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -113,15 +114,31 @@ struct vfmm_handle_s {
   bool                  has_tree = false, has_eval = false;
 
   // reverse mode (vfmm_adjoint): adjoint state (ping-pong for the reorders),
-  // work fields, adjoint expansions, lists by source, checkpoints, the states
-  // of one recomputed segment, caller index of each body, seeds
+  // work fields, adjoint expansions, lists by source, checkpoints, caller
+  // index of each body, seeds
   struct {
-    DevBuf<double>             g[2], w, ckpt, tape, seedx, seeda, part, rows, value;
+    DevBuf<double>             g[2], w, ckpt, seedx, seeda, part, rows, value;
     DevBuf<double2>            Mb, Lb;
     DevBuf<int>                p2pT_start, p2pT_tgt, m2lT_start, m2lT_tgt, orig[2];
     DevBuf<unsigned long long> tkeys, tsorted;
     DevBuf<float4>             seeds32;
     DevBuf<float2>             Lhat32;
+    // one recomputed segment's stage evaluations, swapped into the handle
+    // for the reverse sweep: tree, lists (CSR and sorted keys), local
+    // expansions, FP32 body records, tree permutation, the bodies' J, X,
+    // alpha and radius in tree order, and the tree's bounding box (DevInfo)
+    struct Ctx {
+      Tree                       tree;
+      DevBuf<int>                p2p_start, p2p_src, m2l_start, m2l_src;
+      DevBuf<unsigned long long> p2p_sorted, m2l_sorted;
+      int                        n_p2p = 0, n_m2l = 0, key_bits = 0;
+      DevBuf<double2>            L;
+      DevBuf<float4>             pos32, alp32;
+      DevBuf<uint32_t>           perm;
+      DevBuf<double>             body;
+      DevBuf<DevInfo>            info;
+    };
+    std::vector<Ctx> ctx;
   } adj;
 };
 
@@ -1035,7 +1052,7 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
   // vjp of the evaluation just made (tree, lists, FP64 expansions current;
   // seeds in A.w; adjoint state in tree order), then back to the order the
   // bodies had before this tree
-  auto vjp = [&]() {
+  auto vjp = [&](const DevInfo *info) {
     const int    np = h->lists.n_p2p, nm = h->lists.n_m2l, nc = h->tree.ncells;
     const size_t K3 = 3 * (size_t)(c.p * (c.p + 1) / 2);
     A.p2pT_start.reserve(nc + 1);
@@ -1067,30 +1084,62 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
       b.seeds32 = A.seeds32.p;
       b.R0      = h->tree.R0 > 0 ? h->tree.R0 : 1.0; // as calculate's scaling length
     }
-    adjoint_eval(s, particle_args(h), b, h->info);
+    adjoint_eval(s, particle_args(h), b, info);
     adjoint_scatter(s, A.g[gc].p, A.g[gc ^ 1].p, cap, N, h->ts.perm.p);
     gc ^= 1;
   };
-  vjp();
+  vjp(h->info);
+  // The evaluation context of a stage (everything the transposes read) is
+  // exchanged between the handle and a segment slot: buffers swap owners,
+  // the body fields and the bounding box are copied.
+  using Ctx = std::remove_reference_t<decltype(A)>::Ctx;
+  A.ctx.resize((size_t)every * S);
+  auto exchange = [&](Ctx &x) {
+    std::swap(h->tree, x.tree);
+    std::swap(h->lists.p2p_start, x.p2p_start);
+    std::swap(h->lists.p2p_src, x.p2p_src);
+    std::swap(h->lists.m2l_start, x.m2l_start);
+    std::swap(h->lists.m2l_src, x.m2l_src);
+    std::swap(h->lists.ls.p2p_sorted, x.p2p_sorted);
+    std::swap(h->lists.ls.m2l_sorted, x.m2l_sorted);
+    std::swap(h->lists.n_p2p, x.n_p2p);
+    std::swap(h->lists.n_m2l, x.n_m2l);
+    std::swap(h->lists.ls.key_bits, x.key_bits);
+    std::swap(h->L, x.L);
+    std::swap(h->pos32, x.pos32);
+    std::swap(h->alp32, x.alp32);
+    std::swap(h->ts.perm, x.perm);
+  };
+  const size_t nbody_fields = (size_t)(F_A + 3) * cap; // J, X, alpha: fields 0 .. F_A+2
   // reverse sweep: per segment, recompute its steps from the checkpoint
-  // keeping every stage's input state, then run the stages backwards
-  A.tape.reserve((size_t)every * S * slot);
+  // keeping every stage's evaluation context, then run the stages backwards
   for (int seg = nck - 1; seg >= 0; seg--) {
     const int st0 = seg * every, st1 = std::min(steps, st0 + every);
     load_state(h, A.ckpt.p + (size_t)seg * slot);
     for (int st = st0; st < st1; st++)
       for (int k = 0; k < S; k++) {
-        save_state(h, A.tape.p + (size_t)((st - st0) * S + k) * slot);
-        run_stage(h, k, dt);
+        Ctx &x = A.ctx[(size_t)(st - st0) * S + k];
+        build_tree_and_lists(h);
+        calculate(h);
+        x.body.reserve(nbody_fields + cap);
+        x.info.reserve(1);
+        VFMM_CUDA_TRY(cudaMemcpyAsync(x.body.p, h->soa[h->cur].p, nbody_fields * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        VFMM_CUDA_TRY(cudaMemcpyAsync(x.body.p + nbody_fields, h->soa[h->cur].p + (size_t)F_R * cap, cap * sizeof(double),
+                                      cudaMemcpyDeviceToDevice, s));
+        VFMM_CUDA_TRY(cudaMemcpyAsync(x.info.p, h->info, sizeof(DevInfo), cudaMemcpyDeviceToDevice, s));
+        exchange(x);
+        stage_update(h, k, dt);
       }
     for (int st = st1 - 1; st >= st0; st--)
       for (int k = S - 1; k >= 0; k--) {
-        load_state(h, A.tape.p + (size_t)((st - st0) * S + k) * slot);
-        build_tree_and_lists(h);
-        calculate(h);
+        Ctx &x = A.ctx[(size_t)(st - st0) * S + k];
+        exchange(x);
+        VFMM_CUDA_TRY(cudaMemcpyAsync(h->soa[h->cur].p, x.body.p, nbody_fields * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        VFMM_CUDA_TRY(cudaMemcpyAsync(h->soa[h->cur].p + (size_t)F_R * cap, x.body.p + nbody_fields, cap * sizeof(double),
+                                      cudaMemcpyDeviceToDevice, s));
         adjoint_stage_pre(s, A.g[gc].p, A.w.p, cap, N, c.integrator, k, dt);
         adjoint_seeds(s, h->soa[h->cur].p, A.w.p, cap, N, c.stretching);
-        vjp();
+        vjp(x.info.p);
       }
   }
   A.rows.reserve(3 * (size_t)N);
