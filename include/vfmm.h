@@ -274,7 +274,9 @@ int vfmm_phase_times(vfmm_handle h, float *ms, int n);
 /* Sizes of the last tree: cells, leaves, P2P pairs, M2L pairs, P2P body-body
  * interactions (self pairs excluded), max level. */
 int vfmm_tree_stats(vfmm_handle h, uint64_t *stats, int n);
-/* Page-lock a host range for fast copies (cudaHostRegister). */
+/* Page-lock and map a host range (cudaHostRegister, mapped).  Calls given
+ * bodies that lie wholly in such a range read and write them directly from
+ * the transposing kernels over the host link, with no staging copy. */
 int vfmm_host_register(void *ptr, size_t bytes);
 int vfmm_host_unregister(void *ptr);
 /* Fill a device scratch buffer larger than L2 to evict cached data. */

@@ -225,19 +225,48 @@ void ensure_bodies(vfmm_handle h, size_t n)
   h->n = (int)n;
 }
 
+// The device address of `bytes` of host memory at p when all of it is pinned
+// and mapped (vfmm_host_register), else null: both ends must resolve to one
+// contiguous mapping.
+void *mapped_host(const void *p, size_t bytes)
+{
+  cudaPointerAttributes a{}, z{};
+  const char           *q = static_cast<const char *>(p);
+  if (cudaPointerGetAttributes(&a, q) != cudaSuccess || cudaPointerGetAttributes(&z, q + bytes - 1) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || z.type != cudaMemoryTypeHost || !a.devicePointer || !z.devicePointer)
+    return nullptr;
+  if (static_cast<char *>(z.devicePointer) - static_cast<char *>(a.devicePointer) != (ptrdiff_t)(bytes - 1))
+    return nullptr;
+  return a.devicePointer;
+}
+
+// Bodies in: from pinned, mapped host memory the transposing kernel reads the
+// records directly over the host link (one pass); otherwise a copy to the
+// device staging buffer first.
 void upload(vfmm_handle h, const vfmm_body *b, size_t n)
 {
   ensure_bodies(h, n);
-  VFMM_CUDA_TRY(cudaMemcpyAsync(h->aos.p, b, n * sizeof(vfmm_body), cudaMemcpyHostToDevice, h->stream));
-  aos_to_soa(h->stream, h->aos.p, h->soa[h->cur].p, h->cap, (int)n);
+  if (const void *d = mapped_host(b, n * sizeof(vfmm_body)))
+    aos_to_soa(h->stream, static_cast<const double *>(d), h->soa[h->cur].p, h->cap, (int)n);
+  else {
+    VFMM_CUDA_TRY(cudaMemcpyAsync(h->aos.p, b, n * sizeof(vfmm_body), cudaMemcpyHostToDevice, h->stream));
+    aos_to_soa(h->stream, h->aos.p, h->soa[h->cur].p, h->cap, (int)n);
+  }
 }
 
 void download(vfmm_handle h, vfmm_body *b, size_t n)
 {
   if ((int)n != h->n)
     throw Error(VFMM_ERR_INVALID, "body count differs from the bodies on the device");
-  soa_to_aos(h->stream, h->soa[h->cur].p, h->cap, h->aos.p, (int)n);
-  VFMM_CUDA_TRY(cudaMemcpyAsync(b, h->aos.p, n * sizeof(vfmm_body), cudaMemcpyDeviceToHost, h->stream));
+  if (void *d = mapped_host(b, n * sizeof(vfmm_body)))
+    soa_to_aos(h->stream, h->soa[h->cur].p, h->cap, static_cast<double *>(d), (int)n);
+  else {
+    soa_to_aos(h->stream, h->soa[h->cur].p, h->cap, h->aos.p, (int)n);
+    VFMM_CUDA_TRY(cudaMemcpyAsync(b, h->aos.p, n * sizeof(vfmm_body), cudaMemcpyDeviceToHost, h->stream));
+  }
   VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
 }
 
@@ -1385,7 +1414,7 @@ int vfmm_tree_stats(vfmm_handle h, uint64_t *st, int n)
 
 int vfmm_host_register(void *ptr, size_t bytes)
 {
-  const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
   return e == cudaSuccess ? VFMM_OK : VFMM_ERR_CUDA;
 }
 
