@@ -1379,10 +1379,15 @@ __device__ __forceinline__ void load_seeds32(const AdjDev &a, int i, float *ub, 
   Jb[6] = s3.x, Jb[7] = s3.y, Jb[8] = s3.z;
 }
 
-// Per target: xbar_i += sum of ds/dd (FP32, leaf-relative).
+// Per target: xbar_i += sum of ds/dd (FP32, leaf-relative).  The source
+// bodies of the target leaf's P2P row are staged in shared memory in chunks,
+// already shifted into the target leaf's frame; every target thread (or group
+// of threads) runs over the chunk, whose partial sums fold into a two-sum.
+constexpr int ADJ_CH_T = 512, ADJ_CH_S = 384;
 __global__ void __launch_bounds__(128) k_adj_p2p32_tgt(AdjDev a)
 {
-  __shared__ float red[2][128 * 3];
+  __shared__ float4 Sp[ADJ_CH_T], Sa[ADJ_CH_T];
+  __shared__ float  red[2][128 * 3];
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
     const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
     const int    q0 = a.p2p_start[c], q1 = a.p2p_start[c + 1];
@@ -1392,18 +1397,38 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_tgt(AdjDev a)
       const int TG = nbc <= 32 ? 32 : (nbc <= 64 ? 64 : 128), G = 128 / TG;
       const int tt = threadIdx.x % TG, g = threadIdx.x / TG;
       float     hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
+      float4    pi = make_float4(0.f, 0.f, 0.f, 0.f);
+      float     ub[3], Jb[9], ct[3];
       if (tt < nbc) {
-        const int    i  = b0 + tc + tt;
-        const float4 pi = a.pos32[i];
-        float        ub[3], Jb[9], ct[3];
-        load_seeds32(a, i, ub, Jb, ct);
-        for (int q = q0 + g; q < q1; q += G) {
+        pi = a.pos32[b0 + tc + tt];
+        load_seeds32(a, b0 + tc + tt, ub, Jb, ct);
+      }
+      int q = q0, off = 0;
+      while (q < q1) {
+        int cnt = 0;
+        __syncthreads();
+        while (q < q1 && cnt < ADJ_CH_T) {
           const int   sc = a.p2p_src[q], sb = a.cv.body[sc], sn = a.cv.nbody[sc];
+          const int   take = min(sn - off, ADJ_CH_T - cnt);
           const float ox = (float)(a.cv.x[sc] - cx), oy = (float)(a.cv.y[sc] - cy), oz = (float)(a.cv.z[sc] - cz);
-          float       s[3] = {0.f, 0.f, 0.f};
-          for (int j = sb; j < sb + sn; j++) {
-            const float4 pj = a.pos32[j], aj = a.alp32[j];
-            const float  dx = pi.x - (pj.x + ox), dy = pi.y - (pj.y + oy), dz = pi.z - (pj.z + oz);
+          for (int k = threadIdx.x; k < take; k += 128) {
+            const float4 p = a.pos32[sb + off + k];
+            Sp[cnt + k]    = make_float4(p.x + ox, p.y + oy, p.z + oz, p.w);
+            Sa[cnt + k]    = a.alp32[sb + off + k];
+          }
+          cnt += take;
+          off += take;
+          if (off == sn) {
+            q++;
+            off = 0;
+          }
+        }
+        __syncthreads();
+        if (tt < nbc) {
+          float s[3] = {0.f, 0.f, 0.f};
+          for (int j = g; j < cnt; j += G) {
+            const float4 pj = Sp[j], aj = Sa[j];
+            const float  dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             if (dx * dx + dy * dy + dz * dz != 0.f) {
               float gd[3], wa[3];
               pair_adj32(dx, dy, dz, aj.x, aj.y, aj.z, aj.w, pj.w, ub, Jb, ct, gd, wa);
@@ -1438,9 +1463,12 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_tgt(AdjDev a)
 }
 
 // Per source: xbar_j -= sum of ds/dd, alphabar_j += sum of ds/dalpha_j (FP32).
+// The target bodies of the source leaf's transposed row are staged (position
+// in the source leaf's frame and FP32 seeds) in chunks.
 __global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
 {
-  __shared__ float red[2][128 * 6];
+  __shared__ float4 Tp[ADJ_CH_S], Ts[ADJ_CH_S][4];
+  __shared__ float  red[2][128 * 6];
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
     const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
     const int    q0 = a.p2pT_start[c], q1 = a.p2pT_start[c + 1];
@@ -1450,19 +1478,44 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
       const int TG = nbc <= 32 ? 32 : (nbc <= 64 ? 64 : 128), G = 128 / TG;
       const int tt = threadIdx.x % TG, g = threadIdx.x / TG;
       float     hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float4    pj = make_float4(0.f, 0.f, 0.f, 0.f), aj = pj;
       if (tt < nbc) {
-        const int    j  = b0 + tc + tt;
-        const float4 pj = a.pos32[j], aj = a.alp32[j];
-        for (int q = q0 + g; q < q1; q += G) {
+        pj = a.pos32[b0 + tc + tt];
+        aj = a.alp32[b0 + tc + tt];
+      }
+      int q = q0, off = 0;
+      while (q < q1) {
+        int cnt = 0;
+        __syncthreads();
+        while (q < q1 && cnt < ADJ_CH_S) {
           const int   tcell = a.p2pT_tgt[q], tb = a.cv.body[tcell], tn = a.cv.nbody[tcell];
+          const int   take = min(tn - off, ADJ_CH_S - cnt);
           const float ox = (float)(a.cv.x[tcell] - cx), oy = (float)(a.cv.y[tcell] - cy), oz = (float)(a.cv.z[tcell] - cz);
-          float       s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-          for (int i = tb; i < tb + tn; i++) {
-            const float4 pi = a.pos32[i];
-            const float  dx = (pi.x + ox) - pj.x, dy = (pi.y + oy) - pj.y, dz = (pi.z + oz) - pj.z;
+          for (int k = threadIdx.x; k < take; k += 128) {
+            const int    i = tb + off + k;
+            const float4 p = a.pos32[i];
+            Tp[cnt + k]    = make_float4(p.x + ox, p.y + oy, p.z + oz, 0.f);
+            for (int v = 0; v < 4; v++)
+              Ts[cnt + k][v] = a.seeds32[4 * (size_t)i + v];
+          }
+          cnt += take;
+          off += take;
+          if (off == tn) {
+            q++;
+            off = 0;
+          }
+        }
+        __syncthreads();
+        if (tt < nbc) {
+          float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+          for (int i = g; i < cnt; i += G) {
+            const float4 pi = Tp[i];
+            const float  dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             if (dx * dx + dy * dy + dz * dz != 0.f) {
-              float ub[3], Jb[9], ct[3], gd[3], wa[3];
-              load_seeds32(a, i, ub, Jb, ct);
+              const float4 s0 = Ts[i][0], s1 = Ts[i][1], s2 = Ts[i][2], s3 = Ts[i][3];
+              const float  ub[3] = {s0.x, s0.y, s0.z}, ct[3] = {s0.w, s1.x, s1.y};
+              const float  Jb[9] = {s1.z, s1.w, s2.x, s2.y, s2.z, s2.w, s3.x, s3.y, s3.z};
+              float        gd[3], wa[3];
               pair_adj32(dx, dy, dz, aj.x, aj.y, aj.z, aj.w, pj.w, ub, Jb, ct, gd, wa);
               for (int k = 0; k < 3; k++) {
                 s[k] -= gd[k];
@@ -1507,20 +1560,17 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
 // every rescaling is then by 2^{-k}, k >= 0, exact or a negligible underflow
 // (the MAC keeps |d| >= 2 max(R_s, R_t)).  One warp per source cell.  The outputs (n, m), all three components,
 // are packed onto the lanes by term count ((P-n)(P-n+1)/2 terms each) so that
-// every lane has nearly the same work; a lane walks its outputs' terms in one
-// flattened loop of `iters` steps and adds each finished output into a
-// per-warp accumulator in shared memory, which only it writes.
-__global__ void k_adj_lhat32(const double2 *__restrict__ Lb, float2 *__restrict__ Lh, const int *__restrict__ level, int ncells, int K,
-                             double R0)
+// every lane has nearly the same work (see m2lt_schedule).
+__global__ void k_adj_lhat32(AdjDev a, int ncells, int K)
 {
   const long total = (long)ncells * 3 * K;
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(e / (3 * K)), r = (int)(e % (3 * K));
+    const int c = (int)(e / (3 * K)), r = (int)(e % (3 * K)), lev = a.cv.level[c];
     int       j, k;
     jk_of(r / 3, j, k);
-    const double  sc = ((j & 1) ? -1.0 : 1.0) * pow(ldexp(R0, -level[c]), -(double)(j + 1)); // (-1)^j R_t^{-(j+1)}
-    const double2 v  = Lb[e];
-    Lh[e]            = make_float2((float)(v.x * sc), (float)(v.y * sc));
+    const double  sc = ((j & 1) ? -1.0 : 1.0) * ldexp(a.iR0pow[j + 1], lev * (j + 1)); // (-1)^j R_t^{-(j+1)}
+    const double2 v  = a.Lb[e];
+    a.Lhat32[e]      = make_float2((float)(v.x * sc), (float)(v.y * sc));
   }
 }
 
@@ -1765,7 +1815,7 @@ void eval_adjoint_P(cudaStream_t s, const ExpArgs &e, const AdjDev &d)
   if (d.pos32) {
     const M2LTSchedule &sc    = m2lt_schedule<P>();
     const size_t        bytes = AdjM2L32Sizes<P>::bytes(sc.npieces);
-    k_adj_lhat32<<<grid_for((long)e.ncells * 3 * K, 256), 256, 0, s>>>(d.Lb, d.Lhat32, e.cells.level, e.ncells, K, d.R0);
+    k_adj_lhat32<<<grid_for((long)e.ncells * 3 * K, 256), 256, 0, s>>>(d, e.ncells, K);
     count_launch();
     VFMM_SMEM_ONCE(bytes, k_adj_m2l32<P>);
     k_adj_m2l32<P><<<grid_for(e.ncells, 4, 152 * 16), 128, bytes, s>>>(d, e.ncells, sc.table, sc.pstart, sc.nslot, sc.iters, sc.npieces);
