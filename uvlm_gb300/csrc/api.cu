@@ -74,6 +74,7 @@ struct vfmm_handle_s {
   cudaEvent_t  ev[16]{};
   cudaEvent_t  ph[8]{};
   bool         ph_valid = false;
+  bool         timing   = true; // record the phase events (off inside a batch: fewer driver calls)
   std::string  err;
   unsigned long long launches = 0;
 
@@ -388,10 +389,12 @@ void build_tree_and_lists(vfmm_handle h)
   cudaStream_t s = h->stream;
   h->has_tree    = false;
   h->has_eval    = false;
-  VFMM_CUDA_TRY(cudaEventRecord(h->ph[0], s));
+  if (h->timing)
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[0], s));
   build_tree(s, h->soa, h->cur, h->cap, h->n, h->cfg.ncrit, h->info, h->hinfo, h->ts, h->tree);
   build_lists(s, h->tree, h->tree, h->cfg.theta, h->info, h->hinfo, h->lists, &h->info->p2p_interactions);
-  VFMM_CUDA_TRY(cudaEventRecord(h->ph[1], s));
+  if (h->timing)
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[1], s));
   h->has_tree = true;
   h->has_eval = false;
 }
@@ -478,22 +481,30 @@ void calculate(vfmm_handle h)
     m.R0      = h->tree.R0 > 0 ? h->tree.R0 : 1.0;
     p2m_mixed(s, e, m);
     m2m_mixed(s, e, m);
-    VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
+    if (h->timing)
+      VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
     m2l_mixed(s, e, m);
-    VFMM_CUDA_TRY(cudaEventRecord(h->ph[3], s));
+    if (h->timing)
+      VFMM_CUDA_TRY(cudaEventRecord(h->ph[3], s));
     l2l_mixed(s, e, m);
-    VFMM_CUDA_TRY(cudaEventRecord(h->ph[4], s));
+    if (h->timing)
+      VFMM_CUDA_TRY(cudaEventRecord(h->ph[4], s));
     l2p_p2p_mixed(s, e, m, h->soa[h->cur].p);
-    VFMM_CUDA_TRY(cudaEventRecord(h->ph[5], s));
+    if (h->timing)
+      VFMM_CUDA_TRY(cudaEventRecord(h->ph[5], s));
   } else {
     upward_pass(s, e);
-    VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
+    if (h->timing)
+      VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
     m2l_pass(s, e);
-    VFMM_CUDA_TRY(cudaEventRecord(h->ph[3], s));
+    if (h->timing)
+      VFMM_CUDA_TRY(cudaEventRecord(h->ph[3], s));
     downward_l2l(s, e);
-    VFMM_CUDA_TRY(cudaEventRecord(h->ph[4], s));
+    if (h->timing)
+      VFMM_CUDA_TRY(cudaEventRecord(h->ph[4], s));
     l2p_p2p_pass(s, e, h->soa[h->cur].p);
-    VFMM_CUDA_TRY(cudaEventRecord(h->ph[5], s));
+    if (h->timing)
+      VFMM_CUDA_TRY(cudaEventRecord(h->ph[5], s));
   }
   h->has_eval = true;
 }
@@ -665,8 +676,9 @@ void stage_update(vfmm_handle h, int stage, double dt)
   a.csm           = h->cfg.viscous == VFMM_CSM;
   a.nu            = h->cfg.nu;
   finish_and_update(h->stream, h->soa[h->cur].p, h->cap, h->n, a);
-  VFMM_CUDA_TRY(cudaEventRecord(h->ph[6], h->stream));
-  h->ph_valid = true;
+  if (h->timing)
+    VFMM_CUDA_TRY(cudaEventRecord(h->ph[6], h->stream));
+  h->ph_valid = h->timing;
 }
 
 // Evaluation, viscosity and the stage update of a stage whose tree and lists
@@ -708,17 +720,21 @@ void advance_batch(vfmm_handle *hs, vfmm_body *const *bodies, const size_t *ns, 
       try {
         VFMM_CUDA_TRY(cudaSetDevice(h->device));
         g_launch_counter = &h->launches;
+        h->timing        = false;
         upload(h, bodies[b], ns[b]);
         const int S = stages_of(h->cfg.integrator);
         for (int st = 0; st < S; st++)
           run_stage(h, st, dt);
         download(h, bodies[b], ns[b]);
+        h->timing = true;
       } catch (const Error &e) {
+        h->timing = true;
         codes[b] = e.code;
         msgs[b]  = e.msg;
       } catch (const std::exception &e) {
-        codes[b] = VFMM_ERR_CUDA;
-        msgs[b]  = e.what();
+        h->timing = true;
+        codes[b]  = VFMM_ERR_CUDA;
+        msgs[b]   = e.what();
       }
     }
     g_launch_counter = nullptr;

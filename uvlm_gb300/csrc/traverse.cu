@@ -52,6 +52,7 @@ __global__ void k_traverse_init(CellsView tc, CellsView sc, int2 *front, DevInfo
   info->n_p2p = 0;
   info->n_m2l = 0;
   info->front_n[1] = 0;
+  info->front_n[2] = 0;
   if (tc.nchild[0] == 0 && sc.nchild[0] == 0) {
     p2p[0]           = 0ull; // (0, 0)
     info->n_p2p      = 1;
@@ -62,10 +63,15 @@ __global__ void k_traverse_init(CellsView tc, CellsView sc, int2 *front, DevInfo
   }
 }
 
+// The frontier counters form a ring of three: this step reads n_in, counts
+// into n_out (zero since the step before the previous one) and zeroes
+// n_next, the next step's output, which no block of this step touches.
 __global__ void k_traverse_step(CellsView tc, CellsView sc, const int2 *__restrict__ fin, int *n_in, int cap_in, int2 *fout, int *n_out,
-                                int cap_front, unsigned long long *p2p, unsigned long long *m2l, int *np2p, int *nm2l, int cap_p2p, int cap_m2l,
-                                double theta, int cell_bits, int *overflow)
+                                int *n_next, int cap_front, unsigned long long *p2p, unsigned long long *m2l, int *np2p, int *nm2l, int cap_p2p,
+                                int cap_m2l, double theta, int cell_bits, int *overflow)
 {
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    *n_next = 0;
   // After an overflow the previous step's counter has run past its buffer and
   // some of its slots were left unwritten: the lists are redone with larger
   // buffers, so the remaining steps do nothing.  The clamp keeps every read of
@@ -137,10 +143,9 @@ void traverse(cudaStream_t s, CellsView tc, CellsView sc, int ntc, int nsc, int 
   count_launch();
   const int steps = maxLevelT + maxLevelS + 1;
   for (int it = 0; it < steps; it++) {
-    const int a = it & 1, b = a ^ 1;
-    VFMM_CUDA_TRY(cudaMemsetAsync(&info->front_n[b], 0, sizeof(int), s));
-    k_traverse_step<<<152 * 8, 128, 0, s>>>(tc, sc, ls.front[a].p, &info->front_n[a], (int)ls.front[a].cap, ls.front[b].p, &info->front_n[b],
-                                            (int)ls.front[b].cap,
+    const int a = it & 1, b = a ^ 1; // frontier buffers ping-pong; counters cycle through three
+    k_traverse_step<<<152 * 8, 128, 0, s>>>(tc, sc, ls.front[a].p, &info->front_n[it % 3], (int)ls.front[a].cap, ls.front[b].p,
+                                            &info->front_n[(it + 1) % 3], &info->front_n[(it + 2) % 3], (int)ls.front[b].cap,
                                             ls.p2p_raw.p, ls.m2l_raw.p, &info->n_p2p, &info->n_m2l, (int)ls.p2p_raw.cap, (int)ls.m2l_raw.cap, theta,
                                             cell_bits, &info->overflow);
     count_launch();

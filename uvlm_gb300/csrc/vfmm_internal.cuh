@@ -44,12 +44,12 @@ struct DevInfo {
   int      nnodes;      // cells of the tree
   int      nleaves;
   int      maxLevel;
-  int      front_n[2];  // traversal frontier sizes (ping-pong)
+  int      front_n[3];  // traversal frontier sizes (ring of three: in, out, next out)
   int      n_p2p, n_m2l;
   int      overflow;    // 1 if a capacity was exceeded
   int      nonfinite;   // 1 if an input was NaN/Inf
   unsigned long long p2p_interactions;
-  int      pad[6];
+  int      pad[5];
 };
 
 // Cells in the reference's order (tree.hpp:29-99), structure of arrays.
