@@ -191,7 +191,8 @@ typedef struct vfmm_objective {
  * per body at p = 8), and then run backwards, so device memory holds
  * ceil(steps / checkpoint_every) body states plus stages x checkpoint_every
  * stage evaluations.  With grad_x and grad_alpha both NULL only
- * *value is computed.  Covers Euler, RK2 and RK3 with the cVPM formulation,
+ * *value is computed.  Covers Euler, RK2, RK3 and RK4 (either third stage,
+ * cfg.rk4_fixed) with the cVPM formulation,
  * no viscosity and no relaxation (VFMM_ERR_UNSUPPORTED otherwise).  The
  * reference has no adjoint; its L2P takes one derivative by complex step
  * (multipoleKernels.hpp:630-742, complexify.hpp). */

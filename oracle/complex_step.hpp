@@ -458,7 +458,9 @@ struct Stepper {
     }
   }
 
-  // Stage updates of fmmCalculator.hpp:493-627 (Euler, RK2 Heun, RK3 low storage).
+  // Stage updates of fmmCalculator.hpp:493-711: scheme 0 Euler, 1 RK2 Heun,
+  // 2 RK3 low storage, 3 RK4 as the reference (its third stage steps by
+  // 0.5*dt, :683-689), 4 RK4 with that stage stepping by dt.
   void update(int scheme, int stage, double h)
   {
 #pragma omp parallel for
@@ -480,6 +482,24 @@ struct Stepper {
           q.DO[d] = T(0.5) * q.D[d] + T(0.5) * q.DO[d];
           q.X[d]  = q.XO[d] + T(h) * q.VO[d];
           q.A[d]  = q.AO[d] + T(h) * q.DO[d];
+        } else if (scheme >= 3 && stage == 0) { // stepRK41 :629-649
+          q.XO[d] = q.X[d];
+          q.AO[d] = q.A[d];
+          q.VO[d] = q.U[d];
+          q.DO[d] = q.D[d];
+          q.X[d] += T(0.5 * h) * q.VO[d];
+          q.A[d] += T(0.5 * h) * q.DO[d];
+        } else if (scheme >= 3 && stage < 3) { // stepRK42/43 :650-691
+          const double c = (stage == 2 && scheme == 4) ? 1.0 : 0.5;
+          q.VO[d] += T(2.0) * q.U[d];
+          q.DO[d] += T(2.0) * q.D[d];
+          q.X[d] = q.XO[d] + T(c * h) * q.U[d];
+          q.A[d] = q.AO[d] + T(c * h) * q.D[d];
+        } else if (scheme >= 3) { // stepRK44 :692-711
+          q.VO[d] += q.U[d];
+          q.DO[d] += q.D[d];
+          q.X[d] = q.XO[d] + T(h / 6.0) * q.VO[d];
+          q.A[d] = q.AO[d] + T(h / 6.0) * q.DO[d];
         } else {
           const double A = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
           const double B = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
@@ -494,7 +514,7 @@ struct Stepper {
 
   bool advance(int scheme, double dt, int steps)
   {
-    const int S = scheme == 0 ? 1 : (scheme == 1 ? 2 : 3);
+    const int S = scheme == 0 ? 1 : (scheme == 1 ? 2 : (scheme == 2 ? 3 : 4));
     for (int st = 0; st < steps; st++)
       for (int k = 0; k < S; k++) {
         tree();
@@ -544,7 +564,8 @@ void load(Stepper<T> &s, const Body *src, long n)
 extern "C" {
 
 // The templated FMM step with T = double: `steps` steps of scheme 0 Euler,
-// 1 RK2, 2 RK3 (stretching 0 transposed, 1 classic); b receives X, alpha,
+// 1 RK2, 2 RK3, 3 RK4, 4 RK4 with a full-dt third stage (stretching 0
+// transposed, 1 classic); b receives X, alpha,
 // velocity, J, dadt of the last stage in its tree order.  For the check
 // against vo_advance.
 int vo_cs_advance(Body *b, long n, int P, int ncrit, double theta, int scheme, int stretching, double dt, int steps)

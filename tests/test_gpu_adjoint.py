@@ -1,7 +1,7 @@
 """Reverse-mode gradients (vfmm_adjoint) against central finite differences of
 the same FP64 forward: directional derivatives of the objective along random
 directions of the initial positions and strengths, one evaluation alone and
-through Euler, RK2 and RK3 steps with checkpointing.
+through Euler, RK2, RK3 and RK4 steps with checkpointing.
 
 The FMM is piecewise smooth: at theta = 0.5 cells two apart on the octree
 lattice sit exactly on the MAC boundary |dX| theta = R_i + R_j
@@ -67,12 +67,18 @@ def test_evaluation_gradient_full_tree(vfmm_lib):
     assert worst(errs) < TOL, errs
 
 
-@pytest.mark.parametrize("integration,stretching", [("Euler", "Transposed"), ("RK2", "Transposed"), ("RK3", "Transposed"),
-                                                    ("RK2", "Classic")])
-def test_step_gradients(vfmm_lib, integration, stretching):
+@pytest.mark.parametrize("integration,stretching,rk4_fixed", [("Euler", "Transposed", False), ("RK2", "Transposed", False),
+                                                              ("RK3", "Transposed", False), ("RK2", "Classic", False),
+                                                              ("RK4", "Transposed", False), ("RK4", "Transposed", True),
+                                                              ("RK4", "Classic", False)])
+def test_step_gradients(vfmm_lib, integration, stretching, rk4_fixed):
+    """Under RK4 with the full-step third stage the ring of seed 3 sits on a
+    branch boundary of the map (the oracle's one-sided differences along the
+    first direction disagree by 100%), so that case takes the ring of seed 5,
+    on which both RK4 forms are smooth."""
     from uvlm_gb300 import FMMCalculator, workloads
-    b = workloads.ring(24, seed=3)
-    with FMMCalculator(p=8, ncrit=32, theta=0.47, integration=integration, stretching=stretching) as c:
+    b = workloads.ring(24, seed=5 if rk4_fixed else 3)
+    with FMMCalculator(p=8, ncrit=32, theta=0.47, integration=integration, stretching=stretching, rk4_fixed=rk4_fixed) as c:
         _, _, _, errs = fd_check(c, b, 0.02, 2, every=1, nd=2, h=1e-8)
     assert worst(errs) < 1e-5, errs  # h = 1e-8: rounding of the differences ~1e-7
 
@@ -121,7 +127,7 @@ def test_mixed_gradient_close_to_fp64(vfmm_lib):
 def test_adjoint_rejects_what_it_does_not_cover(vfmm_lib):
     from uvlm_gb300 import FMMCalculator, VfmmError, workloads
     b = workloads.cloud(500, seed=8)
-    for kw in (dict(integration="RK4"), dict(formulation="rVPM"), dict(viscous="PSE", nu=0.01), dict(relax=0.3)):
+    for kw in (dict(formulation="rVPM"), dict(viscous="PSE", nu=0.01), dict(relax=0.3)):
         with FMMCalculator(p=4, ncrit=32, theta=0.5, **kw) as c:
             with pytest.raises(VfmmError):
                 c.adjoint(b, 0.01, 1)
@@ -140,8 +146,11 @@ def _complex_step(b, P, ncrit, theta, scheme, dt, steps, dirs_x, dirs_a, energy=
     return val.value, der
 
 
-@pytest.mark.parametrize("theta,steps", [(0.5, 0), (0.47, 2)])
-def test_gradient_matches_complex_step(vfmm_lib, theta, steps):
+# the oracle's scheme numbers: 2 RK3, 3 RK4 with the reference's half-step
+# third stage, 4 RK4 with a full-step third stage
+@pytest.mark.parametrize("theta,steps,integration,rk4_fixed", [(0.5, 0, "RK3", False), (0.47, 2, "RK3", False),
+                                                               (0.47, 2, "RK4", False), (0.47, 1, "RK4", True)])
+def test_gradient_matches_complex_step(vfmm_lib, theta, steps, integration, rk4_fixed):
     """Directional derivatives from the adjoint against the oracle's whole-step
     complex step (real parts, trees and lists untouched by the step).  Multi-step
     runs use theta = 0.47: CPU and GPU trajectories differ by rounding, and only
@@ -152,9 +161,10 @@ def test_gradient_matches_complex_step(vfmm_lib, theta, steps):
     nd = 3
     dx = rng.normal(size=(nd, b.size, 3))
     da = rng.normal(size=(nd, b.size, 3)) * np.abs(b["alpha"]).max()
-    with FMMCalculator(p=8, ncrit=32, theta=theta, integration="RK3") as c:
+    with FMMCalculator(p=8, ncrit=32, theta=theta, integration=integration, rk4_fixed=rk4_fixed) as c:
         v, gx, ga = c.adjoint(b, 0.02, steps, 1)
-    vc, der = _complex_step(b, 8, 32, theta, 2, 0.02, steps, dx, da)
+    scheme = 2 if integration == "RK3" else (4 if rk4_fixed else 3)
+    vc, der = _complex_step(b, 8, 32, theta, scheme, 0.02, steps, dx, da)
     assert abs(v - vc) <= 1e-10 * abs(vc)
     for k in range(nd):
         an = float((gx * dx[k]).sum() + (ga * da[k]).sum())

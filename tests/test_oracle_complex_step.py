@@ -22,6 +22,21 @@ def test_templated_step_equals_the_reference_restatement():
         assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), f
 
 
+def test_templated_rk4_equals_the_reference_restatement():
+    """RK4 with the reference's half-step third stage (oracle scheme 3) and
+    with a full-step one (scheme 4, rk4_fixed of the restatement)."""
+    L = oracle()
+    b = workloads.ring(16, seed=4)
+    n = b.size
+    for fixed in (0, 1):
+        b1, b2 = b.copy(), b.copy()
+        assert L.vo_advance(b1.ctypes.data, n, 8, 32, 0.5, 0.02, 2, 3, 0, 0, 0.0, fixed, 0, 0.0) == 0
+        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, 3 + fixed, 0, 0.02, 2) == 0
+        for f, tol in (("X", 1e-14), ("alpha", 1e-14), ("velocity", 1e-12), ("J", 1e-11), ("dadt", 1e-11)):
+            a, r = b2[f].reshape(n, -1), b1[f].reshape(n, -1)
+            assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), (fixed, f)
+
+
 def test_complex_step_against_central_differences():
     L = oracle()
     b = workloads.ring(16, seed=3)

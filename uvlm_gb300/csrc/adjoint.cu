@@ -1015,7 +1015,7 @@ __global__ void k_adj_seeds(const double *soa, double *w, size_t cap, int n, int
 // The transposed stage update (bodies.cu k_stage_update) in the tree order
 // of the stage: the stage's cotangent of (u, dalpha/dt) into W_COT, the
 // adjoint state g updated except for the evaluation's own contribution.
-__global__ void k_adj_stage_pre(double *g, double *w, size_t cap, int n, int scheme, int stage, double h)
+__global__ void k_adj_stage_pre(double *g, double *w, size_t cap, int n, int scheme, int stage, double h, int rk4_fixed)
 {
   const double A  = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
   const double Bc = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
@@ -1043,6 +1043,28 @@ __global__ void k_adj_stage_pre(double *g, double *w, size_t cap, int n, int sch
         *xb = *ab = 0;
         *vb       = 0.5 * vt;
         *db       = 0.5 * dt_;
+      } else if (scheme == VFMM_RK4 && stage == 0) { // xold = x; v = f; x' = x + h/2 v
+        Wc(k)     = *vb + 0.5 * h * *xb;
+        Wc(3 + k) = *db + 0.5 * h * *ab;
+        *xb += *xob;
+        *ab += *aob;
+        *vb = *db = *xob = *aob = 0;
+      } else if (scheme == VFMM_RK4 && stage < 3) { // v' = v + 2f; x' = xold + c h f
+        const double c = (stage == 2 && rk4_fixed) ? 1.0 : 0.5;
+        Wc(k)          = 2.0 * *vb + c * h * *xb;
+        Wc(3 + k)      = 2.0 * *db + c * h * *ab;
+        *xob += *xb;
+        *aob += *ab;
+        *xb = *ab = 0;
+      } else if (scheme == VFMM_RK4) { // v' = v + f; x' = xold + h/6 v'
+        const double vt = *vb + (h / 6.0) * *xb, dt_ = *db + (h / 6.0) * *ab;
+        Wc(k)           = vt;
+        Wc(3 + k)       = dt_;
+        *xob += *xb;
+        *aob += *ab;
+        *xb = *ab = 0;
+        *vb       = vt;
+        *db       = dt_;
       } else { // RK3: Q' = A Q + h f; x' = x + B Q'
         const double qx = *vb + Bc * *xb, qa = *db + Bc * *ab;
         Wc(k)           = h * qx;
@@ -1928,9 +1950,9 @@ void adjoint_seeds(cudaStream_t s, const double *soa, double *w, size_t cap, int
   VFMM_LAUNCH_CHECK();
 }
 
-void adjoint_stage_pre(cudaStream_t s, double *g, double *w, size_t cap, int n, int scheme, int stage, double dt)
+void adjoint_stage_pre(cudaStream_t s, double *g, double *w, size_t cap, int n, int scheme, int stage, double dt, int rk4_fixed)
 {
-  k_adj_stage_pre<<<grid_for(n, 256), 256, 0, s>>>(g, w, cap, n, scheme, stage, dt);
+  k_adj_stage_pre<<<grid_for(n, 256), 256, 0, s>>>(g, w, cap, n, scheme, stage, dt, rk4_fixed);
   count_launch();
   VFMM_LAUNCH_CHECK();
 }

@@ -1026,8 +1026,6 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
              double *gx, double *ga)
 {
   const vfmm_config &c = h->cfg;
-  if (c.integrator != VFMM_EULER && c.integrator != VFMM_RK2 && c.integrator != VFMM_RK3)
-    throw Error(VFMM_ERR_UNSUPPORTED, "the adjoint covers Euler, RK2 and RK3");
   if (c.formulation != VFMM_CVPM || c.viscous != VFMM_INVISCID || c.relax != 0)
     throw Error(VFMM_ERR_UNSUPPORTED, "the adjoint covers the inviscid cVPM path without relaxation");
   if (!bodies || !obj || !value)
@@ -1182,7 +1180,7 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
         VFMM_CUDA_TRY(cudaMemcpyAsync(h->soa[h->cur].p, x.body.p, nbody_fields * sizeof(double), cudaMemcpyDeviceToDevice, s));
         VFMM_CUDA_TRY(cudaMemcpyAsync(h->soa[h->cur].p + (size_t)F_R * cap, x.body.p + nbody_fields, cap * sizeof(double),
                                       cudaMemcpyDeviceToDevice, s));
-        adjoint_stage_pre(s, A.g[gc].p, A.w.p, cap, N, c.integrator, k, dt);
+        adjoint_stage_pre(s, A.g[gc].p, A.w.p, cap, N, c.integrator, k, dt, c.rk4_fixed);
         adjoint_seeds(s, h->soa[h->cur].p, A.w.p, cap, N, c.stretching);
         vjp(x.info.p);
       }

@@ -278,7 +278,7 @@ constexpr int ADJ_PARTIALS = 152 * 2 * 17;
 // the seeds in b.w (W_SU, W_SJ, W_ASTR): adds to g[G_XB], g[G_AB].
 void adjoint_eval(cudaStream_t s, const ExpArgs &e, const AdjBufs &b, const DevInfo *info);
 void adjoint_seeds(cudaStream_t s, const double *soa, double *w, size_t cap, int n, int stretching);
-void adjoint_stage_pre(cudaStream_t s, double *g, double *w, size_t cap, int n, int scheme, int stage, double dt);
+void adjoint_stage_pre(cudaStream_t s, double *g, double *w, size_t cap, int n, int scheme, int stage, double dt, int rk4_fixed);
 void adjoint_objective(cudaStream_t s, const double *soa, size_t cap, int n, const int *orig, const double *seed_x, const double *seed_a, double wE,
                        const double wI[3], double *g, double *w, double *part, double *value);
 void adjoint_scatter(cudaStream_t s, const double *in, double *out, size_t cap, int n, const uint32_t *perm);
