@@ -288,6 +288,18 @@ int vfmm_flush_l2(vfmm_handle h);
  * FP64/FP32 pipes rather than on tensor cores. */
 int vfmm_measure_fma_peak(vfmm_handle h, int precision, double *tflops);
 
+/* ---- output --------------------------------------------------------------- */
+
+/* Writes n bodies to `path` as legacy-VTK polydata, the file of the
+ * reference driver's writeTovtk (src/main.cpp:127-164): POINTS X, one
+ * VERTICES cell per body, POINT_DATA with VECTORS alpha and velocity and
+ * SCALARS radius.  binary = 0: ASCII, byte-identical to the reference's file
+ * (numbers as printf "%g"); binary = 1: the same dataset as legacy-VTK
+ * BINARY data (big-endian FP64 values, 32-bit vertex indices, n < 2^31).
+ * Host only; needs no handle and no GPU.  VFMM_ERR_INVALID on a null
+ * argument or when the file cannot be written. */
+int vfmm_write_vtk(const vfmm_body *bodies, size_t n, const char *path, int binary);
+
 /* ---- no allocation -------------------------------------------------------- */
 
 /* No counterpart in the reference.  Root cell of the octree -- centre out[0..2]

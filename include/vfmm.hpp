@@ -63,6 +63,15 @@ public:
   Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
 };
 
+// The particle file of the reference driver's writeTovtk lambda
+// (src/main.cpp:127-164), which writes "output" + step + ".vtk"; ASCII is
+// byte-identical to it, binary keeps full FP64 values.
+inline void writeVTK(const exafmm::Bodies &particles, const std::string &path, bool binary = false)
+{
+  if (vfmm_write_vtk(particles.data(), particles.size(), path.c_str(), binary ? 1 : 0) != VFMM_OK)
+    throw Error(VFMM_ERR_INVALID, "writeVTK: cannot write " + path);
+}
+
 template <typename Host, typename Device, typename IntegrationScheme, typename ViscousScheme, typename Formulation, typename Stretching>
 struct FMMCalculator {
   // nu: the viscosity of the PSE/CSM schemes, which the reference declares

@@ -2,12 +2,13 @@
 // against include/vfmm.hpp and linked with libvfmm.so.  Builds a small ring
 // of particles, takes one RK3 step, prints the mean velocity and reads the
 // velocity at the ring's centre through getSensorData (Gamma / 2R = 0.5 for
-// this ring); exit code 0 on success.
+// this ring); with a path argument it writes the particles there as the
+// reference driver's VTK file (main.cpp:127-164); exit code 0 on success.
 #include <cmath>
 #include <cstdio>
 #include "vfmm.hpp"
 
-int main()
+int main(int argc, char **argv)
 {
   typedef Vortex::FMMCalculator<int, int, Vortex::RK3, Vortex::Inviscid, Vortex::cVPM, Vortex::Transposed> FMMCalculator;
   exafmm::Bodies particles;
@@ -33,6 +34,8 @@ int main()
     energy              = calc.adjoint(particles, 0.01, 1, 1, 1.0, wI, gx, ga); // before advance reorders the bodies
     calc.advance(particles, 0.01);
     calc.getSensorData(sensors);
+    if (argc > 1)
+      Vortex::writeVTK(particles, argv[1]);
   } catch (const Vortex::Error &e) {
     std::fprintf(stderr, "vfmm error %d: %s\n", e.code, e.what());
     return 1;

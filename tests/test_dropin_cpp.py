@@ -25,6 +25,8 @@ def test_dropin_runs(vfmm_lib, tmp_path):
     r = subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), SRC, "-L" + libdir, "-lvfmm",
                         "-Wl,-rpath," + libdir, "-o", exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    vtk = tmp_path / "output1.vtk"
+    r = subprocess.run([exe, str(vtk)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "centre uz" in r.stdout
+    assert vtk.read_bytes().startswith(b"# vtk DataFile Version 3.0\nvtk output\nASCII\nDATASET POLYDATA\nPOINTS 2000 double\n")

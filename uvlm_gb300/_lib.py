@@ -102,6 +102,7 @@ _PROTOS = {
     "vfmm_flush_l2": (_i, [_H]),
     "vfmm_measure_fma_peak": (_i, [_H, _i, ctypes.POINTER(ctypes.c_double)]),
     "vfmm_bounds_noalloc": (_i, [_vp, _vp, _vp, _sz, _vp, _vp]),
+    "vfmm_write_vtk": (_i, [_vp, _sz, ctypes.c_char_p, _i]),
 }
 
 _LIB = None

@@ -13,6 +13,7 @@ time step and overwrites `bodies`.  Every call goes through libvfmm.so.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -218,6 +219,16 @@ def direct(targets: np.ndarray, sources: np.ndarray) -> np.ndarray:
 
 def new_bodies(n: int) -> np.ndarray:
     return np.zeros(n, BODY_DTYPE)
+
+
+def write_vtk(bodies: np.ndarray, path: str, binary: bool = False) -> None:
+    """vfmm_write_vtk: the particles as legacy-VTK polydata, the reference
+    driver's writeTovtk file (src/main.cpp:127-164); ASCII is byte-identical
+    to it, binary keeps full FP64 values.  Host only."""
+    b = _lib.as_bodies(bodies)
+    code = lib().vfmm_write_vtk(b.ctypes.data, b.size, os.fsencode(path), int(bool(binary)))
+    if code != 0:
+        raise _lib.VfmmError(code, f"cannot write {path}")
 
 
 def advance_batch(calculators: list, bodies: list, dt: float) -> None:
