@@ -66,7 +66,7 @@ typedef struct {
   int    rk4_fixed;   /* 1: RK4 stage 3 uses dt; 0: 0.5*dt as the reference (fmmCalculator.hpp:683-689) */
   int    device;      /* CUDA device ordinal; -1 = the caller's current device */
   int    viscous;     /* VFMM_INVISCID, VFMM_PSE or VFMM_CSM, applied after every evaluation of a stage */
-  int    m2l_batch;   /* mixed mode: M2L sources per batch, 8, 16, 24 or 32; 0 = by p (32 up to 10, 24 to 12, else 16) */
+  int    m2l_batch;   /* mixed mode: M2L sources per batch, 8, 16, 24, 30 or 32 (at most 227 KB of staging: 32 to p = 14, 30 to p = 15); 0 = by p (30 up to 10, 24 to 12, else 16) */
   double nu;          /* kinematic viscosity for PSE/CSM (the reference leaves its _nu unset, fmmCalculator.hpp:56) */
   int    reserved[2];
 } vfmm_config;
@@ -154,7 +154,8 @@ typedef struct {
 } vfmm_tuning;
 
 /* Opt-in autotuner: times one stage (best of two after a warm-up) of `bodies`
- * for leaf sizes 16..256 and, in mixed mode, M2L source batches 16/24/32, and
+ * for leaf sizes 16..256 and, in mixed mode, M2L source batches 16/24/30/32
+ * (those whose staging fits in shared memory at this p), and
  * keeps the fastest in the handle (vfmm_get_config shows ncrit and m2l_batch).  A
  * leaf size other than the reference's compile-time ncrit (exafmmTypes.hpp:14)
  * builds a different tree and lists, so results are no longer those of the

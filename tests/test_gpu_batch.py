@@ -86,7 +86,7 @@ def test_m2l_batch_config(vfmm_lib):
     from uvlm_gb300 import FMMCalculator, VfmmError, workloads
     b = workloads.cloud(30000, seed=31)
     out = {}
-    for prec, mb in (("fp64", 0), ("mixed", 16), ("mixed", 24), ("mixed", 32)):
+    for prec, mb in (("fp64", 0), ("mixed", 16), ("mixed", 24), ("mixed", 30), ("mixed", 32)):
         with FMMCalculator(p=10, ncrit=64, theta=0.5, precision=prec, m2l_batch=mb) as c:
             assert c.config.m2l_batch == mb
             bb = b.copy()
@@ -94,9 +94,14 @@ def test_m2l_batch_config(vfmm_lib):
             c.calculate()
             c.copyBodies2Host(bb)
             out[mb] = bb
-    for mb in (16, 24, 32):
+    for mb in (16, 24, 30, 32):
         assert np.array_equal(out[mb]["X"], out[0]["X"])
         err = np.linalg.norm(out[mb]["velocity"] - out[0]["velocity"]) / np.linalg.norm(out[0]["velocity"])
         assert err < 1e-6
     with pytest.raises(VfmmError):
         FMMCalculator(p=10, ncrit=64, theta=0.5, precision="mixed", m2l_batch=12)
+    for p, mb in ((15, 32), (16, 30)):  # staging above a block's 227 KB of shared memory
+        with pytest.raises(VfmmError):
+            FMMCalculator(p=p, ncrit=64, theta=0.5, precision="mixed", m2l_batch=mb)
+    with FMMCalculator(p=16, ncrit=64, theta=0.5, precision="mixed", m2l_batch=24) as c:
+        assert c.config.m2l_batch == 24

@@ -293,6 +293,7 @@ struct M2LV2 {
   static constexpr size_t bytes = (size_t)(SB * (MSTR + YSTR)) * sizeof(zf) + SB * (sizeof(float4) + 2 * sizeof(int));
   // per-warp partial locals [P][3K] reuse the staging arrays after the last batch
   static_assert(P * 3 * K <= SB * (MSTR + YSTR), "per-warp partials fit in the staging arrays");
+  static_assert(bytes == m2l32_smem_bytes(P, SB), "the host-side size check uses the same layout");
 };
 
 template <int P, int SB>
@@ -888,6 +889,8 @@ static void m2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   (void)PP; // the folded FP32 multipoles were written by P2M and M2M
   if (m.m2l_batch == 32)
     m2l32_launch<P, 32>(s, d, e, m);
+  else if (m.m2l_batch == 30)
+    m2l32_launch<P, 30>(s, d, e, m);
   else if (m.m2l_batch == 24)
     m2l32_launch<P, 24>(s, d, e, m);
   else if (m.m2l_batch == 8)
