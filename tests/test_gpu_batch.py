@@ -64,7 +64,7 @@ def test_autotune(vfmm_lib):
     b = workloads.cloud(60000, seed=21)
     with FMMCalculator(p=8, ncrit=64, theta=0.5, integration="Euler", precision="mixed") as c:
         t = c.autotune(b, 0.01)
-        assert t["tried"] == 27 and t["ncrit"] in (16, 24, 32, 48, 64, 96, 128, 192, 256) and t["m2l_batch"] in (16, 24, 32)
+        assert t["tried"] == 36 and t["ncrit"] in (16, 24, 32, 48, 64, 96, 128, 192, 256) and t["m2l_batch"] in (16, 24, 30, 32)
         assert t["ms_per_stage"] <= t["default_ms_per_stage"]
         bb = b.copy()
         c.init(bb)
