@@ -290,10 +290,11 @@ struct M2LV2 {
   static constexpr int K = nterms(P), PP = P * P;
   static constexpr int MSTR = 3 * PP + 1;            // complex stride of a staged multipole
   static constexpr int YSTR = PP + M2L_YOFF + 1;     // complex stride of a staged harmonic table
-  static constexpr size_t bytes = (size_t)(SB * (MSTR + YSTR)) * sizeof(zf) + SB * (sizeof(float4) + 2 * sizeof(int));
+  static constexpr size_t bytes = (size_t)(SB * (MSTR + YSTR)) * sizeof(zf); // dynamic: multipoles, harmonics
+  static constexpr size_t meta  = 2 * (size_t)SB * (sizeof(float4) + 2 * sizeof(int)) + 16; // static, with the masks and padding
   // per-warp partial locals [P][3K] reuse the staging arrays after the last batch
   static_assert(P * 3 * K <= SB * (MSTR + YSTR), "per-warp partials fit in the staging arrays");
-  static_assert(bytes == m2l32_smem_bytes(P, SB), "the host-side size check uses the same layout");
+  static_assert(bytes + meta == m2l32_smem_bytes(P, SB), "the host-side size check uses the same layout");
 };
 
 template <int P, int SB>
@@ -302,15 +303,18 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
   using G = M2LV2<P, SB>;
   constexpr int K = G::K, PP = G::PP, MSTR = G::MSTR, YSTR = G::YSTR, KH = G::KH;
   extern __shared__ float4 smem32[];
-  // 16-byte-aligned fields first: per source (d / R_s, 1 / R_s), source index, level
-  float4 *Off = smem32;
-  int    *Src = reinterpret_cast<int *>(Off + SB);
-  int    *Lvl = Src + SB;
-  static_assert((SB * (sizeof(float4) + 2 * sizeof(int))) % 16 == 0, "keeps the complex arrays aligned");
-  zf *Ms = reinterpret_cast<zf *>(Lvl + SB);
+  zf *Ms = reinterpret_cast<zf *>(smem32);
   zf *Ys = Ms + SB * MSTR;
   zf *Lw = Ms; // [P][3K] after the batches
-  __shared__ unsigned cross_mask; // batch sources on another level than the target
+  // Source metadata of a batch, two buffers: per source (d / R_s, 1 / R_s),
+  // index, level, and the mask of sources on another level than the target.
+  // Warp 0 (degree 0, the lightest m-loop) stages batch k + 1 into the other
+  // buffer after its own compute of batch k, so each batch needs no barrier
+  // between staging its metadata and using it beyond the one that ends the
+  // previous batch.
+  __shared__ float4   OffB[2][SB];
+  __shared__ int      SrcB[2][SB], LvlB[2][SB];
+  __shared__ unsigned cmaskB[2];
   static_assert(SB <= 32, "one warp stages a batch");
   const int n = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int4 me = lanes[n * 32 + lane];
@@ -329,26 +333,32 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
     const int    q0 = a.m2l_start[t], q1 = a.m2l_start[t + 1];
     const double tx = a.cv.x[t], ty = a.cv.y[t], tz = a.cv.z[t];
     const int    lt = a.cv.level[t];
-    for (int qb = q0; qb < q1; qb += SB) {
-      const int nb = min(SB, q1 - qb);
-      __syncthreads();
-      if (threadIdx.x < 32) { // nb <= SB <= 32: warp 0 stages the batch's sources
-        bool cl = false;
-        if (threadIdx.x < nb) {
-          const int    s   = a.m2l_src[qb + threadIdx.x];
-          const int    ls  = a.cv.level[s];
-          const double iRs = ldexp(a.iR0, ls);
-          Src[threadIdx.x] = s;
-          Lvl[threadIdx.x] = ls;
-          Off[threadIdx.x] = make_float4((float)((tx - a.cv.x[s]) * iRs), (float)((ty - a.cv.y[s]) * iRs), (float)((tz - a.cv.z[s]) * iRs),
-                                         (float)iRs);
-          cl = ls != lt;
-        }
-        const unsigned msk = __ballot_sync(0xffffffffu, cl);
-        if (threadIdx.x == 0)
-          cross_mask = msk;
+    // warp 0 (all 32 lanes, n == 0) stages the sources qb .. qb + cnt - 1 into buffer buf
+    auto stage_meta = [&](int buf, int qb, int cnt) {
+      bool cl = false;
+      if (lane < cnt) {
+        const int    s   = a.m2l_src[qb + lane];
+        const int    ls  = a.cv.level[s];
+        const double iRs = ldexp(a.iR0, ls);
+        SrcB[buf][lane]  = s;
+        LvlB[buf][lane]  = ls;
+        OffB[buf][lane]  = make_float4((float)((tx - a.cv.x[s]) * iRs), (float)((ty - a.cv.y[s]) * iRs), (float)((tz - a.cv.z[s]) * iRs),
+                                       (float)iRs);
+        cl               = ls != lt;
       }
-      __syncthreads();
+      const unsigned msk = __ballot_sync(0xffffffffu, cl);
+      if (lane == 0)
+        cmaskB[buf] = msk;
+    };
+    // buffer 0 was last read before the barriers that ended the previous cell
+    if (n == 0 && q0 < q1)
+      stage_meta(0, q0, min(SB, q1 - q0));
+    for (int qb = q0, k = 0; qb < q1; qb += SB, k ^= 1) {
+      const int nb = min(SB, q1 - qb);
+      __syncthreads(); // the previous batch's compute is done; this batch's metadata is visible
+      const float4 *Off = OffB[k];
+      const int    *Src = SrcB[k];
+      const int    *Lvl = LvlB[k];
       // stage multipoles: asynchronous copies of Mp32, all in flight at once
       // while the harmonics are made; sources on another level than the
       // target are scaled by 2^{(lt - ls) n} afterwards
@@ -372,7 +382,7 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
       }
       cp_async_wait_all();
       __syncthreads();
-      const unsigned cmask = cross_mask;
+      const unsigned cmask = cmaskB[k];
       if (cmask) { // block-uniform: sources on another level than the target
         for (int r = threadIdx.x; r < 3 * PP; r += nthreads) {
           const int nn = (int)sqrtf((float)(r / 3)); // degree of entry n^2+n+m (exact for these small integers)
@@ -442,6 +452,9 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
           }
         }
       }
+      // the other buffer was last read before this batch's first barrier
+      if (n == 0 && qb + SB < q1)
+        stage_meta(k ^ 1, qb + SB, min(SB, q1 - qb - SB));
     }
     // combine: replicas inside the warp (deterministic tree), then warps in order
     const int T = me.w >> 8;

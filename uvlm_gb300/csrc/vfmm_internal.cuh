@@ -230,13 +230,15 @@ struct MixedArgs {
 };
 // Columns per half-tile of the mixed M2L lane tiles: at most 32 tiles per degree.
 __host__ __device__ constexpr int m2l_half_width(int P) { return P >= 16 ? 4 : 2; }
-// Dynamic shared memory of k_m2l32v2<P, SB>: per source of a batch, a staged
-// multipole (3P^2 + 1 complex floats), a harmonic table (P^2 + 5) and its
-// offset, index and level (24 bytes).  A batch fits when this is at most the
-// 227 KB a block can opt in to.
+// Shared memory of k_m2l32v2<P, SB>: per source of a batch, a staged
+// multipole (3P^2 + 1 complex floats) and a harmonic table (P^2 + 5), both
+// dynamic; and, static, two buffers of the sources' offsets, indices and
+// levels (24 bytes each) with their cross-level masks and alignment (16
+// bytes).  A batch fits when the total is at most the 227 KB a block can opt
+// in to.
 __host__ __device__ constexpr size_t m2l32_smem_bytes(int P, int SB)
 {
-  return (size_t)SB * ((3 * P * P + 1) + (P * P + 5)) * 8 + (size_t)SB * 24;
+  return (size_t)SB * ((3 * P * P + 1) + (P * P + 5)) * 8 + 2 * (size_t)SB * 24 + 16;
 }
 constexpr bool m2l_batch_fits(int P, int SB) { return m2l32_smem_bytes(P, SB) <= (size_t)227 * 1024; }
 std::vector<int4> m2l_lane_table(int P, int kh, int sb);
