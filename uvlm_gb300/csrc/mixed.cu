@@ -275,6 +275,12 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// Asynchronous 16-byte global -> shared copy through L2 (both addresses 16-byte aligned).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 
 // v * 2^e, equal to ldexpf(v, e): a multiply by the exactly built power of
 // two inside the normal exponent range, ldexpf outside it.
@@ -619,7 +625,7 @@ __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v)
 // are combined in a fixed order, and the result becomes FP64 for the
 // stretching epilogue.  All lanes run the same trip counts.
 template <int P>
-__global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
+__global__ void __launch_bounds__(128, 6) k_l2p_p2p32(DevMixed a, double *out)
 {
   using S = L2P32Sizes<P>;
   constexpr int K = S::K, K1 = S::K1, K2 = S::K2, CH = S::CH, LG = 128;
@@ -629,6 +635,8 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
   float4 *Sa   = Sp + CH;  // staged strengths, w = 1/sigma
   float4 *Loff = Sa + CH;  // per source leaf of the current group: centre offset, w = body start (int bits)
   int    *Lcnt = reinterpret_cast<int *>(Loff + LG);
+  __shared__ int Lpre[LG + 1]; // exclusive prefix of Lcnt over the group; Lpre[ng] = the group's bodies
+  static_assert(CH % 128 == 0, "every thread stages the same number of chunk elements");
   zf     *Lc   = reinterpret_cast<zf *>(Lcnt + LG);
   zf     *U    = Lc + 3 * K;
   zf     *JJ   = U + 3 * K1;
@@ -738,27 +746,73 @@ __global__ void __launch_bounds__(128) k_l2p_p2p32(DevMixed a, double *out)
           Lcnt[threadIdx.x] = a.cv.nbody[sc];
         }
         __syncthreads();
-        int lq = 0, lo_off = 0; // next leaf of the group, body offset inside it (uniform)
-        while (lq < ng) {
-          int cnt = 0;
-          while (lq < ng && cnt < CH) {
-            const float4 o = Loff[lq];
-            const int    sn = Lcnt[lq], take = min(sn - lo_off, CH - cnt), sb = __float_as_int(o.w) + lo_off;
-            for (int i = threadIdx.x; i < take; i += 128) {
-              float4 p = a.pos32[sb + i];
+        if (threadIdx.x < 32) { // warp 0: exclusive prefix of the group's body counts, four per lane
+          const int l = threadIdx.x;
+          int       c[4], sum = 0;
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            c[u] = 4 * l + u < ng ? Lcnt[4 * l + u] : 0;
+            sum += c[u];
+          }
+          int incl = sum;
+#pragma unroll
+          for (int d = 1; d < 32; d <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, d);
+            if (l >= d)
+              incl += v;
+          }
+          int run = incl - sum;
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            if (4 * l + u < ng)
+              Lpre[4 * l + u] = run;
+            run += c[u];
+          }
+          if (l == 31)
+            Lpre[ng] = incl;
+        }
+        __syncthreads();
+        // The group's source bodies as one sequence (leaf by leaf) cut into
+        // chunks of CH.  Every thread copies its elements e = tid + 128 i of a
+        // chunk with cp.async (all in flight at once), finds each element's
+        // leaf by binary search over Lpre, and after the copies land moves
+        // its own positions from the source leaf's frame to the target's.
+        const int total = Lpre[ng];
+        for (int c0 = 0; c0 < total; c0 += CH) {
+          const int cnt = min(CH, total - c0);
+          int       lqs[CH / 128];
+#pragma unroll
+          for (int i = 0; i < CH / 128; i++) {
+            const int e = threadIdx.x + 128 * i;
+            lqs[i]      = -1;
+            if (e < cnt) {
+              const int g = c0 + e;
+              int       lb = 0, ub = ng - 1; // the last leaf with Lpre <= g
+              while (lb < ub) {
+                const int mid = (lb + ub + 1) >> 1;
+                if (Lpre[mid] <= g)
+                  lb = mid;
+                else
+                  ub = mid - 1;
+              }
+              lqs[i]       = lb;
+              const int bi = __float_as_int(Loff[lb].w) + (g - Lpre[lb]);
+              cp_async16(Sp + e, a.pos32 + bi);
+              cp_async16(Sa + e, a.alp32 + bi);
+            }
+          }
+          cp_async_wait_all();
+#pragma unroll
+          for (int i = 0; i < CH / 128; i++)
+            if (lqs[i] >= 0) {
+              const int    e = threadIdx.x + 128 * i;
+              const float4 o = Loff[lqs[i]];
+              float4       p = Sp[e];
               p.x += o.x;
               p.y += o.y;
               p.z += o.z;
-              Sp[cnt + i] = p;
-              Sa[cnt + i] = a.alp32[sb + i];
+              Sp[e] = p;
             }
-            cnt += take;
-            lo_off += take;
-            if (lo_off == sn) {
-              lq++;
-              lo_off = 0;
-            }
-          }
           __syncthreads();
           if (active) {
             for (int j0 = g; j0 < cnt; j0 += 16 * Gt) {
