@@ -1405,11 +1405,59 @@ __device__ __forceinline__ void load_seeds32(const AdjDev &a, int i, float *ub, 
 // bodies of the target leaf's P2P row are staged in shared memory in chunks,
 // already shifted into the target leaf's frame; every target thread (or group
 // of threads) runs over the chunk, whose partial sums fold into a two-sum.
-constexpr int ADJ_CH_T = 512, ADJ_CH_S = 384;
+constexpr int ADJ_CH_T = 512, ADJ_CH_S = 384, ADJ_LG = 32;
+
+// Warp 0 stages the leaves list[q .. q + ng - 1] (ng <= 32) of a P2P row:
+// Loff[l] = the leaf's centre minus (cx, cy, cz) in FP32, w = its first body
+// (int bits); Lpre[0 .. ng] = the exclusive prefix of the leaves' body counts.
+// The row's bodies, leaf after leaf, then form one sequence of Lpre[ng].
+__device__ __forceinline__ void stage_row_leaves(const AdjDev &a, const int *list, int q, int ng, double cx, double cy, double cz, float4 *Loff,
+                                                 int *Lpre)
+{
+  const int l   = threadIdx.x & 31;
+  int       cnt = 0;
+  if (l < ng) {
+    const int sc = list[q + l];
+    cnt          = a.cv.nbody[sc];
+    Loff[l]      = make_float4((float)(a.cv.x[sc] - cx), (float)(a.cv.y[sc] - cy), (float)(a.cv.z[sc] - cz), __int_as_float(a.cv.body[sc]));
+  }
+  int incl = cnt;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, d);
+    if (l >= d)
+      incl += v;
+  }
+  if (l < ng)
+    Lpre[l] = incl - cnt;
+  if (l == ng - 1)
+    Lpre[ng] = incl;
+}
+
+// The leaf holding element g of that sequence: the last l < ng with Lpre[l] <= g.
+__device__ __forceinline__ int row_leaf_of(const int *Lpre, int ng, int g)
+{
+  int lb = 0, ub = ng - 1;
+  while (lb < ub) {
+    const int mid = (lb + ub + 1) >> 1;
+    if (Lpre[mid] <= g)
+      lb = mid;
+    else
+      ub = mid - 1;
+  }
+  return lb;
+}
+
+// Chunks of a row's bodies are staged by all threads at once: each copies
+// its elements e = tid + 128 i with cp.async (in flight together), then
+// shifts its own positions into the frame of the block's leaf.
 __global__ void __launch_bounds__(128) k_adj_p2p32_tgt(AdjDev a)
 {
   __shared__ float4 Sp[ADJ_CH_T], Sa[ADJ_CH_T];
   __shared__ float  red[2][128 * 3];
+  __shared__ float4 Loff[ADJ_LG];
+  __shared__ int    Lpre[ADJ_LG + 1];
+  static_assert(ADJ_CH_T % 128 == 0 && ADJ_CH_S % 128 == 0, "every thread stages the same number of chunk elements");
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
     const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
     const int    q0 = a.p2p_start[c], q1 = a.p2p_start[c + 1];
@@ -1425,42 +1473,53 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_tgt(AdjDev a)
         pi = a.pos32[b0 + tc + tt];
         load_seeds32(a, b0 + tc + tt, ub, Jb, ct);
       }
-      int q = q0, off = 0;
-      while (q < q1) {
-        int cnt = 0;
+      for (int qg = q0; qg < q1; qg += ADJ_LG) {
+        const int ng = min(ADJ_LG, q1 - qg);
         __syncthreads();
-        while (q < q1 && cnt < ADJ_CH_T) {
-          const int   sc = a.p2p_src[q], sb = a.cv.body[sc], sn = a.cv.nbody[sc];
-          const int   take = min(sn - off, ADJ_CH_T - cnt);
-          const float ox = (float)(a.cv.x[sc] - cx), oy = (float)(a.cv.y[sc] - cy), oz = (float)(a.cv.z[sc] - cz);
-          for (int k = threadIdx.x; k < take; k += 128) {
-            const float4 p = a.pos32[sb + off + k];
-            Sp[cnt + k]    = make_float4(p.x + ox, p.y + oy, p.z + oz, p.w);
-            Sa[cnt + k]    = a.alp32[sb + off + k];
-          }
-          cnt += take;
-          off += take;
-          if (off == sn) {
-            q++;
-            off = 0;
-          }
-        }
+        if (threadIdx.x < 32)
+          stage_row_leaves(a, a.p2p_src, qg, ng, cx, cy, cz, Loff, Lpre);
         __syncthreads();
-        if (tt < nbc) {
-          float s[3] = {0.f, 0.f, 0.f};
-          for (int j = g; j < cnt; j += G) {
-            const float4 pj = Sp[j], aj = Sa[j];
-            const float  dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            if (dx * dx + dy * dy + dz * dz != 0.f) {
-              float gd[3], wa[3];
-              pair_adj32(dx, dy, dz, aj.x, aj.y, aj.z, aj.w, pj.w, ub, Jb, ct, gd, wa);
-              s[0] += gd[0];
-              s[1] += gd[1];
-              s[2] += gd[2];
+        const int total = Lpre[ng];
+        for (int c0 = 0; c0 < total; c0 += ADJ_CH_T) {
+          const int cnt = min(ADJ_CH_T, total - c0);
+          if (c0 > 0)
+            __syncthreads();
+          int lqs[ADJ_CH_T / 128];
+#pragma unroll
+          for (int i = 0; i < ADJ_CH_T / 128; i++) {
+            const int e = threadIdx.x + 128 * i;
+            lqs[i]      = e < cnt ? row_leaf_of(Lpre, ng, c0 + e) : -1;
+            if (lqs[i] >= 0) {
+              const int bi = __float_as_int(Loff[lqs[i]].w) + (c0 + e - Lpre[lqs[i]]);
+              cp_async16(Sp + e, a.pos32 + bi);
+              cp_async16(Sa + e, a.alp32 + bi);
             }
           }
-          for (int k = 0; k < 3; k++)
-            two_sum_acc(hi[k], lo[k], s[k]);
+          cp_async_wait_all();
+#pragma unroll
+          for (int i = 0; i < ADJ_CH_T / 128; i++)
+            if (lqs[i] >= 0) {
+              const int    e = threadIdx.x + 128 * i;
+              const float4 o = Loff[lqs[i]], p = Sp[e];
+              Sp[e]          = make_float4(p.x + o.x, p.y + o.y, p.z + o.z, p.w);
+            }
+          __syncthreads();
+          if (tt < nbc) {
+            float s[3] = {0.f, 0.f, 0.f};
+            for (int j = g; j < cnt; j += G) {
+              const float4 pj = Sp[j], aj = Sa[j];
+              const float  dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+              if (dx * dx + dy * dy + dz * dz != 0.f) {
+                float gd[3], wa[3];
+                pair_adj32(dx, dy, dz, aj.x, aj.y, aj.z, aj.w, pj.w, ub, Jb, ct, gd, wa);
+                s[0] += gd[0];
+                s[1] += gd[1];
+                s[2] += gd[2];
+              }
+            }
+            for (int k = 0; k < 3; k++)
+              two_sum_acc(hi[k], lo[k], s[k]);
+          }
         }
       }
       __syncthreads();
@@ -1491,6 +1550,8 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
 {
   __shared__ float4 Tp[ADJ_CH_S], Ts[ADJ_CH_S][4];
   __shared__ float  red[2][128 * 6];
+  __shared__ float4 Loff[ADJ_LG];
+  __shared__ int    Lpre[ADJ_LG + 1];
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
     const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
     const int    q0 = a.p2pT_start[c], q1 = a.p2pT_start[c + 1];
@@ -1505,48 +1566,58 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
         pj = a.pos32[b0 + tc + tt];
         aj = a.alp32[b0 + tc + tt];
       }
-      int q = q0, off = 0;
-      while (q < q1) {
-        int cnt = 0;
+      for (int qg = q0; qg < q1; qg += ADJ_LG) {
+        const int ng = min(ADJ_LG, q1 - qg);
         __syncthreads();
-        while (q < q1 && cnt < ADJ_CH_S) {
-          const int   tcell = a.p2pT_tgt[q], tb = a.cv.body[tcell], tn = a.cv.nbody[tcell];
-          const int   take = min(tn - off, ADJ_CH_S - cnt);
-          const float ox = (float)(a.cv.x[tcell] - cx), oy = (float)(a.cv.y[tcell] - cy), oz = (float)(a.cv.z[tcell] - cz);
-          for (int k = threadIdx.x; k < take; k += 128) {
-            const int    i = tb + off + k;
-            const float4 p = a.pos32[i];
-            Tp[cnt + k]    = make_float4(p.x + ox, p.y + oy, p.z + oz, 0.f);
-            for (int v = 0; v < 4; v++)
-              Ts[cnt + k][v] = a.seeds32[4 * (size_t)i + v];
-          }
-          cnt += take;
-          off += take;
-          if (off == tn) {
-            q++;
-            off = 0;
-          }
-        }
+        if (threadIdx.x < 32)
+          stage_row_leaves(a, a.p2pT_tgt, qg, ng, cx, cy, cz, Loff, Lpre);
         __syncthreads();
-        if (tt < nbc) {
-          float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-          for (int i = g; i < cnt; i += G) {
-            const float4 pi = Tp[i];
-            const float  dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            if (dx * dx + dy * dy + dz * dz != 0.f) {
-              const float4 s0 = Ts[i][0], s1 = Ts[i][1], s2 = Ts[i][2], s3 = Ts[i][3];
-              const float  ub[3] = {s0.x, s0.y, s0.z}, ct[3] = {s0.w, s1.x, s1.y};
-              const float  Jb[9] = {s1.z, s1.w, s2.x, s2.y, s2.z, s2.w, s3.x, s3.y, s3.z};
-              float        gd[3], wa[3];
-              pair_adj32(dx, dy, dz, aj.x, aj.y, aj.z, aj.w, pj.w, ub, Jb, ct, gd, wa);
-              for (int k = 0; k < 3; k++) {
-                s[k] -= gd[k];
-                s[3 + k] += wa[k];
-              }
+        const int total = Lpre[ng];
+        for (int c0 = 0; c0 < total; c0 += ADJ_CH_S) {
+          const int cnt = min(ADJ_CH_S, total - c0);
+          if (c0 > 0)
+            __syncthreads();
+          int lqs[ADJ_CH_S / 128];
+#pragma unroll
+          for (int i = 0; i < ADJ_CH_S / 128; i++) {
+            const int e = threadIdx.x + 128 * i;
+            lqs[i]      = e < cnt ? row_leaf_of(Lpre, ng, c0 + e) : -1;
+            if (lqs[i] >= 0) {
+              const int bi = __float_as_int(Loff[lqs[i]].w) + (c0 + e - Lpre[lqs[i]]);
+              cp_async16(Tp + e, a.pos32 + bi);
+              for (int v = 0; v < 4; v++)
+                cp_async16(&Ts[e][v], a.seeds32 + 4 * (size_t)bi + v);
             }
           }
-          for (int k = 0; k < 6; k++)
-            two_sum_acc(hi[k], lo[k], s[k]);
+          cp_async_wait_all();
+#pragma unroll
+          for (int i = 0; i < ADJ_CH_S / 128; i++)
+            if (lqs[i] >= 0) {
+              const int    e = threadIdx.x + 128 * i;
+              const float4 o = Loff[lqs[i]], p = Tp[e];
+              Tp[e]          = make_float4(p.x + o.x, p.y + o.y, p.z + o.z, 0.f);
+            }
+          __syncthreads();
+          if (tt < nbc) {
+            float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int i = g; i < cnt; i += G) {
+              const float4 pi = Tp[i];
+              const float  dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+              if (dx * dx + dy * dy + dz * dz != 0.f) {
+                const float4 s0 = Ts[i][0], s1 = Ts[i][1], s2 = Ts[i][2], s3 = Ts[i][3];
+                const float  ub[3] = {s0.x, s0.y, s0.z}, ct[3] = {s0.w, s1.x, s1.y};
+                const float  Jb[9] = {s1.z, s1.w, s2.x, s2.y, s2.z, s2.w, s3.x, s3.y, s3.z};
+                float        gd[3], wa[3];
+                pair_adj32(dx, dy, dz, aj.x, aj.y, aj.z, aj.w, pj.w, ub, Jb, ct, gd, wa);
+                for (int k = 0; k < 3; k++) {
+                  s[k] -= gd[k];
+                  s[3 + k] += wa[k];
+                }
+              }
+            }
+            for (int k = 0; k < 6; k++)
+              two_sum_acc(hi[k], lo[k], s[k]);
+          }
         }
       }
       __syncthreads();

@@ -267,20 +267,6 @@ __global__ void __launch_bounds__(128) k_l2l32(DevMixed a, const int *cells, int
 // m2l_lane_table.
 constexpr int M2L_YOFF = 4; // leading pad of each staged harmonic table
 
-// Asynchronous 8-byte global -> shared copy (cp.async, sm_80+) and the wait
-// for all of this thread's copies.
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
-{
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-// Asynchronous 16-byte global -> shared copy through L2 (both addresses 16-byte aligned).
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
 
 // v * 2^e, equal to ldexpf(v, e): a multiply by the exactly built power of
 // two inside the normal exponent range, ldexpf outside it.

@@ -300,4 +300,19 @@ void adjoint_rows(cudaStream_t s, const double *g, size_t cap, int n, int field,
 // ---- direct.cu
 void direct_sum(cudaStream_t s, const double *tx, const double *ty, const double *tz, int nt, const double *src, size_t scap, int ns, double *out /*12*nt*/);
 
+// Asynchronous global -> shared copies (cp.async): 8 bytes through L1, 16
+// bytes through L2 (both addresses aligned to the size), and the wait for all
+// of this thread's copies.
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 } // namespace vfmm
