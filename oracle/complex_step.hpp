@@ -512,7 +512,25 @@ struct Stepper {
     }
   }
 
-  bool advance(int scheme, double dt, int steps)
+  // Relaxation (relaxation.hpp:8-19, applied after the last stage as the
+  // restatement does): alpha = (1 - f) alpha + f |alpha| w / |w| with
+  // w = (J21 - J12, J02 - J20, J10 - J01); bodies with w = 0 keep alpha.
+  void relax_all(double f)
+  {
+#pragma omp parallel for
+    for (long i = 0; i < n; i++) {
+      BodyT<T> &q    = b[i];
+      const T   w[3] = {q.J[7] - q.J[5], q.J[2] - q.J[6], q.J[3] - q.J[1]};
+      const T   nw2  = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+      if (re(nw2) == 0.0)
+        continue;
+      const T nw = sqrt_(nw2), na = sqrt_(q.A[0] * q.A[0] + q.A[1] * q.A[1] + q.A[2] * q.A[2]);
+      for (int d = 0; d < 3; d++)
+        q.A[d] = T(1 - f) * q.A[d] + T(f) * na * w[d] / nw;
+    }
+  }
+
+  bool advance(int scheme, double dt, int steps, double relax = 0.0)
   {
     const int S = scheme == 0 ? 1 : (scheme == 1 ? 2 : (scheme == 2 ? 3 : 4));
     for (int st = 0; st < steps; st++)
@@ -522,6 +540,8 @@ struct Stepper {
           return false;
         evaluate();
         update(scheme, k, dt);
+        if (k == S - 1 && relax > 0)
+          relax_all(relax);
       }
     return true;
   }
@@ -565,16 +585,17 @@ extern "C" {
 
 // The templated FMM step with T = double: `steps` steps of scheme 0 Euler,
 // 1 RK2, 2 RK3, 3 RK4, 4 RK4 with a full-dt third stage (stretching 0
-// transposed, 1 classic); b receives X, alpha,
+// transposed, 1 classic), relaxation factor `relax` after each step's last
+// stage (0: none); b receives X, alpha,
 // velocity, J, dadt of the last stage in its tree order.  For the check
 // against vo_advance.
-int vo_cs_advance(Body *b, long n, int P, int ncrit, double theta, int scheme, int stretching, double dt, int steps)
+int vo_cs_advance(Body *b, long n, int P, int ncrit, double theta, int scheme, int stretching, double dt, int steps, double relax)
 {
   using namespace vo::cstep;
   Stepper<double> s;
   s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta;
   load(s, b, n);
-  if (!s.advance(scheme, dt, steps))
+  if (!s.advance(scheme, dt, steps, relax))
     return -1;
   for (long i = 0; i < n; i++) {
     for (int d = 0; d < 3; d++) {
@@ -591,9 +612,10 @@ int vo_cs_advance(Body *b, long n, int P, int ncrit, double theta, int scheme, i
 
 // Objective after `steps` steps (see Stepper::objective) and, for each of nd
 // directions (dirs_x, dirs_a: nd x n x 3, in the order of b), its directional
-// derivative by complex step.  value gets the real objective.
+// derivative by complex step, with relaxation factor `relax` after each
+// step's last stage (0: none).  value gets the real objective.
 int vo_cs_objective(const Body *b, long n, int P, int ncrit, double theta, int scheme, int stretching, double dt, int steps, double wE,
-                    const double *wI, const double *dirs_x, const double *dirs_a, int nd, double *value, double *deriv)
+                    const double *wI, const double *dirs_x, const double *dirs_a, int nd, double *value, double *deriv, double relax)
 {
   using namespace vo::cstep;
   const double h = 1e-30;
@@ -601,7 +623,7 @@ int vo_cs_objective(const Body *b, long n, int P, int ncrit, double theta, int s
     Stepper<double> s;
     s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta;
     load(s, b, n);
-    if (!s.advance(scheme, dt, steps))
+    if (!s.advance(scheme, dt, steps, relax))
       return -1;
     *value = s.objective(wE, wI);
     if (!s.ok)
@@ -616,7 +638,7 @@ int vo_cs_objective(const Body *b, long n, int P, int ncrit, double theta, int s
         s.b[i].X[d].i = h * dirs_x[((size_t)k * n + i) * 3 + d];
         s.b[i].A[d].i = h * dirs_a[((size_t)k * n + i) * 3 + d];
       }
-    if (!s.advance(scheme, dt, steps))
+    if (!s.advance(scheme, dt, steps, relax))
       return -1;
     const CS v = s.objective(wE, wI);
     if (!s.ok)

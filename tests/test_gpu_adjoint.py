@@ -127,13 +127,13 @@ def test_mixed_gradient_close_to_fp64(vfmm_lib):
 def test_adjoint_rejects_what_it_does_not_cover(vfmm_lib):
     from uvlm_gb300 import FMMCalculator, VfmmError, workloads
     b = workloads.cloud(500, seed=8)
-    for kw in (dict(formulation="rVPM"), dict(viscous="PSE", nu=0.01), dict(relax=0.3)):
+    for kw in (dict(formulation="rVPM"), dict(viscous="PSE", nu=0.01), dict(viscous="CSM", nu=0.01)):
         with FMMCalculator(p=4, ncrit=32, theta=0.5, **kw) as c:
             with pytest.raises(VfmmError):
                 c.adjoint(b, 0.01, 1)
 
 
-def _complex_step(b, P, ncrit, theta, scheme, dt, steps, dirs_x, dirs_a, energy=1.0, impulse=(0.0, 0.0, 1.0)):
+def _complex_step(b, P, ncrit, theta, scheme, dt, steps, dirs_x, dirs_a, energy=1.0, impulse=(0.0, 0.0, 1.0), relax=0.0):
     import ctypes
     from oracle.oracle import oracle
     L = oracle()
@@ -142,7 +142,7 @@ def _complex_step(b, P, ncrit, theta, scheme, dt, steps, dirs_x, dirs_a, energy=
     val, der = ctypes.c_double(), np.zeros(nd)
     dx, da = np.ascontiguousarray(dirs_x), np.ascontiguousarray(dirs_a)
     assert L.vo_cs_objective(b.ctypes.data, n, P, ncrit, theta, scheme, 0, dt, steps, energy, wI.ctypes.data, dx.ctypes.data,
-                             da.ctypes.data, nd, ctypes.byref(val), der.ctypes.data) == 0
+                             da.ctypes.data, nd, ctypes.byref(val), der.ctypes.data, relax) == 0
     return val.value, der
 
 
@@ -169,6 +169,33 @@ def test_gradient_matches_complex_step(vfmm_lib, theta, steps, integration, rk4_
     for k in range(nd):
         an = float((gx * dx[k]).sum() + (ga * da[k]).sum())
         assert abs(an - der[k]) <= 1e-8 * abs(der[k]), (k, an, der[k])
+
+
+@pytest.mark.parametrize("integration,scheme", [("RK2", 1), ("RK3", 2)])
+def test_gradient_with_relaxation(vfmm_lib, integration, scheme):
+    """Relaxation after each step (relaxation.hpp:8-19): the adjoint against
+    the oracle's complex step of the same relaxed steps, and against central
+    differences.  The ring of seed 5: on it the oracle's one-sided differences
+    along these directions agree to rounding for both schemes (on the rings
+    of seeds 2 and 3 relaxation puts the map on a branch boundary)."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.ring(16, seed=5)
+    rng = np.random.default_rng(13)
+    nd = 3
+    dx = rng.normal(size=(nd, b.size, 3))
+    da = rng.normal(size=(nd, b.size, 3)) * np.abs(b["alpha"]).max()
+    with FMMCalculator(p=8, ncrit=32, theta=0.47, integration=integration, relax=0.3) as c:
+        v, gx, ga = c.adjoint(b, 0.02, 2, 1)
+        _, _, _, errs = fd_check(c, b, 0.02, 2, every=1, nd=2, h=1e-8, seed=4)
+    assert worst(errs) < 1e-5, errs
+    vc, der = _complex_step(b, 8, 32, 0.47, scheme, 0.02, 2, dx, da, relax=0.3)
+    assert abs(v - vc) <= 1e-10 * abs(vc)
+    for k in range(nd):
+        an = float((gx * dx[k]).sum() + (ga * da[k]).sum())
+        assert abs(an - der[k]) <= 1e-8 * abs(der[k]), (k, an, der[k])
+    with FMMCalculator(p=8, ncrit=32, theta=0.47, integration=integration) as c:
+        v0, gx0, _ = c.adjoint(b, 0.02, 2, 1)
+    assert abs(v0 - v) > 1e-6 * abs(v) and not np.allclose(gx0, gx), "relaxation made no difference"
 
 
 def test_mixed_evaluation_gradient_close_to_fp64(vfmm_lib):

@@ -10,13 +10,19 @@ from oracle.oracle import oracle
 from uvlm_gb300 import workloads
 
 
+def advance_plain(L, b, scheme):
+    bb = b.copy()
+    assert L.vo_cs_advance(bb.ctypes.data, bb.size, 8, 32, 0.5, scheme, 0, 0.02, 2, 0.0) == 0
+    return bb
+
+
 def test_templated_step_equals_the_reference_restatement():
     L = oracle()
     b = workloads.ring(16, seed=3)
     n = b.size
     b1, b2 = b.copy(), b.copy()
     assert L.vo_advance(b1.ctypes.data, n, 8, 32, 0.5, 0.02, 2, 2, 0, 0, 0.0, 0, 0, 0.0) == 0
-    assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, 2, 0, 0.02, 2) == 0
+    assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, 2, 0, 0.02, 2, 0.0) == 0
     for f, tol in (("X", 1e-14), ("alpha", 1e-14), ("velocity", 1e-12), ("J", 1e-11), ("dadt", 1e-11)):
         a, r = b2[f].reshape(n, -1), b1[f].reshape(n, -1)
         assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), f
@@ -31,10 +37,26 @@ def test_templated_rk4_equals_the_reference_restatement():
     for fixed in (0, 1):
         b1, b2 = b.copy(), b.copy()
         assert L.vo_advance(b1.ctypes.data, n, 8, 32, 0.5, 0.02, 2, 3, 0, 0, 0.0, fixed, 0, 0.0) == 0
-        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, 3 + fixed, 0, 0.02, 2) == 0
+        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, 3 + fixed, 0, 0.02, 2, 0.0) == 0
         for f, tol in (("X", 1e-14), ("alpha", 1e-14), ("velocity", 1e-12), ("J", 1e-11), ("dadt", 1e-11)):
             a, r = b2[f].reshape(n, -1), b1[f].reshape(n, -1)
             assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), (fixed, f)
+
+
+def test_templated_step_with_relaxation_equals_the_reference_restatement():
+    """Relaxation after each step's last stage (relaxation.hpp:8-19) in the
+    templated step against vo_advance's."""
+    L = oracle()
+    b = workloads.ring(16, seed=5)
+    n = b.size
+    for scheme in (0, 2):
+        b1, b2 = b.copy(), b.copy()
+        assert L.vo_advance(b1.ctypes.data, n, 8, 32, 0.5, 0.02, 2, scheme, 0, 0, 0.3, 0, 0, 0.0) == 0
+        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, scheme, 0, 0.02, 2, 0.3) == 0
+        for f, tol in (("X", 1e-14), ("alpha", 1e-13), ("velocity", 1e-12), ("J", 1e-11), ("dadt", 1e-11)):
+            a, r = b2[f].reshape(n, -1), b1[f].reshape(n, -1)
+            assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), (scheme, f)
+        assert not np.allclose(b2["alpha"], advance_plain(L, b, scheme)["alpha"], rtol=1e-6), "relaxation changed nothing"
 
 
 def test_complex_step_against_central_differences():
@@ -50,7 +72,7 @@ def test_complex_step_against_central_differences():
         v, der = ctypes.c_double(), np.zeros(1)
         args = (dx.ctypes.data, da.ctypes.data, 1) if dirs else (None, None, 0)
         assert L.vo_cs_objective(bb.ctypes.data, n, 8, 32, 0.47, 2, 0, 0.02, 1, 1.0, wI.ctypes.data, *args, ctypes.byref(v),
-                                 der.ctypes.data) == 0
+                                 der.ctypes.data, 0.0) == 0
         return v.value, der[0]
 
     _, cs = value(b, True)

@@ -988,7 +988,7 @@ __global__ void __launch_bounds__(128) k_adj_p2p_src(AdjDev a)
 // Seeds of an evaluation from the stage cotangent (cu, ca) of (u, dalpha/dt):
 // ubar = cu and, for dalpha/dt = J^T alpha (transposed) or J alpha
 // (classic), Jbar and the direct alphabar.
-__global__ void k_adj_seeds(const double *soa, double *w, size_t cap, int n, int stretching)
+__global__ void k_adj_seeds(const double *soa, double *w, size_t cap, int n, int stretching, int add_relax)
 {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     auto         S  = [&](int f) -> double & { return w[(size_t)f * cap + i]; };
@@ -1003,11 +1003,50 @@ __global__ void k_adj_seeds(const double *soa, double *w, size_t cap, int n, int
         // classic:    dadt_r  = sum_c J[r][c] alpha_c  -> Jbar[r][c]  = ca_r alpha_c
         S(W_SJ + 3 * r + cc) = stretching == VFMM_TRANSPOSED ? al[r] * ca[cc] : ca[r] * al[cc];
       }
+    if (add_relax) { // w = (J21 - J12, J02 - J20, J10 - J01) of the relaxation after this stage
+      const double wb[3] = {S(W_WB), S(W_WB + 1), S(W_WB + 2)};
+      S(W_SJ + 7) += wb[0];
+      S(W_SJ + 5) -= wb[0];
+      S(W_SJ + 2) += wb[1];
+      S(W_SJ + 6) -= wb[1];
+      S(W_SJ + 3) += wb[2];
+      S(W_SJ + 1) -= wb[2];
+    }
     for (int cc = 0; cc < 3; cc++) {
       double v = 0;
       for (int r = 0; r < 3; r++)
         v += (stretching == VFMM_TRANSPOSED ? Bf(F_J + 3 * cc + r) : Bf(F_J + 3 * r + cc)) * ca[r];
       S(W_ASTR + cc) = v;
+    }
+  }
+}
+
+// Transposed relaxation (relaxation.hpp:8-19 as bodies.cu relax_one applies
+// it after a step's last stage update): alpha' = (1 - f) alpha_u + f |alpha_u|
+// w / |w| with w = (J21 - J12, J02 - J20, J10 - J01) of the stage's
+// evaluation.  g[AB] holds the cotangent of alpha' and leaves with that of
+// alpha_u; w[W_WB] gets the cotangent of w, which k_adj_seeds adds to the J
+// seeds.  Where w = 0 relaxation is the identity.
+__global__ void k_adj_relax(double *g, double *w, const double *soa, const double *au, size_t cap, int n, double f)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    auto         J     = [&](int k) { return soa[(size_t)(F_J + k) * cap + i]; };
+    const double om[3] = {J(7) - J(5), J(2) - J(6), J(3) - J(1)};
+    const double nw    = sqrt(om[0] * om[0] + om[1] * om[1] + om[2] * om[2]);
+    double      *wb    = w + (size_t)W_WB * cap + i;
+    if (nw == 0.0) {
+      wb[0] = wb[cap] = wb[2 * cap] = 0.0;
+      continue;
+    }
+    const double a[3]  = {au[i], au[cap + i], au[2 * cap + i]};
+    const double na    = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    double      *ab    = g + (size_t)G_AB * cap + i;
+    const double ga[3] = {ab[0], ab[cap], ab[2 * cap]};
+    const double wh[3] = {om[0] / nw, om[1] / nw, om[2] / nw};
+    const double dot   = wh[0] * ga[0] + wh[1] * ga[1] + wh[2] * ga[2]; // d alpha'/d|alpha_u| . gbar
+    for (int d = 0; d < 3; d++) {
+      ab[(size_t)d * cap] = (1 - f) * ga[d] + (na > 0 ? f * dot * a[d] / na : 0.0);
+      wb[(size_t)d * cap] = f * na / nw * (ga[d] - dot * wh[d]);
     }
   }
 }
@@ -2014,9 +2053,16 @@ void adjoint_eval(cudaStream_t s, const ExpArgs &e, const AdjBufs &b, const DevI
   VFMM_LAUNCH_CHECK();
 }
 
-void adjoint_seeds(cudaStream_t s, const double *soa, double *w, size_t cap, int n, int stretching)
+void adjoint_seeds(cudaStream_t s, const double *soa, double *w, size_t cap, int n, int stretching, int add_relax)
 {
-  k_adj_seeds<<<grid_for(n, 256), 256, 0, s>>>(soa, w, cap, n, stretching);
+  k_adj_seeds<<<grid_for(n, 256), 256, 0, s>>>(soa, w, cap, n, stretching, add_relax);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+void adjoint_relax(cudaStream_t s, double *g, double *w, const double *soa, const double *alpha_u, size_t cap, int n, double f)
+{
+  k_adj_relax<<<grid_for(n, 256), 256, 0, s>>>(g, w, soa, alpha_u, cap, n, f);
   count_launch();
   VFMM_LAUNCH_CHECK();
 }

@@ -665,7 +665,9 @@ void rbf(vfmm_handle h, vfmm_body *particles, size_t n, vfmm_body *points, size_
   h->has_eval = false; // the particle tree is current, its expansions are not
 }
 
-void stage_update(vfmm_handle h, int stage, double dt)
+// relax = false leaves out the relaxation after the last stage (the caller
+// applies it with relax_bodies: the same arithmetic on the same values).
+void stage_update(vfmm_handle h, int stage, double dt, bool relax = true)
 {
   StageArgs a{};
   a.scheme        = h->cfg.integrator;
@@ -676,7 +678,7 @@ void stage_update(vfmm_handle h, int stage, double dt)
   a.store_initial = (stage == 0 && (a.scheme == VFMM_RK2 || a.scheme == VFMM_RK4)) ? 1 : 0;
   a.do_update     = 1;
   a.dt            = dt;
-  a.relax         = (stage == stages_of(a.scheme) - 1) ? h->cfg.relax : 0.0;
+  a.relax         = (relax && stage == stages_of(a.scheme) - 1) ? h->cfg.relax : 0.0;
   a.csm           = h->cfg.viscous == VFMM_CSM;
   a.nu            = h->cfg.nu;
   finish_and_update(h->stream, h->soa[h->cur].p, h->cap, h->n, a);
@@ -1032,8 +1034,8 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
              double *gx, double *ga)
 {
   const vfmm_config &c = h->cfg;
-  if (c.formulation != VFMM_CVPM || c.viscous != VFMM_INVISCID || c.relax != 0)
-    throw Error(VFMM_ERR_UNSUPPORTED, "the adjoint covers the inviscid cVPM path without relaxation");
+  if (c.formulation != VFMM_CVPM || c.viscous != VFMM_INVISCID)
+    throw Error(VFMM_ERR_UNSUPPORTED, "the adjoint covers the inviscid cVPM path");
   if (!bodies || !obj || !value)
     throw Error(VFMM_ERR_INVALID, "null argument");
   if (steps < 0 || every < 1)
@@ -1160,6 +1162,10 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
     std::swap(h->ts.perm, x.perm);
   };
   const size_t nbody_fields = (size_t)(F_A + 3) * cap; // J, X, alpha: fields 0 .. F_A+2
+  // with relaxation, the last stage's context also keeps alpha after the
+  // update and before the relaxation, which the transposed relaxation needs
+  const bool   relax        = c.relax > 0;
+  auto relaxed_stage = [&](int k) { return relax && k == S - 1; };
   // reverse sweep: per segment, recompute its steps from the checkpoint
   // keeping every stage's evaluation context, then run the stages backwards
   for (int seg = nck - 1; seg >= 0; seg--) {
@@ -1170,14 +1176,20 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
         Ctx &x = A.ctx[(size_t)(st - st0) * S + k];
         build_tree_and_lists(h);
         calculate(h);
-        x.body.reserve(nbody_fields + cap);
+        x.body.reserve(nbody_fields + cap + (relaxed_stage(k) ? 3 * cap : 0));
         x.info.reserve(1);
         VFMM_CUDA_TRY(cudaMemcpyAsync(x.body.p, h->soa[h->cur].p, nbody_fields * sizeof(double), cudaMemcpyDeviceToDevice, s));
         VFMM_CUDA_TRY(cudaMemcpyAsync(x.body.p + nbody_fields, h->soa[h->cur].p + (size_t)F_R * cap, cap * sizeof(double),
                                       cudaMemcpyDeviceToDevice, s));
         VFMM_CUDA_TRY(cudaMemcpyAsync(x.info.p, h->info, sizeof(DevInfo), cudaMemcpyDeviceToDevice, s));
         exchange(x);
-        stage_update(h, k, dt);
+        if (relaxed_stage(k)) {
+          stage_update(h, k, dt, false);
+          VFMM_CUDA_TRY(cudaMemcpyAsync(x.body.p + nbody_fields + cap, h->soa[h->cur].p + (size_t)F_A * cap, 3 * cap * sizeof(double),
+                                        cudaMemcpyDeviceToDevice, s));
+          relax_bodies(s, h->soa[h->cur].p, cap, N, c.relax);
+        } else
+          stage_update(h, k, dt);
       }
     for (int st = st1 - 1; st >= st0; st--)
       for (int k = S - 1; k >= 0; k--) {
@@ -1186,8 +1198,10 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
         VFMM_CUDA_TRY(cudaMemcpyAsync(h->soa[h->cur].p, x.body.p, nbody_fields * sizeof(double), cudaMemcpyDeviceToDevice, s));
         VFMM_CUDA_TRY(cudaMemcpyAsync(h->soa[h->cur].p + (size_t)F_R * cap, x.body.p + nbody_fields, cap * sizeof(double),
                                       cudaMemcpyDeviceToDevice, s));
+        if (relaxed_stage(k))
+          adjoint_relax(s, A.g[gc].p, A.w.p, h->soa[h->cur].p, x.body.p + nbody_fields + cap, cap, N, c.relax);
         adjoint_stage_pre(s, A.g[gc].p, A.w.p, cap, N, c.integrator, k, dt, c.rk4_fixed);
-        adjoint_seeds(s, h->soa[h->cur].p, A.w.p, cap, N, c.stretching);
+        adjoint_seeds(s, h->soa[h->cur].p, A.w.p, cap, N, c.stretching, relaxed_stage(k));
         vjp(x.info.p);
       }
   }
