@@ -166,7 +166,7 @@ P2P_FLOPS = 84  # per body-body interaction, counted from multipoleKernels.hpp:2
 # DRAM bytes (read + write) per unit of the two mixed-precision evaluation
 # kernels at p = 10, from one ncu capture of a 2^19-body cloud
 # (profiles/k_m2l32v2_k_l2p_p2p32_cloud512K_p10.md): per M2L pair, per body.
-NCU_TRAFFIC_MIXED_P10 = {"m2l": 361.1e6 / 3881744, "l2p_p2p": 172.0e6 / 524288}
+NCU_TRAFFIC_MIXED_P10 = {"m2l": 359.0e6 / 3881744, "l2p_p2p": 170.9e6 / 524288}
 
 
 def measured_peaks() -> dict:
