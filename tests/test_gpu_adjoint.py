@@ -198,14 +198,17 @@ def test_gradient_with_relaxation(vfmm_lib, integration, scheme):
     assert abs(v0 - v) > 1e-6 * abs(v) and not np.allclose(gx0, gx), "relaxation made no difference"
 
 
-def test_mixed_evaluation_gradient_close_to_fp64(vfmm_lib):
-    """One evaluation (steps = 0) of a cloud at high order: the FP32 transposes
-    against the FP64 ones."""
+@pytest.mark.parametrize("n,p,ncrit,theta", [(20000, 12, 64, 0.5), (8000, 8, 16, 0.3)])
+def test_mixed_evaluation_gradient_close_to_fp64(vfmm_lib, n, p, ncrit, theta):
+    """One evaluation (steps = 0) of a cloud: the FP32 transposes against the
+    FP64 ones.  At theta = 0.3 (the reference's default) and leaves of 16 most
+    P2P rows span more than 32 leaves, so the transposed P2P kernels stage
+    their rows in several groups."""
     from uvlm_gb300 import FMMCalculator, workloads
-    b = workloads.cloud(20000, seed=12)
+    b = workloads.cloud(n, seed=12)
     res = {}
     for prec in ("fp64", "mixed"):
-        with FMMCalculator(p=12, ncrit=64, theta=0.5, integration="Euler", precision=prec) as c:
+        with FMMCalculator(p=p, ncrit=ncrit, theta=theta, integration="Euler", precision=prec) as c:
             res[prec] = c.adjoint(b, 0.01, 0)
     for k in (1, 2):
         a, r = res["mixed"][k], res["fp64"][k]
