@@ -284,14 +284,15 @@ void read_info(vfmm_handle h) { read_info(h->stream, h->info, h->hinfo); }
 // Tree of the n bodies in soa[cur] (field-major, capacity cap).  The bodies
 // are gathered into tree order in soa[cur ^ 1] and cur flips, as buildTree
 // permutes its bodies (tree.hpp:101-113).  One host sync (node counts).
+// `fields` selects the body fields carried into the new order (all by default).
 void tree_enqueue(cudaStream_t s, DevBuf<double> *soa, int &cur, size_t cap, int n, int ncrit, DevInfo *info, DevInfo *hinfo, TreeScratch &ts,
-                  Tree &t)
+                  Tree &t, uint64_t fields = (1ull << NFIELD) - 1)
 {
   VFMM_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(DevInfo), s));
   check_finite(s, soa[cur].p, cap, n, info);
   tree_bounds(s, soa[cur].p + (size_t)F_X * cap, cap, n, info, ts);
   tree_sort_bodies(s, soa[cur].p + (size_t)F_X * cap, cap, n, ncrit, info, ts);
-  gather_bodies(s, soa[cur].p, soa[cur ^ 1].p, cap, ts.perm.p, n, (1ull << NFIELD) - 1);
+  gather_bodies(s, soa[cur].p, soa[cur ^ 1].p, cap, ts.perm.p, n, fields);
   cur ^= 1;
   const int nncap = n + MAXL * (n / (ncrit + 1)) + 64;
   for (auto *b : {&t.nchild, &t.nbody, &t.child, &t.body, &t.level, &t.parent, &t.level_cells, &t.leaf_cells})
@@ -321,9 +322,9 @@ void tree_finish(cudaStream_t s, DevInfo *hinfo, Tree &t)
 }
 
 void build_tree(cudaStream_t s, DevBuf<double> *soa, int &cur, size_t cap, int n, int ncrit, DevInfo *info, DevInfo *hinfo, TreeScratch &ts,
-                Tree &t)
+                Tree &t, uint64_t fields = (1ull << NFIELD) - 1)
 {
-  tree_enqueue(s, soa, cur, cap, n, ncrit, info, hinfo, ts, t);
+  tree_enqueue(s, soa, cur, cap, n, ncrit, info, hinfo, ts, t, fields);
   tree_finish(s, hinfo, t);
 }
 
@@ -385,15 +386,24 @@ void build_lists(cudaStream_t s, Tree &tt, Tree &st, double theta, DevInfo *info
   }
 }
 
-// Tree and lists of the bodies in soa[cur]; bodies are reordered into tree order.
-void build_tree_and_lists(vfmm_handle h)
+// Tree and lists of the bodies in soa[cur]; bodies are reordered into tree
+// order.  for_evaluation: an evaluation follows that rewrites velocity, J and
+// dadt of every body before anything reads them, so those fields are not
+// carried into the new order.
+void build_tree_and_lists(vfmm_handle h, bool for_evaluation = false)
 {
   cudaStream_t s = h->stream;
   h->has_tree    = false;
   h->has_eval    = false;
   if (h->timing)
     VFMM_CUDA_TRY(cudaEventRecord(h->ph[0], s));
-  build_tree(s, h->soa, h->cur, h->cap, h->n, h->cfg.ncrit, h->info, h->hinfo, h->ts, h->tree);
+  uint64_t fields = (1ull << NFIELD) - 1;
+  if (for_evaluation) {
+    const int outputs[] = {F_J, F_J + 1, F_J + 2, F_J + 3, F_J + 4, F_J + 5, F_J + 6, F_J + 7, F_J + 8, F_U, F_U + 1, F_U + 2, F_DADT, F_DADT + 1, F_DADT + 2};
+    for (int f : outputs)
+      fields &= ~(1ull << f);
+  }
+  build_tree(s, h->soa, h->cur, h->cap, h->n, h->cfg.ncrit, h->info, h->hinfo, h->ts, h->tree, fields);
   build_lists(s, h->tree, h->tree, h->cfg.theta, h->info, h->hinfo, h->lists, &h->info->p2p_interactions);
   if (h->timing)
     VFMM_CUDA_TRY(cudaEventRecord(h->ph[1], s));
@@ -700,7 +710,7 @@ void evaluate_and_update(vfmm_handle h, int stage, double dt)
 
 void run_stage(vfmm_handle h, int stage, double dt)
 {
-  build_tree_and_lists(h);
+  build_tree_and_lists(h, true);
   evaluate_and_update(h, stage, dt);
 }
 
@@ -1074,7 +1084,7 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
     if (grad && st % every == 0)
       save_state(h, A.ckpt.p + (size_t)(st / every) * slot);
     for (int k = 0; k < S; k++) {
-      build_tree_and_lists(h);
+      build_tree_and_lists(h, true);
       track();
       evaluate_and_update(h, k, dt);
     }
@@ -1082,7 +1092,7 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
   // the objective on the final state; evaluations of the reverse sweep run in
   // the handle's precision (mixed: FP32 P2P^T and M2L^T, the rest FP64)
   const bool mixed = c.precision == VFMM_MIXED;
-  build_tree_and_lists(h);
+  build_tree_and_lists(h, true);
   track();
   calculate(h);
   for (auto *b : {&A.g[0], &A.g[1]})
@@ -1174,7 +1184,7 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
     for (int st = st0; st < st1; st++)
       for (int k = 0; k < S; k++) {
         Ctx &x = A.ctx[(size_t)(st - st0) * S + k];
-        build_tree_and_lists(h);
+        build_tree_and_lists(h, true);
         calculate(h);
         x.body.reserve(nbody_fields + cap + (relaxed_stage(k) ? 3 * cap : 0));
         x.info.reserve(1);
