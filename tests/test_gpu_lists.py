@@ -52,3 +52,35 @@ def test_mixed_mode_degenerate_bounding_box(vfmm_lib):
                 c.advance(bb, 0.01)
             assert np.isfinite(bb["velocity"]).all() and np.isfinite(bb["J"]).all()
             assert np.array_equal(bb["X"], b["X"]) and np.array_equal(bb["alpha"], b["alpha"])
+
+
+def test_tree_deeper_than_the_key_hint(vfmm_lib):
+    """A tree build computes keys only a few levels below the depth of the
+    tree its handle built last (at least 8 levels) and rebuilds with full
+    keys when a cell at that depth still holds more than ncrit bodies.  A
+    handle whose previous tree was shallow then gets a cluster 12 levels
+    deep: tree, lists and body order must equal a fresh handle's, as must
+    an advance step through the same two trees."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    shallow = workloads.cloud(3000, seed=1)
+    deep = workloads.cloud(6000, seed=2)
+    deep["X"][:300] = deep["X"][0] + 1e-5 * np.random.default_rng(3).normal(size=(300, 3))
+    out = []
+    for warm in (True, False):
+        with FMMCalculator(p=6, ncrit=16, theta=0.5) as c:
+            if warm:
+                b0 = shallow.copy()
+                c.init(b0)
+                assert c.stats()["max_level"] <= 4
+            b = deep.copy()
+            c.init(b)
+            cells = c.tree()
+            p2p, m2l = c.lists()
+            depth = c.stats()["max_level"]
+            c.calculate()
+            c.copyBodies2Host(b)
+            out.append((b, cells, p2p, m2l, depth))
+    (b1, c1, p1, m1, d1), (b2, c2, p2, m2, d2) = out
+    assert d1 == d2 and d1 > 11
+    assert np.array_equal(b1, b2) and np.array_equal(c1, c2)
+    assert np.array_equal(p1, p2) and np.array_equal(m1, m2)

@@ -291,16 +291,27 @@ void tree_enqueue(cudaStream_t s, DevBuf<double> *soa, int &cur, size_t cap, int
   VFMM_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(DevInfo), s));
   check_finite(s, soa[cur].p, cap, n, info);
   tree_bounds(s, soa[cur].p + (size_t)F_X * cap, cap, n, info, ts);
-  tree_sort_bodies(s, soa[cur].p + (size_t)F_X * cap, cap, n, ncrit, info, ts);
-  gather_bodies(s, soa[cur].p, soa[cur ^ 1].p, cap, ts.perm.p, n, fields);
-  cur ^= 1;
   const int nncap = n + MAXL * (n / (ncrit + 1)) + 64;
   for (auto *b : {&t.nchild, &t.nbody, &t.child, &t.body, &t.level, &t.parent, &t.level_cells, &t.leaf_cells})
     b->reserve(nncap);
   for (auto *b : {&t.x, &t.y, &t.z, &t.R})
     b->reserve(nncap);
   t.level_start.reserve(MAXL + 2);
-  tree_build_cells(s, n, ncrit, nncap, info, ts, t.view(), t.level_cells.p, t.level_start.p, t.leaf_cells.p);
+  // Keys only a few levels below the tree this Tree last held (at least 8
+  // levels: 24 bits, three radix passes instead of eight); the full 21 levels
+  // for a first build or when a cell at that depth holds more than ncrit
+  // bodies.  Leaves, cells and body order do not depend on the key depth as
+  // long as every leaf lies above it.
+  int levels = t.ncells > 0 ? std::min(MAXL, std::max(8, t.maxLevel + 3)) : MAXL;
+  for (;;) {
+    tree_sort_bodies(s, soa[cur].p + (size_t)F_X * cap, cap, n, ncrit, levels, info, ts);
+    gather_bodies(s, soa[cur].p, soa[cur ^ 1].p, cap, ts.perm.p, n, fields);
+    if (tree_build_cells(s, n, ncrit, nncap, info, ts, t.view(), t.level_cells.p, t.level_start.p, t.leaf_cells.p))
+      break;
+    levels = MAXL; // soa[cur] still holds the incoming order
+    VFMM_CUDA_TRY(cudaMemsetAsync(&info->deeper, 0, sizeof(int), s));
+  }
+  cur ^= 1;
   VFMM_CUDA_TRY(cudaMemcpyAsync(t.level_start_host, t.level_start.p, sizeof(int) * (MAXL + 2), cudaMemcpyDeviceToHost, s));
   VFMM_CUDA_TRY(cudaMemcpyAsync(hinfo, info, sizeof(DevInfo), cudaMemcpyDeviceToHost, s));
 }

@@ -132,8 +132,10 @@ __device__ __forceinline__ bool dgreater(double a, double b)
   return ka > kb;
 }
 
+// Octant keys of the first `levels` levels (the digit of level l at bits
+// 3 (MAXL - 1 - l), deeper digits zero).
 __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, int n, const DevInfo *info,
-                       uint64_t *keys, uint32_t *idx)
+                       int levels, uint64_t *keys, uint32_t *idx)
 {
   // the centre chain's half-widths R0 / 2^(l+1), the same division for every body
   __shared__ double half[MAXL];
@@ -145,7 +147,7 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
     double       c[3] = {info->X0[0], info->X0[1], info->X0[2]};
     uint64_t     key  = 0;
 #pragma unroll 1
-    for (int l = 0; l < MAXL; l++) {
+    for (int l = 0; l < levels; l++) {
       const int b0 = dgreater(p[0], c[0]), b1 = dgreater(p[1], c[1]), b2 = dgreater(p[2], c[2]);
       key          = (key << 3) | (uint64_t)(b0 | (b1 << 1) | (b2 << 2));
       const double r = half[l];
@@ -153,19 +155,21 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
       c[1]           = __dadd_rn(c[1], b1 ? r : -r);
       c[2]           = __dadd_rn(c[2], b2 ? r : -r);
     }
-    keys[i] = key;
+    keys[i] = levels < MAXL ? key << (3 * (MAXL - levels)) : key;
     idx[i]  = (uint32_t)i;
   }
 }
 
 // Leaf level of each sorted body: the shallowest level whose prefix count is
-// <= ncrit (tree.hpp:43: a cell with <= ncrit bodies is a leaf).
-__global__ void k_leaf_level(const uint64_t *__restrict__ sk, int n, int ncrit, int *lvl, int *lo, int *hi, DevInfo *info)
+// <= ncrit (tree.hpp:43: a cell with <= ncrit bodies is a leaf).  Keys of
+// `levels` < MAXL levels that leave a cell at that depth with more than ncrit
+// bodies set info->deeper (the build is redone with full keys).
+__global__ void k_leaf_level(const uint64_t *__restrict__ sk, int n, int ncrit, int levels, int *lvl, int *lo, int *hi, DevInfo *info)
 {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint64_t key = sk[i];
     int            a = 0, b = n, L = -1;
-    for (int l = 0; l <= MAXL; l++) {
+    for (int l = 0; l <= levels; l++) {
       if (l > 0) {
         const int      sh = 3 * (MAXL - l);
         const uint64_t p  = key >> sh;
@@ -178,8 +182,11 @@ __global__ void k_leaf_level(const uint64_t *__restrict__ sk, int n, int ncrit, 
       }
     }
     if (L < 0) {
-      atomicExch(&info->err, (int)VFMM_ERR_DEPTH);
-      L = MAXL;
+      if (levels < MAXL)
+        atomicExch(&info->deeper, 1);
+      else
+        atomicExch(&info->err, (int)VFMM_ERR_DEPTH);
+      L = levels;
     }
     lvl[i] = L;
     lo[i]  = a;
@@ -383,7 +390,7 @@ static void cub_call(TreeScratch &ts, F f)
 
 // Steps 2-5: keys, sort, leaf levels and the final body permutation
 // (ts.perm[p] = incoming index of the body at tree position p).
-void tree_sort_bodies(cudaStream_t s, const double *X, size_t cap, int n, int ncrit, DevInfo *info, TreeScratch &ts)
+void tree_sort_bodies(cudaStream_t s, const double *X, size_t cap, int n, int ncrit, int levels, DevInfo *info, TreeScratch &ts)
 {
   ts.keys.reserve(n);
   ts.skeys.reserve(n);
@@ -396,14 +403,14 @@ void tree_sort_bodies(cudaStream_t s, const double *X, size_t cap, int n, int nc
   ts.cnt.reserve(n);
   ts.off.reserve(n);
   const int g = grid_for(n, 256);
-  k_keys<<<g, 256, 0, s>>>(X, X + cap, X + 2 * cap, n, info, ts.keys.p, ts.idx.p);
+  k_keys<<<g, 256, 0, s>>>(X, X + cap, X + 2 * cap, n, info, levels, ts.keys.p, ts.idx.p);
   count_launch();
   VFMM_LAUNCH_CHECK();
   cub_call(ts, [&](void *tmp, size_t &bytes) {
-    return cub::DeviceRadixSort::SortPairs(tmp, bytes, ts.keys.p, ts.skeys.p, ts.idx.p, ts.sidx.p, n, 0, 3 * MAXL, s);
+    return cub::DeviceRadixSort::SortPairs(tmp, bytes, ts.keys.p, ts.skeys.p, ts.idx.p, ts.sidx.p, n, 3 * (MAXL - levels), 3 * MAXL, s);
   });
   count_launch();
-  k_leaf_level<<<g, 256, 0, s>>>(ts.skeys.p, n, ncrit, ts.lvl.p, ts.lo.p, ts.hi.p, info);
+  k_leaf_level<<<g, 256, 0, s>>>(ts.skeys.p, n, ncrit, levels, ts.lvl.p, ts.lo.p, ts.hi.p, info);
   count_launch();
   k_leaf_perm<<<g, 256, 0, s>>>(ts.sidx.p, ts.lo.p, ts.hi.p, n, ts.perm.p);
   count_launch();
@@ -411,7 +418,7 @@ void tree_sort_bodies(cudaStream_t s, const double *X, size_t cap, int n, int nc
 }
 
 // Step 6.  `nncap` bounds the node count (n + MAXL*n/(ncrit+1) + 64).
-void tree_build_cells(cudaStream_t s, int n, int ncrit, int nncap, DevInfo *info, TreeScratch &ts, CellsView cv, int *level_cells, int *level_start,
+bool tree_build_cells(cudaStream_t s, int n, int ncrit, int nncap, DevInfo *info, TreeScratch &ts, CellsView cv, int *level_cells, int *level_start,
                       int *leaf_cells)
 {
   const int g = grid_for(n, 256);
@@ -435,10 +442,13 @@ void tree_build_cells(cudaStream_t s, int n, int ncrit, int nncap, DevInfo *info
   count_launch();
   VFMM_LAUNCH_CHECK();
   // The node count is needed on the host for the radix sort and scans below.
-  int h_off = 0, h_cnt = 0;
+  int h_off = 0, h_cnt = 0, h_deeper = 0;
   VFMM_CUDA_TRY(cudaMemcpyAsync(&h_off, ts.off.p + (n - 1), sizeof(int), cudaMemcpyDeviceToHost, s));
   VFMM_CUDA_TRY(cudaMemcpyAsync(&h_cnt, ts.cnt.p + (n - 1), sizeof(int), cudaMemcpyDeviceToHost, s));
+  VFMM_CUDA_TRY(cudaMemcpyAsync(&h_deeper, &info->deeper, sizeof(int), cudaMemcpyDeviceToHost, s));
   VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h_deeper)
+    return false;
   const int nn = h_off + h_cnt;
   if (nn > nncap)
     throw Error(VFMM_ERR_CAPACITY, "tree node capacity exceeded");
@@ -471,6 +481,7 @@ void tree_build_cells(cudaStream_t s, int n, int ncrit, int nncap, DevInfo *info
   k_set_leaves<<<1, 32, 0, s>>>(leafoff, leafflag, nn, info);
   count_launch();
   VFMM_LAUNCH_CHECK();
+  return true;
 }
 
 } // namespace vfmm

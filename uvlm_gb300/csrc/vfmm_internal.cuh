@@ -49,7 +49,8 @@ struct DevInfo {
   int      overflow;    // 1 if a capacity was exceeded
   int      nonfinite;   // 1 if an input was NaN/Inf
   unsigned long long p2p_interactions;
-  int      pad[5];
+  int      deeper;      // 1 if a cell at the key depth holds more than ncrit bodies (keys too short)
+  int      pad[4];
 };
 
 // Cells in the reference's order (tree.hpp:29-99), structure of arrays.
@@ -140,8 +141,10 @@ struct TreeScratch {
 };
 void tree_bounds(cudaStream_t s, const double *X, size_t cap, int n, DevInfo *info, TreeScratch &ts);
 void bbox_partial_into(cudaStream_t s, const double *x, const double *y, const double *z, int n, double *part, int nb);
-void tree_sort_bodies(cudaStream_t s, const double *X, size_t cap, int n, int ncrit, DevInfo *info, TreeScratch &ts);
-void tree_build_cells(cudaStream_t s, int n, int ncrit, int nnodes, DevInfo *info, TreeScratch &ts, CellsView cv, int *level_cells,
+void tree_sort_bodies(cudaStream_t s, const double *X, size_t cap, int n, int ncrit, int levels, DevInfo *info, TreeScratch &ts);
+// false (nothing built) when the keys were too short for the tree: a cell at
+// their depth holds more than ncrit bodies
+bool tree_build_cells(cudaStream_t s, int n, int ncrit, int nnodes, DevInfo *info, TreeScratch &ts, CellsView cv, int *level_cells,
                       int *level_start, int *leaf_cells);
 
 // ---- traverse.cu
