@@ -109,19 +109,25 @@ def test_seeds_follow_the_bodies(vfmm_lib):
     assert worst(errs) < TOL, errs
 
 
-def test_mixed_gradient_close_to_fp64(vfmm_lib):
+@pytest.mark.parametrize("kw,tol", [(dict(integration="RK3"), 1e-5), (dict(integration="RK4"), 1e-5),
+                                    (dict(integration="RK2", relax=0.3), 3e-5)])
+def test_mixed_gradient_close_to_fp64(vfmm_lib, kw, tol):
     """Mixed precision (FP32 forward kernels, FP32 P2P^T and M2L^T in the
     reverse sweep): the gradient differs from the all-FP64 one by FP32
-    rounding of the trajectory and of the transposed passes."""
+    rounding of the trajectory and of the transposed passes (RK3, RK4, and
+    RK2 with relaxation).  Relaxation rescales alpha by |alpha| / |w| with w
+    a difference of J entries, which amplifies J's FP32 rounding (measured
+    1.1e-5 on this case; the FP64 relaxation adjoint matches the complex step
+    to 1e-8)."""
     from uvlm_gb300 import FMMCalculator, workloads
     b = workloads.leapfrog(16, seed=7)
     res = {}
     for prec in ("fp64", "mixed"):
-        with FMMCalculator(p=8, ncrit=32, theta=0.47, integration="RK3", precision=prec) as c:
+        with FMMCalculator(p=8, ncrit=32, theta=0.47, precision=prec, **kw) as c:
             res[prec] = c.adjoint(b, 0.01, 3, 2)
     for k in (1, 2):
         a, r = res["mixed"][k], res["fp64"][k]
-        assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-5
+        assert np.linalg.norm(a - r) / np.linalg.norm(r) < tol
 
 
 def test_adjoint_rejects_what_it_does_not_cover(vfmm_lib):
