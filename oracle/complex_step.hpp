@@ -156,12 +156,12 @@ Cx<T> deriv_coef(const Cx<T> *c, int n, int mu, int axis, int stride, int comp)
 
 template <class T>
 struct BodyT {
-  T X[3], A[3], R, U[3], J[9], D[3], VO[3], DO[3], XO[3], AO[3];
+  T X[3], A[3], R, U[3], J[9], D[3], VO[3], DO[3], XO[3], AO[3], DR, RO, DRO;
 };
 
 template <class T>
 struct Stepper {
-  int                 P, ncrit, K, stretching;
+  int                 P, ncrit, K, stretching, formulation = 0; // formulation 1: rVPM
   double              theta;
   long                n;
   std::vector<BodyT<T>> b;
@@ -455,6 +455,46 @@ struct Stepper {
           v += (stretching == 0 ? q.J[3 * c + a] : q.J[3 * a + c]) * q.A[c];
         q.D[a] = v;
       }
+      q.DR = T(0.0);
+      if (formulation == 1) { // rVPM terms, fmmCalculator.hpp:407-418
+        const T na    = sqrt_(q.A[0] * q.A[0] + q.A[1] * q.A[1] + q.A[2] * q.A[2]);
+        const T ah[3] = {q.A[0] / na, q.A[1] / na, q.A[2] / na};
+        const T dot   = q.D[0] * ah[0] + q.D[1] * ah[1] + q.D[2] * ah[2];
+        for (int a = 0; a < 3; a++)
+          q.D[a] -= T(3. / 5.) * dot * ah[a];
+        q.DR -= T(1.0 / 5.0) * q.R / na * dot;
+      }
+    }
+  }
+
+  // The radius's share of the stage updates (as the strengths', with drdt).
+  static void update_radius(BodyT<T> &q, int scheme, int stage, double h)
+  {
+    if (scheme == 0)
+      q.R += q.DR * T(h);
+    else if (scheme == 1 && stage == 0) {
+      q.RO  = q.R;
+      q.DRO = q.DR;
+      q.R += T(h) * q.DRO;
+    } else if (scheme == 1) {
+      q.DRO = T(0.5) * q.DR + T(0.5) * q.DRO;
+      q.R   = q.RO + T(h) * q.DRO;
+    } else if (scheme >= 3 && stage == 0) {
+      q.RO  = q.R;
+      q.DRO = q.DR;
+      q.R += T(0.5 * h) * q.DRO;
+    } else if (scheme >= 3 && stage < 3) {
+      const double c = (stage == 2 && scheme == 4) ? 1.0 : 0.5;
+      q.DRO += T(2.0) * q.DR;
+      q.R = q.RO + T(c * h) * q.DR;
+    } else if (scheme >= 3) {
+      q.DRO += q.DR;
+      q.R = q.RO + T(h / 6.0) * q.DRO;
+    } else {
+      const double A = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
+      const double B = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
+      q.DRO          = stage == 0 ? T(h) * q.DR : T(A) * q.DRO + T(h) * q.DR;
+      q.R += T(B) * q.DRO;
     }
   }
 
@@ -466,6 +506,7 @@ struct Stepper {
 #pragma omp parallel for
     for (long i = 0; i < n; i++) {
       BodyT<T> &q = b[i];
+      update_radius(q, scheme, stage, h);
       for (int d = 0; d < 3; d++) {
         if (scheme == 0) {
           q.X[d] += q.U[d] * T(h);
@@ -585,19 +626,21 @@ extern "C" {
 
 // The templated FMM step with T = double: `steps` steps of scheme 0 Euler,
 // 1 RK2, 2 RK3, 3 RK4, 4 RK4 with a full-dt third stage (stretching 0
-// transposed, 1 classic), relaxation factor `relax` after each step's last
-// stage (0: none); b receives X, alpha,
+// transposed, 1 classic; formulation 0 cVPM, 1 rVPM), relaxation factor
+// `relax` after each step's last stage (0: none); b receives X, alpha, radius, drdt,
 // velocity, J, dadt of the last stage in its tree order.  For the check
 // against vo_advance.
-int vo_cs_advance(Body *b, long n, int P, int ncrit, double theta, int scheme, int stretching, double dt, int steps, double relax)
+int vo_cs_advance(Body *b, long n, int P, int ncrit, double theta, int scheme, int stretching, double dt, int steps, double relax, int formulation)
 {
   using namespace vo::cstep;
   Stepper<double> s;
-  s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta;
+  s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta, s.formulation = formulation;
   load(s, b, n);
   if (!s.advance(scheme, dt, steps, relax))
     return -1;
   for (long i = 0; i < n; i++) {
+    b[i].radius = s.b[i].R;
+    b[i].drdt   = s.b[i].DR;
     for (int d = 0; d < 3; d++) {
       b[i].X[d]        = s.b[i].X[d];
       b[i].alpha[d]    = s.b[i].A[d];
@@ -615,13 +658,14 @@ int vo_cs_advance(Body *b, long n, int P, int ncrit, double theta, int scheme, i
 // derivative by complex step, with relaxation factor `relax` after each
 // step's last stage (0: none).  value gets the real objective.
 int vo_cs_objective(const Body *b, long n, int P, int ncrit, double theta, int scheme, int stretching, double dt, int steps, double wE,
-                    const double *wI, const double *dirs_x, const double *dirs_a, int nd, double *value, double *deriv, double relax)
+                    const double *wI, const double *dirs_x, const double *dirs_a, int nd, double *value, double *deriv, double relax,
+                    int formulation)
 {
   using namespace vo::cstep;
   const double h = 1e-30;
   {
     Stepper<double> s;
-    s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta;
+    s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta, s.formulation = formulation;
     load(s, b, n);
     if (!s.advance(scheme, dt, steps, relax))
       return -1;
@@ -631,7 +675,7 @@ int vo_cs_objective(const Body *b, long n, int P, int ncrit, double theta, int s
   }
   for (int k = 0; k < nd; k++) {
     Stepper<CS> s;
-    s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta;
+    s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta, s.formulation = formulation;
     load(s, b, n);
     for (long i = 0; i < n; i++)
       for (int d = 0; d < 3; d++) {

@@ -139,7 +139,8 @@ def test_adjoint_rejects_what_it_does_not_cover(vfmm_lib):
                 c.adjoint(b, 0.01, 1)
 
 
-def _complex_step(b, P, ncrit, theta, scheme, dt, steps, dirs_x, dirs_a, energy=1.0, impulse=(0.0, 0.0, 1.0), relax=0.0):
+def _complex_step(b, P, ncrit, theta, scheme, dt, steps, dirs_x, dirs_a, energy=1.0, impulse=(0.0, 0.0, 1.0), relax=0.0,
+                  formulation=0):
     import ctypes
     from oracle.oracle import oracle
     L = oracle()
@@ -148,7 +149,7 @@ def _complex_step(b, P, ncrit, theta, scheme, dt, steps, dirs_x, dirs_a, energy=
     val, der = ctypes.c_double(), np.zeros(nd)
     dx, da = np.ascontiguousarray(dirs_x), np.ascontiguousarray(dirs_a)
     assert L.vo_cs_objective(b.ctypes.data, n, P, ncrit, theta, scheme, 0, dt, steps, energy, wI.ctypes.data, dx.ctypes.data,
-                             da.ctypes.data, nd, ctypes.byref(val), der.ctypes.data, relax) == 0
+                             da.ctypes.data, nd, ctypes.byref(val), der.ctypes.data, relax, formulation) == 0
     return val.value, der
 
 
