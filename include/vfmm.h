@@ -194,8 +194,9 @@ typedef struct vfmm_objective {
  * stage evaluations.  With grad_x and grad_alpha both NULL only
  * *value is computed.  Covers Euler, RK2, RK3 and RK4 (either third stage,
  * cfg.rk4_fixed), with or without relaxation (cfg.relax; its stage contexts
- * then also keep alpha before each relaxation), for the cVPM formulation
- * without viscosity (VFMM_ERR_UNSUPPORTED otherwise).  The
+ * then also keep alpha before each relaxation), for the cVPM and rVPM
+ * formulations (rVPM evolves the radii: the gradient runs through them)
+ * without viscosity (VFMM_ERR_UNSUPPORTED for PSE/CSM).  The
  * reference has no adjoint; its L2P takes one derivative by complex step
  * (multipoleKernels.hpp:630-742, complexify.hpp). */
 int vfmm_adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int steps, int checkpoint_every, const vfmm_objective *objective,

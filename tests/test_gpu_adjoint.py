@@ -133,7 +133,7 @@ def test_mixed_gradient_close_to_fp64(vfmm_lib, kw, tol):
 def test_adjoint_rejects_what_it_does_not_cover(vfmm_lib):
     from uvlm_gb300 import FMMCalculator, VfmmError, workloads
     b = workloads.cloud(500, seed=8)
-    for kw in (dict(formulation="rVPM"), dict(viscous="PSE", nu=0.01), dict(viscous="CSM", nu=0.01)):
+    for kw in (dict(viscous="PSE", nu=0.01), dict(viscous="CSM", nu=0.01)):
         with FMMCalculator(p=4, ncrit=32, theta=0.5, **kw) as c:
             with pytest.raises(VfmmError):
                 c.adjoint(b, 0.01, 1)
@@ -203,6 +203,37 @@ def test_gradient_with_relaxation(vfmm_lib, integration, scheme):
     with FMMCalculator(p=8, ncrit=32, theta=0.47, integration=integration) as c:
         v0, gx0, _ = c.adjoint(b, 0.02, 2, 1)
     assert abs(v0 - v) > 1e-6 * abs(v) and not np.allclose(gx0, gx), "relaxation made no difference"
+
+
+@pytest.mark.parametrize("integration,scheme,seed", [("RK2", 1, 4), ("RK3", 2, 5)])
+def test_gradient_rvpm(vfmm_lib, integration, scheme, seed):
+    """rVPM (fmmCalculator.hpp:407-418): the radii evolve with dr/dt, so the
+    gradient runs through the radius cotangents of the pair weights, the rVPM
+    terms and the stage updates.  Against the oracle's complex step of the
+    same steps (rings on which the oracle's complex step and central
+    differences agree to 1e-5 along these directions), and mixed against
+    FP64."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.ring(16, seed=seed)
+    rng = np.random.default_rng(11)
+    nd = 3
+    dx = rng.normal(size=(nd, b.size, 3))
+    da = rng.normal(size=(nd, b.size, 3)) * np.abs(b["alpha"]).max()
+    res = {}
+    for prec in ("fp64", "mixed"):
+        with FMMCalculator(p=8, ncrit=32, theta=0.47, integration=integration, formulation="rVPM", precision=prec) as c:
+            res[prec] = c.adjoint(b, 0.02, 2, 1)
+    v, gx, ga = res["fp64"]
+    vc, der = _complex_step(b, 8, 32, 0.47, scheme, 0.02, 2, dx, da, formulation=1)
+    assert abs(v - vc) <= 1e-10 * abs(vc)
+    for k in range(nd):
+        an = float((gx * dx[k]).sum() + (ga * da[k]).sum())
+        assert abs(an - der[k]) <= 1e-8 * abs(der[k]), (k, an, der[k])
+    for k in (1, 2):
+        a, r = res["mixed"][k], res["fp64"][k]
+        err = np.linalg.norm(a - r) / np.linalg.norm(r)
+        print(f"rVPM {integration}: mixed vs FP64 gradient {err:.3e}")
+        assert err < 1e-4
 
 
 @pytest.mark.parametrize("n,p,ncrit,theta", [(20000, 12, 64, 0.5), (8000, 8, 16, 0.3)])

@@ -846,7 +846,7 @@ __global__ void __launch_bounds__(128) k_adj_p2m(AdjDev a)
 // t2 = (2/sqrt(pi)) sqrt(RS) e^-RS, c4 = 1/(4 pi r^3).
 // gd = ds/dd (to x_i; minus to x_j), wa = ds/dalpha_j.
 __device__ __forceinline__ void pair_adj(double dx, double dy, double dz, const double *al, double sg, const double *ub, const double *Jb,
-                                         const double *ct, double *gd, double *wa)
+                                         const double *ct, double *gd, double *wa, double *sgb = nullptr)
 {
   const double R2 = dx * dx + dy * dy + dz * dz;
   const double S2 = sg * sg, RS = R2 / S2 / 2.0, sqrtRS = sqrt(RS);
@@ -873,6 +873,10 @@ __device__ __forceinline__ void pair_adj(double dx, double dy, double dz, const 
     gd[k]            = fq * d[k] - q * axu[k] - h * (jtd + axm[k]);
     wa[k]            = -q * uxd[k] - h * mxd[k] - q * ct[k];
   }
+  // ds/dsigma of the source radius: sigma dq/dsigma = -(3q + R^2 h) and
+  // sigma dh/dsigma = -(5h + 2 R^2 h_{r^2}) for s = -q (A + C) - h B
+  if (sgb)
+    *sgb = ((3.0 * q + R2 * h) * (A + C) + (5.0 * h + 2.0 * R2 * hR2) * Bv) / sg;
 }
 
 __device__ __forceinline__ void load_seeds(const AdjDev &a, int i, double *ub, double *Jb, double *ct)
@@ -937,7 +941,7 @@ __global__ void __launch_bounds__(128) k_adj_p2p_tgt(AdjDev a)
 // Per source: xbar_j -= sum over its near targets of ds/dd, alphabar_j += ds/dalpha_j.
 __global__ void __launch_bounds__(128) k_adj_p2p_src(AdjDev a)
 {
-  __shared__ double red[128 * 6];
+  __shared__ double red[128 * 7];
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
     const int c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
     const int q0 = a.p2pT_start[c], q1 = a.p2pT_start[c + 1];
@@ -945,7 +949,7 @@ __global__ void __launch_bounds__(128) k_adj_p2p_src(AdjDev a)
       const int nbc = min(128, nb - tc);
       const int TG = nbc <= 32 ? 32 : (nbc <= 64 ? 64 : 128), G = 128 / TG;
       const int tt = threadIdx.x % TG, g = threadIdx.x / TG;
-      double    s[6] = {0, 0, 0, 0, 0, 0};
+      double    s[7] = {0, 0, 0, 0, 0, 0, 0};
       if (tt < nbc) {
         const int    j  = b0 + tc + tt;
         const double xj = B(a, F_X, j), yj = B(a, F_X + 1, j), zj = B(a, F_X + 2, j);
@@ -956,28 +960,29 @@ __global__ void __launch_bounds__(128) k_adj_p2p_src(AdjDev a)
           for (int i = tb; i < tb + tn; i++) {
             const double dx = B(a, F_X, i) - xj, dy = B(a, F_X + 1, i) - yj, dz = B(a, F_X + 2, i) - zj;
             if (dx * dx + dy * dy + dz * dz != 0) {
-              double ub[3], Jb[9], ct[3], gd[3], wa[3];
+              double ub[3], Jb[9], ct[3], gd[3], wa[3], sgb;
               load_seeds(a, i, ub, Jb, ct);
-              pair_adj(dx, dy, dz, al, sg, ub, Jb, ct, gd, wa);
+              pair_adj(dx, dy, dz, al, sg, ub, Jb, ct, gd, wa, &sgb);
               for (int k = 0; k < 3; k++) {
                 s[k] -= gd[k];
                 s[3 + k] += wa[k];
               }
+              s[6] += sgb;
             }
           }
         }
       }
       __syncthreads();
-      for (int k = 0; k < 6; k++)
-        red[threadIdx.x * 6 + k] = s[k];
+      for (int k = 0; k < 7; k++)
+        red[threadIdx.x * 7 + k] = s[k];
       __syncthreads();
       if (threadIdx.x < nbc) {
         const int j = b0 + tc + threadIdx.x;
-        for (int k = 0; k < 6; k++) {
+        for (int k = 0; k < 7; k++) {
           double v = 0;
           for (int gg = 0; gg < G; gg++)
-            v += red[(gg * TG + threadIdx.x) * 6 + k];
-          W(a, k < 3 ? W_XNS + k : W_ANS + k - 3, j) = v;
+            v += red[(gg * TG + threadIdx.x) * 7 + k];
+          W(a, k < 3 ? W_XNS + k : (k < 6 ? W_ANS + k - 3 : W_RNS), j) = v;
         }
       }
     }
@@ -988,13 +993,37 @@ __global__ void __launch_bounds__(128) k_adj_p2p_src(AdjDev a)
 // Seeds of an evaluation from the stage cotangent (cu, ca) of (u, dalpha/dt):
 // ubar = cu and, for dalpha/dt = J^T alpha (transposed) or J alpha
 // (classic), Jbar and the direct alphabar.
-__global__ void k_adj_seeds(const double *soa, double *w, size_t cap, int n, int stretching, int add_relax)
+__global__ void k_adj_seeds(const double *soa, double *w, size_t cap, int n, int stretching, int add_relax, int formulation)
 {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     auto         S  = [&](int f) -> double & { return w[(size_t)f * cap + i]; };
     auto         Bf = [&](int f) { return soa[(size_t)f * cap + i]; };
-    const double ca[3] = {S(W_COT + 3), S(W_COT + 4), S(W_COT + 5)};
+    double       ca[3] = {S(W_COT + 3), S(W_COT + 4), S(W_COT + 5)};
     const double al[3] = {Bf(F_A), Bf(F_A + 1), Bf(F_A + 2)};
+    double       ab_rvpm[3] = {0, 0, 0}, rb_rvpm = 0;
+    if (formulation == VFMM_RVPM) {
+      // rVPM terms (fmmCalculator.hpp:407-418) with d the stretching term:
+      // dalpha/dt = d - 3/5 (d.alpha) alpha / |alpha|^2, dr/dt = -1/5 r (d.alpha) / |alpha|^2.
+      // Their cotangents (ca, cr) give d's cotangent (which then seeds the
+      // stretching as ca does for cVPM) and direct alpha and r cotangents.
+      double ds[3];
+      for (int dd = 0; dd < 3; dd++) {
+        double v = 0;
+        for (int e = 0; e < 3; e++)
+          v += (stretching == VFMM_TRANSPOSED ? Bf(F_J + 3 * e + dd) : Bf(F_J + 3 * dd + e)) * al[e];
+        ds[dd] = v;
+      }
+      const double cr = S(W_COT + 6), rr = Bf(F_R);
+      const double q2 = al[0] * al[0] + al[1] * al[1] + al[2] * al[2], sd = ds[0] * al[0] + ds[1] * al[1] + ds[2] * al[2];
+      const double cal = ca[0] * al[0] + ca[1] * al[1] + ca[2] * al[2];
+      for (int dd = 0; dd < 3; dd++)
+        ab_rvpm[dd] = -0.6 * (cal * ds[dd] + sd * ca[dd]) / q2 + 1.2 * sd * cal * al[dd] / (q2 * q2) -
+                      0.2 * rr * cr * (ds[dd] / q2 - 2.0 * sd * al[dd] / (q2 * q2));
+      rb_rvpm = -0.2 * sd * cr / q2;
+      for (int dd = 0; dd < 3; dd++)
+        ca[dd] -= (0.6 * cal + 0.2 * rr * cr) * al[dd] / q2;
+    }
+    S(W_RD) = rb_rvpm;
     for (int k = 0; k < 3; k++)
       S(W_SU + k) = S(W_COT + k);
     for (int r = 0; r < 3; r++)
@@ -1016,7 +1045,7 @@ __global__ void k_adj_seeds(const double *soa, double *w, size_t cap, int n, int
       double v = 0;
       for (int r = 0; r < 3; r++)
         v += (stretching == VFMM_TRANSPOSED ? Bf(F_J + 3 * cc + r) : Bf(F_J + 3 * r + cc)) * ca[r];
-      S(W_ASTR + cc) = v;
+      S(W_ASTR + cc) = v + ab_rvpm[cc];
     }
   }
 }
@@ -1112,18 +1141,55 @@ __global__ void k_adj_stage_pre(double *g, double *w, size_t cap, int n, int sch
         *db             = A * qa;
       }
     }
+    // the radius with its rate and registers (DRDTOLD, ROLD), as a strength
+    // component with dalpha/dt; Wc(6) is the cotangent of dr/dt
+    double *rb = &G(G_RB), *rdb = &G(G_RDB), *rob = &G(G_ROB);
+    if (scheme == VFMM_EULER)
+      Wc(6) = h * *rb;
+    else if (scheme == VFMM_RK2 && stage == 0) {
+      Wc(6) = *rdb + h * *rb;
+      *rb += *rob;
+      *rdb = *rob = 0;
+    } else if (scheme == VFMM_RK2) {
+      const double t = *rdb + h * *rb;
+      Wc(6)          = 0.5 * t;
+      *rob += *rb;
+      *rb  = 0;
+      *rdb = 0.5 * t;
+    } else if (scheme == VFMM_RK4 && stage == 0) {
+      Wc(6) = *rdb + 0.5 * h * *rb;
+      *rb += *rob;
+      *rdb = *rob = 0;
+    } else if (scheme == VFMM_RK4 && stage < 3) {
+      const double c = (stage == 2 && rk4_fixed) ? 1.0 : 0.5;
+      Wc(6)          = 2.0 * *rdb + c * h * *rb;
+      *rob += *rb;
+      *rb = 0;
+    } else if (scheme == VFMM_RK4) {
+      const double t = *rdb + (h / 6.0) * *rb;
+      Wc(6)          = t;
+      *rob += *rb;
+      *rb  = 0;
+      *rdb = t;
+    } else {
+      const double qr = *rdb + Bc * *rb;
+      Wc(6)           = h * qr;
+      *rdb            = A * qr;
+    }
   }
 }
 
 // g[XB] += the evaluation's position adjoints, g[AB] += its strength adjoints.
 __global__ void k_adj_combine(double *g, const double *w, size_t cap, int n)
 {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     for (int k = 0; k < 3; k++) {
       const size_t o = (size_t)k * cap + i;
       g[(size_t)G_XB * cap + o] += w[(size_t)W_XF * cap + o] + w[(size_t)W_XNT * cap + o] + w[(size_t)W_XNS * cap + o];
       g[(size_t)G_AB * cap + o] += w[(size_t)W_ASTR * cap + o] + w[(size_t)W_AP2M * cap + o] + w[(size_t)W_ANS * cap + o];
     }
+    g[(size_t)G_RB * cap + i] += w[(size_t)W_RNS * cap + i] + w[(size_t)W_RD * cap + i];
+  }
 }
 
 // Bounding-box terms.  Per block: sum xbar_far (3), sum e (1),
@@ -1304,6 +1370,8 @@ __global__ void __launch_bounds__(OBJ_THREADS) k_adj_objective(const double *soa
     }
     for (int k = 0; k < 9; k++)
       w[(size_t)(W_SJ + k) * cap + i] = 0;
+    g[(size_t)G_RB * cap + i] = g[(size_t)G_RDB * cap + i] = g[(size_t)G_ROB * cap + i] = 0;
+    w[(size_t)W_RD * cap + i] = 0;
   }
   red[threadIdx.x] = acc;
   __syncthreads();
@@ -1386,7 +1454,7 @@ __device__ __forceinline__ void radial_F(float s, float &F, float &F1, float &F2
 
 // ds/dd and ds/dalpha of one pair in FP32 (the algebra of pair_adj).
 __device__ __forceinline__ void pair_adj32(float dx, float dy, float dz, float ax, float ay, float az, float isg, float w2, const float *ub,
-                                           const float *Jb, const float *ct, float *gd, float *wa)
+                                           const float *Jb, const float *ct, float *gd, float *wa, float *sgb = nullptr)
 {
   const float R2 = dx * dx + dy * dy + dz * dz;
   float       F, F1, F2;
@@ -1407,6 +1475,8 @@ __device__ __forceinline__ void pair_adj32(float dx, float dy, float dz, float a
   wa[0] = -q * uxd0 - h * mxd0 - q * ct[0];
   wa[1] = -q * uxd1 - h * mxd1 - q * ct[1];
   wa[2] = -q * uxd2 - h * mxd2 - q * ct[2];
+  if (sgb) // ds/dsigma of the source radius, as pair_adj
+    *sgb = isg * ((3.f * q + R2 * h) * (A + C) + (5.f * h + 2.f * R2 * hR2) * Bv);
 }
 
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float v)
@@ -1588,9 +1658,11 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_tgt(AdjDev a)
 __global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
 {
   __shared__ float4 Tp[ADJ_CH_S], Ts[ADJ_CH_S][4];
-  __shared__ float  red[2][128 * 6];
   __shared__ float4 Loff[ADJ_LG];
   __shared__ int    Lpre[ADJ_LG + 1];
+  // partial sums (hi, lo) of the 7 outputs, in the seed staging buffer once a tile's chunks are done
+  float *red0 = reinterpret_cast<float *>(&Ts[0][0]), *red1 = red0 + 128 * 7;
+  static_assert(sizeof(Ts) >= 2 * 128 * 7 * sizeof(float), "the reduction fits in the staging buffer");
   for (int li = blockIdx.x; li < a.nleaves; li += gridDim.x) {
     const int    c = a.leaf_cells[li], b0 = a.cv.body[c], nb = a.cv.nbody[c];
     const int    q0 = a.p2pT_start[c], q1 = a.p2pT_start[c + 1];
@@ -1599,7 +1671,7 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
       const int nbc = min(128, nb - tc);
       const int TG = nbc <= 32 ? 32 : (nbc <= 64 ? 64 : 128), G = 128 / TG;
       const int tt = threadIdx.x % TG, g = threadIdx.x / TG;
-      float     hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float     hi[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       float4    pj = make_float4(0.f, 0.f, 0.f, 0.f), aj = pj;
       if (tt < nbc) {
         pj = a.pos32[b0 + tc + tt];
@@ -1638,7 +1710,7 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
             }
           __syncthreads();
           if (tt < nbc) {
-            float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float s[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             for (int i = g; i < cnt; i += G) {
               const float4 pi = Tp[i];
               const float  dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -1646,34 +1718,35 @@ __global__ void __launch_bounds__(128) k_adj_p2p32_src(AdjDev a)
                 const float4 s0 = Ts[i][0], s1 = Ts[i][1], s2 = Ts[i][2], s3 = Ts[i][3];
                 const float  ub[3] = {s0.x, s0.y, s0.z}, ct[3] = {s0.w, s1.x, s1.y};
                 const float  Jb[9] = {s1.z, s1.w, s2.x, s2.y, s2.z, s2.w, s3.x, s3.y, s3.z};
-                float        gd[3], wa[3];
-                pair_adj32(dx, dy, dz, aj.x, aj.y, aj.z, aj.w, pj.w, ub, Jb, ct, gd, wa);
+                float        gd[3], wa[3], sgb;
+                pair_adj32(dx, dy, dz, aj.x, aj.y, aj.z, aj.w, pj.w, ub, Jb, ct, gd, wa, &sgb);
                 for (int k = 0; k < 3; k++) {
                   s[k] -= gd[k];
                   s[3 + k] += wa[k];
                 }
+                s[6] += sgb;
               }
             }
-            for (int k = 0; k < 6; k++)
+            for (int k = 0; k < 7; k++)
               two_sum_acc(hi[k], lo[k], s[k]);
           }
         }
       }
       __syncthreads();
-      for (int k = 0; k < 6; k++) {
-        red[0][threadIdx.x * 6 + k] = hi[k];
-        red[1][threadIdx.x * 6 + k] = lo[k];
+      for (int k = 0; k < 7; k++) {
+        red0[threadIdx.x * 7 + k] = hi[k];
+        red1[threadIdx.x * 7 + k] = lo[k];
       }
       __syncthreads();
       if (threadIdx.x < nbc) {
         const int j = b0 + tc + threadIdx.x;
-        for (int k = 0; k < 6; k++) {
+        for (int k = 0; k < 7; k++) {
           float h = 0.f, l = 0.f;
           for (int gg = 0; gg < G; gg++) {
-            two_sum_acc(h, l, red[0][(gg * TG + threadIdx.x) * 6 + k]);
-            l += red[1][(gg * TG + threadIdx.x) * 6 + k];
+            two_sum_acc(h, l, red0[(gg * TG + threadIdx.x) * 7 + k]);
+            l += red1[(gg * TG + threadIdx.x) * 7 + k];
           }
-          W(a, k < 3 ? W_XNS + k : W_ANS + k - 3, j) = (double)h + (double)l;
+          W(a, k < 3 ? W_XNS + k : (k < 6 ? W_ANS + k - 3 : W_RNS), j) = (double)h + (double)l;
         }
       }
     }
@@ -2053,9 +2126,9 @@ void adjoint_eval(cudaStream_t s, const ExpArgs &e, const AdjBufs &b, const DevI
   VFMM_LAUNCH_CHECK();
 }
 
-void adjoint_seeds(cudaStream_t s, const double *soa, double *w, size_t cap, int n, int stretching, int add_relax)
+void adjoint_seeds(cudaStream_t s, const double *soa, double *w, size_t cap, int n, int stretching, int add_relax, int formulation)
 {
-  k_adj_seeds<<<grid_for(n, 256), 256, 0, s>>>(soa, w, cap, n, stretching, add_relax);
+  k_adj_seeds<<<grid_for(n, 256), 256, 0, s>>>(soa, w, cap, n, stretching, add_relax, formulation);
   count_launch();
   VFMM_LAUNCH_CHECK();
 }

@@ -1055,8 +1055,8 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
              double *gx, double *ga)
 {
   const vfmm_config &c = h->cfg;
-  if (c.formulation != VFMM_CVPM || c.viscous != VFMM_INVISCID)
-    throw Error(VFMM_ERR_UNSUPPORTED, "the adjoint covers the inviscid cVPM path");
+  if (c.viscous != VFMM_INVISCID)
+    throw Error(VFMM_ERR_UNSUPPORTED, "the adjoint covers the inviscid path");
   if (!bodies || !obj || !value)
     throw Error(VFMM_ERR_INVALID, "null argument");
   if (steps < 0 || every < 1)
@@ -1222,7 +1222,7 @@ void adjoint(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, int st
         if (relaxed_stage(k))
           adjoint_relax(s, A.g[gc].p, A.w.p, h->soa[h->cur].p, x.body.p + nbody_fields + cap, cap, N, c.relax);
         adjoint_stage_pre(s, A.g[gc].p, A.w.p, cap, N, c.integrator, k, dt, c.rk4_fixed);
-        adjoint_seeds(s, h->soa[h->cur].p, A.w.p, cap, N, c.stretching, relaxed_stage(k));
+        adjoint_seeds(s, h->soa[h->cur].p, A.w.p, cap, N, c.stretching, relaxed_stage(k), c.formulation);
         vjp(x.info.p);
       }
   }

@@ -266,14 +266,17 @@ void rbf_op(cudaStream_t s, int op, double *soa, size_t cap, int n, const double
 
 // ---- adjoint.cu: reverse mode of the FP64 evaluation and of the stage updates
 // Adjoint state of the bodies, permuted with them between stages: positions,
-// strengths and the RK registers (VOLD/DOLD, XOLD/AOLD).
-enum AdjG { G_XB = 0, G_AB = 3, G_VB = 6, G_DB = 9, G_XOB = 12, G_AOB = 15, NG = 18 };
+// strengths and the RK registers (VOLD/DOLD, XOLD/AOLD); radius and its
+// registers (DRDTOLD, ROLD).
+enum AdjG { G_XB = 0, G_AB = 3, G_VB = 6, G_DB = 9, G_XOB = 12, G_AOB = 15, G_RB = 18, G_RDB = 19, G_ROB = 20, NG = 21 };
 // Work fields of one evaluation's adjoint: seeds of u and J, far-field
 // position adjoints and dilation terms, near-field position and strength
 // adjoints (per target / per source), P2M^T and stretching strength
-// adjoints, the stage cotangent of (u, dalpha/dt), and the cotangent of the
-// relaxation's vorticity w.
-enum AdjW { W_SU = 0, W_SJ = 3, W_XF = 12, W_EF = 15, W_XNT = 16, W_XNS = 19, W_ANS = 22, W_AP2M = 25, W_ASTR = 28, W_COT = 31, W_WB = 37, NW = 40 };
+// adjoints, the stage cotangent of (u, dalpha/dt, dr/dt), the cotangent of
+// the relaxation's vorticity w, and radius adjoints (near field per source;
+// the rVPM terms).
+enum AdjW { W_SU = 0, W_SJ = 3, W_XF = 12, W_EF = 15, W_XNT = 16, W_XNS = 19, W_ANS = 22, W_AP2M = 25, W_ASTR = 28, W_COT = 31, W_WB = 38,
+            W_RNS = 41, W_RD = 42, NW = 43 };
 struct AdjBufs {
   double    *g; // adjoint state, NG fields
   double    *w; // work, NW fields
@@ -292,7 +295,7 @@ constexpr int ADJ_PARTIALS = 152 * 2 * 17;
 // vjp of the evaluation whose tree, lists and FP64 expansions are in e, with
 // the seeds in b.w (W_SU, W_SJ, W_ASTR): adds to g[G_XB], g[G_AB].
 void adjoint_eval(cudaStream_t s, const ExpArgs &e, const AdjBufs &b, const DevInfo *info);
-void adjoint_seeds(cudaStream_t s, const double *soa, double *w, size_t cap, int n, int stretching, int add_relax);
+void adjoint_seeds(cudaStream_t s, const double *soa, double *w, size_t cap, int n, int stretching, int add_relax, int formulation);
 void adjoint_stage_pre(cudaStream_t s, double *g, double *w, size_t cap, int n, int scheme, int stage, double dt, int rk4_fixed);
 void adjoint_relax(cudaStream_t s, double *g, double *w, const double *soa, const double *alpha_u, size_t cap, int n, double f);
 void adjoint_objective(cudaStream_t s, const double *soa, size_t cap, int n, const int *orig, const double *seed_x, const double *seed_a, double wE,
