@@ -492,7 +492,7 @@ def run_adjoint(args, dist: Dist) -> dict | None:
         val, der = ctypes.c_double(), np.zeros(nd)
         t0 = time.perf_counter()
         oracle().vo_cs_objective(b8.ctypes.data, n8, 8, 32, 0.47, 2, 0, args.dt, steps, 1.0, wI.ctypes.data, dx.ctypes.data,
-                                 da.ctypes.data, nd, ctypes.byref(val), der.ctypes.data, 0.0, 0)
+                                 da.ctypes.data, nd, ctypes.byref(val), der.ctypes.data, 0.0, 0, 0, 0.0)
         tcs = time.perf_counter() - t0
         an = np.einsum("kij,ij->k", dx, gx8) + np.einsum("kij,ij->k", da, ga8)
         check = {"case": "2 rings x 32 stations x 127 (8,128 bodies), FP64, theta 0.47, 50 RK3 steps", "directions": nd,

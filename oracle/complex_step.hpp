@@ -162,6 +162,8 @@ struct BodyT {
 template <class T>
 struct Stepper {
   int                 P, ncrit, K, stretching, formulation = 0; // formulation 1: rVPM
+  int                 viscous = 0;                              // 1 PSE, 2 CSM, with viscosity nu
+  double              nu      = 0.0;
   double              theta;
   long                n;
   std::vector<BodyT<T>> b;
@@ -571,6 +573,60 @@ struct Stepper {
     }
   }
 
+  // calculateViscosity after an evaluation (fmmCalculator.hpp:713-724), as
+  // the restatement does it: PSE (multipoleKernels.hpp:415-450) over the P2P
+  // pairs, per target and source leaf sum (vol_i alpha_j - vol_j alpha_i)
+  // e^{-R^2/(2 s^2)} / s^5, s^2 = sigma_i^2 + sigma_j^2, times nu / sqrt(2) /
+  // pi / sqrt(pi) into dalpha/dt; CSM (fmmCalculator.hpp:334-337) adds
+  // (sqrt(sigma^2 + 2 nu dt) - sigma) / dt to dr/dt.
+  void viscosity(double dt)
+  {
+    if (viscous == 2) {
+#pragma omp parallel for
+      for (long i = 0; i < n; i++)
+        b[i].DR += (sqrt_(b[i].R * b[i].R + T(2.0 * nu * dt)) - b[i].R) / T(dt);
+      return;
+    }
+    if (viscous != 1)
+      return;
+    const long        nc = (long)cells.size();
+    std::vector<long> start(nc + 1, 0);
+    for (auto &pr : p2p)
+      start[pr.first + 1]++;
+    for (long c = 0; c < nc; c++)
+      start[c + 1] += start[c];
+    std::vector<long> src(p2p.size()), fill(start.begin(), start.end() - 1);
+    for (auto &pr : p2p)
+      src[fill[pr.first]++] = (long)pr.second;
+    const double pi     = 3.14159265358979323846264338327950288;
+    const double prefix = nu / 1.41421356237309504880168872420969808 * inv_pi * inv_sqrtpi;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long c = 0; c < nc; c++)
+      for (long qq = start[c]; qq < start[c + 1]; qq++) {
+        const Cell &S = cells[src[qq]];
+        for (uint64_t i = cells[c].BodyOffset; i < cells[c].BodyOffset + cells[c].NBODY; i++) {
+          T sum[3] = {T(0.0), T(0.0), T(0.0)};
+          for (uint64_t j = S.BodyOffset; j < S.BodyOffset + S.NBODY; j++) {
+            T dX[3];
+            for (int d = 0; d < 3; d++)
+              dX[d] = b[i].X[d] - b[j].X[d];
+            const T R2 = dX[0] * dX[0] + dX[1] * dX[1] + dX[2] * dX[2];
+            if (re(R2) != 0) {
+              const T oo    = T(1.0) / (b[i].R * b[i].R + b[j].R * b[j].R);
+              const T s5    = oo * oo * sqrt_(oo);
+              const T vol_i = T(4. / 3. * pi) * b[i].R * b[i].R * b[i].R;
+              const T vol_j = T(4. / 3. * pi) * b[j].R * b[j].R * b[j].R;
+              const T e     = exp_(T(-0.5) * R2 * oo);
+              for (int d = 0; d < 3; d++)
+                sum[d] += (vol_i * b[j].A[d] - vol_j * b[i].A[d]) * e * s5;
+            }
+          }
+          for (int d = 0; d < 3; d++)
+            b[i].D[d] += sum[d] * T(prefix);
+        }
+      }
+  }
+
   bool advance(int scheme, double dt, int steps, double relax = 0.0)
   {
     const int S = scheme == 0 ? 1 : (scheme == 1 ? 2 : (scheme == 2 ? 3 : 4));
@@ -580,6 +636,7 @@ struct Stepper {
         if (!ok)
           return false;
         evaluate();
+        viscosity(dt);
         update(scheme, k, dt);
         if (k == S - 1 && relax > 0)
           relax_all(relax);
@@ -626,15 +683,18 @@ extern "C" {
 
 // The templated FMM step with T = double: `steps` steps of scheme 0 Euler,
 // 1 RK2, 2 RK3, 3 RK4, 4 RK4 with a full-dt third stage (stretching 0
-// transposed, 1 classic; formulation 0 cVPM, 1 rVPM), relaxation factor
-// `relax` after each step's last stage (0: none); b receives X, alpha, radius, drdt,
+// transposed, 1 classic; formulation 0 cVPM, 1 rVPM; viscous 0 none, 1 PSE,
+// 2 CSM with viscosity nu), relaxation factor `relax` after each step's last
+// stage (0: none); b receives X, alpha, radius, drdt,
 // velocity, J, dadt of the last stage in its tree order.  For the check
 // against vo_advance.
-int vo_cs_advance(Body *b, long n, int P, int ncrit, double theta, int scheme, int stretching, double dt, int steps, double relax, int formulation)
+int vo_cs_advance(Body *b, long n, int P, int ncrit, double theta, int scheme, int stretching, double dt, int steps, double relax, int formulation,
+                  int viscous, double nu)
 {
   using namespace vo::cstep;
   Stepper<double> s;
   s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta, s.formulation = formulation;
+  s.viscous = viscous, s.nu = nu;
   load(s, b, n);
   if (!s.advance(scheme, dt, steps, relax))
     return -1;
@@ -656,16 +716,18 @@ int vo_cs_advance(Body *b, long n, int P, int ncrit, double theta, int scheme, i
 // Objective after `steps` steps (see Stepper::objective) and, for each of nd
 // directions (dirs_x, dirs_a: nd x n x 3, in the order of b), its directional
 // derivative by complex step, with relaxation factor `relax` after each
-// step's last stage (0: none).  value gets the real objective.
+// step's last stage (0: none), formulation and viscosity as vo_cs_advance.
+// value gets the real objective.
 int vo_cs_objective(const Body *b, long n, int P, int ncrit, double theta, int scheme, int stretching, double dt, int steps, double wE,
                     const double *wI, const double *dirs_x, const double *dirs_a, int nd, double *value, double *deriv, double relax,
-                    int formulation)
+                    int formulation, int viscous, double nu)
 {
   using namespace vo::cstep;
   const double h = 1e-30;
   {
     Stepper<double> s;
     s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta, s.formulation = formulation;
+    s.viscous = viscous, s.nu = nu;
     load(s, b, n);
     if (!s.advance(scheme, dt, steps, relax))
       return -1;
@@ -676,6 +738,7 @@ int vo_cs_objective(const Body *b, long n, int P, int ncrit, double theta, int s
   for (int k = 0; k < nd; k++) {
     Stepper<CS> s;
     s.P = P, s.ncrit = ncrit, s.K = P * (P + 1) / 2, s.stretching = stretching, s.theta = theta, s.formulation = formulation;
+    s.viscous = viscous, s.nu = nu;
     load(s, b, n);
     for (long i = 0; i < n; i++)
       for (int d = 0; d < 3; d++) {

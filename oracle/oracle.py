@@ -49,8 +49,8 @@ def oracle() -> ctypes.CDLL:
         L.vo_direct.restype = None
         L.vo_relax.argtypes = [_vp, _L, _d]
         L.vo_relax.restype = None
-        L.vo_cs_advance.argtypes = [_vp, _L, _i, _i, _d, _i, _i, _d, _i, _d, _i]
-        L.vo_cs_objective.argtypes = [_vp, _L, _i, _i, _d, _i, _i, _d, _i, _d, _vp, _vp, _vp, _i, _vp, _vp, _d, _i]
+        L.vo_cs_advance.argtypes = [_vp, _L, _i, _i, _d, _i, _i, _d, _i, _d, _i, _i, _d]
+        L.vo_cs_objective.argtypes = [_vp, _L, _i, _i, _d, _i, _i, _d, _i, _d, _vp, _vp, _vp, _i, _vp, _vp, _d, _i, _i, _d]
         _ORA = L
     return _ORA
 

@@ -149,7 +149,7 @@ def _complex_step(b, P, ncrit, theta, scheme, dt, steps, dirs_x, dirs_a, energy=
     val, der = ctypes.c_double(), np.zeros(nd)
     dx, da = np.ascontiguousarray(dirs_x), np.ascontiguousarray(dirs_a)
     assert L.vo_cs_objective(b.ctypes.data, n, P, ncrit, theta, scheme, 0, dt, steps, energy, wI.ctypes.data, dx.ctypes.data,
-                             da.ctypes.data, nd, ctypes.byref(val), der.ctypes.data, relax, formulation) == 0
+                             da.ctypes.data, nd, ctypes.byref(val), der.ctypes.data, relax, formulation, 0, 0.0) == 0
     return val.value, der
 
 

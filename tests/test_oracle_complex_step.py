@@ -12,7 +12,7 @@ from uvlm_gb300 import workloads
 
 def advance_plain(L, b, scheme):
     bb = b.copy()
-    assert L.vo_cs_advance(bb.ctypes.data, bb.size, 8, 32, 0.5, scheme, 0, 0.02, 2, 0.0, 0) == 0
+    assert L.vo_cs_advance(bb.ctypes.data, bb.size, 8, 32, 0.5, scheme, 0, 0.02, 2, 0.0, 0, 0, 0.0) == 0
     return bb
 
 
@@ -22,7 +22,7 @@ def test_templated_step_equals_the_reference_restatement():
     n = b.size
     b1, b2 = b.copy(), b.copy()
     assert L.vo_advance(b1.ctypes.data, n, 8, 32, 0.5, 0.02, 2, 2, 0, 0, 0.0, 0, 0, 0.0) == 0
-    assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, 2, 0, 0.02, 2, 0.0, 0) == 0
+    assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, 2, 0, 0.02, 2, 0.0, 0, 0, 0.0) == 0
     for f, tol in (("X", 1e-14), ("alpha", 1e-14), ("velocity", 1e-12), ("J", 1e-11), ("dadt", 1e-11)):
         a, r = b2[f].reshape(n, -1), b1[f].reshape(n, -1)
         assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), f
@@ -37,7 +37,7 @@ def test_templated_rk4_equals_the_reference_restatement():
     for fixed in (0, 1):
         b1, b2 = b.copy(), b.copy()
         assert L.vo_advance(b1.ctypes.data, n, 8, 32, 0.5, 0.02, 2, 3, 0, 0, 0.0, fixed, 0, 0.0) == 0
-        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, 3 + fixed, 0, 0.02, 2, 0.0, 0) == 0
+        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, 3 + fixed, 0, 0.02, 2, 0.0, 0, 0, 0.0) == 0
         for f, tol in (("X", 1e-14), ("alpha", 1e-14), ("velocity", 1e-12), ("J", 1e-11), ("dadt", 1e-11)):
             a, r = b2[f].reshape(n, -1), b1[f].reshape(n, -1)
             assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), (fixed, f)
@@ -52,7 +52,7 @@ def test_templated_step_with_relaxation_equals_the_reference_restatement():
     for scheme in (0, 2):
         b1, b2 = b.copy(), b.copy()
         assert L.vo_advance(b1.ctypes.data, n, 8, 32, 0.5, 0.02, 2, scheme, 0, 0, 0.3, 0, 0, 0.0) == 0
-        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, scheme, 0, 0.02, 2, 0.3, 0) == 0
+        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, scheme, 0, 0.02, 2, 0.3, 0, 0, 0.0) == 0
         for f, tol in (("X", 1e-14), ("alpha", 1e-13), ("velocity", 1e-12), ("J", 1e-11), ("dadt", 1e-11)):
             a, r = b2[f].reshape(n, -1), b1[f].reshape(n, -1)
             assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), (scheme, f)
@@ -68,12 +68,31 @@ def test_templated_rvpm_step_equals_the_reference_restatement():
     for scheme in (1, 2):
         b1, b2 = b.copy(), b.copy()
         assert L.vo_advance(b1.ctypes.data, n, 8, 32, 0.5, 0.02, 2, scheme, 0, 1, 0.0, 0, 0, 0.0) == 0
-        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, scheme, 0, 0.02, 2, 0.0, 1) == 0
+        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, scheme, 0, 0.02, 2, 0.0, 1, 0, 0.0) == 0
         for f, tol in (("X", 1e-14), ("alpha", 1e-13), ("radius", 1e-14), ("drdt", 1e-11), ("velocity", 1e-12), ("J", 1e-11),
                        ("dadt", 1e-11)):
             a, r = b2[f].reshape(n, -1), b1[f].reshape(n, -1)
             assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), (scheme, f)
         assert not np.array_equal(b2["radius"], b["radius"]), "rVPM left the radii unchanged"
+
+
+def test_templated_viscous_step_equals_the_reference_restatement():
+    """PSE (multipoleKernels.hpp:415-450) and CSM (fmmCalculator.hpp:334-337)
+    in the templated step against vo_advance's, RK2."""
+    L = oracle()
+    b = workloads.cloud(3000, seed=7)
+    n = b.size
+    for viscous in (1, 2):
+        b1, b2 = b.copy(), b.copy()
+        assert L.vo_advance(b1.ctypes.data, n, 8, 32, 0.5, 0.02, 2, 1, 0, 0, 0.0, 0, viscous, 0.01) == 0
+        assert L.vo_cs_advance(b2.ctypes.data, n, 8, 32, 0.5, 1, 0, 0.02, 2, 0.0, 0, viscous, 0.01) == 0
+        for f, tol in (("X", 1e-14), ("alpha", 1e-13), ("radius", 1e-14), ("velocity", 1e-12), ("J", 1e-11), ("dadt", 1e-11)):
+            a, r = b2[f].reshape(n, -1), b1[f].reshape(n, -1)
+            assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), (viscous, f)
+        plain = b.copy()
+        assert L.vo_cs_advance(plain.ctypes.data, n, 8, 32, 0.5, 1, 0, 0.02, 2, 0.0, 0, 0, 0.0) == 0
+        changed = "alpha" if viscous == 1 else "radius"
+        assert not np.allclose(b2[changed], plain[changed], rtol=1e-9, atol=0), (viscous, "viscosity changed nothing")
 
 
 def test_complex_step_against_central_differences():
@@ -89,7 +108,7 @@ def test_complex_step_against_central_differences():
         v, der = ctypes.c_double(), np.zeros(1)
         args = (dx.ctypes.data, da.ctypes.data, 1) if dirs else (None, None, 0)
         assert L.vo_cs_objective(bb.ctypes.data, n, 8, 32, 0.47, 2, 0, 0.02, 1, 1.0, wI.ctypes.data, *args, ctypes.byref(v),
-                                 der.ctypes.data, 0.0, 0) == 0
+                                 der.ctypes.data, 0.0, 0, 0, 0.0) == 0
         return v.value, der[0]
 
     _, cs = value(b, True)
