@@ -1,7 +1,9 @@
 """The closed-form adjoint of one near-field pair used by the reverse-mode P2P
 (adjoint.cu pair_adj), restated in numpy and checked against 40-digit central
 differences of the forward pair terms of the team P2P
-(multipoleKernels.hpp:239-283).  CPU only."""
+(multipoleKernels.hpp:239-283), including the derivative in the source's
+radius; and the transpose of the rVPM terms (fmmCalculator.hpp:407-418) of
+k_adj_seeds.  CPU only."""
 import numpy as np
 import pytest
 
@@ -30,7 +32,7 @@ def forward_s(mp, d, al, sg, ub, Jb):
 
 
 def pair_adj(d, al, sg, ub, Jb):
-    """(ds/dd, ds/dalpha) as adjoint.cu computes them."""
+    """(ds/dd, ds/dalpha, ds/dsigma) as adjoint.cu computes them."""
     from math import erf, exp, pi, sqrt
     R2 = d @ d
     S2 = sg * sg
@@ -48,7 +50,8 @@ def pair_adj(d, al, sg, ub, Jb):
     A, B, C = al @ uxd, al @ mxd, al @ ct
     wa = -q * uxd - h * mxd - q * ct
     gd = (-h * (A + C) - 2 * hR2 * B) * d - q * np.cross(al, ub) - h * (Jb.T @ np.cross(d, al) + np.cross(al, m))
-    return gd, wa
+    sgb = ((3 * q + R2 * h) * (A + C) + (5 * h + 2 * R2 * hR2) * B) / sg
+    return gd, wa, sgb
 
 
 def test_pair_adjoint_against_high_precision_differences():
@@ -60,7 +63,9 @@ def test_pair_adjoint_against_high_precision_differences():
         d = rng.normal(size=3) * rng.uniform(0.02, 1.0)
         al, sg = rng.normal(size=3), rng.uniform(0.02, 0.5)
         ub, Jb = rng.normal(size=3), rng.normal(size=(3, 3))
-        gd, wa = pair_adj(d, al, sg, ub, Jb)
+        gd, wa, sgb = pair_adj(d, al, sg, ub, Jb)
+        fs = (forward_s(mp, d, al, mp.mpf(sg) + hh, ub, Jb) - forward_s(mp, d, al, mp.mpf(sg) - hh, ub, Jb)) / (2 * hh)
+        assert abs(float(fs) - sgb) <= 1e-9 * max(abs(sgb), np.abs(wa).max())
         for k in range(3):
             e = [hh if i == k else 0 for i in range(3)]
             fd = (forward_s(mp, [mp.mpf(x) + y for x, y in zip(d, e)], al, sg, ub, Jb)
@@ -69,3 +74,40 @@ def test_pair_adjoint_against_high_precision_differences():
             fa = (forward_s(mp, d, [mp.mpf(x) + y for x, y in zip(al, e)], sg, ub, Jb)
                   - forward_s(mp, d, [mp.mpf(x) - y for x, y in zip(al, e)], sg, ub, Jb)) / (2 * hh)
             assert abs(float(fa) - wa[k]) <= 1e-9 * np.abs(wa).max()
+
+
+def test_rvpm_terms_transpose():
+    """k_adj_seeds' transpose of the rVPM terms: with d the stretching term,
+    dalpha/dt = d - 3/5 (d.alpha) alpha/|alpha|^2 and dr/dt = -1/5 r (d.alpha)/|alpha|^2;
+    cotangents (ca, cr) of (dalpha/dt, dr/dt) give those of d, alpha and r."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    rng = np.random.default_rng(4)
+
+    def fwd(al, ds, r, ca, cr):
+        na = mp.sqrt(sum(x * x for x in al))
+        ah = [x / na for x in al]
+        dot = sum(x * y for x, y in zip(ds, ah))
+        dadt = [x - mp.mpf(3) / 5 * dot * y for x, y in zip(ds, ah)]
+        drdt = -mp.mpf(1) / 5 * r / na * dot
+        return sum(mp.mpf(c) * x for c, x in zip(ca, dadt)) + mp.mpf(cr) * drdt
+
+    hh = mp.mpf("1e-15")
+    for _ in range(40):
+        al, ds, ca = rng.normal(size=3), rng.normal(size=3), rng.normal(size=3)
+        r, cr = rng.uniform(0.05, 0.5), rng.normal()
+        q2, sd, cal = al @ al, ds @ al, ca @ al
+        ab = -0.6 * (cal * ds + sd * ca) / q2 + 1.2 * sd * cal * al / q2**2 - 0.2 * r * cr * (ds / q2 - 2 * sd * al / q2**2)
+        rb = -0.2 * sd * cr / q2
+        cs = ca - (0.6 * cal + 0.2 * r * cr) * al / q2
+        A = [mp.mpf(x) for x in al]
+        D = [mp.mpf(x) for x in ds]
+        R = mp.mpf(r)
+        for k in range(3):
+            e = [hh if i == k else 0 for i in range(3)]
+            fa = (fwd([x + y for x, y in zip(A, e)], D, R, ca, cr) - fwd([x - y for x, y in zip(A, e)], D, R, ca, cr)) / (2 * hh)
+            fd = (fwd(A, [x + y for x, y in zip(D, e)], R, ca, cr) - fwd(A, [x - y for x, y in zip(D, e)], R, ca, cr)) / (2 * hh)
+            assert abs(float(fa) - ab[k]) <= 1e-10 * (1 + np.abs(ab).max())
+            assert abs(float(fd) - cs[k]) <= 1e-10 * (1 + np.abs(cs).max())
+        fr = (fwd(A, D, R + hh, ca, cr) - fwd(A, D, R - hh, ca, cr)) / (2 * hh)
+        assert abs(float(fr) - rb) <= 1e-10 * (1 + abs(rb))
