@@ -73,6 +73,7 @@ def ref(P: int, ncrit: int, theta: float) -> ctypes.CDLL:
     L.ref_advance.argtypes = [_vp, _L, _d, _i, _i, _i]
     L.ref_sensors.argtypes = [_vp, _L, _vp, _L]
     L.ref_advance_viscous.argtypes = [_vp, _L, _d, _i, _i, _i, _d]
+    L.ref_advance_rvpm.argtypes = [_vp, _L, _d, _i, _i]
     L.ref_rbf.argtypes = [_vp, _L, _vp, _L, _PL]
     L.ref_direct.argtypes = [_vp, _L, _vp, _L]
     L.ref_direct.restype = None

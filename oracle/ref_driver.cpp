@@ -167,6 +167,18 @@ int ref_advance(void *bodies, long n, double dt, int steps, int scheme, int stre
   return -1;
 }
 
+// FMMCalculator::advance with the rVPM formulation (fmmCalculator.hpp:407-418:
+// the radii evolve) and transposed stretching, `steps` times; scheme 1 RK2,
+// 2 RK3.
+int ref_advance_rvpm(void *bodies, long n, double dt, int steps, int scheme)
+{
+  if (scheme == 1)
+    return run_advance<Calc<Vortex::RK2, Vortex::Transposed, Vortex::rVPM>>(bodies, n, dt, steps);
+  if (scheme == 2)
+    return run_advance<Calc<Vortex::RK3, Vortex::Transposed, Vortex::rVPM>>(bodies, n, dt, steps);
+  return -1;
+}
+
 // FMMCalculator::advance with a viscous scheme (fmmCalculator.hpp:713-724,
 // called after every calculate): viscous 1 = Vortex::PSE (multipoleKernels.hpp:
 // 415-450), 2 = Vortex::CSM (fmmCalculator.hpp:334-337).  The reference never

@@ -10,7 +10,7 @@ committed and read by the tests everywhere.
 Each body carries its input index in `drdt_old`, a field the evaluation never
 touches, so the tree permutation can be read from the permuted output.
 
-Usage:  python tests/golden/make_golden.py [viscous|rbf]   (only those cases)
+Usage:  python tests/golden/make_golden.py [viscous|rbf|rvpm]   (only those cases)
 """
 from __future__ import annotations
 
@@ -123,6 +123,22 @@ def viscous_case(name, b, P, ncrit, theta, dt, steps, scheme, viscous, nu):
          out_J=out["J"])
 
 
+def rvpm_case(name, b, P, ncrit, theta, dt, steps, scheme):
+    """advance with Vortex::rVPM (the radii evolve), transposed stretching."""
+    R = O.ref(P, ncrit, theta)
+    out = b.copy()
+    rc = R.ref_advance_rvpm(out.ctypes.data, out.size, dt, steps, scheme)
+    assert rc == 0
+    save(name, P=P, ncrit=ncrit, theta=theta, dt=dt, steps=steps, scheme=scheme, stretching=0, formulation=1,
+         **inputs_of(b), out_X=out["X"], out_alpha=out["alpha"], out_radius=out["radius"], out_velocity=out["velocity"],
+         out_J=out["J"])
+
+
+def rvpm_cases():
+    rvpm_case("advance_rvpm_rk2_ring", workloads.ring(8, seed=17), 6, 32, 0.5, 0.01, 2, 1)
+    rvpm_case("advance_rvpm_rk3_cloud", workloads.cloud(600, seed=18), 6, 16, 0.5, 0.05, 2, 2)
+
+
 def viscous_cases():
     viscous_case("advance_pse_cloud", workloads.cloud(700, seed=14), 6, 16, 0.5, 0.05, 2, 1, 1, 0.01)
     viscous_case("advance_pse_rk3_ring", workloads.ring(8, seed=15), 6, 32, 0.5, 0.01, 1, 2, 1, 0.005)
@@ -197,7 +213,10 @@ if __name__ == "__main__":
         viscous_cases()
     elif sys.argv[1:] == ["rbf"]:
         rbf_cases()
+    elif sys.argv[1:] == ["rvpm"]:
+        rvpm_cases()
     else:
         main()
         viscous_cases()
         rbf_cases()
+        rvpm_cases()

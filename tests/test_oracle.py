@@ -74,6 +74,18 @@ def test_advance_viscous(name):
         assert rel(out[f], d["out_" + f]) < 1e-11, f
 
 
+@pytest.mark.parametrize("name", ["advance_rvpm_rk2_ring", "advance_rvpm_rk3_cloud"])
+def test_advance_rvpm(name):
+    """The rVPM formulation (fmmCalculator.hpp:407-418): the radii evolve with dr/dt."""
+    d = golden(name)
+    b = golden_bodies(d)
+    out = O.advance(b, int(d["P"]), int(d["ncrit"]), float(d["theta"]), float(d["dt"]), int(d["steps"]), int(d["scheme"]),
+                    int(d["stretching"]), formulation=1)
+    for f in ["X", "alpha", "radius", "velocity", "J"]:
+        assert rel(out[f], d["out_" + f]) < 1e-11, f
+    assert not np.allclose(np.sort(d["out_radius"]), np.sort(b["radius"]), rtol=1e-9, atol=0), "the radii did not change"
+
+
 def test_sensors():
     d = golden("sensors_p6")
     b = golden_bodies(d)
