@@ -62,6 +62,8 @@ def parse(argv=None):
     ap.add_argument("--workload", default="cloud", choices=["cloud", "rings64", "adjoint"],
                     help="cloud: the headline N = 2^20 cloud; rings64: 64 independent rings, batched; "
                          "adjoint: reverse-mode gradient of the leapfrogging rings")
+    ap.add_argument("--orders", default="6,14",
+                    help="other expansion orders of the cloud reported beside the headline (stage times, errors); '' = none")
     ap.add_argument("--adj-steps", type=int, default=50, help="adjoint workload: RK3 steps")
     ap.add_argument("--cs-dirs", type=int, default=2, help="adjoint workload: complex-step check directions (0 = none)")
     return ap.parse_args(argv)
@@ -196,7 +198,7 @@ def cpu_baseline(args, threads: int | None = None) -> dict:
 
 
 def config_of(args, l2: str) -> dict:
-    return {"workload": "uniform cloud, one RK2 stage", "n_bodies": args.n, "p": args.p, "theta": args.theta,
+    return {"workload": "uniform cloud, one RK2 stage of the same initial state every step", "n_bodies": args.n, "p": args.p, "theta": args.theta,
             "ncrit": args.ncrit, "integrator": "RK2", "precision": args.precision, "l2": l2}
 
 
@@ -217,7 +219,7 @@ def run_reference(args, dist: Dist) -> dict | None:
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform cloud)",
-            "config": config_of(args, "n/a (CPU)"), "impl": "reference",
+            "config": dict(config_of(args, "n/a (CPU)"), precision="fp64"), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": "port", "sample": r["sample"]},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     return line
@@ -232,24 +234,29 @@ def run_ours(args, dist: Dist) -> dict | None:
     h = calc.handle
     L = lib()
     bodies = workloads.cloud(n, seed=1000 + dist.rank)
-    calc.load(bodies)
+    # every step is the same stage of the same cloud: the initial bodies are
+    # loaded again before each step (outside the timed region), so each timed
+    # step builds the same tree and lists and does the same work
     for w in range(args.warmup):
-        calc.stage(w % 2, args.dt)
+        calc.load(bodies)
+        calc.stage(0, args.dt)
     L.vfmm_synchronize(h)
     dist.barrier()
     clocks = ClockSampler(dist.local_rank)
     clocks.start()
-    launches0 = L.vfmm_launch_count(h)
+    launches = 0
     times = []
     ms = ctypes.c_float()
     for k in range(args.steps):
+        calc.load(bodies)   # restore the initial state (untimed)
         L.vfmm_flush_l2(h)  # evict L2 between timed steps (untimed)
         L.vfmm_event_record(h, 0)
-        calc.stage((args.warmup + k) % 2, args.dt)
+        launches0 = L.vfmm_launch_count(h)
+        calc.stage(0, args.dt)
+        launches += L.vfmm_launch_count(h) - launches0
         L.vfmm_event_record(h, 1)
         L.vfmm_event_elapsed(h, 0, 1, ctypes.byref(ms))
         times.append(ms.value * 1e-3)
-    launches = L.vfmm_launch_count(h) - launches0 - args.steps  # minus the L2 flushes
     L.vfmm_synchronize(h)
     clk = clocks.stop()
     dist.barrier()
@@ -282,12 +289,13 @@ def run_ours(args, dist: Dist) -> dict | None:
             "algorithmic_flops_per_launch": f_dom, "kernel_ms": t_dom}
 
     # end to end through the public API: vfmm_advance on pinned host AoS bodies
-    host = workloads.cloud(n, seed=2000 + dist.rank)
+    host = bodies.copy()
     L.vfmm_host_register(host.ctypes.data, host.nbytes)
     calc.advance(host, args.dt)  # warm-up
     dist.barrier()
     e2e_t = []
     for _ in range(args.e2e_steps):
+        host[:] = bodies  # the same initial cloud every step (untimed)
         t0 = time.perf_counter()
         calc.advance(host, args.dt)
         e2e_t.append(time.perf_counter() - t0)
@@ -297,13 +305,20 @@ def run_ours(args, dist: Dist) -> dict | None:
     e2e_value = dist.world * n * stages * len(e2e_t) / e2e_total
 
     accuracy = None
-    if not args.no_accuracy and dist.rank == 0:
-        accuracy = measure_accuracy(args, calc)
+    if not args.no_accuracy and dist.rank == 0 and args.precision == "mixed":
+        accuracy = accuracy_at(args.p, bodies, args, mixed_calc=calc)
     calc.close()
 
     fp64 = None
     if args.precision == "mixed" and args.fp64_steps > 0:
         fp64 = time_fp64(args, dist, bodies)
+    orders = []
+    if args.precision == "mixed" and args.orders:
+        for p in [int(x) for x in args.orders.split(",") if x.strip()]:
+            o = time_order(p, bodies, args, dist, steps=3, fp64_steps=1)
+            if dist.rank == 0 and not args.no_accuracy:
+                o["accuracy"] = accuracy_at(p, bodies, args)
+            orders.append(o)
     if dist.rank != 0:
         return None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
@@ -321,6 +336,8 @@ def run_ours(args, dist: Dist) -> dict | None:
     if fp64:
         line["fp64"] = fp64
         line["fp64"]["speedup_mixed_vs_fp64"] = fp64["ms_per_step"] / line["ms_per_step"]
+    if orders:
+        line["other_orders"] = orders
     if args.autotune:
         with FMMCalculator(p=args.p, ncrit=args.ncrit, theta=args.theta, integration="RK2", precision=args.precision,
                            device=dist.local_rank) as ct:
@@ -333,65 +350,110 @@ def run_ours(args, dist: Dist) -> dict | None:
 
 
 def time_fp64(args, dist: Dist, bodies) -> dict:
-    """The plain FP64 GPU FMM on the same workload (the drop-in mode), timed the
-    same way for the mixed-vs-FP64 comparison."""
-    from uvlm_gb300 import FMMCalculator, lib
-    L = lib()
-    c = FMMCalculator(p=args.p, ncrit=args.ncrit, theta=args.theta, integration="RK2", precision="fp64",
-                      device=dist.local_rank)
-    h = c.handle
-    c.load(bodies)
-    c.stage(0, args.dt)
-    ms = ctypes.c_float()
-    t = []
-    for k in range(args.fp64_steps):
-        L.vfmm_flush_l2(h)
-        L.vfmm_event_record(h, 0)
-        c.stage((1 + k) % 2, args.dt)
-        L.vfmm_event_record(h, 1)
-        L.vfmm_event_elapsed(h, 0, 1, ctypes.byref(ms))
-        t.append(ms.value)
-    ph = c.phase_times()
-    c.close()
+    """The plain FP64 GPU FMM on the same fixed workload (the drop-in mode),
+    timed the same way for the mixed-vs-FP64 comparison."""
+    from uvlm_gb300 import FMMCalculator
+    with FMMCalculator(p=args.p, ncrit=args.ncrit, theta=args.theta, integration="RK2", precision="fp64",
+                       device=dist.local_rank) as c:
+        t = time_fixed_stage(c, bodies, args.dt, args.fp64_steps, warmup=1)
+        ph = c.phase_times()
     tot = dist.max(sum(t))
     return {"ms_per_step": tot / len(t), "value": dist.world * args.n * len(t) / (tot * 1e-3), "steps": len(t),
             "phases_ms": ph}
 
 
-def measure_accuracy(args, calc) -> dict:
-    """rel-L2 velocity and J errors of this run's FMM on 4096 targets against the
-    FP64 direct sum with the reference's regularised kernel."""
-    from uvlm_gb300 import direct, workloads
-    b = workloads.cloud(args.n, seed=3000)
-    b["drdt_old"] = np.arange(b.size)  # survives init/calculate: recovers the tree permutation
-    from uvlm_gb300 import FMMCalculator
+def evaluate_state(c, bodies):
+    """init + calculate of `bodies` on calculator c; returns the bodies in
+    tree order, with a column of their original indices."""
+    bb = bodies.copy()
+    bb["drdt_old"] = np.arange(bb.size)  # survives init/calculate: recovers the tree permutation
+    c.init(bb)
+    c.calculate()
+    c.copyBodies2Host(bb)
+    return bb
 
-    def evaluate(c):
-        bb = b.copy()
-        c.init(bb)
-        c.calculate()
-        c.copyBodies2Host(bb)
-        return bb[np.argsort(bb["drdt_old"].astype(np.int64))]
 
-    def rl2(a, r):
-        return float(np.linalg.norm(a - r) / np.linalg.norm(r))
-    fmm = evaluate(calc)
-    src = workloads.cloud(args.n, seed=3000)
-    ref = direct(src[:4096].copy(), src)
-    acc = {"direct_targets": 4096,
-           "velocity_rel_l2_vs_direct": rl2(fmm["velocity"][:4096], ref["velocity"]),
-           "J_rel_l2_vs_direct": rl2(fmm["J"][:4096], ref["J"]),
-           "note_direct": "FP64 all-pairs sum with the regularised kernel; the reference's far field uses the "
-                          "singular kernel, so this error is the model's (same for FP64 and mixed)"}
-    if args.precision == "mixed":
-        with FMMCalculator(p=args.p, ncrit=args.ncrit, theta=args.theta, precision="fp64") as c64:
-            f64 = evaluate(c64)
-        acc.update({"velocity_rel_l2_vs_fp64_fmm": rl2(fmm["velocity"], f64["velocity"]),
-                    "J_rel_l2_vs_fp64_fmm": rl2(fmm["J"], f64["J"]),
-                    "dadt_rel_l2_vs_fp64_fmm": rl2(fmm["dadt"], f64["dadt"]),
-                    "fp64_velocity_rel_l2_vs_direct": rl2(f64["velocity"][:4096], ref["velocity"]),
-                    "bodies_compared": int(args.n)})
+def rl2(a, r) -> float:
+    return float(np.linalg.norm(a - r) / np.linalg.norm(r))
+
+
+def accuracy_at(p: int, bodies, args, mixed_calc=None, targets: int = 4096) -> dict:
+    """Errors of the timed state (the initial cloud, one evaluation) at order p:
+    mixed against the FP64 FMM on every body, and both against the
+    model-consistent FP64 direct sum (regularised kernel on P2P-list leaf
+    pairs, singular elsewhere: the sum the FMM approximates) on `targets`
+    bodies; FP64 FMM against the plain regularised direct sum beside it."""
+    from uvlm_gb300 import FMMCalculator, direct
+    own = mixed_calc is None
+    cm = mixed_calc or FMMCalculator(p=p, ncrit=args.ncrit, theta=args.theta, precision="mixed")
+    mix = evaluate_state(cm, bodies)
+    if own:
+        cm.close()
+    with FMMCalculator(p=p, ncrit=args.ncrit, theta=args.theta, precision="fp64") as c64:
+        f64 = evaluate_state(c64, bodies)
+        tgt = np.sort(np.random.default_rng(4096).choice(bodies.size, size=min(targets, bodies.size), replace=False))
+        um, Jm = c64.direct_model(tgt)
+    assert (mix["X"] == f64["X"]).all(), "mixed and FP64 trees differ"
+    Jm = Jm.reshape(-1, 9)
+    acc = {"p": p,
+           "velocity_rel_l2_vs_fp64_fmm": rl2(mix["velocity"], f64["velocity"]),
+           "J_rel_l2_vs_fp64_fmm": rl2(mix["J"], f64["J"]),
+           "dadt_rel_l2_vs_fp64_fmm": rl2(mix["dadt"], f64["dadt"]),
+           "bodies_compared": int(bodies.size),
+           "model_direct_targets": int(tgt.size),
+           "mixed_velocity_rel_l2_vs_model_direct": rl2(mix["velocity"][tgt], um),
+           "mixed_J_rel_l2_vs_model_direct": rl2(mix["J"][tgt].reshape(-1, 9), Jm),
+           "fp64_velocity_rel_l2_vs_model_direct": rl2(f64["velocity"][tgt], um),
+           "fp64_J_rel_l2_vs_model_direct": rl2(f64["J"][tgt].reshape(-1, 9), Jm)}
+    if p == args.p:
+        ref = direct(f64[tgt].copy(), f64)  # all pairs regularised (order of the sources is immaterial)
+        acc["fp64_velocity_rel_l2_vs_regularised_direct"] = rl2(f64["velocity"][tgt], ref["velocity"])
+        acc["mixed_velocity_rel_l2_vs_regularised_direct"] = rl2(mix["velocity"][tgt], ref["velocity"])
+    acc["note"] = ("timed state (initial cloud, one evaluation).  *_vs_fp64_fmm: precision error of the mixed path "
+                   "(the <=1e-6 bar); *_vs_model_direct: FP64 direct sum with the FMM's own kernel split, so "
+                   "the FMM's truncation error at this order and theta (the reference's MAC on cell half-widths), the "
+                   "same for FP64 and mixed; *_vs_regularised_direct: all pairs regularised, which the reference's "
+                   "singular far field does not approximate")
     return acc
+
+
+def time_order(p: int, bodies, args, dist: Dist, steps: int, fp64_steps: int) -> dict:
+    """Mixed and FP64 stage times of the same fixed workload at order p."""
+    from uvlm_gb300 import FMMCalculator
+    out = {"p": p}
+    for prec, k in (("mixed", steps), ("fp64", fp64_steps)):
+        if k <= 0:
+            continue
+        with FMMCalculator(p=p, ncrit=args.ncrit, theta=args.theta, integration="RK2", precision=prec,
+                           device=dist.local_rank) as c:
+            t = time_fixed_stage(c, bodies, args.dt, k, warmup=1)
+            out[f"{prec}_ms_per_stage"] = dist.max(sum(t)) / len(t)
+            if prec == "mixed":
+                out["phases_ms"] = c.phase_times()
+    if "fp64_ms_per_stage" in out and "mixed_ms_per_stage" in out:
+        out["speedup_mixed_vs_fp64"] = out["fp64_ms_per_stage"] / out["mixed_ms_per_stage"]
+    return out
+
+
+def time_fixed_stage(c, bodies, dt: float, steps: int, warmup: int = 1) -> list:
+    """ms of `steps` timed stages, each from the same loaded state, L2 flushed."""
+    from uvlm_gb300 import lib
+    L = lib()
+    h = c.handle
+    ms = ctypes.c_float()
+    for _ in range(warmup):
+        c.load(bodies)
+        c.stage(0, dt)
+    t = []
+    for _ in range(steps):
+        c.load(bodies)
+        L.vfmm_flush_l2(h)
+        L.vfmm_event_record(h, 0)
+        c.stage(0, dt)
+        L.vfmm_event_record(h, 1)
+        L.vfmm_event_elapsed(h, 0, 1, ctypes.byref(ms))
+        t.append(ms.value)
+    return t
 
 
 def run_rings64(args, dist: Dist) -> dict | None:

@@ -263,6 +263,19 @@ int vfmm_num_stages(vfmm_handle h);
  * the same velocity. */
 int vfmm_direct(vfmm_handle h, vfmm_body *targets, size_t nt, const vfmm_body *sources, size_t ns);
 
+/* No counterpart in the reference (an accuracy yardstick for its FMM).  FP64
+ * direct sum with the FMM's own kernel split, on the handle's current tree:
+ * pairs whose leaves are on the P2P list use the regularised kernel
+ * (multipoleKernels.hpp:239-283), all other pairs the singular Biot-Savart
+ * kernel that the multipole and local expansions represent
+ * (multipoleKernels.hpp:519-552, :631-742).  Its difference from the FMM is
+ * the expansions' truncation error alone.  targets[i] are body indices in
+ * tree order (the order vfmm_init leaves the caller's bodies in); out
+ * receives nt records of 12 doubles: velocity[3], J[3][3] row-major.  Needs
+ * the tree of the current positions (after vfmm_init or vfmm_calculate, not
+ * after a stage update): VFMM_ERR_STATE otherwise. */
+int vfmm_direct_model(vfmm_handle h, const uint32_t *targets, size_t nt, double *out);
+
 /* ---- instrumentation ----------------------------------------------------- */
 
 /* Record event `slot` (0..15) on the handle's stream; elapsed ms between two
@@ -315,7 +328,8 @@ int vfmm_write_vtk(const vfmm_body *bodies, size_t n, const char *path, int bina
  * touch the allocator): its scratch is a fixed 29,184-byte array in the
  * library, present on every GPU that loads it.  n must be 1 .. 2^31-1.  The
  * first call on a device looks up the array's address and should come before
- * any stream capture.  Calls that overlap on the GPU share the array and race:
+ * any stream capture; the address is kept for the life of the process, so do
+ * not call this after cudaDeviceReset on that device.  Calls that overlap on the GPU share the array and race:
  * serialise them. */
 int vfmm_bounds_noalloc(const double *x, const double *y, const double *z, size_t n, double *out, void *stream);
 

@@ -47,6 +47,8 @@ def oracle() -> ctypes.CDLL:
         L.vo_sensors.argtypes = [_vp, _L, _vp, _L, _i, _i, _d]
         L.vo_direct.argtypes = [_vp, _L, _vp, _L]
         L.vo_direct.restype = None
+        L.vo_direct_model.argtypes = [_vp, _L, _vp, _L, _vp, _L, _vp, _L, _vp]
+        L.vo_direct_model.restype = None
         L.vo_relax.argtypes = [_vp, _L, _d]
         L.vo_relax.restype = None
         L.vo_cs_advance.argtypes = [_vp, _L, _i, _i, _d, _i, _i, _d, _i, _d, _i, _i, _d]
@@ -149,3 +151,14 @@ def direct(targets: np.ndarray, sources: np.ndarray) -> np.ndarray:
     t = targets.copy()
     oracle().vo_direct(t.ctypes.data, t.size, sources.ctypes.data, sources.size)
     return t
+
+
+def direct_model(bodies: np.ndarray, cells: np.ndarray, p2p: np.ndarray, targets) -> np.ndarray:
+    """Direct sum with the FMM's kernel split (regularised on P2P-list leaf
+    pairs, singular elsewhere) at tree-order bodies `targets`; [nt, 12]."""
+    t = np.ascontiguousarray(np.asarray(targets, dtype=np.uint32))
+    pairs = np.ascontiguousarray(p2p, dtype=np.uint64)
+    out = np.zeros((t.size, 12))
+    oracle().vo_direct_model(bodies.ctypes.data, bodies.size, cells.ctypes.data, cells.size, pairs.ctypes.data,
+                             len(pairs), t.ctypes.data, t.size, out.ctypes.data)
+    return out

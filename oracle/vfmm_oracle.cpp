@@ -1093,6 +1093,65 @@ void vo_direct(Body *t, long nt, const Body *s, long ns)
   }
 }
 
+// Model-consistent direct sum (the accuracy yardstick of the FMM): for each
+// target body (index into the tree-order bodies), every other body
+// contributes through the regularised kernel (multipoleKernels.hpp:239-283)
+// when its leaf is on the target leaf's P2P list, else through the singular
+// Biot-Savart kernel that the expansions represent (multipoleKernels.hpp:
+// 519-552, :631-742).  out: nt records of 12 (velocity, J row-major).
+void vo_direct_model(const Body *b, long n, const Cell *cells, long nc, const uint64_t *p2p, long np2p, const uint32_t *tgt, long nt,
+                     double *out)
+{
+  std::vector<long> leaf_of(n, -1);
+  for (long c = 0; c < nc; c++)
+    if (cells[c].NCHILD == 0)
+      for (uint64_t i = cells[c].BodyOffset; i < cells[c].BodyOffset + cells[c].NBODY; i++)
+        leaf_of[i] = c;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (long t = 0; t < nt; t++) {
+    const Body       &bi = b[tgt[t]];
+    const long        ct = leaf_of[tgt[t]];
+    std::vector<char> near(nc, 0);
+    for (long q = 0; q < np2p; q++)
+      if ((long)p2p[2 * q] == ct)
+        near[p2p[2 * q + 1]] = 1;
+    double s[12] = {0};
+    for (long j = 0; j < n; j++) {
+      const Body &bj = b[j];
+      double      dX[3];
+      for (int d = 0; d < 3; d++)
+        dX[d] = bi.X[d] - bj.X[d];
+      const double R2 = dX[0] * dX[0] + dX[1] * dX[1] + dX[2] * dX[2];
+      if (R2 == 0)
+        continue;
+      const double c4 = 0.25 * inv_pi / R2 / std::sqrt(R2);
+      double       g = 1.0, aux = -3.0 / R2;
+      if (near[leaf_of[j]]) {
+        const double S2 = bj.radius * bj.radius, RS = R2 / S2 / 2.0, sq = std::sqrt(RS);
+        const double t2 = 2.0 * inv_sqrtpi * sq * std::exp(-RS);
+        g   = std::erf(sq) - t2;
+        aux = t2 / S2 - 3.0 * g / R2;
+      }
+      const double cr[3] = {c4 * (dX[1] * bj.alpha[2] - dX[2] * bj.alpha[1]), c4 * (dX[2] * bj.alpha[0] - dX[0] * bj.alpha[2]),
+                            c4 * (dX[0] * bj.alpha[1] - dX[1] * bj.alpha[0])};
+      for (int a = 0; a < 3; a++)
+        s[a] += cr[a] * g;
+      for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 3; c++)
+          s[3 + 3 * a + c] += aux * cr[a] * dX[c];
+      const double a2 = g * c4;
+      s[6] -= a2 * bj.alpha[2];
+      s[9] += a2 * bj.alpha[1];
+      s[4] += a2 * bj.alpha[2];
+      s[10] -= a2 * bj.alpha[0];
+      s[5] -= a2 * bj.alpha[1];
+      s[8] += a2 * bj.alpha[0];
+    }
+    for (int k = 0; k < 12; k++)
+      out[12 * t + k] = -s[k];
+  }
+}
+
 // Time-step relaxation alone (on J already present in the bodies).
 void vo_relax(Body *b, long n, double f)
 {

@@ -11,7 +11,8 @@ pytestmark = pytest.mark.gpu
 
 EVAL = ["cloud_p6_c16_t05", "ring_p8_c32_t05", "cloud_p10_c64_t05", "cloud_p4_c128_t03", "cloud_p14_c32_t05",
         "classic_rvpm_p6", "root_leaf", "coincident", "lattice_ties"]
-ADV = ["advance_rk2_ring", "advance_rk3_cloud", "advance_euler_cloud", "advance_rk4_cloud"]
+ADV = ["advance_rk2_ring", "advance_rk3_cloud", "advance_euler_cloud", "advance_rk4_cloud", "advance_rvpm_rk2_ring",
+       "advance_rvpm_rk3_cloud"]
 TOL = 1e-10
 SCHEMES = {0: "Euler", 1: "RK2", 2: "RK3", 3: "RK4"}
 
@@ -110,6 +111,57 @@ def test_larger_against_oracle(vfmm_lib, kind, n, P, ncrit):
         c.copyBodies2Host(bb)
     for f in ["velocity", "J", "dadt"]:
         assert rel(bb[f], ref[f]) < TOL, f
+
+
+def test_ring_configuration_against_oracle(vfmm_lib):
+    """The plain FP64 ring configuration as specified: 256 stations x 127
+    points (32,512 bodies), p = 8, theta = 0.5, leaf 32, ten RK2 steps of
+    dt = 0.01 with relaxation (factor 0.3) after each step, through
+    vfmm_advance, against the oracle restatement of the reference's advance."""
+    import time
+    from oracle import oracle as O
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.ring(256, seed=0)
+    assert b.size == 32512
+    t0 = time.perf_counter()
+    ref = O.advance(b, 8, 32, 0.5, 0.01, 10, 1, relax=0.3)
+    t_cpu = time.perf_counter() - t0
+    with FMMCalculator(p=8, ncrit=32, theta=0.5, integration="RK2", relax=0.3) as c:
+        bb = b.copy()
+        c.advance(bb.copy(), 0.01)  # warm-up (buffers, kernels)
+        bb = b.copy()
+        t0 = time.perf_counter()
+        for _ in range(10):
+            c.advance(bb, 0.01)
+        t_gpu = time.perf_counter() - t0
+    print(f"ring 32,512 bodies, 10 RK2 steps with relaxation: GPU FP64 {t_gpu:.3f} s, oracle (CPU) {t_cpu:.2f} s")
+    for f in ["X", "alpha", "radius", "velocity", "J"]:
+        assert rel(bb[f], ref[f]) < TOL, f
+
+
+def test_direct_model_against_oracle(vfmm_lib):
+    """vfmm_direct_model (regularised kernel on P2P-list leaf pairs, singular
+    elsewhere) against the oracle's restatement on the same tree; and the FMM's
+    distance from it equals the oracle FMM's (the truncation error)."""
+    from oracle import oracle as O
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(20000, seed=31)
+    with FMMCalculator(p=10, ncrit=64, theta=0.5) as c:
+        bb = b.copy()
+        c.init(bb)
+        cells = c.tree()
+        p2p, _ = c.lists()
+        tgt = np.arange(0, bb.size, 61)
+        u, J = c.direct_model(tgt)
+        c.calculate()
+        c.copyBodies2Host(bb)
+    ref = O.direct_model(bb, cells, p2p, tgt)
+    assert rel(u, ref[:, :3]) < 1e-12
+    assert rel(J.reshape(-1, 9), ref[:, 3:]) < 1e-12
+    e_gpu = rel_l2(bb["velocity"][tgt], u)
+    fmm = O.calculate(b, 10, 64, 0.5)
+    e_cpu = rel_l2(fmm["velocity"][tgt], ref[:, :3])
+    assert e_cpu > 1e-6 and abs(e_gpu - e_cpu) < 1e-8, (e_gpu, e_cpu)
 
 
 def test_direct_sum_against_oracle(vfmm_lib):

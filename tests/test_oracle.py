@@ -116,3 +116,28 @@ def test_relaxation_aligns_strength_with_vorticity():
     b["J"][0] = [[0, -1, 0], [1, 0, 0], [0, 0, 0]]  # omega = (0, 0, 2)
     O.oracle().vo_relax(b.ctypes.data, 1, 0.5)
     np.testing.assert_allclose(b["alpha"][0], [0.5, 0.0, 0.5], atol=1e-15)
+
+
+def test_direct_model_is_the_fmm_kernel_split():
+    """The model-consistent direct sum (regularised kernel on P2P-list leaf
+    pairs, singular elsewhere) is the sum the reference's FMM approximates:
+    with every leaf pair on the P2P list it is the plain regularised direct
+    sum, and the FMM's distance from it shrinks as the order grows
+    (truncation error alone)."""
+    from uvlm_gb300 import workloads
+    b = workloads.cloud(1500, seed=9)
+    tb, cells = O.build_tree(b, 32)
+    tgt = np.arange(0, tb.size, 7)
+    leaves = np.flatnonzero(cells["NCHILD"] == 0)
+    every = np.array([(i, j) for i in leaves for j in leaves], dtype=np.uint64)
+    allnear = O.direct_model(tb, cells, every, tgt)
+    ref = O.direct(tb[tgt].copy(), tb)
+    assert rel(allnear[:, :3], ref["velocity"]) < 1e-13
+    assert rel(allnear[:, 3:], ref["J"].reshape(-1, 9)) < 1e-13
+    p2p, _ = O.lists(cells, 0.5)
+    model = O.direct_model(tb, cells, p2p, tgt)
+    errs = []
+    for P in (4, 8, 12, 16):
+        fmm = O.calculate(b, P, 32, 0.5)
+        errs.append(np.linalg.norm(fmm["velocity"][tgt] - model[:, :3]) / np.linalg.norm(model[:, :3]))
+    assert all(e1 < 0.6 * e0 for e0, e1 in zip(errs, errs[1:])), errs

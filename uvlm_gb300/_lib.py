@@ -91,6 +91,7 @@ _PROTOS = {
     "vfmm_stage": (_i, [_H, _i, _d]),
     "vfmm_num_stages": (_i, [_H]),
     "vfmm_direct": (_i, [_H, _vp, _sz, _vp, _sz]),
+    "vfmm_direct_model": (_i, [_H, _vp, _sz, _vp]),
     "vfmm_event_record": (_i, [_H, _i]),
     "vfmm_event_elapsed": (_i, [_H, _i, _i, ctypes.POINTER(ctypes.c_float)]),
     "vfmm_synchronize": (_i, [_H]),

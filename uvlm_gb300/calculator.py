@@ -150,6 +150,16 @@ class FMMCalculator:
         del keep
         return (value.value, gx, ga) if gradient else value.value
 
+    def direct_model(self, targets) -> tuple[np.ndarray, np.ndarray]:
+        """vfmm_direct_model: FP64 direct sum with this FMM's own kernel split
+        (regularised on P2P-list leaf pairs, singular elsewhere) at the bodies
+        with tree-order indices `targets`, on the tree of the last init;
+        returns (velocity [nt, 3], J [nt, 3, 3])."""
+        t = np.ascontiguousarray(np.asarray(targets, dtype=np.uint32))
+        out = np.zeros((t.size, 12))
+        self._check(lib().vfmm_direct_model(self._h, t.ctypes.data, t.size, out.ctypes.data))
+        return out[:, :3].copy(), out[:, 3:].reshape(-1, 3, 3).copy()
+
     def relax(self, f: float) -> None:
         self._check(lib().vfmm_relax(self._h, float(f)))
 

@@ -5,6 +5,7 @@
 //   advance   = stages of init + calculate + stage update    (:919-1005)
 // All work runs on the handle's stream; the host synchronises twice per
 // tree build (node counts, pair counts) and at the end of each API call.
+#include <climits>
 #include <algorithm>
 #include <atomic>
 #include <thread>
@@ -113,6 +114,7 @@ struct vfmm_handle_s {
   DevBuf<unsigned char> flushbuf;
   DevBuf<double>        dtmp;
   bool                  has_tree = false, has_eval = false;
+  bool                  moved    = false; // a stage update moved the bodies after the last tree build
 
   // reverse mode (vfmm_adjoint): adjoint state (ping-pong for the reorders),
   // work fields, adjoint expansions, lists by source, checkpoints, caller
@@ -420,6 +422,7 @@ void build_tree_and_lists(vfmm_handle h, bool for_evaluation = false)
     VFMM_CUDA_TRY(cudaEventRecord(h->ph[1], s));
   h->has_tree = true;
   h->has_eval = false;
+  h->moved    = false;
 }
 
 void ensure_items(vfmm_handle h)
@@ -698,6 +701,7 @@ void stage_update(vfmm_handle h, int stage, double dt, bool relax = true)
   a.rk4_fixed     = h->cfg.rk4_fixed;
   a.store_initial = (stage == 0 && (a.scheme == VFMM_RK2 || a.scheme == VFMM_RK4)) ? 1 : 0;
   a.do_update     = 1;
+  h->moved        = true;
   a.dt            = dt;
   a.relax         = (relax && stage == stages_of(a.scheme) - 1) ? h->cfg.relax : 0.0;
   a.csm           = h->cfg.viscous == VFMM_CSM;
@@ -766,9 +770,16 @@ void advance_batch(vfmm_handle *hs, vfmm_body *const *bodies, const size_t *ns, 
     }
     g_launch_counter = nullptr;
   };
-  if (T == 1)
+  if (T == 1) {
+    // on the caller's thread: leave its current device and launch counter as they were
+    int                 dev0  = -1;
+    unsigned long long *prev  = g_launch_counter;
+    const bool          haved = cudaGetDevice(&dev0) == cudaSuccess;
     work();
-  else {
+    g_launch_counter = prev;
+    if (haved)
+      cudaSetDevice(dev0);
+  } else {
     std::vector<std::thread> pool;
     for (int t = 0; t < T; t++)
       pool.emplace_back(work);
@@ -1414,6 +1425,31 @@ int vfmm_direct(vfmm_handle h, vfmm_body *targets, size_t nt, const vfmm_body *s
       for (int k = 0; k < 9; k++)
         targets[i].J[k / 3][k % 3] = ho[(3 + k) * nt + i];
     }
+  });
+}
+
+int vfmm_direct_model(vfmm_handle h, const uint32_t *targets, size_t nt, double *out)
+{
+  return guarded(h, [&] {
+    if (!targets || !out || nt == 0)
+      throw Error(VFMM_ERR_INVALID, "empty target set");
+    if (!h->has_tree || h->moved)
+      throw Error(VFMM_ERR_STATE, "the model direct sum needs the tree of the current positions: call init first");
+    if (nt > (size_t)INT_MAX / 16)
+      throw Error(VFMM_ERR_INVALID, "too many targets");
+    for (size_t i = 0; i < nt; i++)
+      if (targets[i] >= (uint32_t)h->n)
+        throw Error(VFMM_ERR_INVALID, "target index out of range");
+    cudaStream_t s       = h->stream;
+    const int    nchunks = std::max(1, std::min(64, h->n / 4096));
+    h->dtmp.reserve((size_t)nt * 12 * (nchunks + 2) + nt / 2 + 1);
+    double   *scratch = h->dtmp.p, *dout = scratch + (size_t)nt * 12 * (nchunks + 1);
+    uint32_t *dtgt    = reinterpret_cast<uint32_t *>(dout + (size_t)nt * 12);
+    VFMM_CUDA_TRY(cudaMemcpyAsync(dtgt, targets, nt * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    direct_model_sum(s, h->soa[h->cur].p, h->cap, h->n, h->tree.view(), h->tree.leaf_cells.p, h->tree.nleaves, h->lists.p2p_start.p,
+                     h->lists.p2p_src.p, dtgt, (int)nt, scratch, nchunks, dout);
+    VFMM_CUDA_TRY(cudaMemcpyAsync(out, dout, nt * 12 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VFMM_CUDA_TRY(cudaStreamSynchronize(s));
   });
 }
 

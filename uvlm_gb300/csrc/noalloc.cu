@@ -20,7 +20,10 @@
 //
 // Set-up: the first call on each device looks up the array's device address
 // (cudaGetSymbolAddress) with that device current; make that first call before
-// any stream capture begins.
+// any stream capture begins.  The address is kept for the life of the process:
+// cudaDeviceReset unloads the library's device module, and the array may come
+// back elsewhere, so this entry point must not be used after a reset of that
+// device.
 #include <climits>
 #include <mutex>
 #include "vfmm_internal.cuh"

@@ -39,7 +39,10 @@ __device__ __forceinline__ int lower_bound_u64(const uint64_t *a, int lo, int hi
 __global__ void k_bbox_partial(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, int n, double *part)
 {
   double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // 64-bit index: n may be close to 2^31 - 1, where i + gridDim.x * blockDim.x
+  // would overflow an int
+  const long long step = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
     const double v[3] = {x[i], y[i], z[i]};
     for (int d = 0; d < 3; d++) {
       mn[d] = fmin(v[d], mn[d]);
@@ -142,7 +145,10 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
   if (threadIdx.x < MAXL)
     half[threadIdx.x] = __ddiv_rn(info->R0, (double)(1 << (threadIdx.x + 1)));
   __syncthreads();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // 64-bit index: n may be close to 2^31 - 1, where i + gridDim.x * blockDim.x
+  // would overflow an int
+  const long long step = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
     const double p[3] = {x[i], y[i], z[i]};
     double       c[3] = {info->X0[0], info->X0[1], info->X0[2]};
     uint64_t     key  = 0;
@@ -166,7 +172,10 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
 // bodies set info->deeper (the build is redone with full keys).
 __global__ void k_leaf_level(const uint64_t *__restrict__ sk, int n, int ncrit, int levels, int *lvl, int *lo, int *hi, DevInfo *info)
 {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // 64-bit index: n may be close to 2^31 - 1, where i + gridDim.x * blockDim.x
+  // would overflow an int
+  const long long step = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
     const uint64_t key = sk[i];
     int            a = 0, b = n, L = -1;
     for (int l = 0; l <= levels; l++) {
@@ -197,7 +206,10 @@ __global__ void k_leaf_level(const uint64_t *__restrict__ sk, int n, int ncrit, 
 // Inside a leaf, bodies keep their incoming relative order.
 __global__ void k_leaf_perm(const uint32_t *__restrict__ sidx, const int *__restrict__ lo, const int *__restrict__ hi, int n, uint32_t *perm)
 {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // 64-bit index: n may be close to 2^31 - 1, where i + gridDim.x * blockDim.x
+  // would overflow an int
+  const long long step = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
     const int      a = lo[i], b = hi[i];
     const uint32_t me = sidx[i];
     int            rank = 0;
@@ -219,7 +231,10 @@ __device__ __forceinline__ int common_digits(uint64_t a, uint64_t b)
 // Number of cells whose first body is sorted body i.
 __global__ void k_node_count(const uint64_t *__restrict__ sk, const int *__restrict__ lvl, int n, int *cnt)
 {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // 64-bit index: n may be close to 2^31 - 1, where i + gridDim.x * blockDim.x
+  // would overflow an int
+  const long long step = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
     const int L = lvl[i];
     if (i == 0)
       cnt[i] = L + 1;
@@ -233,7 +248,10 @@ __global__ void k_node_count(const uint64_t *__restrict__ sk, const int *__restr
 __global__ void k_node_write(const uint64_t *__restrict__ sk, const int *__restrict__ lvl, const int *__restrict__ hi, const int *__restrict__ off,
                              const int *__restrict__ cnt, int n, int *nlevel, int *nstart, int *ncount, int ncap, DevInfo *info)
 {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // 64-bit index: n may be close to 2^31 - 1, where i + gridDim.x * blockDim.x
+  // would overflow an int
+  const long long step = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
     const int c = cnt[i];
     if (c == 0)
       continue;

@@ -1,6 +1,8 @@
 // Internal declarations shared by the vfmm CUDA translation units.
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
+#include <mutex>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -77,21 +79,48 @@ inline void count_launch()
 
 #define VFMM_LAUNCH_CHECK() VFMM_CUDA_TRY(cudaGetLastError())
 
-// Raise a kernel's dynamic shared-memory limit once per process.  A
-// function-local static is initialised exactly once even when several host
-// threads launch (vfmm_advance_batch runs systems on a thread pool).
-// The kernel comes last so that template arguments may contain commas.
-#define VFMM_SMEM_ONCE(bytes, ...)                                                                                                      \
-  do {                                                                                                                                  \
-    static const cudaError_t vfmm_attr_ = cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bytes)); \
-    VFMM_CUDA_TRY(vfmm_attr_);                                                                                                          \
-  } while (0)
-
 struct Error {
   int         code;
   std::string msg;
   Error(int c, std::string m) : code(c), msg(std::move(m)) {}
 };
+
+// Raise a kernel's dynamic shared-memory limit once per device.  The
+// attribute belongs to the device that is current when it is set, and handles
+// on different GPUs may share a process (vfmm_config.device), so each call
+// site keeps one flag per device ordinal; a mutex makes the first setting
+// thread-safe (vfmm_advance_batch runs systems on a thread pool).  The kernel
+// comes last so that template arguments may contain commas.
+struct PerDeviceOnce {
+  static constexpr int NDEV = 64;
+  std::mutex           mu;
+  std::atomic<bool>    done[NDEV] = {};
+  template <class F>
+  void run(F &&f)
+  {
+    int dev = 0;
+    VFMM_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NDEV) { // beyond the table: set it every time (cheap)
+      VFMM_CUDA_TRY(f());
+      return;
+    }
+    if (done[dev].load(std::memory_order_acquire))
+      return;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[dev].load(std::memory_order_relaxed))
+      return;
+    VFMM_CUDA_TRY(f());
+    done[dev].store(true, std::memory_order_release);
+  }
+};
+
+#define VFMM_SMEM_ONCE(bytes, ...)                                                                              \
+  do {                                                                                                          \
+    static ::vfmm::PerDeviceOnce vfmm_once_;                                                                    \
+    vfmm_once_.run([&]() { return cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                                       (int)(bytes)); });                                        \
+  } while (0)
+
 
 // Grow-only device buffer.
 template <class T>
@@ -307,6 +336,11 @@ void adjoint_rows(cudaStream_t s, const double *g, size_t cap, int n, int field,
 
 // ---- direct.cu
 void direct_sum(cudaStream_t s, const double *tx, const double *ty, const double *tz, int nt, const double *src, size_t scap, int ns, double *out /*12*nt*/);
+// Model-consistent FP64 direct sum on a built tree: singular kernel for all
+// pairs plus (regularised - singular) over each target leaf's P2P row;
+// scratch holds (nchunks + 1) * 12 * nt doubles; out is [nt][12].
+void direct_model_sum(cudaStream_t s, const double *soa, size_t cap, int n, CellsView cv, const int *leaf_cells, int nleaves, const int *p2p_start,
+                      const int *p2p_src, const uint32_t *tgt, int nt, double *scratch, int nchunks, double *out);
 
 // Asynchronous global -> shared copies (cp.async): 8 bytes through L1, 16
 // bytes through L2 (both addresses aligned to the size), and the wait for all
