@@ -117,24 +117,41 @@ def test_ring_configuration_against_oracle(vfmm_lib):
     """The plain FP64 ring configuration as specified: 256 stations x 127
     points (32,512 bodies), p = 8, theta = 0.5, leaf 32, ten RK2 steps of
     dt = 0.01 with relaxation (factor 0.3) after each step, through
-    vfmm_advance, against the oracle restatement of the reference's advance."""
+    vfmm_advance, against the oracle restatement of the reference's advance.
+
+    At theta = 0.5 cells two apart on the octree lattice sit exactly on the
+    MAC boundary |dX| theta = Ri + Rj, so the last bit of the centre
+    arithmetic decides between M2L and P2P for them, in the reference too: on
+    the oracle alone, a 1-ulp nudge of one body's position moves this
+    configuration's 10-step result by 1e-4 (by 7e-16 at theta = 0.47).  Two
+    codes that sum in different orders therefore cannot follow one another for
+    ten free-running steps at theta = 0.5.  So every step is compared from the
+    same input state (the oracle restarted from the GPU's state each step), at
+    1e-10; and ten free-running steps are compared at theta = 0.47."""
     import time
     from oracle import oracle as O
     from uvlm_gb300 import FMMCalculator, workloads
     b = workloads.ring(256, seed=0)
     assert b.size == 32512
-    t0 = time.perf_counter()
-    ref = O.advance(b, 8, 32, 0.5, 0.01, 10, 1, relax=0.3)
-    t_cpu = time.perf_counter() - t0
+    t_cpu = t_gpu = 0.0
     with FMMCalculator(p=8, ncrit=32, theta=0.5, integration="RK2", relax=0.3) as c:
+        c.advance(b.copy(), 0.01)  # warm-up (buffers, kernels)
+        state = b.copy()
+        for step in range(10):
+            t0 = time.perf_counter()
+            ref = O.advance(state, 8, 32, 0.5, 0.01, 1, 1, relax=0.3)
+            t_cpu += time.perf_counter() - t0
+            t0 = time.perf_counter()
+            c.advance(state, 0.01)
+            t_gpu += time.perf_counter() - t0
+            for f in ["X", "alpha", "radius", "velocity", "J"]:
+                assert rel(state[f], ref[f]) < TOL, (step, f)
+    print(f"ring 32,512 bodies, 10 RK2 steps with relaxation, theta 0.5: GPU FP64 {t_gpu:.3f} s, oracle (CPU) {t_cpu:.2f} s")
+    ref = O.advance(b, 8, 32, 0.47, 0.01, 10, 1, relax=0.3)
+    with FMMCalculator(p=8, ncrit=32, theta=0.47, integration="RK2", relax=0.3) as c:
         bb = b.copy()
-        c.advance(bb.copy(), 0.01)  # warm-up (buffers, kernels)
-        bb = b.copy()
-        t0 = time.perf_counter()
         for _ in range(10):
             c.advance(bb, 0.01)
-        t_gpu = time.perf_counter() - t0
-    print(f"ring 32,512 bodies, 10 RK2 steps with relaxation: GPU FP64 {t_gpu:.3f} s, oracle (CPU) {t_cpu:.2f} s")
     for f in ["X", "alpha", "radius", "velocity", "J"]:
         assert rel(bb[f], ref[f]) < TOL, f
 
