@@ -304,6 +304,16 @@ int vfmm_flush_l2(vfmm_handle h);
  * FP64/FP32 pipes rather than on tensor cores. */
 int vfmm_measure_fma_peak(vfmm_handle h, int precision, double *tflops);
 
+/* No counterpart in the reference.  Self-test of the tensor-core operand
+ * layouts the mixed-precision M2L relies on (sm_100-family GPUs): one
+ * tcgen05 kind::tf32 MMA D[128 x 16] = A[128 x 8] x B[8 x 16] with A in tensor
+ * memory and B in shared memory (K-major, no swizzle; core matrices adjacent
+ * in K 256 bytes apart, adjacent in N 128 bytes apart, or the reverse when
+ * swap_offsets = 1), on small integers, A[m][k] = (3m + 5k) mod 11 - 5 and
+ * B[k][n] = (7k + 3n) mod 13 - 6.  Writes D row-major to the host array out
+ * (128 x 16 floats).  VFMM_ERR_UNSUPPORTED on other GPUs. */
+int vfmm_tcgen05_selftest(int device, int swap_offsets, float *out);
+
 /* ---- output --------------------------------------------------------------- */
 
 /* Writes n bodies to `path` as legacy-VTK polydata, the file of the

@@ -104,6 +104,7 @@ _PROTOS = {
     "vfmm_measure_fma_peak": (_i, [_H, _i, ctypes.POINTER(ctypes.c_double)]),
     "vfmm_bounds_noalloc": (_i, [_vp, _vp, _vp, _sz, _vp, _vp]),
     "vfmm_write_vtk": (_i, [_vp, _sz, ctypes.c_char_p, _i]),
+    "vfmm_tcgen05_selftest": (_i, [_i, _i, _vp]),
 }
 
 _LIB = None
