@@ -233,7 +233,8 @@ def rel_l2(a, b):
 
 @pytest.mark.parametrize("kind,n,P,ncrit,theta", [("cloud", 40000, 10, 64, 0.5), ("cloud", 20000, 14, 64, 0.5), ("cloud", 20000, 6, 64, 0.5),
                                                   ("ring", 96, 8, 32, 0.5), ("cloud", 15000, 16, 64, 0.5), ("ring", 48, 15, 32, 0.5),
-                                                  ("cloud", 3000, 3, 16, 0.5), ("cloud", 20000, 8, 32, 0.3)])
+                                                  ("cloud", 3000, 3, 16, 0.5), ("cloud", 20000, 8, 32, 0.3),
+                                                  ("cloud", 30000, 9, 64, 0.5), ("ring", 64, 10, 32, 0.5), ("cloud", 20000, 10, 32, 0.3)])
 def test_mixed_matches_fp64_fmm(vfmm_lib, kind, n, P, ncrit, theta):
     """The mixed path (FP32 expansion kernels and P2P, FP64 tree) against the
     FP64 path on the same tree: relative L2 error of velocity and of J below

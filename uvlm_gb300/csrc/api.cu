@@ -110,6 +110,8 @@ struct vfmm_handle_s {
   int             items_P = 0, items_per_lane = 0, items_batch = 0;
   DevBuf<float2>  Mp32;
   DevBuf<float4>  pos32, alp32;
+  TcScratch       tcs;                // tensor-core M2L (mixed mode, p = 8..10)
+  int            *eval_err = nullptr; // device: error raised by an evaluation kernel (bounded waits)
 
   DevBuf<unsigned char> flushbuf;
   DevBuf<double>        dtmp;
@@ -262,6 +264,8 @@ void upload(vfmm_handle h, const vfmm_body *b, size_t n)
   }
 }
 
+void check_eval_err(vfmm_handle h);
+
 void download(vfmm_handle h, vfmm_body *b, size_t n)
 {
   if ((int)n != h->n)
@@ -273,6 +277,7 @@ void download(vfmm_handle h, vfmm_body *b, size_t n)
     VFMM_CUDA_TRY(cudaMemcpyAsync(b, h->aos.p, n * sizeof(vfmm_body), cudaMemcpyDeviceToHost, h->stream));
   }
   VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  check_eval_err(h);
 }
 
 void read_info(cudaStream_t s, DevInfo *info, DevInfo *hinfo)
@@ -481,6 +486,28 @@ ExpArgs particle_args(vfmm_handle h)
   return e;
 }
 
+// The tensor-core M2L (p = 8..10, mixed mode) while it is being tuned:
+// VFMM_M2L_TENSOR=1 in the environment selects it.
+bool tensor_m2l(int p)
+{
+  static const bool on = [] {
+    const char *v = getenv("VFMM_M2L_TENSOR");
+    return v && v[0] == '1';
+  }();
+  return on && p >= TC_PMIN && p <= TC_PMAX;
+}
+
+// Raise the error an evaluation kernel recorded (after a stream sync).
+void check_eval_err(vfmm_handle h)
+{
+  int e = 0;
+  VFMM_CUDA_TRY(cudaMemcpy(&e, h->eval_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    VFMM_CUDA_TRY(cudaMemset(h->eval_err, 0, sizeof(int)));
+    throw Error(e, "a tensor-core M2L wait on the GPU gave up (time limit)");
+  }
+}
+
 void calculate(vfmm_handle h)
 {
   if (!h->has_tree)
@@ -504,6 +531,17 @@ void calculate(vfmm_handle h)
     m.items32 = h->items32.p;
     m.lanes32   = h->lanes32.p;
     m.m2l_batch = h->m2l_batch;
+    if (tensor_m2l(h->cfg.p)) {
+      const size_t rows = (size_t)h->tree.ncells * 3 * tc_kp(h->cfg.p);
+      h->tcs.B.reserve(2 * rows);
+      m.tc           = &h->tcs;
+      m.Bhi          = h->tcs.B.p;
+      m.Blo          = h->tcs.B.p + rows;
+      m.m2l_keys     = h->lists.ls.m2l_sorted.p;
+      m.m2l_key_bits = h->lists.ls.key_bits;
+      m.n_m2l        = h->lists.n_m2l;
+      m.eval_err     = h->eval_err;
+    }
     // the FP32 kernels' scaling length: any positive value is exact; R0 = 0
     // (every body at one point, a single root leaf without far field) uses 1
     m.R0      = h->tree.R0 > 0 ? h->tree.R0 : 1.0;
@@ -830,6 +868,8 @@ int vfmm_create(const vfmm_config *cfg, vfmm_handle *out)
     for (auto &e : h->ph)
       VFMM_CUDA_TRY(cudaEventCreate(&e));
     VFMM_CUDA_TRY(cudaMalloc((void **)&h->info, sizeof(DevInfo)));
+    VFMM_CUDA_TRY(cudaMalloc((void **)&h->eval_err, sizeof(int)));
+    VFMM_CUDA_TRY(cudaMemset(h->eval_err, 0, sizeof(int)));
     VFMM_CUDA_TRY(cudaMallocHost((void **)&h->hinfo, sizeof(DevInfo)));
     std::memset(h->hinfo, 0, sizeof(DevInfo));
     VFMM_CUDA_TRY(cudaMalloc((void **)&h->sinfo, sizeof(DevInfo)));
@@ -877,6 +917,16 @@ int vfmm_destroy(vfmm_handle h)
     b->release();
   h->ts.bbox_part.release();
   h->ts.cub_tmp.release();
+  h->tcs.B.release();
+  for (auto *b : {&h->tcs.tkeys, &h->tcs.tkeys_sorted, &h->tcs.pkeys, &h->tcs.pkeys_sorted})
+    b->release();
+  for (auto *b : {&h->tcs.tile_of, &h->tcs.col_of, &h->tcs.tile_cells, &h->tcs.tile_level, &h->tcs.tile_start, &h->tcs.meta})
+    b->release();
+  h->tcs.pvals.release();
+  h->tcs.pvals_sorted.release();
+  h->tcs.cub_tmp.release();
+  if (h->eval_err)
+    cudaFree(h->eval_err);
   if (h->info)
     cudaFree(h->info);
   if (h->hinfo)
@@ -1474,7 +1524,10 @@ int vfmm_event_elapsed(vfmm_handle h, int a, int b, float *ms)
 
 int vfmm_synchronize(vfmm_handle h)
 {
-  return guarded(h, [&] { VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream)); });
+  return guarded(h, [&] {
+    VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    check_eval_err(h);
+  });
 }
 
 uint64_t vfmm_launch_count(vfmm_handle h) { return h ? h->launches : 0; }

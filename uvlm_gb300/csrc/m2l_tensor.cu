@@ -4,6 +4,8 @@
 // with A in tensor memory and B in shared memory (K-major, no swizzle), on
 // small integers (exact in TF32 and FP32), so that the host can check the
 // operand layouts the M2L kernel relies on element by element.
+#include <cub/cub.cuh>
+#include "harmonics.cuh"
 #include "tcgen05.cuh"
 #include "vfmm_internal.cuh"
 
@@ -79,6 +81,554 @@ __global__ void __launch_bounds__(128) k_tc_selftest(float *out, int swap_offset
   }
 }
 
+// ============================================================================
+// M2L on the tensor cores, by offset class.
+//
+// In the scaled variables of the mixed path, the M2L of a pair (target t,
+// source s) with d = X_t - X_s is a linear map of the source's scaled
+// multipole that depends only on the offset in units of the target's
+// half-width, o = d / R_t, and on the level difference delta = l_t - l_s:
+//   L_j^k(t) = (-1)^j R_t^(-j-1) sum_{n <= p-1-j} sum_{m=-n..n}
+//              2^(delta n) M'_n^m(s) S'_{j+n}^{m-k}(o)
+// (multipoleKernels.hpp:519-552 with the truncation j + n <= p - 1 that its
+// zero-initialised harmonics impose).  On an octree, same-level pairs have
+// o = 2 x (integer vector), so the targets of one level share a few hundred
+// offset classes, and every class is one operator A(delta, o) applied to many
+// multipoles.
+//
+// Real form.  Inputs per component: Mt_n^0 (real part; the imaginary part of
+// an m = 0 coefficient of a real field is zero) and Re/Im Mt_n^m, m = 1..n, in
+// the order n^2, n^2 + 2m - 1 (Re), n^2 + 2m (Im): P^2 values, padded to KP.
+// Outputs: Re/Im L_j^k, k <= j, row 2 tri(j, k) + (0: Re, 1: Im): P(P+1)
+// rows <= 128 for P <= 10.  With M'_n^m = (-1)^m Mt_n^m, M'_n^-m = conj(Mt_n^m)
+// and (c1, d1) = S'_q^{m-k}, (c2, d2) = S'_q^{-m-k}, q = j + n:
+//   Re L += a [(-1)^m c1 + c2] + b [-(-1)^m d1 + d2]
+//   Im L += a [(-1)^m d1 + d2] + b [(-1)^m c1 - c2]      (Mt_n^m = a + i b).
+//
+// Layout of one tile: 32 targets of one level (the same octant within their
+// parents where possible, so that their offset sets coincide), D = A B with
+// A (128 rows x KP) in tensor memory and B (KP x 96: target x component) in
+// shared memory, accumulated over all classes of the tile in TMEM.  FP32 is
+// kept by three TF32 products, A_hi B_hi + A_hi B_lo + A_lo B_hi, where x_hi
+// is x with the low 13 mantissa bits cleared and x_lo = x - x_hi.
+// ============================================================================
+
+// Class key: bits 0..10 oz + 1024, 11..21 oy + 1024, 22..32 ox + 1024,
+// 33..37 delta + 16, offsets in units of the finer cell's half-width; a pair
+// outside that range gets the sentinel class and is contracted on its own.
+constexpr int      TC_CLASS_BITS = 38;
+constexpr uint64_t TC_SENTINEL   = (1ull << TC_CLASS_BITS) - 1;
+constexpr int      TC_COL_SHIFT  = 27; // pair value: column << 27 | source cell
+
+template <int P>
+struct TcM2L {
+  static constexpr int    KR = P * P, KP = (KR + 7) / 8 * 8, NR = P * (P + 1);
+  static constexpr int    TT = 32, N = 3 * TT, KC = KP / 4;
+  static constexpr int    SBO = 128, LBO = (N / 8) * 128; // bytes: N-adjacent, K-adjacent core matrices
+  static constexpr int    BBYTES = KC * LBO;              // one B operand (hi or lo)
+  static constexpr int    STAGE  = 2 * BBYTES;            // hi + lo
+  static constexpr int    DCOL = 0, ACOL = N, ABUF = 2 * KP;
+  static constexpr size_t smem = 2 * (size_t)STAGE + 1024; // two stages + alignment slack
+  static_assert(N + 2 * ABUF <= 512, "D and two A buffers fit in the 512 TMEM columns");
+  static_assert(NR <= 128, "the output rows fit the 128 TMEM lanes");
+  static_assert(KC % 2 == 0, "B rows are gathered 32 bytes at a time");
+};
+
+struct TcArgs {
+  const unsigned long long *keys; // sorted: tile << 38 | class
+  const uint32_t           *vals; // column << 27 | source
+  int                       npairs;
+  const int                *tile_start; // [ntiles + 1]
+  const int                *tile_cells; // [ntiles][32], -1 = none
+  const int                *tile_level;
+  const int                *ntiles;     // device scalar
+  const float              *Bhi, *Blo;  // [cell][3][KP]
+  CellsView                 cv;
+  double2                  *L;
+  double                    iR0pow[PMAX + 2]; // R0^-n
+  int                      *err;
+};
+
+
+// v * 2^e for any e (exact power-of-two scaling, ldexpf outside the normal range)
+__device__ __forceinline__ float tc_scale2(float v, int e)
+{
+  return (e >= -126 && e <= 127) ? v * __int_as_float((e + 127) << 23) : ldexpf(v, e);
+}
+
+// Two-sum accumulation: hi + lo gains v without losing its low-order bits.
+__device__ __forceinline__ void tc_two_sum(float &hi, float &lo, float v)
+{
+  const float s  = hi + v;
+  const float bb = s - hi;
+  lo += (hi - (s - bb)) + (v - bb);
+  hi = s;
+}
+
+// One block (256 threads, one per SM: 512 TMEM columns) per tile at a time.
+// Warp w writes and reads TMEM lanes 32 (w % 4) .. + 31 (rows of A and D);
+// warps w and w + 4 split each row's A columns and D columns between them.
+// Per class: warp 0 decodes the members, all threads gather B (cp.async),
+// threads 0..P-1 make S'(o), all threads build their part of A in the TMEM
+// buffer of the class's parity while the previous class's MMAs run; then the
+// previous class's D is added into registers (two-sum), and one thread
+// issues this class's MMAs into a fresh D.  A fresh D per class, with the
+// small products first (A_lo B_hi and A_hi B_lo, then A_hi B_hi, each from
+// the highest degrees down), keeps the tensor core's truncating FP32
+// accumulation to a few units in the last place of each class's sum; the sum
+// over classes is a two-sum in registers.
+template <int P>
+__global__ void __launch_bounds__(256, 1) k_m2l_tc(TcArgs a)
+{
+  using G = TcM2L<P>;
+  constexpr int K = nterms(P), KP = G::KP, N = G::N, NCH = KP / 8;
+  constexpr int C0 = (NCH + 1) / 2;     // A chunks of the first half of the warps
+  constexpr int DH = N / 2;              // D columns per half
+  static_assert(DH % 8 == 0, "D columns per half are whole 8-column loads");
+  extern __shared__ unsigned char tc_smem_raw[];
+  unsigned char *sB = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ cx<float> Ys[P * P];
+  __shared__ int       srcS[2][32];
+  __shared__ float4    offS[2]; // class offset o (target units), w = delta (as int bits)
+  __shared__ int       tcell[32];
+  __shared__ int       nextE[2];
+  __shared__ uint32_t  tbase;
+  __shared__ __align__(8) uint64_t mbar[2];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quarter = warp & 3, half = warp >> 2;
+
+  if (warp == 0) {
+    tc::tmem_alloc(&tbase, 512);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(&mbar[0], 1);
+    tc::mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tb = tbase;
+
+  // this thread's output row (TMEM lane)
+  const int  row   = 32 * quarter + lane;
+  const bool rlive = row < G::NR;
+  int        rj = 0, rk = 0;
+  if (rlive) {
+    const int jks = row >> 1;
+    while ((rj + 1) * (rj + 2) / 2 <= jks)
+      rj++;
+    rk = jks - rj * (rj + 1) / 2;
+  }
+  const int      rpart = row & 1;
+  const uint32_t lane_base = tc::tmem_addr(tb, 32 * quarter, 0);
+
+  float acc_hi[DH], acc_lo[DH];
+  // add D (this thread's row, columns [DH half, DH half + DH)) into the accumulators
+  auto drain = [&]() {
+#pragma unroll
+    for (int c8 = 0; c8 < DH / 8; c8++) {
+      uint32_t v[8];
+      tc::tmem_ld8(lane_base + G::DCOL + DH * half + 8 * c8, v);
+      tc::tmem_ld_wait();
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        tc_two_sum(acc_hi[8 * c8 + i], acc_lo[8 * c8 + i], __uint_as_float(v[i]));
+    }
+  };
+
+  const int ntiles = *a.ntiles;
+  unsigned  g      = 0; // classes issued by this block so far
+  bool      failed = false;
+  for (int T = blockIdx.x; T < ntiles && !failed; T += gridDim.x) {
+    const int p0 = a.tile_start[T], p1 = a.tile_start[T + 1];
+    const int lt = a.tile_level[T];
+    if (tid < 32)
+      tcell[tid] = a.tile_cells[T * 32 + tid];
+    if (p0 >= p1)
+      continue; // (every tile has pairs; kept for safety: its cells' L stay zero)
+#pragma unroll
+    for (int i = 0; i < DH; i++)
+      acc_hi[i] = acc_lo[i] = 0.f;
+    const unsigned first = g;
+    for (int e = p0; e < p1;) {
+      const int s = g & 1;
+      // (1) members of the class starting at e (warp 0)
+      if (warp == 0) {
+        const unsigned long long k0  = a.keys[e];
+        const bool               in  = e + lane < p1;
+        const unsigned long long kl  = in ? a.keys[e + lane] : ~0ull;
+        const bool               sen = (k0 & TC_SENTINEL) == TC_SENTINEL;
+        const unsigned           eq  = __ballot_sync(0xffffffffu, in && kl == k0);
+        const int                cnt = sen ? 1 : __popc(eq); // members are contiguous from lane 0
+        srcS[s][lane] = -1;
+        __syncwarp();
+        if (lane < cnt) {
+          const uint32_t v = a.vals[e + lane];
+          srcS[s][v >> TC_COL_SHIFT] = (int)(v & ((1u << TC_COL_SHIFT) - 1));
+        }
+        if (lane == 0) {
+          float4 o;
+          if (!sen) {
+            const int   dz = (int)(k0 & 2047) - 1024, dy = (int)((k0 >> 11) & 2047) - 1024, dx = (int)((k0 >> 22) & 2047) - 1024;
+            const int   dl = (int)((k0 >> 33) & 31) - 16;
+            const float f  = dl < 0 ? ldexpf(1.f, dl) : 1.f; // offsets are in units of the finer cell
+            o              = make_float4(dx * f, dy * f, dz * f, __int_as_float(dl));
+          } else {
+            const uint32_t v  = a.vals[e];
+            const int      sc = (int)(v & ((1u << TC_COL_SHIFT) - 1)), t = tcell[v >> TC_COL_SHIFT];
+            const double   iR = 1.0 / a.cv.R[t];
+            o = make_float4((float)((a.cv.x[t] - a.cv.x[sc]) * iR), (float)((a.cv.y[t] - a.cv.y[sc]) * iR),
+                            (float)((a.cv.z[t] - a.cv.z[sc]) * iR), __int_as_float(lt - a.cv.level[sc]));
+          }
+          offS[s]  = o;
+          nextE[s] = e + cnt;
+        }
+      }
+      __syncthreads();
+      // (2) B of this class into stage s (its last reader, the MMAs of class
+      // g - 2, completed before class g - 1 was issued), and S'(o)
+      {
+        unsigned char *bst = sB + s * G::STAGE;
+        constexpr int  KC2 = G::KC / 2, TASKS = 2 * N * KC2;
+        for (int w = tid; w < TASKS; w += 256) {
+          const int which = w / (N * KC2), rem = w - which * (N * KC2);
+          const int n = rem % N, cp2 = rem / N;
+          const int src = srcS[s][n / 3], d = n % 3;
+          unsigned char *dst = bst + which * G::BBYTES + (2 * cp2) * G::LBO + (n >> 3) * G::SBO + (n & 7) * 16;
+          if (src >= 0) {
+            const float *gsrc = (which ? a.Blo : a.Bhi) + ((size_t)src * 3 + d) * KP + 8 * cp2;
+            cp_async16(dst, gsrc);
+            cp_async16(dst + G::LBO, gsrc + 4);
+          } else {
+            *reinterpret_cast<float4 *>(dst)          = make_float4(0.f, 0.f, 0.f, 0.f);
+            *reinterpret_cast<float4 *>(dst + G::LBO) = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
+      }
+      const float4 o  = offS[s];
+      const int    dl = __float_as_int(o.w);
+      if (tid < P) {
+        const int    m  = tid;
+        const double r2 = (double)o.x * o.x + (double)o.y * o.y + (double)o.z * o.z;
+        singular_column_emit<float, P>(m, o.x, o.y, o.z, (float)(1.0 / r2), (float)(1.0 / sqrt(r2)), [&](int q, cx<float> c) {
+          Ys[q * q + q + m] = (m & 1) ? cx<float>{-c.r, -c.i} : c;
+          if (m > 0)
+            Ys[q * q + q - m] = conj(c);
+        });
+      }
+      __syncthreads();
+      // (3) this thread's chunks of its row of A(delta, o) into TMEM buffer s
+      {
+        const uint32_t ahi = lane_base + G::ACOL + s * G::ABUF, alo = ahi + KP;
+#pragma unroll
+        for (int c8 = 0; c8 < NCH; c8++) {
+          if ((c8 < C0) != (half == 0))
+            continue; // warp-uniform
+          float v8[8];
+#pragma unroll
+          for (int i = 0; i < 8; i++) {
+            const int col = 8 * c8 + i;
+            float     v   = 0.f;
+            if (col < P * P) {
+              // column -> (n, m, Re/Im) of the input, compile-time
+              int n = 0;
+              while ((n + 1) * (n + 1) <= col)
+                n++;
+              const int r = col - n * n, m = (r + 1) / 2, pin = (r > 0 && (r & 1) == 0) ? 1 : 0;
+              if (rlive && n <= P - 1 - rj) {
+                const int q = rj + n, base = q * q + q - rk;
+                if (m == 0) {
+                  const cx<float> y0 = Ys[base];
+                  v                  = rpart ? y0.i : y0.r;
+                } else {
+                  const cx<float> y1 = Ys[base + m], y2 = Ys[base - m];
+                  const float     sg = (m & 1) ? -1.f : 1.f;
+                  if (rpart == 0)
+                    v = pin ? fmaf(-sg, y1.i, y2.i) : fmaf(sg, y1.r, y2.r);
+                  else
+                    v = pin ? fmaf(sg, y1.r, -y2.r) : fmaf(sg, y1.i, y2.i);
+                }
+                v = tc_scale2(v, dl * n);
+              }
+            }
+            v8[i] = v;
+          }
+          uint32_t h[8], l[8];
+#pragma unroll
+          for (int i = 0; i < 8; i++) {
+            const float vh = tc::tf32_trunc(v8[i]);
+            h[i]           = __float_as_uint(vh);
+            l[i]           = __float_as_uint(tc::tf32_trunc(v8[i] - vh));
+          }
+          tc::tmem_st8(ahi + 8 * c8, h);
+          tc::tmem_st8(alo + 8 * c8, l);
+        }
+      }
+      // (4) the previous class's MMAs: wait, then add its D into the accumulators
+      {
+        const bool ok = g == first || tc::mbar_wait_bounded(&mbar[(g - 1) & 1], ((g - 1) >> 1) & 1);
+        if (__syncthreads_or(!ok)) { // block-uniform: every thread leaves together
+          if (tid == 0)
+            atomicExch(a.err, VFMM_ERR_TIMEOUT);
+          failed = true;
+          break;
+        }
+        tc::fence_after_sync();
+        if (g != first)
+          drain();
+      }
+      // (5) operands complete and visible to the tensor core; D free
+      cp_async_wait_all();
+      tc::fence_proxy_async_smem();
+      tc::tmem_st_wait();
+      tc::fence_before_sync();
+      __syncthreads();
+      // (6) one thread issues the class's MMAs into a fresh D and commits
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t     sb = tc::smem_u32(sB + s * G::STAGE);
+        const uint32_t     D = tc::tmem_addr(tb, 0, G::DCOL), Ahi = tc::tmem_addr(tb, 0, G::ACOL + s * G::ABUF), Alo = Ahi + KP;
+        constexpr uint32_t idesc = tc::idesc_tf32(128, N);
+#pragma unroll 1
+        for (int kk = NCH - 1; kk >= 0; kk--) {
+          tc::mma_tf32_ts(D, Alo + 8 * kk, tc::smem_desc_noswizzle(sb + 2 * kk * G::LBO, G::LBO, G::SBO), idesc, kk == NCH - 1 ? 0u : 1u);
+          tc::mma_tf32_ts(D, Ahi + 8 * kk, tc::smem_desc_noswizzle(sb + G::BBYTES + 2 * kk * G::LBO, G::LBO, G::SBO), idesc, 1u);
+        }
+#pragma unroll 1
+        for (int kk = NCH - 1; kk >= 0; kk--)
+          tc::mma_tf32_ts(D, Ahi + 8 * kk, tc::smem_desc_noswizzle(sb + 2 * kk * G::LBO, G::LBO, G::SBO), idesc, 1u);
+        tc::mma_commit(&mbar[s]);
+      }
+      e = nextE[s];
+      g++;
+    }
+    if (failed)
+      break;
+    // the tile's last class
+    const unsigned last = g - 1;
+    if (__syncthreads_or(!tc::mbar_wait_bounded(&mbar[last & 1], (last >> 1) & 1))) {
+      if (tid == 0)
+        atomicExch(a.err, VFMM_ERR_TIMEOUT);
+      failed = true;
+      break;
+    }
+    tc::fence_after_sync();
+    drain();
+    // epilogue: L (FP64) = accumulated rows scaled by (-1)^j R_t^(-j-1)
+    if (rlive) {
+      const int    jks   = row >> 1;
+      const double scale = ((rj & 1) ? -1.0 : 1.0) * ldexp(a.iR0pow[rj + 1], lt * (rj + 1));
+#pragma unroll
+      for (int i = 0; i < DH; i++) {
+        const int col = DH * half + i, t = col / 3, d = col - 3 * t, cell = tcell[t];
+        if (cell >= 0)
+          reinterpret_cast<double *>(a.L)[2 * ((size_t)cell * 3 * K + 3 * jks + d) + rpart] = ((double)acc_hi[i] + (double)acc_lo[i]) * scale;
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads(); // D is drained and tcell read before the next tile
+  }
+  cp_async_wait_all(); // no copy of this block stays in flight
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tb, 512);
+  }
+}
+
+// ---------------------------------------------------------------- tiles and classes
+// Sort key of a target cell: level, octant within its parent, index; cells
+// without M2L sources sort last.
+__global__ void k_tc_target_keys(CellsView cv, const int *__restrict__ m2l_start, int ncells, unsigned long long *keys)
+{
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x) {
+    unsigned long long k = ~0ull;
+    if (m2l_start[c + 1] > m2l_start[c]) {
+      const int p   = cv.parent[c];
+      unsigned  oct = 0;
+      if (p >= 0)
+        oct = (cv.x[c] > cv.x[p] ? 1u : 0u) | (cv.y[c] > cv.y[p] ? 2u : 0u) | (cv.z[c] > cv.z[p] ? 4u : 0u);
+      k = ((unsigned long long)cv.level[c] << 40) | ((unsigned long long)oct << 32) | (unsigned)c;
+    }
+    keys[c] = k;
+  }
+}
+
+// meta: [0, L) first sorted index of each level (-1: none), [L, 2L) one past
+// its last, [2L, 3L) its first tile, [3L] the tile count (L = MAXL + 1).
+constexpr int TC_L = MAXL + 1;
+
+__global__ void k_tc_level_bounds(const unsigned long long *__restrict__ sk, int n, int *meta)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long k = sk[i];
+    if (k == ~0ull)
+      continue;
+    const int l = (int)(k >> 40);
+    if (i == 0 || (int)(sk[i - 1] >> 40) != l)
+      meta[l] = i;
+    if (i == n - 1 || sk[i + 1] == ~0ull || (int)(sk[i + 1] >> 40) != l)
+      meta[TC_L + l] = i + 1;
+  }
+}
+
+__global__ void k_tc_tile_bases(int *meta)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0)
+    return;
+  int base = 0;
+  for (int l = 0; l < TC_L; l++) {
+    meta[2 * TC_L + l] = base;
+    if (meta[l] >= 0)
+      base += (meta[TC_L + l] - meta[l] + 31) / 32;
+  }
+  meta[3 * TC_L] = base;
+}
+
+__global__ void k_tc_assign(const unsigned long long *__restrict__ sk, int n, const int *__restrict__ meta, int *tile_cells, int *tile_level,
+                            int *tile_of, int *col_of)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long k = sk[i];
+    if (k == ~0ull)
+      continue;
+    const int l = (int)(k >> 40), c = (int)(k & 0xffffffffu);
+    const int pos = i - meta[l], T = meta[2 * TC_L + l] + pos / 32, col = pos % 32;
+    tile_cells[T * 32 + col] = c;
+    tile_of[c]               = T;
+    col_of[c]                = col;
+    if (col == 0)
+      tile_level[T] = l;
+  }
+}
+
+// Pair (t, s) -> key tile(t) << 38 | class, value column(t) << 27 | s.
+__global__ void k_tc_pair_keys(const unsigned long long *__restrict__ pk, int n, int kb, CellsView cv, const int *__restrict__ tile_of,
+                               const int *__restrict__ col_of, unsigned long long *keys, uint32_t *vals)
+{
+  const unsigned long long smask = (1ull << kb) - 1;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int          t = (int)(pk[q] >> kb), s = (int)(pk[q] & smask);
+    const int          dl = cv.level[t] - cv.level[s];
+    const double       iRf = 1.0 / fmin(cv.R[t], cv.R[s]);
+    const long long    ox = llrint((cv.x[t] - cv.x[s]) * iRf), oy = llrint((cv.y[t] - cv.y[s]) * iRf), oz = llrint((cv.z[t] - cv.z[s]) * iRf);
+    unsigned long long cls = TC_SENTINEL;
+    if (dl >= -14 && dl <= 14 && llabs(ox) <= 1022 && llabs(oy) <= 1022 && llabs(oz) <= 1022)
+      cls = ((unsigned long long)(dl + 16) << 33) | ((unsigned long long)(ox + 1024) << 22) | ((unsigned long long)(oy + 1024) << 11) |
+            (unsigned long long)(oz + 1024);
+    keys[q] = ((unsigned long long)tile_of[t] << TC_CLASS_BITS) | cls;
+    vals[q] = ((uint32_t)col_of[t] << TC_COL_SHIFT) | (uint32_t)s;
+  }
+}
+
+// First sorted pair of each tile; tile_start[ntiles] = n.
+__global__ void k_tc_tile_ranges(const unsigned long long *__restrict__ keys, int n, const int *__restrict__ meta, int *tile_start)
+{
+  const int nt = meta[3 * TC_L];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
+    const int T  = i < n ? (int)(keys[i] >> TC_CLASS_BITS) : nt;
+    const int Tp = i > 0 ? (int)(keys[i - 1] >> TC_CLASS_BITS) : -1;
+    for (int r = Tp + 1; r <= T; r++)
+      tile_start[r] = i;
+  }
+}
+
+template <int P>
+static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+{
+  using G     = TcM2L<P>;
+  TcScratch &S = *m.tc;
+  const int  nc = e.ncells, np = m.n_m2l;
+  VFMM_CUDA_TRY(cudaMemsetAsync(e.L, 0, sizeof(double2) * (size_t)nc * 3 * nterms(P), s));
+  if (np == 0 || nc == 0)
+    return;
+  if (nc >= (1 << TC_COL_SHIFT))
+    throw Error(VFMM_ERR_CAPACITY, "tensor-core M2L: more than 2^27 cells");
+  const int ntmax = nc / 32 + TC_L + 1; // tiles: per level ceil(count / 32)
+  int       tile_bits = 1;
+  while ((1ll << tile_bits) <= ntmax)
+    tile_bits++;
+  if (TC_CLASS_BITS + tile_bits > 64)
+    throw Error(VFMM_ERR_CAPACITY, "tensor-core M2L: too many tiles for a 64-bit pair key");
+  S.tkeys.reserve(nc);
+  S.tkeys_sorted.reserve(nc);
+  S.tile_of.reserve(nc);
+  S.col_of.reserve(nc);
+  S.meta.reserve(3 * TC_L + 1);
+  S.tile_cells.reserve((size_t)ntmax * 32);
+  S.tile_level.reserve(ntmax);
+  S.tile_start.reserve(ntmax + 1);
+  S.pkeys.reserve(np);
+  S.pkeys_sorted.reserve(np);
+  S.pvals.reserve(np);
+  S.pvals_sorted.reserve(np);
+  size_t b1 = 0, b2 = 0;
+  VFMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(nullptr, b1, S.tkeys.p, S.tkeys_sorted.p, nc, 0, 45, s));
+  VFMM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, b2, S.pkeys.p, S.pkeys_sorted.p, S.pvals.p, S.pvals_sorted.p, np, 0,
+                                                TC_CLASS_BITS + tile_bits, s));
+  S.cub_tmp.reserve(std::max(b1, b2));
+
+  VFMM_CUDA_TRY(cudaMemsetAsync(S.meta.p, 0xFF, sizeof(int) * (3 * TC_L + 1), s));
+  VFMM_CUDA_TRY(cudaMemsetAsync(S.tile_cells.p, 0xFF, sizeof(int) * (size_t)ntmax * 32, s));
+  k_tc_target_keys<<<grid_for(nc, 256), 256, 0, s>>>(e.cells, e.m2l_start, nc, S.tkeys.p);
+  count_launch();
+  size_t bytes = S.cub_tmp.cap;
+  VFMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(S.cub_tmp.p, bytes, S.tkeys.p, S.tkeys_sorted.p, nc, 0, 45, s));
+  count_launch();
+  k_tc_level_bounds<<<grid_for(nc, 256), 256, 0, s>>>(S.tkeys_sorted.p, nc, S.meta.p);
+  count_launch();
+  k_tc_tile_bases<<<1, 32, 0, s>>>(S.meta.p);
+  count_launch();
+  k_tc_assign<<<grid_for(nc, 256), 256, 0, s>>>(S.tkeys_sorted.p, nc, S.meta.p, S.tile_cells.p, S.tile_level.p, S.tile_of.p, S.col_of.p);
+  count_launch();
+  k_tc_pair_keys<<<grid_for(np, 256), 256, 0, s>>>(m.m2l_keys, np, m.m2l_key_bits, e.cells, S.tile_of.p, S.col_of.p, S.pkeys.p, S.pvals.p);
+  count_launch();
+  bytes = S.cub_tmp.cap;
+  VFMM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.cub_tmp.p, bytes, S.pkeys.p, S.pkeys_sorted.p, S.pvals.p, S.pvals_sorted.p, np, 0,
+                                                TC_CLASS_BITS + tile_bits, s));
+  count_launch();
+  k_tc_tile_ranges<<<grid_for(np + 1, 256), 256, 0, s>>>(S.pkeys_sorted.p, np, S.meta.p, S.tile_start.p);
+  count_launch();
+
+  TcArgs a{};
+  a.keys       = S.pkeys_sorted.p;
+  a.vals       = S.pvals_sorted.p;
+  a.npairs     = np;
+  a.tile_start = S.tile_start.p;
+  a.tile_cells = S.tile_cells.p;
+  a.tile_level = S.tile_level.p;
+  a.ntiles     = S.meta.p + 3 * TC_L;
+  a.Bhi        = m.Bhi;
+  a.Blo        = m.Blo;
+  a.cv         = e.cells;
+  a.L          = e.L;
+  a.err        = m.eval_err;
+  const double iR0 = 1.0 / m.R0;
+  a.iR0pow[0]      = 1.0;
+  for (int k = 1; k < PMAX + 2; k++)
+    a.iR0pow[k] = a.iR0pow[k - 1] * iR0;
+  VFMM_SMEM_ONCE(G::smem, k_m2l_tc<P>);
+  int dev = 0, nsm = 0;
+  VFMM_CUDA_TRY(cudaGetDevice(&dev));
+  VFMM_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  k_m2l_tc<P><<<std::max(1, std::min(nsm, ntmax)), 256, G::smem, s>>>(a);
+  count_launch();
+  VFMM_LAUNCH_CHECK();
+}
+
+void m2l_tensor(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+{
+  switch (e.P) {
+  case 8: m2l_tc_P<8>(s, e, m); break;
+  case 9: m2l_tc_P<9>(s, e, m); break;
+  case 10: m2l_tc_P<10>(s, e, m); break;
+  default: throw Error(VFMM_ERR_UNSUPPORTED, "tensor-core M2L: order outside 8..10");
+  }
+}
+
 } // namespace vfmm
 
 extern "C" int vfmm_tcgen05_selftest(int device, int swap_offsets, float *out)
@@ -115,3 +665,4 @@ extern "C" int vfmm_tcgen05_selftest(int device, int swap_offsets, float *out)
   cudaFree(d);
   return rc;
 }
+

@@ -19,6 +19,7 @@
 // sums folded into a float-float (two-sum) accumulator.
 #include <algorithm>
 #include "harmonics.cuh"
+#include "tcgen05.cuh"
 #include "vfmm_internal.cuh"
 
 namespace vfmm {
@@ -44,6 +45,7 @@ struct DevMixed {
   double        R0, iR0;
   double        R0pow[PMAX + 1], iR0pow[PMAX + 1]; // R0^n, R0^-n
   int           stretching, formulation;
+  float        *Bhi, *Blo; // tensor-core M2L operand rows [cell][3][tc_kp(P)] (null: not used)
 };
 
 // R_c^n and R_c^-n for a cell at `level` (R_c = R0 / 2^level): exact
@@ -62,6 +64,28 @@ __device__ __forceinline__ void store_mfold(const DevMixed &a, int PP, int c, in
   row[(nn + m) * 3 + d] = (m & 1) ? make_float2(-re, -im) : make_float2(re, im);
   if (m > 0)
     row[(nn - m) * 3 + d] = make_float2(re, -im);
+}
+
+// The scaled multipole Mt_n^m (m >= 0, component d) of cell c as a row of
+// the tensor-core M2L's B operand: Mt_n^0 (real part) at n^2, Re/Im Mt_n^m at
+// n^2 + 2m - 1 and n^2 + 2m, each as TF32 hi and lo parts; the padding after
+// P^2 is zeroed with the (0, 0) term.
+template <int P>
+__device__ __forceinline__ void store_btc(const DevMixed &a, int c, int n, int m, int d, float re, float im)
+{
+  constexpr int KP = tc_kp(P);
+  float        *hi = a.Bhi + ((size_t)c * 3 + d) * KP, *lo = a.Blo + ((size_t)c * 3 + d) * KP;
+  const int     col = n * n + (m ? 2 * m - 1 : 0);
+  const float   rh = tc::tf32_trunc(re), ih = tc::tf32_trunc(im);
+  hi[col]          = rh;
+  lo[col]          = tc::tf32_trunc(re - rh);
+  if (m) {
+    hi[col + 1] = ih;
+    lo[col + 1] = tc::tf32_trunc(im - ih);
+  }
+  if (n == 0)
+    for (int k = P * P; k < KP; k++)
+      hi[k] = lo[k] = 0.f;
 }
 
 __device__ __forceinline__ void jk_of_m(int jks, int &j, int &k)
@@ -155,6 +179,8 @@ __global__ void __launch_bounds__(64) k_p2m32(DevMixed a)
         const double s = cell_Rpow(a, lev, n);
         a.M[(size_t)c * 3 * K + o] = make_double2(acc[i].r * s, acc[i].i * s);
         store_mfold(a, P * P, c, n, m, o % 3, acc[i].r, acc[i].i);
+        if (a.Bhi)
+          store_btc<P>(a, c, n, m, o % 3, acc[i].r, acc[i].i);
       }
     }
   }
@@ -206,6 +232,8 @@ __global__ void __launch_bounds__(128) k_m2m32(DevMixed a, const int *cells, int
       const double2 old = *q;
       *q                = make_double2(old.x + (double)sum.r * s, old.y + (double)sum.i * s);
       store_mfold(a, P * P, c, j, k, d, sum.r, sum.i);
+      if (a.Bhi)
+        store_btc<P>(a, c, j, k, d, sum.r, sum.i);
     }
   }
 }
@@ -906,6 +934,8 @@ static DevMixed dev_mixed(const ExpArgs &e, const MixedArgs &m)
   }
   d.stretching  = e.stretching;
   d.formulation = e.formulation;
+  d.Bhi         = m.Bhi;
+  d.Blo         = m.Blo;
   return d;
 }
 
@@ -1022,7 +1052,13 @@ static void l2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   }
 
 void p2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(p2m32_P, s, e, m) }
-void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(m2l32_P, s, e, m) }
+void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+{
+  if (m.tc)
+    m2l_tensor(s, e, m);
+  else
+    VFMM_DISPATCH_M(m2l32_P, s, e, m)
+}
 void m2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(m2m32_P, s, e, m) }
 void l2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(l2l32_P, s, e, m) }
 void l2p_p2p_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out) { VFMM_DISPATCH_M(l2p32_P, s, e, m, out) }

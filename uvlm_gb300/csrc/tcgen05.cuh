@@ -62,6 +62,22 @@ __device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence
 // core's reads (async proxy).
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// x with the 13 low mantissa bits cleared: exactly representable in TF32; x -
+// tf32_trunc(x) is exact in FP32 and carries the next 13 bits.
+__host__ __device__ __forceinline__ float tf32_trunc(float v)
+{
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
+#else
+  unsigned u;
+  __builtin_memcpy(&u, &v, 4);
+  u &= 0xFFFFE000u;
+  float r;
+  __builtin_memcpy(&r, &u, 4);
+  return r;
+#endif
+}
+
 // ---- descriptors --------------------------------------------------------------
 // Shared-memory matrix descriptor, no swizzle: start address, leading byte
 // offset (K direction), stride byte offset (M/N direction); bit 46 is the

@@ -252,6 +252,21 @@ void l2p_sensor_pass(cudaStream_t s, const ExpArgs &a, double *soa_out);
 std::vector<int4> m2l_schedule(int P, int lanes, int kb, int maxItems, int *itemsPerLane);
 
 // ---- mixed.cu (FP32 P2M / M2M / M2L / L2L / L2P+P2P, FP64 expansion arrays)
+// Scratch of the tensor-core M2L (m2l_tensor.cu): the sources' multipoles as
+// TF32 hi/lo operand rows [cell][3][tc_kp(P)], target tiles and the pairs
+// sorted by (tile, offset class).
+struct TcScratch {
+  DevBuf<float>              B;
+  DevBuf<unsigned long long> tkeys, tkeys_sorted, pkeys, pkeys_sorted;
+  DevBuf<uint32_t>           pvals, pvals_sorted;
+  DevBuf<int>                tile_of, col_of, tile_cells, tile_level, tile_start, meta;
+  DevBuf<unsigned char>      cub_tmp;
+};
+// Padded K extent of one component's multipole operand row (P^2 real terms).
+__host__ __device__ constexpr int tc_kp(int P) { return (P * P + 7) / 8 * 8; }
+// Orders the tensor-core M2L handles: the P(P+1) output rows fit the 128 TMEM lanes.
+constexpr int TC_PMIN = 8, TC_PMAX = 10;
+
 struct MixedArgs {
   float2       *Mp32;
   float4       *pos32, *alp32;
@@ -259,7 +274,17 @@ struct MixedArgs {
   const int4   *lanes32; // k_m2l32v2 lane table, see m2l_lane_table
   int           m2l_batch; // sources staged per batch in k_m2l32v2 (8, 16 or 32)
   double        R0;
+  // tensor-core M2L (null tc: the CUDA-core kernel k_m2l32v2): operand rows
+  // written by P2M/M2M, the traversal's sorted (target << key_bits | source)
+  // M2L keys, and the device error word of the evaluation
+  TcScratch                *tc;
+  float                    *Bhi, *Blo;
+  const unsigned long long *m2l_keys;
+  int                       m2l_key_bits, n_m2l;
+  int                      *eval_err;
 };
+// The tensor-core M2L for P in TC_PMIN..TC_PMAX (m2l_tensor.cu).
+void m2l_tensor(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
 // Columns per half-tile of the mixed M2L lane tiles: at most 32 tiles per degree.
 __host__ __device__ constexpr int m2l_half_width(int P) { return P >= 16 ? 4 : 2; }
 // Shared memory of k_m2l32v2<P, SB>: per source of a batch, a staged
