@@ -486,15 +486,15 @@ ExpArgs particle_args(vfmm_handle h)
   return e;
 }
 
-// The tensor-core M2L (p = 8..10, mixed mode) while it is being tuned:
-// VFMM_M2L_TENSOR=1 in the environment selects it.
+// The tensor-core M2L runs for p = 8..10 in mixed mode; VFMM_M2L_TENSOR=0 in
+// the environment selects the CUDA-core kernel instead (for comparisons).
 bool tensor_m2l(int p)
 {
-  static const bool on = [] {
+  static const bool off = [] {
     const char *v = getenv("VFMM_M2L_TENSOR");
-    return v && v[0] == '1';
+    return v && v[0] == '0';
   }();
-  return on && p >= TC_PMIN && p <= TC_PMAX;
+  return !off && p >= TC_PMIN && p <= TC_PMAX;
 }
 
 // Raise the error an evaluation kernel recorded (after a stream sync).
@@ -504,7 +504,7 @@ void check_eval_err(vfmm_handle h)
   VFMM_CUDA_TRY(cudaMemcpy(&e, h->eval_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (e) {
     VFMM_CUDA_TRY(cudaMemset(h->eval_err, 0, sizeof(int)));
-    throw Error(e, "a tensor-core M2L wait on the GPU gave up (time limit)");
+    throw Error(e, e == VFMM_ERR_TIMEOUT ? "a tensor-core M2L wait on the GPU gave up (time limit)" : "tensor-core M2L: more operator classes than its hash holds");
   }
 }
 
@@ -922,6 +922,13 @@ int vfmm_destroy(vfmm_handle h)
     b->release();
   for (auto *b : {&h->tcs.tile_of, &h->tcs.col_of, &h->tcs.tile_cells, &h->tcs.tile_level, &h->tcs.tile_start, &h->tcs.meta})
     b->release();
+  for (auto *b : {&h->tcs.hkeys, &h->tcs.cls_of})
+    b->release();
+  h->tcs.hid.release();
+  h->tcs.cidq.release();
+  h->tcs.table.release();
+  if (h->tcs.ncls_host)
+    cudaFreeHost(h->tcs.ncls_host);
   h->tcs.pvals.release();
   h->tcs.pvals_sorted.release();
   h->tcs.cub_tmp.release();

@@ -4,6 +4,7 @@
 // with A in tensor memory and B in shared memory (K-major, no swizzle), on
 // small integers (exact in TF32 and FP32), so that the host can check the
 // operand layouts the M2L kernel relies on element by element.
+#include <algorithm>
 #include <cub/cub.cuh>
 #include "harmonics.cuh"
 #include "tcgen05.cuh"
@@ -108,8 +109,8 @@ __global__ void __launch_bounds__(128) k_tc_selftest(float *out, int swap_offset
 // Layout of one tile: 32 targets of one level (the same octant within their
 // parents where possible, so that their offset sets coincide), D = A B with
 // A (128 rows x KP) in tensor memory and B (KP x 96: target x component) in
-// shared memory, accumulated over all classes of the tile in TMEM.  FP32 is
-// kept by three TF32 products, A_hi B_hi + A_hi B_lo + A_lo B_hi, where x_hi
+// shared memory, one class at a time (see k_m2l_tc).  FP32 is kept by three
+// TF32 products, A_hi B_hi + A_hi B_lo + A_lo B_hi, where x_hi
 // is x with the low 13 mantissa bits cleared and x_lo = x - x_hi.
 // ============================================================================
 
@@ -143,6 +144,8 @@ struct TcArgs {
   const int                *tile_level;
   const int                *ntiles;     // device scalar
   const float              *Bhi, *Blo;  // [cell][3][KP]
+  const float4             *table;      // operators, see k_tc_class_ops
+  const int                *cidq;       // table index of each group, at its first pair
   CellsView                 cv;
   double2                  *L;
   double                    iR0pow[PMAX + 2]; // R0^-n
@@ -165,37 +168,251 @@ __device__ __forceinline__ void tc_two_sum(float &hi, float &lo, float v)
   hi = s;
 }
 
-// One block (256 threads, one per SM: 512 TMEM columns) per tile at a time.
-// Warp w writes and reads TMEM lanes 32 (w % 4) .. + 31 (rows of A and D);
-// warps w and w + 4 split each row's A columns and D columns between them.
-// Per class: warp 0 decodes the members, all threads gather B (cp.async),
-// threads 0..P-1 make S'(o), all threads build their part of A in the TMEM
-// buffer of the class's parity while the previous class's MMAs run; then the
-// previous class's D is added into registers (two-sum), and one thread
-// issues this class's MMAs into a fresh D.  A fresh D per class, with the
-// small products first (A_lo B_hi and A_hi B_lo, then A_hi B_hi, each from
-// the highest degrees down), keeps the tensor core's truncating FP32
-// accumulation to a few units in the last place of each class's sum; the sum
-// over classes is a two-sum in registers.
+// Operator classes of one evaluation: an open-addressing hash of the class
+// keys (TC_HASH slots) gives each class an index; the operators of the first
+// `cap` indices are built once into a table, in the order the M2L kernel
+// reads them: [class][hi, lo][chunk of 8 columns][128 rows][8].
+constexpr int      TC_HASH  = 1 << 14;
+constexpr uint64_t TC_EMPTY = ~0ull;
+__device__ __forceinline__ unsigned tc_hash(unsigned long long k) { return (unsigned)((k * 0x9E3779B97F4A7C15ull) >> 50); }
+
+// Value of column `col` of row (j, k, part) of the operator A(delta, o), from
+// the folded harmonics Ys = S'(o) (see the derivation above).
 template <int P>
-__global__ void __launch_bounds__(256, 1) k_m2l_tc(TcArgs a)
+__device__ __forceinline__ float tc_op_value(int col, int rj, int rk, int rpart, bool rlive, int dl, const cx<float> *Ys)
+{
+  if (col >= P * P || !rlive)
+    return 0.f;
+  int n = 0;
+  while ((n + 1) * (n + 1) <= col)
+    n++;
+  if (n > P - 1 - rj)
+    return 0.f;
+  const int r = col - n * n, m = (r + 1) / 2, pin = (r > 0 && (r & 1) == 0) ? 1 : 0;
+  const int q = rj + n, base = q * q + q - rk;
+  float     v;
+  if (m == 0) {
+    const cx<float> y0 = Ys[base];
+    v                  = rpart ? y0.i : y0.r;
+  } else {
+    const cx<float> y1 = Ys[base + m], y2 = Ys[base - m];
+    const float     sg = (m & 1) ? -1.f : 1.f;
+    if (rpart == 0)
+      v = pin ? fmaf(-sg, y1.i, y2.i) : fmaf(sg, y1.r, y2.r);
+    else
+      v = pin ? fmaf(sg, y1.r, -y2.r) : fmaf(sg, y1.i, y2.i);
+  }
+  return tc_scale2(v, dl * n);
+}
+
+// Folded singular harmonics S'(o), column m = 0 .. P-1 on threads 0 .. P-1.
+template <int P>
+__device__ __forceinline__ void tc_harmonics(float4 o, cx<float> *Ys)
+{
+  if (threadIdx.x < P) {
+    const int    m  = threadIdx.x;
+    const double r2 = (double)o.x * o.x + (double)o.y * o.y + (double)o.z * o.z;
+    singular_column_emit<float, P>(m, o.x, o.y, o.z, (float)(1.0 / r2), (float)(1.0 / sqrt(r2)), [&](int q, cx<float> c) {
+      Ys[q * q + q + m] = (m & 1) ? cx<float>{-c.r, -c.i} : c;
+      if (m > 0)
+        Ys[q * q + q - m] = conj(c);
+    });
+  }
+}
+
+// Row r of a 128-row operator: (j, k, part) of output L_j^k, or not live.
+__device__ __forceinline__ void tc_row_of(int r, int NR, int &rj, int &rk, int &rpart, bool &rlive)
+{
+  rlive = r < NR;
+  rj = rk = 0;
+  rpart   = r & 1;
+  if (rlive) {
+    const int jks = r >> 1;
+    while ((rj + 1) * (rj + 2) / 2 <= jks)
+      rj++;
+    rk = jks - rj * (rj + 1) / 2;
+  }
+}
+
+// Offset o (target units) and level difference of a class key.
+__device__ __forceinline__ float4 tc_class_offset(unsigned long long k0)
+{
+  const int   dz = (int)(k0 & 2047) - 1024, dy = (int)((k0 >> 11) & 2047) - 1024, dx = (int)((k0 >> 22) & 2047) - 1024;
+  const int   dl = (int)((k0 >> 33) & 31) - 16;
+  const float f  = dl < 0 ? ldexpf(1.f, dl) : 1.f; // offsets are in units of the finer cell
+  return make_float4(dx * f, dy * f, dz * f, __int_as_float(dl));
+}
+
+// Insert the class of every (tile, class) group into the hash.
+__global__ void k_tc_class_insert(const unsigned long long *__restrict__ keys, int n, unsigned long long *hkeys, int *err)
+{
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const unsigned long long c = keys[q] & TC_SENTINEL;
+    if (c == TC_SENTINEL || (q > 0 && keys[q - 1] == keys[q]))
+      continue;
+    unsigned h = tc_hash(c), probes = 0;
+    for (;;) {
+      const unsigned long long cur = hkeys[h];
+      if (cur == c)
+        break;
+      if (cur == TC_EMPTY) {
+        const unsigned long long prev = atomicCAS(&hkeys[h], TC_EMPTY, c);
+        if (prev == TC_EMPTY || prev == c)
+          break;
+      }
+      h = (h + 1) & (TC_HASH - 1);
+      if (++probes >= TC_HASH) { // full: more classes than slots
+        atomicExch(err, VFMM_ERR_CAPACITY);
+        break;
+      }
+    }
+  }
+}
+
+// Class index per occupied slot (in slot order) and the class count.
+__global__ void __launch_bounds__(1024) k_tc_class_ids(const unsigned long long *__restrict__ hkeys, int *hid, unsigned long long *cls_of, int *count)
+{
+  constexpr int PER = TC_HASH / 1024;
+  __shared__ int wsum[32];
+  int            c = 0;
+  for (int i = 0; i < PER; i++)
+    c += hkeys[threadIdx.x * PER + i] != TC_EMPTY;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int       incl = c;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d)
+      incl += v;
+  }
+  if (lane == 31)
+    wsum[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    const int v = wsum[lane];
+    int       iv = v;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, iv, d);
+      if (lane >= d)
+        iv += u;
+    }
+    wsum[lane] = iv - v;
+    if (lane == 31)
+      *count = iv;
+  }
+  __syncthreads();
+  int id = wsum[w] + incl - c;
+  for (int i = 0; i < PER; i++) {
+    const int                slot = threadIdx.x * PER + i;
+    const unsigned long long k    = hkeys[slot];
+    hid[slot]                     = k != TC_EMPTY ? id : -1;
+    if (k != TC_EMPTY)
+      cls_of[id++] = k;
+  }
+}
+
+// Operators of classes 0 .. min(count, cap) - 1: one block of 128 threads (rows) per class.
+template <int P>
+__global__ void __launch_bounds__(128) k_tc_class_ops(const unsigned long long *__restrict__ cls_of, const int *__restrict__ count, int cap, float4 *table)
+{
+  using G = TcM2L<P>;
+  constexpr int KP = G::KP, NCH = KP / 8;
+  __shared__ cx<float> Ys[P * P];
+  const int n = min(*count, cap);
+  int       rj, rk, rpart;
+  bool      rlive;
+  tc_row_of(threadIdx.x, G::NR, rj, rk, rpart, rlive);
+  for (int id = blockIdx.x; id < n; id += gridDim.x) {
+    const float4 o = tc_class_offset(cls_of[id]);
+    __syncthreads();
+    tc_harmonics<P>(o, Ys);
+    __syncthreads();
+    const int dl = __float_as_int(o.w);
+    for (int c8 = 0; c8 < NCH; c8++) {
+      float h[8], l[8];
+      for (int i = 0; i < 8; i++) {
+        const float v = tc_op_value<P>(8 * c8 + i, rj, rk, rpart, rlive, dl, Ys), vh = tc::tf32_trunc(v);
+        h[i]          = vh;
+        l[i]          = tc::tf32_trunc(v - vh);
+      }
+      float4 *th = table + ((((size_t)id * 2 + 0) * NCH + c8) * 128 + threadIdx.x) * 2;
+      float4 *tl = table + ((((size_t)id * 2 + 1) * NCH + c8) * 128 + threadIdx.x) * 2;
+      th[0]      = make_float4(h[0], h[1], h[2], h[3]);
+      th[1]      = make_float4(h[4], h[5], h[6], h[7]);
+      tl[0]      = make_float4(l[0], l[1], l[2], l[3]);
+      tl[1]      = make_float4(l[4], l[5], l[6], l[7]);
+    }
+  }
+}
+
+// Table index of each (tile, class) group, at its first pair: -1 for a
+// sentinel pair or a class beyond the table (the kernel builds those).
+__global__ void k_tc_class_index(const unsigned long long *__restrict__ keys, int n, const unsigned long long *__restrict__ hkeys,
+                                 const int *__restrict__ hid, const int *__restrict__ count, int cap, int *cidq)
+{
+  const int ncls = min(*count, cap);
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const unsigned long long c = keys[q] & TC_SENTINEL;
+    if (q > 0 && keys[q - 1] == keys[q] && c != TC_SENTINEL)
+      continue;
+    int id = -1;
+    if (c != TC_SENTINEL)
+      for (unsigned h = tc_hash(c), probes = 0; probes < TC_HASH; h = (h + 1) & (TC_HASH - 1), probes++) {
+        const unsigned long long k = hkeys[h];
+        if (k == c) {
+          id = hid[h];
+          break;
+        }
+        if (k == TC_EMPTY)
+          break;
+      }
+    cidq[q] = id < ncls ? id : -1;
+  }
+}
+
+// Per-class metadata ring of the M2L kernel (three slots: the class whose
+// MMAs run, the next one being staged, the one after being decoded).
+struct TcMeta {
+  float4 off;   // offset o (target units), w = delta (int bits)
+  int    cid;   // table index, -1: build here
+  int    tile;  // -1: no more classes
+  int    last;  // 1: last class of its tile
+  int    level; // target level
+  int    src[32];
+};
+
+// One block (384 threads, one per SM: 512 TMEM columns) walks its tiles'
+// classes in order.  Warp w writes and reads TMEM lanes 32 (w % 4) .. + 31
+// (rows of A and D); warps w, w + 4, w + 8 split each row's A chunks and D
+// columns.  Iteration c:
+//   1. B(c) and A(c) complete -> barrier -> one thread issues the MMAs of
+//      class c into a fresh D (small products first: A_lo B_hi and A_hi B_lo,
+//      then A_hi B_hi, each from the highest degrees down), commit;
+//   2. warp 1 decodes class c + 2 into the metadata ring;
+//   3. all threads stage class c + 1 while the tensor core works: B by
+//      cp.async into the other shared-memory stage, the nonzero chunks of
+//      their operator rows from the table (L2) into the other TMEM A buffer
+//      (classes without a table entry build their operator here);
+//   4. thread 0 waits for class c's MMAs; all threads add D into registers;
+//      at the last class of a tile they write its local expansions (FP64).
+// A fresh D per class keeps the tensor core's truncating FP32 accumulation
+// to a few units in the last place of each class's sum; the classes are
+// summed in FP32 in two levels (groups of 8, then the groups).
+template <int P>
+__global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
 {
   using G = TcM2L<P>;
   constexpr int K = nterms(P), KP = G::KP, N = G::N, NCH = KP / 8;
-  constexpr int C0 = (NCH + 1) / 2;     // A chunks of the first half of the warps
-  constexpr int DH = N / 2;              // D columns per half
-  static_assert(DH % 8 == 0, "D columns per half are whole 8-column loads");
+  constexpr int DT = N / 3; // D columns per third
+  static_assert(DT % 16 == 0, "each thread drains its D columns 16 at a time");
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char *sB = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
   __shared__ cx<float> Ys[P * P];
-  __shared__ int       srcS[2][32];
-  __shared__ float4    offS[2]; // class offset o (target units), w = delta (as int bits)
-  __shared__ int       tcell[32];
-  __shared__ int       nextE[2];
+  __shared__ TcMeta    meta[3];
   __shared__ uint32_t  tbase;
   __shared__ __align__(8) uint64_t mbar[2];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, half = warp >> 2;
+  const int quarter = warp & 3, third = warp >> 2;
+  const int c_lo = (NCH * third) / 3, c_hi = (NCH * (third + 1)) / 3; // A chunks of this third
 
   if (warp == 0) {
     tc::tmem_alloc(&tbase, 512);
@@ -211,224 +428,234 @@ __global__ void __launch_bounds__(256, 1) k_m2l_tc(TcArgs a)
   tc::fence_after_sync();
   const uint32_t tb = tbase;
 
-  // this thread's output row (TMEM lane)
-  const int  row   = 32 * quarter + lane;
-  const bool rlive = row < G::NR;
-  int        rj = 0, rk = 0;
-  if (rlive) {
-    const int jks = row >> 1;
-    while ((rj + 1) * (rj + 2) / 2 <= jks)
-      rj++;
-    rk = jks - rj * (rj + 1) / 2;
-  }
-  const int      rpart = row & 1;
+  // this thread's output row (TMEM lane) and its nonzero operator chunks
+  const int row = 32 * quarter + lane;
+  int       rj, rk, rpart;
+  bool      rlive;
+  tc_row_of(row, G::NR, rj, rk, rpart, rlive);
+  const int      nz        = rlive ? ((P - rj) * (P - rj) + 7) / 8 : 0;
+  const int      nzw       = __reduce_max_sync(0xffffffffu, nz); // the warp's largest
   const uint32_t lane_base = tc::tmem_addr(tb, 32 * quarter, 0);
+  { // zero both A buffers once: chunks beyond a row's nonzero ones stay zero
+    const uint32_t z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int b = 0; b < 2; b++)
+      for (int c8 = c_lo; c8 < c_hi; c8++) {
+        tc::tmem_st8(lane_base + G::ACOL + b * G::ABUF + 8 * c8, z);
+        tc::tmem_st8(lane_base + G::ACOL + b * G::ABUF + KP + 8 * c8, z);
+      }
+    tc::tmem_st_wait();
+  }
+  // this thread's B gather: column n (target n / 3, component n % 3) of the
+  // hi (which = 0) or lo (1) operand, K chunk pairs [cp_lo, cp_hi)
+  constexpr int KC2 = G::KC / 2;
+  const int     gcol = tid % N, gwhich = (tid / N) & 1, ghalf = tid / (2 * N); // 384 = 96 x 2 x 2
+  const int     cp_lo = ghalf ? KC2 / 2 : 0, cp_hi = ghalf ? KC2 : KC2 / 2;
+  const int     gdoff = gwhich * G::BBYTES + (gcol >> 3) * G::SBO + (gcol & 7) * 16;
+  const float  *gbase = (gwhich ? a.Blo : a.Bhi) + (gcol % 3) * KP;
 
-  float acc_hi[DH], acc_lo[DH];
-  // add D (this thread's row, columns [DH half, DH half + DH)) into the accumulators
-  auto drain = [&]() {
+  // warp 1's walker over this block's tiles and classes
+  const int ntiles = *a.ntiles;
+  int       wT = blockIdx.x, we = 0, wp1 = 0;
+  if (warp == 1 && wT < ntiles) {
+    we  = a.tile_start[wT];
+    wp1 = a.tile_start[wT + 1];
+  }
+  auto decode = [&](TcMeta &M) { // warp 1: the class at the walker into M
+    while (wT < ntiles && we >= wp1) {
+      wT += gridDim.x;
+      if (wT < ntiles) {
+        we  = a.tile_start[wT];
+        wp1 = a.tile_start[wT + 1];
+      }
+    }
+    if (wT >= ntiles) {
+      if (lane == 0)
+        M.tile = -1;
+      return;
+    }
+    const unsigned long long k0  = a.keys[we];
+    const bool               in  = we + lane < wp1;
+    const unsigned long long kl  = in ? a.keys[we + lane] : ~0ull;
+    const uint32_t           v   = in ? a.vals[we + lane] : 0u;
+    const bool               sen = (k0 & TC_SENTINEL) == TC_SENTINEL;
+    const unsigned           eq  = __ballot_sync(0xffffffffu, in && kl == k0);
+    const int                cnt = sen ? 1 : __popc(eq); // members are contiguous from lane 0
+    M.src[lane]                  = -1;
+    __syncwarp();
+    if (lane < cnt)
+      M.src[v >> TC_COL_SHIFT] = (int)(v & ((1u << TC_COL_SHIFT) - 1));
+    if (lane == 0) {
+      const int lt = a.tile_level[wT];
+      float4    o;
+      if (!sen)
+        o = tc_class_offset(k0);
+      else {
+        const int    sc = (int)(v & ((1u << TC_COL_SHIFT) - 1)), t = a.tile_cells[wT * 32 + (v >> TC_COL_SHIFT)];
+        const double iR = 1.0 / a.cv.R[t];
+        o = make_float4((float)((a.cv.x[t] - a.cv.x[sc]) * iR), (float)((a.cv.y[t] - a.cv.y[sc]) * iR), (float)((a.cv.z[t] - a.cv.z[sc]) * iR),
+                        __int_as_float(lt - a.cv.level[sc]));
+      }
+      M.off   = o;
+      M.cid   = a.cidq[we];
+      M.tile  = wT;
+      M.last  = we + cnt >= wp1;
+      M.level = lt;
+    }
+    we += cnt;
+  };
+
+  // stage class M into shared-memory stage / TMEM buffer b (all threads)
+  auto stage = [&](const TcMeta &M, int b) {
+    unsigned char *dst = sB + b * G::STAGE + gdoff;
+    const int      src = M.src[gcol / 3];
+    if (src >= 0) {
+      const float *g = gbase + (size_t)src * 3 * KP;
+#pragma unroll 4
+      for (int cp2 = cp_lo; cp2 < cp_hi; cp2++) {
+        cp_async16(dst + (2 * cp2) * G::LBO, g + 8 * cp2);
+        cp_async16(dst + (2 * cp2 + 1) * G::LBO, g + 8 * cp2 + 4);
+      }
+    } else {
+      for (int cp2 = cp_lo; cp2 < cp_hi; cp2++) {
+        *reinterpret_cast<float4 *>(dst + (2 * cp2) * G::LBO)     = make_float4(0.f, 0.f, 0.f, 0.f);
+        *reinterpret_cast<float4 *>(dst + (2 * cp2 + 1) * G::LBO) = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    const uint32_t ahi = lane_base + G::ACOL + b * G::ABUF, alo = ahi + KP;
+    const int      cid = M.cid;
+    if (cid >= 0) {
+      const float4 *th = a.table + ((size_t)cid * 2 * NCH) * 128 * 2;
+      const float4 *tl = th + (size_t)NCH * 128 * 2;
+      for (int c8 = c_lo; c8 < min(c_hi, nzw); c8++) {
+        float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), h1 = h0, l0 = h0, l1 = h0;
+        if (c8 < nz) {
+          const size_t o8 = ((size_t)c8 * 128 + row) * 2;
+          h0              = __ldg(th + o8);
+          h1              = __ldg(th + o8 + 1);
+          l0              = __ldg(tl + o8);
+          l1              = __ldg(tl + o8 + 1);
+        }
+        const uint32_t hv[8] = {__float_as_uint(h0.x), __float_as_uint(h0.y), __float_as_uint(h0.z), __float_as_uint(h0.w),
+                                __float_as_uint(h1.x), __float_as_uint(h1.y), __float_as_uint(h1.z), __float_as_uint(h1.w)};
+        const uint32_t lv[8] = {__float_as_uint(l0.x), __float_as_uint(l0.y), __float_as_uint(l0.z), __float_as_uint(l0.w),
+                                __float_as_uint(l1.x), __float_as_uint(l1.y), __float_as_uint(l1.z), __float_as_uint(l1.w)};
+        tc::tmem_st8(ahi + 8 * c8, hv);
+        tc::tmem_st8(alo + 8 * c8, lv);
+      }
+    } else { // block-uniform: a class without a table entry builds its operator here
+      __syncthreads(); // Ys free
+      tc_harmonics<P>(M.off, Ys);
+      __syncthreads();
+      const int dl = __float_as_int(M.off.w);
+      for (int c8 = c_lo; c8 < c_hi; c8++) {
+        uint32_t hv[8], lv[8];
 #pragma unroll
-    for (int c8 = 0; c8 < DH / 8; c8++) {
-      uint32_t v[8];
-      tc::tmem_ld8(lane_base + G::DCOL + DH * half + 8 * c8, v);
-      tc::tmem_ld_wait();
-#pragma unroll
-      for (int i = 0; i < 8; i++)
-        tc_two_sum(acc_hi[8 * c8 + i], acc_lo[8 * c8 + i], __uint_as_float(v[i]));
+        for (int i = 0; i < 8; i++) {
+          const float v = tc_op_value<P>(8 * c8 + i, rj, rk, rpart, rlive, dl, Ys), vh = tc::tf32_trunc(v);
+          hv[i]         = __float_as_uint(vh);
+          lv[i]         = __float_as_uint(tc::tf32_trunc(v - vh));
+        }
+        tc::tmem_st8(ahi + 8 * c8, hv);
+        tc::tmem_st8(alo + 8 * c8, lv);
+      }
     }
   };
 
-  const int ntiles = *a.ntiles;
-  unsigned  g      = 0; // classes issued by this block so far
-  bool      failed = false;
-  for (int T = blockIdx.x; T < ntiles && !failed; T += gridDim.x) {
-    const int p0 = a.tile_start[T], p1 = a.tile_start[T + 1];
-    const int lt = a.tile_level[T];
-    if (tid < 32)
-      tcell[tid] = a.tile_cells[T * 32 + tid];
-    if (p0 >= p1)
-      continue; // (every tile has pairs; kept for safety: its cells' L stay zero)
+  float acc[DT], tot[DT]; // sum of the current group of 8 classes, sum of the groups
 #pragma unroll
-    for (int i = 0; i < DH; i++)
-      acc_hi[i] = acc_lo[i] = 0.f;
-    const unsigned first = g;
-    for (int e = p0; e < p1;) {
-      const int s = g & 1;
-      // (1) members of the class starting at e (warp 0)
-      if (warp == 0) {
-        const unsigned long long k0  = a.keys[e];
-        const bool               in  = e + lane < p1;
-        const unsigned long long kl  = in ? a.keys[e + lane] : ~0ull;
-        const bool               sen = (k0 & TC_SENTINEL) == TC_SENTINEL;
-        const unsigned           eq  = __ballot_sync(0xffffffffu, in && kl == k0);
-        const int                cnt = sen ? 1 : __popc(eq); // members are contiguous from lane 0
-        srcS[s][lane] = -1;
-        __syncwarp();
-        if (lane < cnt) {
-          const uint32_t v = a.vals[e + lane];
-          srcS[s][v >> TC_COL_SHIFT] = (int)(v & ((1u << TC_COL_SHIFT) - 1));
-        }
-        if (lane == 0) {
-          float4 o;
-          if (!sen) {
-            const int   dz = (int)(k0 & 2047) - 1024, dy = (int)((k0 >> 11) & 2047) - 1024, dx = (int)((k0 >> 22) & 2047) - 1024;
-            const int   dl = (int)((k0 >> 33) & 31) - 16;
-            const float f  = dl < 0 ? ldexpf(1.f, dl) : 1.f; // offsets are in units of the finer cell
-            o              = make_float4(dx * f, dy * f, dz * f, __int_as_float(dl));
-          } else {
-            const uint32_t v  = a.vals[e];
-            const int      sc = (int)(v & ((1u << TC_COL_SHIFT) - 1)), t = tcell[v >> TC_COL_SHIFT];
-            const double   iR = 1.0 / a.cv.R[t];
-            o = make_float4((float)((a.cv.x[t] - a.cv.x[sc]) * iR), (float)((a.cv.y[t] - a.cv.y[sc]) * iR),
-                            (float)((a.cv.z[t] - a.cv.z[sc]) * iR), __int_as_float(lt - a.cv.level[sc]));
-          }
-          offS[s]  = o;
-          nextE[s] = e + cnt;
-        }
-      }
-      __syncthreads();
-      // (2) B of this class into stage s (its last reader, the MMAs of class
-      // g - 2, completed before class g - 1 was issued), and S'(o)
-      {
-        unsigned char *bst = sB + s * G::STAGE;
-        constexpr int  KC2 = G::KC / 2, TASKS = 2 * N * KC2;
-        for (int w = tid; w < TASKS; w += 256) {
-          const int which = w / (N * KC2), rem = w - which * (N * KC2);
-          const int n = rem % N, cp2 = rem / N;
-          const int src = srcS[s][n / 3], d = n % 3;
-          unsigned char *dst = bst + which * G::BBYTES + (2 * cp2) * G::LBO + (n >> 3) * G::SBO + (n & 7) * 16;
-          if (src >= 0) {
-            const float *gsrc = (which ? a.Blo : a.Bhi) + ((size_t)src * 3 + d) * KP + 8 * cp2;
-            cp_async16(dst, gsrc);
-            cp_async16(dst + G::LBO, gsrc + 4);
-          } else {
-            *reinterpret_cast<float4 *>(dst)          = make_float4(0.f, 0.f, 0.f, 0.f);
-            *reinterpret_cast<float4 *>(dst + G::LBO) = make_float4(0.f, 0.f, 0.f, 0.f);
-          }
-        }
-      }
-      const float4 o  = offS[s];
-      const int    dl = __float_as_int(o.w);
-      if (tid < P) {
-        const int    m  = tid;
-        const double r2 = (double)o.x * o.x + (double)o.y * o.y + (double)o.z * o.z;
-        singular_column_emit<float, P>(m, o.x, o.y, o.z, (float)(1.0 / r2), (float)(1.0 / sqrt(r2)), [&](int q, cx<float> c) {
-          Ys[q * q + q + m] = (m & 1) ? cx<float>{-c.r, -c.i} : c;
-          if (m > 0)
-            Ys[q * q + q - m] = conj(c);
-        });
-      }
-      __syncthreads();
-      // (3) this thread's chunks of its row of A(delta, o) into TMEM buffer s
-      {
-        const uint32_t ahi = lane_base + G::ACOL + s * G::ABUF, alo = ahi + KP;
-#pragma unroll
-        for (int c8 = 0; c8 < NCH; c8++) {
-          if ((c8 < C0) != (half == 0))
-            continue; // warp-uniform
-          float v8[8];
-#pragma unroll
-          for (int i = 0; i < 8; i++) {
-            const int col = 8 * c8 + i;
-            float     v   = 0.f;
-            if (col < P * P) {
-              // column -> (n, m, Re/Im) of the input, compile-time
-              int n = 0;
-              while ((n + 1) * (n + 1) <= col)
-                n++;
-              const int r = col - n * n, m = (r + 1) / 2, pin = (r > 0 && (r & 1) == 0) ? 1 : 0;
-              if (rlive && n <= P - 1 - rj) {
-                const int q = rj + n, base = q * q + q - rk;
-                if (m == 0) {
-                  const cx<float> y0 = Ys[base];
-                  v                  = rpart ? y0.i : y0.r;
-                } else {
-                  const cx<float> y1 = Ys[base + m], y2 = Ys[base - m];
-                  const float     sg = (m & 1) ? -1.f : 1.f;
-                  if (rpart == 0)
-                    v = pin ? fmaf(-sg, y1.i, y2.i) : fmaf(sg, y1.r, y2.r);
-                  else
-                    v = pin ? fmaf(sg, y1.r, -y2.r) : fmaf(sg, y1.i, y2.i);
-                }
-                v = tc_scale2(v, dl * n);
-              }
-            }
-            v8[i] = v;
-          }
-          uint32_t h[8], l[8];
-#pragma unroll
-          for (int i = 0; i < 8; i++) {
-            const float vh = tc::tf32_trunc(v8[i]);
-            h[i]           = __float_as_uint(vh);
-            l[i]           = __float_as_uint(tc::tf32_trunc(v8[i] - vh));
-          }
-          tc::tmem_st8(ahi + 8 * c8, h);
-          tc::tmem_st8(alo + 8 * c8, l);
-        }
-      }
-      // (4) the previous class's MMAs: wait, then add its D into the accumulators
-      {
-        const bool ok = g == first || tc::mbar_wait_bounded(&mbar[(g - 1) & 1], ((g - 1) >> 1) & 1);
-        if (__syncthreads_or(!ok)) { // block-uniform: every thread leaves together
-          if (tid == 0)
-            atomicExch(a.err, VFMM_ERR_TIMEOUT);
-          failed = true;
-          break;
-        }
-        tc::fence_after_sync();
-        if (g != first)
-          drain();
-      }
-      // (5) operands complete and visible to the tensor core; D free
-      cp_async_wait_all();
-      tc::fence_proxy_async_smem();
-      tc::tmem_st_wait();
-      tc::fence_before_sync();
-      __syncthreads();
-      // (6) one thread issues the class's MMAs into a fresh D and commits
-      if (tid == 0) {
-        tc::fence_after_sync();
-        const uint32_t     sb = tc::smem_u32(sB + s * G::STAGE);
-        const uint32_t     D = tc::tmem_addr(tb, 0, G::DCOL), Ahi = tc::tmem_addr(tb, 0, G::ACOL + s * G::ABUF), Alo = Ahi + KP;
-        constexpr uint32_t idesc = tc::idesc_tf32(128, N);
+  for (int i = 0; i < DT; i++)
+    acc[i] = tot[i] = 0.f;
+  int ingroup = 0;
+
+  // prologue: decode classes 0 and 1, stage class 0
+  if (warp == 1) {
+    decode(meta[0]);
+    decode(meta[1]);
+  }
+  __syncthreads();
+  if (meta[0].tile >= 0)
+    stage(meta[0], 0);
+  bool failed = false;
+  for (unsigned c = 0; !failed; c++) {
+    const TcMeta &M = meta[c % 3];
+    if (M.tile < 0)
+      break; // block-uniform (read after a barrier)
+    const int s = c & 1;
+    // 1. operands of class c complete and visible to the tensor core; D drained
+    cp_async_wait_all();
+    tc::fence_proxy_async_smem();
+    tc::tmem_st_wait();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t     D = tc::tmem_addr(tb, 0, G::DCOL), Ahi = tc::tmem_addr(tb, 0, G::ACOL + s * G::ABUF), Alo = Ahi + KP;
+      const uint64_t     dhi = tc::smem_desc_noswizzle(tc::smem_u32(sB + s * G::STAGE), G::LBO, G::SBO);
+      const uint64_t     dlo = tc::smem_desc_noswizzle(tc::smem_u32(sB + s * G::STAGE + G::BBYTES), G::LBO, G::SBO);
+      constexpr uint64_t dk  = (uint64_t)(2 * G::LBO) >> 4; // descriptor start-address step per K step of 8
+      constexpr uint32_t idesc = tc::idesc_tf32(128, N);
 #pragma unroll 1
-        for (int kk = NCH - 1; kk >= 0; kk--) {
-          tc::mma_tf32_ts(D, Alo + 8 * kk, tc::smem_desc_noswizzle(sb + 2 * kk * G::LBO, G::LBO, G::SBO), idesc, kk == NCH - 1 ? 0u : 1u);
-          tc::mma_tf32_ts(D, Ahi + 8 * kk, tc::smem_desc_noswizzle(sb + G::BBYTES + 2 * kk * G::LBO, G::LBO, G::SBO), idesc, 1u);
-        }
-#pragma unroll 1
-        for (int kk = NCH - 1; kk >= 0; kk--)
-          tc::mma_tf32_ts(D, Ahi + 8 * kk, tc::smem_desc_noswizzle(sb + 2 * kk * G::LBO, G::LBO, G::SBO), idesc, 1u);
-        tc::mma_commit(&mbar[s]);
+      for (int kk = NCH - 1; kk >= 0; kk--) {
+        tc::mma_tf32_ts(D, Alo + 8 * kk, dhi + dk * kk, idesc, kk == NCH - 1 ? 0u : 1u);
+        tc::mma_tf32_ts(D, Ahi + 8 * kk, dlo + dk * kk, idesc, 1u);
       }
-      e = nextE[s];
-      g++;
+#pragma unroll 1
+      for (int kk = NCH - 1; kk >= 0; kk--)
+        tc::mma_tf32_ts(D, Ahi + 8 * kk, dhi + dk * kk, idesc, 1u);
+      tc::mma_commit(&mbar[s]);
     }
-    if (failed)
-      break;
-    // the tile's last class
-    const unsigned last = g - 1;
-    if (__syncthreads_or(!tc::mbar_wait_bounded(&mbar[last & 1], (last >> 1) & 1))) {
+    // 2. decode class c + 2 (its slot held class c - 1, finished last iteration)
+    if (warp == 1)
+      decode(meta[(c + 2) % 3]);
+    // 3. stage class c + 1 into the other stage and A buffer (their last
+    // reader, class c - 1, completed before class c was issued)
+    const TcMeta &Mn = meta[(c + 1) % 3];
+    if (Mn.tile >= 0)
+      stage(Mn, s ^ 1);
+    // 4. class c's D into the accumulators; a tile's last class writes its L
+    const bool ok = tid != 0 || tc::mbar_wait_bounded(&mbar[s], (c >> 1) & 1);
+    if (__syncthreads_or(!ok)) { // block-uniform: every thread leaves together
       if (tid == 0)
         atomicExch(a.err, VFMM_ERR_TIMEOUT);
       failed = true;
       break;
     }
     tc::fence_after_sync();
-    drain();
-    // epilogue: L (FP64) = accumulated rows scaled by (-1)^j R_t^(-j-1)
-    if (rlive) {
-      const int    jks   = row >> 1;
-      const double scale = ((rj & 1) ? -1.0 : 1.0) * ldexp(a.iR0pow[rj + 1], lt * (rj + 1));
 #pragma unroll
-      for (int i = 0; i < DH; i++) {
-        const int col = DH * half + i, t = col / 3, d = col - 3 * t, cell = tcell[t];
-        if (cell >= 0)
-          reinterpret_cast<double *>(a.L)[2 * ((size_t)cell * 3 * K + 3 * jks + d) + rpart] = ((double)acc_hi[i] + (double)acc_lo[i]) * scale;
+    for (int h = 0; h < DT; h += 16) {
+      uint32_t v0[8], v1[8];
+      tc::tmem_ld8(lane_base + G::DCOL + DT * third + h, v0);
+      tc::tmem_ld8(lane_base + G::DCOL + DT * third + h + 8, v1);
+      tc::tmem_ld_wait();
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        acc[h + i] += __uint_as_float(v0[i]);
+        acc[h + 8 + i] += __uint_as_float(v1[i]);
       }
     }
-    tc::fence_before_sync();
-    __syncthreads(); // D is drained and tcell read before the next tile
+    if (++ingroup == 8 || M.last) {
+#pragma unroll
+      for (int i = 0; i < DT; i++) {
+        tot[i] += acc[i];
+        acc[i] = 0.f;
+      }
+      ingroup = 0;
+    }
+    if (M.last) {
+      if (rlive) {
+        const int    jks = row >> 1, lt = M.level, T = M.tile;
+        const double scale = ((rj & 1) ? -1.0 : 1.0) * ldexp(a.iR0pow[rj + 1], lt * (rj + 1));
+#pragma unroll
+        for (int i = 0; i < DT; i++) {
+          const int col = DT * third + i, t = col / 3, d = col - 3 * t, cell = a.tile_cells[T * 32 + t];
+          if (cell >= 0)
+            reinterpret_cast<double *>(a.L)[2 * ((size_t)cell * 3 * K + 3 * jks + d) + rpart] = (double)tot[i] * scale;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < DT; i++)
+        tot[i] = 0.f;
+    }
   }
   cp_async_wait_all(); // no copy of this block stays in flight
   tc::fence_before_sync();
@@ -557,7 +784,7 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   S.tkeys_sorted.reserve(nc);
   S.tile_of.reserve(nc);
   S.col_of.reserve(nc);
-  S.meta.reserve(3 * TC_L + 1);
+  S.meta.reserve(3 * TC_L + 2);
   S.tile_cells.reserve((size_t)ntmax * 32);
   S.tile_level.reserve(ntmax);
   S.tile_start.reserve(ntmax + 1);
@@ -571,7 +798,7 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
                                                 TC_CLASS_BITS + tile_bits, s));
   S.cub_tmp.reserve(std::max(b1, b2));
 
-  VFMM_CUDA_TRY(cudaMemsetAsync(S.meta.p, 0xFF, sizeof(int) * (3 * TC_L + 1), s));
+  VFMM_CUDA_TRY(cudaMemsetAsync(S.meta.p, 0xFF, sizeof(int) * (3 * TC_L + 2), s));
   VFMM_CUDA_TRY(cudaMemsetAsync(S.tile_cells.p, 0xFF, sizeof(int) * (size_t)ntmax * 32, s));
   k_tc_target_keys<<<grid_for(nc, 256), 256, 0, s>>>(e.cells, e.m2l_start, nc, S.tkeys.p);
   count_launch();
@@ -593,6 +820,37 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   k_tc_tile_ranges<<<grid_for(np + 1, 256), 256, 0, s>>>(S.pkeys_sorted.p, np, S.meta.p, S.tile_start.p);
   count_launch();
 
+  // operator classes and their table
+  int dev = 0, nsm = 0;
+  VFMM_CUDA_TRY(cudaGetDevice(&dev));
+  VFMM_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  S.hkeys.reserve(TC_HASH);
+  S.hid.reserve(TC_HASH);
+  S.cls_of.reserve(TC_HASH);
+  S.cidq.reserve(np);
+  if (!S.ncls_host) {
+    VFMM_CUDA_TRY(cudaMallocHost((void **)&S.ncls_host, sizeof(int)));
+    *S.ncls_host = 0;
+  }
+  // table capacity: the last evaluation's class count (its copy completed at
+  // the tree build's host synchronisation) with headroom; classes beyond it
+  // are built inside the M2L kernel
+  const int want = *S.ncls_host + *S.ncls_host / 4 + 64;
+  S.cap          = std::min(TC_HASH, std::max(std::max(S.cap, 512), want));
+  constexpr int NCH = G::KP / 8;
+  S.table.reserve((size_t)S.cap * 2 * NCH * 128 * 2);
+  int *count = S.meta.p + 3 * TC_L + 1;
+  VFMM_CUDA_TRY(cudaMemsetAsync(S.hkeys.p, 0xFF, sizeof(unsigned long long) * TC_HASH, s));
+  k_tc_class_insert<<<grid_for(np, 256), 256, 0, s>>>(S.pkeys_sorted.p, np, S.hkeys.p, m.eval_err);
+  count_launch();
+  k_tc_class_ids<<<1, 1024, 0, s>>>(S.hkeys.p, S.hid.p, S.cls_of.p, count);
+  count_launch();
+  k_tc_class_ops<P><<<std::min(S.cap, 2 * nsm), 128, 0, s>>>(S.cls_of.p, count, S.cap, S.table.p);
+  count_launch();
+  k_tc_class_index<<<grid_for(np, 256), 256, 0, s>>>(S.pkeys_sorted.p, np, S.hkeys.p, S.hid.p, count, S.cap, S.cidq.p);
+  count_launch();
+  VFMM_CUDA_TRY(cudaMemcpyAsync(S.ncls_host, count, sizeof(int), cudaMemcpyDeviceToHost, s));
+
   TcArgs a{};
   a.keys       = S.pkeys_sorted.p;
   a.vals       = S.pvals_sorted.p;
@@ -603,6 +861,8 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   a.ntiles     = S.meta.p + 3 * TC_L;
   a.Bhi        = m.Bhi;
   a.Blo        = m.Blo;
+  a.table      = S.table.p;
+  a.cidq       = S.cidq.p;
   a.cv         = e.cells;
   a.L          = e.L;
   a.err        = m.eval_err;
@@ -611,10 +871,7 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   for (int k = 1; k < PMAX + 2; k++)
     a.iR0pow[k] = a.iR0pow[k - 1] * iR0;
   VFMM_SMEM_ONCE(G::smem, k_m2l_tc<P>);
-  int dev = 0, nsm = 0;
-  VFMM_CUDA_TRY(cudaGetDevice(&dev));
-  VFMM_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  k_m2l_tc<P><<<std::max(1, std::min(nsm, ntmax)), 256, G::smem, s>>>(a);
+  k_m2l_tc<P><<<std::max(1, std::min(nsm, ntmax)), 384, G::smem, s>>>(a);
   count_launch();
   VFMM_LAUNCH_CHECK();
 }

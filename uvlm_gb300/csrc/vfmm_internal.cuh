@@ -261,6 +261,15 @@ struct TcScratch {
   DevBuf<uint32_t>           pvals, pvals_sorted;
   DevBuf<int>                tile_of, col_of, tile_cells, tile_level, tile_start, meta;
   DevBuf<unsigned char>      cub_tmp;
+  // operator classes: hash (keys, index per slot), keys by index, index per
+  // pair group, operator table for the first `cap` classes; the class count
+  // of the last evaluation, copied back asynchronously (pinned), sizes the
+  // next table
+  DevBuf<unsigned long long> hkeys, cls_of;
+  DevBuf<int>                hid, cidq;
+  DevBuf<float4>             table;
+  int                        cap       = 0;
+  int                       *ncls_host = nullptr;
 };
 // Padded K extent of one component's multipole operand row (P^2 real terms).
 __host__ __device__ constexpr int tc_kp(int P) { return (P * P + 7) / 8 * 8; }
