@@ -384,15 +384,15 @@ struct TcMeta {
 // classes in order.  Warp w writes and reads TMEM lanes 32 (w % 4) .. + 31
 // (rows of A and D); warps w, w + 4, w + 8 split each row's A chunks and D
 // columns.  Iteration c:
-//   1. B(c) and A(c) complete -> barrier -> one thread issues the MMAs of
+//   1. B(c) and A(c) complete -> barrier -> one thread of warp 3 issues the MMAs of
 //      class c into a fresh D (small products first: A_lo B_hi and A_hi B_lo,
 //      then A_hi B_hi, each from the highest degrees down), commit;
-//   2. warp 1 decodes class c + 2 into the metadata ring;
+//   2. warp 2 decodes class c + 2 into the metadata ring;
 //   3. all threads stage class c + 1 while the tensor core works: B by
 //      cp.async into the other shared-memory stage, the nonzero chunks of
 //      their operator rows from the table (L2) into the other TMEM A buffer
 //      (classes without a table entry build their operator here);
-//   4. thread 0 waits for class c's MMAs; all threads add D into registers;
+//   4. the issuing thread waits for class c's MMAs; all threads add D into registers;
 //      at the last class of a tile they write its local expansions (FP64).
 // A fresh D per class keeps the tensor core's truncating FP32 accumulation
 // to a few units in the last place of each class's sum; the classes are
@@ -412,7 +412,15 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
   __shared__ __align__(8) uint64_t mbar[2];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quarter = warp & 3, third = warp >> 2;
-  const int c_lo = (NCH * third) / 3, c_hi = (NCH * (third + 1)) / 3; // A chunks of this third
+  // Roles.  Thread ISSUER (warp 3, whose TMEM quarter holds the lightest
+  // operator rows) issues the MMAs, which blocks it for about their duration;
+  // its quarter's operator chunks go to warps 7 and 11.  Warp 2 decodes.
+  constexpr int ISSUER = 96, DECODER = 2;
+  int           c_lo = (NCH * third) / 3, c_hi = (NCH * (third + 1)) / 3; // A chunks of this warp
+  if (quarter == 3) {
+    c_lo = third == 0 ? 0 : (third == 1 ? 0 : NCH / 2);
+    c_hi = third == 0 ? 0 : (third == 1 ? NCH / 2 : NCH);
+  }
 
   if (warp == 0) {
     tc::tmem_alloc(&tbase, 512);
@@ -436,7 +444,7 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
   const int      nz        = rlive ? ((P - rj) * (P - rj) + 7) / 8 : 0;
   const int      nzw       = __reduce_max_sync(0xffffffffu, nz); // the warp's largest
   const uint32_t lane_base = tc::tmem_addr(tb, 32 * quarter, 0);
-  { // zero both A buffers once: chunks beyond a row's nonzero ones stay zero
+  { // zero both A buffers once: chunks beyond a row's nonzero ones stay zero (every chunk of every lane: the warps of a quarter cover [0, NCH))
     const uint32_t z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int b = 0; b < 2; b++)
       for (int c8 = c_lo; c8 < c_hi; c8++) {
@@ -453,14 +461,14 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
   const int     gdoff = gwhich * G::BBYTES + (gcol >> 3) * G::SBO + (gcol & 7) * 16;
   const float  *gbase = (gwhich ? a.Blo : a.Bhi) + (gcol % 3) * KP;
 
-  // warp 1's walker over this block's tiles and classes
+  // the decoder warp's walker over this block's tiles and classes
   const int ntiles = *a.ntiles;
   int       wT = blockIdx.x, we = 0, wp1 = 0;
-  if (warp == 1 && wT < ntiles) {
+  if (warp == DECODER && wT < ntiles) {
     we  = a.tile_start[wT];
     wp1 = a.tile_start[wT + 1];
   }
-  auto decode = [&](TcMeta &M) { // warp 1: the class at the walker into M
+  auto decode = [&](TcMeta &M) { // decoder warp: the class at the walker into M
     while (wT < ntiles && we >= wp1) {
       wT += gridDim.x;
       if (wT < ntiles) {
@@ -505,7 +513,8 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
   };
 
   // stage class M into shared-memory stage / TMEM buffer b (all threads)
-  auto stage = [&](const TcMeta &M, int b) {
+  // B of class M into shared-memory stage b (cp.async; all threads)
+  auto gather_b = [&](const TcMeta &M, int b) {
     unsigned char *dst = sB + b * G::STAGE + gdoff;
     const int      src = M.src[gcol / 3];
     if (src >= 0) {
@@ -521,6 +530,10 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
         *reinterpret_cast<float4 *>(dst + (2 * cp2 + 1) * G::LBO) = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
+  };
+  // the operator of class M into TMEM buffer b (all threads: a class without
+  // a table entry synchronises the block)
+  auto stage_a = [&](const TcMeta &M, int b) {
     const uint32_t ahi = lane_base + G::ACOL + b * G::ABUF, alo = ahi + KP;
     const int      cid = M.cid;
     if (cid >= 0) {
@@ -568,13 +581,15 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
   int ingroup = 0;
 
   // prologue: decode classes 0 and 1, stage class 0
-  if (warp == 1) {
+  if (warp == DECODER) {
     decode(meta[0]);
     decode(meta[1]);
   }
   __syncthreads();
-  if (meta[0].tile >= 0)
-    stage(meta[0], 0);
+  if (meta[0].tile >= 0) {
+    gather_b(meta[0], 0);
+    stage_a(meta[0], 0);
+  }
   bool failed = false;
   for (unsigned c = 0; !failed; c++) {
     const TcMeta &M = meta[c % 3];
@@ -587,7 +602,10 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
     tc::tmem_st_wait();
     tc::fence_before_sync();
     __syncthreads();
-    if (tid == 0) {
+    const TcMeta &Mn = meta[(c + 1) % 3];
+    if (warp == ISSUER / 32 && Mn.tile >= 0) // before its blocking issue: stage s ^ 1 is free (class c - 1 completed)
+      gather_b(Mn, s ^ 1);
+    if (tid == ISSUER) {
       tc::fence_after_sync();
       const uint32_t     D = tc::tmem_addr(tb, 0, G::DCOL), Ahi = tc::tmem_addr(tb, 0, G::ACOL + s * G::ABUF), Alo = Ahi + KP;
       const uint64_t     dhi = tc::smem_desc_noswizzle(tc::smem_u32(sB + s * G::STAGE), G::LBO, G::SBO);
@@ -605,17 +623,19 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
       tc::mma_commit(&mbar[s]);
     }
     // 2. decode class c + 2 (its slot held class c - 1, finished last iteration)
-    if (warp == 1)
+    if (warp == DECODER)
       decode(meta[(c + 2) % 3]);
     // 3. stage class c + 1 into the other stage and A buffer (their last
     // reader, class c - 1, completed before class c was issued)
-    const TcMeta &Mn = meta[(c + 1) % 3];
-    if (Mn.tile >= 0)
-      stage(Mn, s ^ 1);
+    if (Mn.tile >= 0) {
+      if (warp != ISSUER / 32)
+        gather_b(Mn, s ^ 1);
+      stage_a(Mn, s ^ 1);
+    }
     // 4. class c's D into the accumulators; a tile's last class writes its L
-    const bool ok = tid != 0 || tc::mbar_wait_bounded(&mbar[s], (c >> 1) & 1);
+    const bool ok = tid != ISSUER || tc::mbar_wait_bounded(&mbar[s], (c >> 1) & 1);
     if (__syncthreads_or(!ok)) { // block-uniform: every thread leaves together
-      if (tid == 0)
+      if (tid == ISSUER)
         atomicExch(a.err, VFMM_ERR_TIMEOUT);
       failed = true;
       break;
