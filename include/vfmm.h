@@ -309,10 +309,13 @@ int vfmm_measure_fma_peak(vfmm_handle h, int precision, double *tflops);
  * tcgen05 kind::tf32 MMA D[128 x 16] = A[128 x 8] x B[8 x 16] with A in tensor
  * memory and B in shared memory (K-major, no swizzle; core matrices adjacent
  * in K 256 bytes apart, adjacent in N 128 bytes apart, or the reverse when
- * swap_offsets = 1), on small integers, A[m][k] = (3m + 5k) mod 11 - 5 and
- * B[k][n] = (7k + 3n) mod 13 - 6.  Writes D row-major to the host array out
- * (128 x 16 floats).  VFMM_ERR_UNSUPPORTED on other GPUs. */
-int vfmm_tcgen05_selftest(int device, int swap_offsets, float *out);
+ * mode bit 0 is set), on small integers, A[m][k] = (3m + 5k) mod 11 - 5 and
+ * B[k][n] = (7k + 3n) mod 13 - 6.  Mode bit 1: the MMA is M = 64 with
+ * A[m][0] = m + 1 and A[m][k > 0] = 0 on a zeroed D, so D[lane][n] =
+ * (a + 1) B[0][n] names the TMEM lane a whose A row lane `lane` received (0:
+ * untouched).  Writes the 128 TMEM lanes x 16 columns of D row-major to the
+ * host array out.  VFMM_ERR_UNSUPPORTED on other GPUs. */
+int vfmm_tcgen05_selftest(int device, int mode, float *out);
 
 /* ---- output --------------------------------------------------------------- */
 

@@ -40,3 +40,21 @@ def test_tcgen05_tf32_mma_layouts(vfmm_lib):
     if not ok0:
         print(out[:4], expected(False)[:4], out1[:4], sep="\n")
     assert ok0 and ok1
+
+
+def test_tcgen05_m64_lane_map(vfmm_lib):
+    """An M = 64 MMA with A in tensor memory: which TMEM lanes it reads A
+    rows from and writes D rows to.  D[lane][0] = (a + 1) B[0][0] with
+    B[0][0] = -6 names the A lane a that fed lane `lane` (0: untouched).  The
+    M2L kernel keeps the rows that need high K columns in exactly these lanes
+    and runs its high-K steps at M = 64."""
+    out = np.zeros((128, 16), np.float32)
+    assert vfmm_lib.vfmm_tcgen05_selftest(0, 2, out.ctypes.data) == 0
+    src = np.rint(-out[:, 0] / 6.0).astype(int) - 1  # -1: lane untouched
+    written = np.flatnonzero(src >= 0)
+    print("M=64 lanes written:", written.tolist())
+    print("fed from A lanes:", src[written].tolist())
+    assert len(written) == 64
+    assert (src[written] == written).all()  # each D row comes from the A row of the same lane
+    expect = np.array([q * 32 + i for q in range(4) for i in range(16)])
+    assert (written == expect).all(), written

@@ -3,7 +3,9 @@
 // k_tc_selftest: one kind::tf32 MMA, D[128 x 16] = A[128 x 8] B[8 x 16],
 // with A in tensor memory and B in shared memory (K-major, no swizzle), on
 // small integers (exact in TF32 and FP32), so that the host can check the
-// operand layouts the M2L kernel relies on element by element.
+// operand layouts the M2L kernel relies on element by element; mode bit 1
+// runs it as M = 64 with A[m][0] = m + 1 (other K zero) on a zeroed D, which
+// shows which TMEM lanes an M = 64 MMA reads and writes.
 #include <algorithm>
 #include <cub/cub.cuh>
 #include "harmonics.cuh"
@@ -12,8 +14,9 @@
 
 namespace vfmm {
 
-__global__ void __launch_bounds__(128) k_tc_selftest(float *out, int swap_offsets, int *err)
+__global__ void __launch_bounds__(128) k_tc_selftest(float *out, int mode, int *err)
 {
+  const bool swap_offsets = mode & 1, m64 = mode & 2;
   __shared__ __align__(1024) float Bs[128]; // K = 8 x N = 16 TF32, 512 bytes
   __shared__ uint32_t             tbase;
   __shared__ __align__(8) uint64_t mbar;
@@ -44,8 +47,11 @@ __global__ void __launch_bounds__(128) k_tc_selftest(float *out, int swap_offset
     uint32_t  v[8];
 #pragma unroll
     for (int k = 0; k < 8; k++)
-      v[k] = __float_as_uint((float)(((m * 3 + k * 5) % 11) - 5));
+      v[k] = __float_as_uint(m64 ? (k == 0 ? (float)(m + 1) : 0.f) : (float)(((m * 3 + k * 5) % 11) - 5));
     tc::tmem_st8(tc::tmem_addr(base, 32 * warp, ACOL), v);
+    const uint32_t z[8] = {0, 0, 0, 0, 0, 0, 0, 0}; // D starts at zero: lanes an M = 64 MMA leaves alone read back 0
+    tc::tmem_st8(tc::tmem_addr(base, 32 * warp, DCOL), z);
+    tc::tmem_st8(tc::tmem_addr(base, 32 * warp, DCOL + 8), z);
   }
   tc::tmem_st_wait();
   tc::fence_before_sync();
@@ -54,7 +60,7 @@ __global__ void __launch_bounds__(128) k_tc_selftest(float *out, int swap_offset
     tc::fence_after_sync();
     const uint32_t lbo = swap_offsets ? 128 : 256, sbo = swap_offsets ? 256 : 128;
     const uint64_t bd  = tc::smem_desc_noswizzle(tc::smem_u32(Bs), lbo, sbo);
-    tc::mma_tf32_ts(tc::tmem_addr(base, 0, DCOL), tc::tmem_addr(base, 0, ACOL), bd, tc::idesc_tf32(128, 16), 0u);
+    tc::mma_tf32_ts(tc::tmem_addr(base, 0, DCOL), tc::tmem_addr(base, 0, ACOL), bd, tc::idesc_tf32(m64 ? 64 : 128, 16), 0u);
     tc::mma_commit(&mbar);
   }
   const bool done = tc::mbar_wait_bounded(&mbar, 0);
@@ -110,8 +116,8 @@ __global__ void __launch_bounds__(128) k_tc_selftest(float *out, int swap_offset
 // parents where possible, so that their offset sets coincide), D = A B with
 // A (128 rows x KP) in tensor memory and B (KP x 96: target x component) in
 // shared memory, one class at a time (see k_m2l_tc).  FP32 is kept by three
-// TF32 products, A_hi B_hi + A_hi B_lo + A_lo B_hi, where x_hi
-// is x with the low 13 mantissa bits cleared and x_lo = x - x_hi.
+// TF32 products, A_hi B_hi + A_hi B_lo + A_lo B_hi, where x_hi is x rounded
+// to TF32 and x_lo is x - x_hi rounded to TF32 (x_hi + x_lo is x to ~2^-22).
 // ============================================================================
 
 // Class key: bits 0..10 oz + 1024, 11..21 oy + 1024, 22..32 ox + 1024,
@@ -234,6 +240,16 @@ __device__ __forceinline__ void tc_row_of(int r, int NR, int &rj, int &rk, int &
   }
 }
 
+// Output row held by TMEM lane L.  An M = 64 MMA covers lanes 0-15 of each
+// 32-lane quarter; those 64 lanes hold rows 0..63 (j <= 7, the rows that need
+// high input degrees), the other 64 lanes rows 64..127 (j >= 7: they need
+// only the first two K steps, input degrees n <= P - 1 - 7 < 4).
+__host__ __device__ __forceinline__ int tc_lane_row(int L)
+{
+  const int q = L >> 5, i = L & 31;
+  return i < 16 ? 16 * q + i : 64 + 16 * q + (i - 16);
+}
+
 // Offset o (target units) and level difference of a class key.
 __device__ __forceinline__ float4 tc_class_offset(unsigned long long k0)
 {
@@ -320,7 +336,7 @@ __global__ void __launch_bounds__(128) k_tc_class_ops(const unsigned long long *
   const int n = min(*count, cap);
   int       rj, rk, rpart;
   bool      rlive;
-  tc_row_of(threadIdx.x, G::NR, rj, rk, rpart, rlive);
+  tc_row_of(tc_lane_row(threadIdx.x), G::NR, rj, rk, rpart, rlive); // table row = TMEM lane
   for (int id = blockIdx.x; id < n; id += gridDim.x) {
     const float4 o = tc_class_offset(cls_of[id]);
     __syncthreads();
@@ -330,9 +346,9 @@ __global__ void __launch_bounds__(128) k_tc_class_ops(const unsigned long long *
     for (int c8 = 0; c8 < NCH; c8++) {
       float h[8], l[8];
       for (int i = 0; i < 8; i++) {
-        const float v = tc_op_value<P>(8 * c8 + i, rj, rk, rpart, rlive, dl, Ys), vh = tc::tf32_trunc(v);
+        const float v = tc_op_value<P>(8 * c8 + i, rj, rk, rpart, rlive, dl, Ys), vh = tc::tf32_rn(v);
         h[i]          = vh;
-        l[i]          = tc::tf32_trunc(v - vh);
+        l[i]          = tc::tf32_rn(v - vh);
       }
       float4 *th = table + ((((size_t)id * 2 + 0) * NCH + c8) * 128 + threadIdx.x) * 2;
       float4 *tl = table + ((((size_t)id * 2 + 1) * NCH + c8) * 128 + threadIdx.x) * 2;
@@ -437,7 +453,7 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
   const uint32_t tb = tbase;
 
   // this thread's output row (TMEM lane) and its nonzero operator chunks
-  const int row = 32 * quarter + lane;
+  const int lane_id = 32 * quarter + lane, row = tc_lane_row(lane_id);
   int       rj, rk, rpart;
   bool      rlive;
   tc_row_of(row, G::NR, rj, rk, rpart, rlive);
@@ -542,7 +558,7 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
       for (int c8 = c_lo; c8 < min(c_hi, nzw); c8++) {
         float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), h1 = h0, l0 = h0, l1 = h0;
         if (c8 < nz) {
-          const size_t o8 = ((size_t)c8 * 128 + row) * 2;
+          const size_t o8 = ((size_t)c8 * 128 + lane_id) * 2;
           h0              = __ldg(th + o8);
           h1              = __ldg(th + o8 + 1);
           l0              = __ldg(tl + o8);
@@ -564,9 +580,9 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
         uint32_t hv[8], lv[8];
 #pragma unroll
         for (int i = 0; i < 8; i++) {
-          const float v = tc_op_value<P>(8 * c8 + i, rj, rk, rpart, rlive, dl, Ys), vh = tc::tf32_trunc(v);
+          const float v = tc_op_value<P>(8 * c8 + i, rj, rk, rpart, rlive, dl, Ys), vh = tc::tf32_rn(v);
           hv[i]         = __float_as_uint(vh);
-          lv[i]         = __float_as_uint(tc::tf32_trunc(v - vh));
+          lv[i]         = __float_as_uint(tc::tf32_rn(v - vh));
         }
         tc::tmem_st8(ahi + 8 * c8, hv);
         tc::tmem_st8(alo + 8 * c8, lv);
@@ -611,14 +627,28 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
       const uint64_t     dhi = tc::smem_desc_noswizzle(tc::smem_u32(sB + s * G::STAGE), G::LBO, G::SBO);
       const uint64_t     dlo = tc::smem_desc_noswizzle(tc::smem_u32(sB + s * G::STAGE + G::BBYTES), G::LBO, G::SBO);
       constexpr uint64_t dk  = (uint64_t)(2 * G::LBO) >> 4; // descriptor start-address step per K step of 8
-      constexpr uint32_t idesc = tc::idesc_tf32(128, N);
+      constexpr uint32_t idesc = tc::idesc_tf32(128, N), idesc64 = tc::idesc_tf32(64, N);
+      constexpr int      KS128 = 2; // K steps that need all 128 rows
+      static_assert((P - 7) * (P - 7) <= 8 * KS128, "rows 64.. (j >= 7) vanish beyond the M = 128 K steps");
+      // K steps 0 and 1 at M = 128 (all rows), the others at M = 64 (the rows
+      // of the lanes 0-15 of each quarter: the other rows are zero there).
+      // The first MMA (M = 128) starts D afresh on every lane; the small
+      // products come first, A_hi B_hi from the highest degrees down.
 #pragma unroll 1
-      for (int kk = NCH - 1; kk >= 0; kk--) {
-        tc::mma_tf32_ts(D, Alo + 8 * kk, dhi + dk * kk, idesc, kk == NCH - 1 ? 0u : 1u);
+      for (int kk = KS128 - 1; kk >= 0; kk--) {
+        tc::mma_tf32_ts(D, Alo + 8 * kk, dhi + dk * kk, idesc, kk == KS128 - 1 ? 0u : 1u);
         tc::mma_tf32_ts(D, Ahi + 8 * kk, dlo + dk * kk, idesc, 1u);
       }
 #pragma unroll 1
-      for (int kk = NCH - 1; kk >= 0; kk--)
+      for (int kk = NCH - 1; kk >= KS128; kk--) {
+        tc::mma_tf32_ts(D, Alo + 8 * kk, dhi + dk * kk, idesc64, 1u);
+        tc::mma_tf32_ts(D, Ahi + 8 * kk, dlo + dk * kk, idesc64, 1u);
+      }
+#pragma unroll 1
+      for (int kk = NCH - 1; kk >= KS128; kk--)
+        tc::mma_tf32_ts(D, Ahi + 8 * kk, dhi + dk * kk, idesc64, 1u);
+#pragma unroll 1
+      for (int kk = KS128 - 1; kk >= 0; kk--)
         tc::mma_tf32_ts(D, Ahi + 8 * kk, dhi + dk * kk, idesc, 1u);
       tc::mma_commit(&mbar[s]);
     }
@@ -908,7 +938,7 @@ void m2l_tensor(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
 
 } // namespace vfmm
 
-extern "C" int vfmm_tcgen05_selftest(int device, int swap_offsets, float *out)
+extern "C" int vfmm_tcgen05_selftest(int device, int mode, float *out)
 {
   using namespace vfmm;
   if (!out)
@@ -929,7 +959,7 @@ extern "C" int vfmm_tcgen05_selftest(int device, int swap_offsets, float *out)
   if (cudaMemset(d, 0, 128 * 16 * sizeof(float) + 16) != cudaSuccess)
     rc = VFMM_ERR_CUDA;
   if (rc == VFMM_OK) {
-    k_tc_selftest<<<1, 128>>>(d, swap_offsets, err);
+    k_tc_selftest<<<1, 128>>>(d, mode, err);
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
       rc = VFMM_ERR_CUDA;
   }

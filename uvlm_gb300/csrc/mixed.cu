@@ -68,7 +68,8 @@ __device__ __forceinline__ void store_mfold(const DevMixed &a, int PP, int c, in
 
 // The scaled multipole Mt_n^m (m >= 0, component d) of cell c as a row of
 // the tensor-core M2L's B operand: Mt_n^0 (real part) at n^2, Re/Im Mt_n^m at
-// n^2 + 2m - 1 and n^2 + 2m, each as TF32 hi and lo parts; the padding after
+// n^2 + 2m - 1 and n^2 + 2m, each as TF32 hi and lo parts (rounded to
+// nearest); the padding after
 // P^2 is zeroed with the (0, 0) term.
 template <int P>
 __device__ __forceinline__ void store_btc(const DevMixed &a, int c, int n, int m, int d, float re, float im)
@@ -76,12 +77,12 @@ __device__ __forceinline__ void store_btc(const DevMixed &a, int c, int n, int m
   constexpr int KP = tc_kp(P);
   float        *hi = a.Bhi + ((size_t)c * 3 + d) * KP, *lo = a.Blo + ((size_t)c * 3 + d) * KP;
   const int     col = n * n + (m ? 2 * m - 1 : 0);
-  const float   rh = tc::tf32_trunc(re), ih = tc::tf32_trunc(im);
+  const float   rh = tc::tf32_rn(re), ih = tc::tf32_rn(im);
   hi[col]          = rh;
-  lo[col]          = tc::tf32_trunc(re - rh);
+  lo[col]          = tc::tf32_rn(re - rh);
   if (m) {
     hi[col + 1] = ih;
-    lo[col + 1] = tc::tf32_trunc(im - ih);
+    lo[col + 1] = tc::tf32_rn(im - ih);
   }
   if (n == 0)
     for (int k = P * P; k < KP; k++)

@@ -90,6 +90,15 @@ __host__ __device__ __forceinline__ float tf32_trunc(float v)
 #endif
 }
 
+// x rounded to the nearest TF32 value (ties away from zero), as an FP32 bit
+// pattern with the 13 low mantissa bits zero; x - tf32_rn(x) is exact in FP32.
+__device__ __forceinline__ float tf32_rn(float v)
+{
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+  return __uint_as_float(r & 0xFFFFE000u);
+}
+
 // ---- descriptors --------------------------------------------------------------
 // Shared-memory matrix descriptor, no swizzle: start address, leading byte
 // offset (K direction), stride byte offset (M/N direction); bit 46 is the
