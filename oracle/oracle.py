@@ -17,7 +17,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
-REF_SRC = "/root/reference/src"
+# the reference's src/ directory (its headers are compiled for the golden fixtures)
+REF_SRC = os.environ.get("UVLM_REF_SRC", "/root/reference/src")
 
 _vp, _L, _i, _d = ctypes.c_void_p, ctypes.c_long, ctypes.c_int, ctypes.c_double
 _PL = ctypes.POINTER(ctypes.c_long)
@@ -61,11 +62,14 @@ def ref_available() -> bool:
     return os.path.isdir(REF_SRC)
 
 
-def ref(P: int, ncrit: int, theta: float) -> ctypes.CDLL:
-    """The reference compiled for (P, ncrit, theta); builds it on first use."""
-    so = os.path.join(HERE, "_ref", f"libref_p{P}_c{ncrit}_t{theta}.so")
+def ref(P: int, ncrit: int, theta: float, openmp: bool = False) -> ctypes.CDLL:
+    """The reference compiled for (P, ncrit, theta); builds it on first use.
+    openmp: the OpenMP build (timing), else the serial one (fixtures)."""
+    tag = "omp_" if openmp else ""
+    so = os.path.join(HERE, "_ref", f"libref_{tag}p{P}_c{ncrit}_t{theta}.so")
     if not os.path.exists(so) or ref_available():  # make rebuilds it when the driver or the shim changed
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_P={P}", f"REF_NCRIT={ncrit}", f"REF_THETA={theta}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref-omp" if openmp else "ref", f"REF_SRC={REF_SRC}", f"REF_P={P}",
+                        f"REF_NCRIT={ncrit}", f"REF_THETA={theta}"], check=True)
     L = ctypes.CDLL(so)
     L.ref_build_tree.argtypes = [_vp, _L, _vp, _L]
     L.ref_build_tree.restype = _L

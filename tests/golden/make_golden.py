@@ -3,9 +3,10 @@
 The reference (kursatyurt/UVLM, src/*.hpp) is compiled from its own sources
 against the project's Kokkos shim (oracle/ref_driver.cpp, oracle/Makefile,
 serial backend: bitwise reproducible) for each (P, ncrit, theta) used below,
-run on seeded inputs, and its outputs saved as .npz.  Needs the reference
-sources at /root/reference (this container only); the fixtures it writes are
-committed and read by the tests everywhere.
+run on seeded inputs, and its outputs saved as .npz.  Needs the reference's
+src/ directory, named by UVLM_REF_SRC (default: the checkout at
+/root/reference/src); the fixtures it writes are committed and read by the
+tests everywhere.
 
 Each body carries its input index in `drdt_old`, a field the evaluation never
 touches, so the tree permutation can be read from the permuted output.
