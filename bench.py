@@ -60,9 +60,12 @@ def parse(argv=None):
     ap.add_argument("--out", default=None, help="also write the JSON line to this file")
     ap.add_argument("--autotune", action="store_true",
                     help="also report the opt-in autotuner's choice (leaf size, M2L batch) and its stage time")
-    ap.add_argument("--workload", default="cloud", choices=["cloud", "rings64", "adjoint"],
+    ap.add_argument("--workload", default="cloud", choices=["cloud", "rings64", "adjoint", "wing", "ring"],
                     help="cloud: the headline N = 2^20 cloud; rings64: 64 independent rings, batched; "
-                         "adjoint: reverse-mode gradient of the leapfrogging rings")
+                         "adjoint: reverse-mode gradient of the leapfrogging rings; wing: wing + wake, 400 RK2 steps "
+                         "of shedding; ring: the 32,512-body ring, 10 RK2 steps with relaxation (FP64)")
+    ap.add_argument("--wing-steps", type=int, default=400, help="wing workload: steps")
+    ap.add_argument("--wing-check", type=int, default=50, help="wing workload: accuracy check every this many steps")
     ap.add_argument("--orders", default="6,14",
                     help="other expansion orders of the cloud reported beside the headline (stage times, errors); '' = none")
     ap.add_argument("--adj-steps", type=int, default=50, help="adjoint workload: RK3 steps")
@@ -577,6 +580,104 @@ def run_adjoint(args, dist: Dist) -> dict | None:
             "forward_seconds": tf, "gradient_over_forward": tg / tf, "objective": v, "complex_step_check": check}
 
 
+def run_wing(args, dist: Dist) -> dict | None:
+    """Wing + wake (workloads.WingWake): AR 8, chord 1, 40 x 10 panels, 5
+    degrees, U = (1, 0, 0), 400 particles shed per step (10 per TE panel), 400
+    RK2 steps of dt = 0.02, mixed precision, p = 10, theta = 0.5, leaf 64.
+    Each step appends the shed particles and advances all of them through
+    vfmm_advance on host arrays (copies included), as the reference's driver
+    calls FMMCalculator::advance (src/main.cpp:291-293).  Every --wing-check
+    steps the current state is evaluated in mixed precision and in FP64 and
+    compared, both against the model-consistent FP64 direct sum on 2048
+    bodies, and one FP64 stage of that state is timed."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    from uvlm_gb300._lib import BODY_DTYPE
+    w = workloads.WingWake(dt=0.02)
+    kw = dict(p=10, ncrit=64, theta=0.5, integration="RK2", device=dist.local_rank)
+    calc = FMMCalculator(precision=args.precision, **kw)
+    bodies = np.zeros(0, BODY_DTYPE)
+    evals, wall, checks = 0.0, 0.0, []
+    for k in range(args.wing_steps):
+        bodies = np.concatenate([bodies, w.shed()])
+        t0 = time.perf_counter()
+        calc.advance(bodies, w.dt)
+        wall += time.perf_counter() - t0
+        evals += 2.0 * bodies.size
+        if dist.rank == 0 and ((k + 1) % args.wing_check == 0 or k + 1 == args.wing_steps):
+            st = bodies.copy()
+            with FMMCalculator(precision="mixed", **kw) as cm, FMMCalculator(precision="fp64", **kw) as c64:
+                mix = evaluate_state(cm, st)
+                f64 = evaluate_state(c64, st)
+                tgt = np.sort(np.random.default_rng(k).choice(st.size, size=min(2048, st.size), replace=False))
+                um, Jm = c64.direct_model(tgt)
+                c64.load(st)
+                t64 = time_fixed_stage(c64, st, w.dt, 1, warmup=0)[0]
+                cm.load(st)
+                tmx = time_fixed_stage(cm, st, w.dt, 1, warmup=1)[0]
+            Jm = Jm.reshape(-1, 9)
+            checks.append({"step": k + 1, "bodies": int(st.size),
+                           "velocity_rel_l2_vs_fp64_fmm": rl2(mix["velocity"], f64["velocity"]),
+                           "J_rel_l2_vs_fp64_fmm": rl2(mix["J"], f64["J"]),
+                           "mixed_velocity_rel_l2_vs_model_direct": rl2(mix["velocity"][tgt], um),
+                           "fp64_velocity_rel_l2_vs_model_direct": rl2(f64["velocity"][tgt], um),
+                           "mixed_J_rel_l2_vs_model_direct": rl2(mix["J"][tgt].reshape(-1, 9), Jm),
+                           "mixed_ms_per_stage": tmx, "fp64_ms_per_stage": t64})
+    calc.close()
+    evals_all = dist.sum(evals)
+    wall_max = dist.max(wall)
+    if dist.rank != 0:
+        return None
+    return {"metric": "particle-evals/sec, wing + wake, 400 RK2 steps of shedding (to 160,000 particles)",
+            "value": evals_all / wall_max, "unit": UNIT, "n_gpus": dist.world, "steps": args.wing_steps, "warmup": 0,
+            "ms_per_step": 1e3 * wall_max / args.wing_steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+            "data": "synthetic (prescribed elliptic bound circulation; no dataset)",
+            "config": {"workload": "wing AR 8, 40 x 10 panels, 5 deg, U = (1, 0, 0), 10 particles shed per TE panel and step, "
+                                   "RK2 dt = 0.02", "final_bodies": int(bodies.size), "p": 10, "theta": 0.5, "ncrit": 64,
+                       "precision": args.precision,
+                       "timing": "host wall clock around vfmm_advance on host arrays (copies included), every step"},
+            "checks": checks}
+
+
+def run_ring(args, dist: Dist) -> dict | None:
+    """The plain FP64 ring (32,512 bodies: 256 stations x 127), p = 8, theta
+    = 0.5, leaf 32, 10 RK2 steps of dt = 0.01 with relaxation (factor 0.3)
+    after each step, through vfmm_advance on host arrays; the oracle
+    restatement of the reference's advance on the host cores beside it."""
+    from oracle import oracle as O
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.ring(256, seed=0)
+    steps = 10
+    with FMMCalculator(p=8, ncrit=32, theta=0.5, integration="RK2", relax=0.3, precision=args.precision,
+                       device=dist.local_rank) as c:
+        c.advance(b.copy(), 0.01)  # warm-up
+        bb = b.copy()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            c.advance(bb, 0.01)
+        tg = dist.max(time.perf_counter() - t0)
+    tc = None
+    cores = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        cores = O.oracle().vo_set_threads(os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        O.advance(b, 8, 32, 0.5, 0.01, steps, 1, relax=0.3)
+        tc = time.perf_counter() - t0
+    if dist.rank != 0:
+        return None
+    evals = dist.world * b.size * 2 * steps
+    line = {"metric": "particle-evals/sec, vortex ring 32,512 bodies, 10 RK2 steps with relaxation", "value": evals / tg,
+            "unit": UNIT, "n_gpus": dist.world, "steps": steps, "warmup": 1, "ms_per_step": 1e3 * tg / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic (seeded ring; no dataset)",
+            "config": {"workload": "ring 256 x 127, RK2 dt 0.01, relaxation 0.3", "bodies": int(b.size), "p": 8, "theta": 0.5,
+                       "ncrit": 32, "precision": args.precision, "timing": "host wall clock around vfmm_advance, copies included"}}
+    if tc is not None:
+        line["cpu_baseline"] = {"value": b.size * 2 * steps / tc, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "the same 10 steps on the host cores", "seconds": tc}
+    return line
+
+
 def main(argv=None):
     args = parse(argv)
     dist = Dist()
@@ -586,6 +687,10 @@ def main(argv=None):
         line = run_rings64(args, dist)
     elif args.workload == "adjoint":
         line = run_adjoint(args, dist)
+    elif args.workload == "wing":
+        line = run_wing(args, dist)
+    elif args.workload == "ring":
+        line = run_ring(args, dist)
     else:
         from uvlm_gb300 import _build, _lib
         if not os.path.exists(_lib.LIB_PATH):

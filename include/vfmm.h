@@ -68,7 +68,8 @@ typedef struct {
   int    viscous;     /* VFMM_INVISCID, VFMM_PSE or VFMM_CSM, applied after every evaluation of a stage */
   int    m2l_batch;   /* mixed mode: M2L sources per batch, 8, 16, 24, 30 or 32 (at most 227 KB of staging: 32 to p = 14, 30 to p = 15); 0 = by p (30 up to 10, 24 to 12, else 16) */
   double nu;          /* kinematic viscosity for PSE/CSM (the reference leaves its _nu unset, fmmCalculator.hpp:56) */
-  int    reserved[2];
+  int    p2p_chunk; /* mixed mode: near-field source bodies the leaf kernel stages per chunk (its P2P tile), 512 or 768; 0 = 768 */
+  int    reserved;
 } vfmm_config;
 
 /* exafmm::Body (exafmmTypes.hpp:18-32), 296 bytes. J[a][b] = du_a/dx_b. */
@@ -150,19 +151,35 @@ typedef struct {
   double ms_per_stage;         /* its measured stage time */
   double default_ms_per_stage; /* the stage time with the configuration before tuning */
   int    tried;                /* configurations timed */
-  int    reserved[3];
+  int    p2p_chunk;            /* chosen P2P tile: near-field sources staged per chunk (mixed mode) */
+  int    reserved[2];
 } vfmm_tuning;
 
 /* Opt-in autotuner: times one stage (best of two after a warm-up) of `bodies`
- * for leaf sizes 16..256 and, in mixed mode, M2L source batches 16/24/30/32
- * (those whose staging fits in shared memory at this p), and
- * keeps the fastest in the handle (vfmm_get_config shows ncrit and m2l_batch).  A
+ * for leaf sizes 16..256 and, in mixed mode, the leaf kernel's P2P tile (512
+ * or 768 staged sources) and, where M2L runs on the CUDA cores, its source
+ * batches 16/24/30/32 (those whose staging fits in shared memory at this p);
+ * keeps the fastest in the handle (vfmm_get_config shows ncrit, m2l_batch
+ * and p2p_chunk).  A
  * leaf size other than the reference's compile-time ncrit (exafmmTypes.hpp:14)
  * builds a different tree and lists, so results are no longer those of the
  * reference at its ncrit.  The bodies on the device afterwards are a copy of
  * `bodies` after one stage; call vfmm_init / vfmm_advance as usual.  No
  * counterpart in the reference. */
 int vfmm_autotune(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, vfmm_tuning *out);
+
+/* Opt-in order choice (no counterpart in the reference, whose P is a
+ * compile-time constant, exafmmTypes.hpp:12): the lowest expansion order p in
+ * pmin..pmax whose velocity error, relative L2 over `targets` bodies spread
+ * over the set, against the model-consistent FP64 direct sum
+ * (vfmm_direct_model) is at most tol, in the handle's precision, leaf size and
+ * theta.  The handle keeps that order; *p_out receives it (pmax when none
+ * meets tol) and *err_out (may be NULL) its error.  The truncation error of
+ * the reference's FMM at theta = 0.5 falls roughly 2.3x per two orders (about
+ * 2e-3 at p = 10 on a uniform cloud), so tol must suit theta.  Leaves the
+ * bodies on the device in tree order after one evaluation. */
+int vfmm_choose_order(vfmm_handle h, const vfmm_body *bodies, size_t n, double tol, int pmin, int pmax, int targets, int *p_out,
+                      double *err_out);
 
 /* Objective of vfmm_adjoint, evaluated on the state after the last step:
  *   energy * E + impulse . I + sum_i seed_x_i . x_i + seed_alpha_i . alpha_i,

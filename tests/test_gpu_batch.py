@@ -57,20 +57,30 @@ def test_batch_rejects_repeated_handles(vfmm_lib):
             advance_batch([c, c], [workloads.cloud(100, seed=1), workloads.cloud(100, seed=2)], 0.01)
 
 
-def test_autotune(vfmm_lib):
-    """The opt-in tuner returns a timed leaf size and batch, keeps them, and the
-    tuned calculator still meets the mixed-mode bar against FP64 at that leaf size."""
+@pytest.mark.parametrize("P,tried", [(8, 18), (12, 72)])
+def test_autotune(vfmm_lib, P, tried):
+    """The opt-in tuner returns a timed leaf size, P2P tile and (where M2L runs
+    on the CUDA cores: p = 12) M2L batch, keeps them, and the tuned calculator
+    still meets the mixed-mode bar against FP64 at that leaf size."""
     from uvlm_gb300 import FMMCalculator, workloads
     b = workloads.cloud(60000, seed=21)
-    with FMMCalculator(p=8, ncrit=64, theta=0.5, integration="Euler", precision="mixed") as c:
+    with FMMCalculator(p=P, ncrit=64, theta=0.5, integration="Euler", precision="mixed") as c:
         t = c.autotune(b, 0.01)
-        assert t["tried"] == 36 and t["ncrit"] in (16, 24, 32, 48, 64, 96, 128, 192, 256) and t["m2l_batch"] in (16, 24, 30, 32)
+        assert t["tried"] == tried and t["ncrit"] in (16, 24, 32, 48, 64, 96, 128, 192, 256)
+        assert t["p2p_chunk"] in (512, 768)
+        import ctypes
+        from uvlm_gb300._lib import vfmm_config
+        cfg = vfmm_config()
+        assert vfmm_lib.vfmm_get_config(c.handle, ctypes.byref(cfg)) == 0
+        assert (cfg.ncrit, cfg.p2p_chunk) == (t["ncrit"], t["p2p_chunk"])
+        if P == 12:
+            assert t["m2l_batch"] in (16, 24, 30, 32)
         assert t["ms_per_stage"] <= t["default_ms_per_stage"]
         bb = b.copy()
         c.init(bb)
         c.calculate()
         c.copyBodies2Host(bb)
-    with FMMCalculator(p=8, ncrit=t["ncrit"], theta=0.5, precision="fp64") as c64:
+    with FMMCalculator(p=P, ncrit=t["ncrit"], theta=0.5, precision="fp64") as c64:
         ref = b.copy()
         c64.init(ref)
         c64.calculate()
@@ -105,3 +115,28 @@ def test_m2l_batch_config(vfmm_lib):
             FMMCalculator(p=p, ncrit=64, theta=0.5, precision="mixed", m2l_batch=mb)
     with FMMCalculator(p=16, ncrit=64, theta=0.5, precision="mixed", m2l_batch=24) as c:
         assert c.config.m2l_batch == 24
+
+
+def test_choose_order(vfmm_lib):
+    """vfmm_choose_order picks the lowest order whose velocity error against
+    the model-consistent direct sum meets the tolerance: the order below it
+    misses the tolerance, and the reported error is the error an evaluation at
+    that order has against vfmm_direct_model."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(20000, seed=33)
+    tol = 5e-3
+    with FMMCalculator(p=4, ncrit=64, theta=0.5, precision="mixed") as c:
+        r = c.choose_order(b, tol, pmin=4, pmax=14, targets=1000)
+        p = r["p"]
+        assert 4 < p < 14 and r["velocity_rel_l2_vs_model_direct"] <= tol
+        lower = c.choose_order(b, tol, pmin=4, pmax=p - 1, targets=1000)
+        assert lower["p"] == p - 1 and lower["velocity_rel_l2_vs_model_direct"] > tol
+    with FMMCalculator(p=p, ncrit=64, theta=0.5, precision="mixed") as c:
+        bb = b.copy()
+        c.init(bb)
+        tgt = (np.arange(1000) * b.size) // 1000
+        u, _ = c.direct_model(tgt)
+        c.calculate()
+        c.copyBodies2Host(bb)
+    err = np.linalg.norm(bb["velocity"][tgt] - u) / np.linalg.norm(u)
+    assert abs(err - r["velocity_rel_l2_vs_model_direct"]) < 1e-9

@@ -43,7 +43,8 @@ INVISCID, PSE, CSM = 0, 1, 2
 
 class vfmm_tuning(ctypes.Structure):
     _fields_ = [("ncrit", ctypes.c_int), ("m2l_batch", ctypes.c_int), ("ms_per_stage", ctypes.c_double),
-                ("default_ms_per_stage", ctypes.c_double), ("tried", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("default_ms_per_stage", ctypes.c_double), ("tried", ctypes.c_int), ("p2p_chunk", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class vfmm_objective(ctypes.Structure):
@@ -56,7 +57,7 @@ class vfmm_config(ctypes.Structure):
                 ("precision", ctypes.c_int), ("integrator", ctypes.c_int), ("stretching", ctypes.c_int),
                 ("formulation", ctypes.c_int), ("relax", ctypes.c_double), ("rk4_fixed", ctypes.c_int),
                 ("device", ctypes.c_int), ("viscous", ctypes.c_int), ("m2l_batch", ctypes.c_int),
-                ("nu", ctypes.c_double), ("reserved", ctypes.c_int * 2)]
+                ("nu", ctypes.c_double), ("p2p_chunk", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
 class VfmmError(RuntimeError):
@@ -80,6 +81,7 @@ _PROTOS = {
     "vfmm_get_sensor_data": (_i, [_H, _vp, _sz]),
     "vfmm_relax": (_i, [_H, _d]),
     "vfmm_autotune": (_i, [_H, _vp, _sz, _d, _vp]),
+    "vfmm_choose_order": (_i, [_H, _vp, _sz, _d, _i, _i, _i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_d)]),
     "vfmm_adjoint": (_i, [_H, _vp, _sz, _d, _i, _i, _vp, ctypes.POINTER(_d), _vp, _vp]),
     "vfmm_diagnostics": (_i, [_H, ctypes.POINTER(_d)]),
     "vfmm_advance_batch": (_i, [ctypes.POINTER(_H), ctypes.POINTER(_vp), ctypes.POINTER(_sz), _i, _d]),

@@ -31,7 +31,7 @@ class FMMCalculator:
     def __init__(self, p: int = 4, ncrit: int = 128, theta: float = 0.3, integration: str = "RK3",
                  viscous: str = "Inviscid", formulation: str = "cVPM", stretching: str = "Transposed",
                  precision: str = "fp64", relax: float = 0.0, rk4_fixed: bool = False, device: int = -1,
-                 nu: float = 0.0, m2l_batch: int = 0):
+                 nu: float = 0.0, m2l_batch: int = 0, p2p_chunk: int = 0):
         cfg = _lib.vfmm_config()
         lib().vfmm_default_config(ctypes.byref(cfg))
         cfg.p, cfg.ncrit, cfg.theta = int(p), int(ncrit), float(theta)
@@ -45,6 +45,7 @@ class FMMCalculator:
         cfg.viscous = _VISC[viscous]
         cfg.nu = float(nu)
         cfg.m2l_batch = int(m2l_batch)
+        cfg.p2p_chunk = int(p2p_chunk)
         h = ctypes.c_void_p()
         code = lib().vfmm_create(ctypes.byref(cfg), ctypes.byref(h))
         if code != 0:
@@ -119,8 +120,19 @@ class FMMCalculator:
         b = _lib.as_bodies(bodies)
         t = _lib.vfmm_tuning()
         self._check(lib().vfmm_autotune(self._h, b.ctypes.data, b.size, float(dt), ctypes.byref(t)))
-        return {"ncrit": t.ncrit, "m2l_batch": t.m2l_batch, "ms_per_stage": t.ms_per_stage,
+        return {"ncrit": t.ncrit, "m2l_batch": t.m2l_batch, "p2p_chunk": t.p2p_chunk, "ms_per_stage": t.ms_per_stage,
                 "default_ms_per_stage": t.default_ms_per_stage, "tried": t.tried}
+
+    def choose_order(self, bodies: np.ndarray, tol: float, pmin: int = 4, pmax: int = 16, targets: int = 2048) -> dict:
+        """vfmm_choose_order: the lowest expansion order whose velocity error
+        against the model-consistent FP64 direct sum is at most tol; this
+        calculator keeps it."""
+        b = _lib.as_bodies(bodies)
+        p, err = ctypes.c_int(), ctypes.c_double()
+        self._check(lib().vfmm_choose_order(self._h, b.ctypes.data, b.size, float(tol), int(pmin), int(pmax), int(targets),
+                                            ctypes.byref(p), ctypes.byref(err)))
+        self.config.p = p.value
+        return {"p": p.value, "velocity_rel_l2_vs_model_direct": err.value}
 
     def adjoint(self, bodies: np.ndarray, dt: float, steps: int, checkpoint_every: int = 10, energy: float = 1.0,
                 impulse=(0.0, 0.0, 1.0), seed_x=None, seed_alpha=None, gradient: bool = True):

@@ -208,6 +208,8 @@ void validate(const vfmm_config &c)
     throw Error(VFMM_ERR_INVALID, "m2l_batch must be 0, 8, 16, 24, 30 or 32");
   if (c.m2l_batch != 0 && c.precision == VFMM_MIXED && !m2l_batch_fits(c.p, c.m2l_batch))
     throw Error(VFMM_ERR_INVALID, "m2l_batch: the batch's staging exceeds a block's shared memory at this p");
+  if (c.p2p_chunk != 0 && c.p2p_chunk != 512 && c.p2p_chunk != 768)
+    throw Error(VFMM_ERR_INVALID, "p2p_chunk must be 0, 512 or 768");
   if (c.viscous != VFMM_INVISCID && c.viscous != VFMM_PSE && c.viscous != VFMM_CSM)
     throw Error(VFMM_ERR_INVALID, "unknown viscous scheme");
   if (!(c.nu >= 0) || !(c.nu < 1e300))
@@ -531,6 +533,7 @@ void calculate(vfmm_handle h)
     m.items32 = h->items32.p;
     m.lanes32   = h->lanes32.p;
     m.m2l_batch = h->m2l_batch;
+    m.p2p_chunk = h->cfg.p2p_chunk;
     if (tensor_m2l(h->cfg.p)) {
       const size_t rows = (size_t)h->tree.ncells * 3 * tc_kp(h->cfg.p);
       h->tcs.B.reserve(2 * rows);
@@ -1065,37 +1068,46 @@ int vfmm_autotune(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, v
       }
       return best;
     };
-    const int  ncrit0 = h->cfg.ncrit, forced0 = h->cfg.m2l_batch;
+    const int  ncrit0 = h->cfg.ncrit, forced0 = h->cfg.m2l_batch, chunk0 = h->cfg.p2p_chunk;
     const bool mixed  = h->cfg.precision == VFMM_MIXED;
     std::memset(out, 0, sizeof(*out));
     out->default_ms_per_stage = time_stage();
     out->ncrit                = ncrit0;
     out->m2l_batch            = h->m2l_batch;
+    out->p2p_chunk            = chunk0 ? chunk0 : 768;
     out->ms_per_stage         = out->default_ms_per_stage;
     const int leaf[] = {16, 24, 32, 48, 64, 96, 128, 192, 256};
     const int bat[]  = {16, 24, 30, 32};
+    const int chk[]  = {768, 512};
+    // the CUDA-core M2L's source batch matters only where the tensor-core M2L does not run
+    const int nbat = mixed && !tensor_m2l(h->cfg.p) ? 4 : 1;
     try {
       for (int nc : leaf)
-        for (int b = 0; b < (mixed ? 4 : 1); b++) {
-          if (mixed && !m2l_batch_fits(h->cfg.p, bat[b]))
-            continue;
-          h->cfg.ncrit     = nc;
-          h->cfg.m2l_batch = mixed ? bat[b] : 0;
-          const float ms   = time_stage();
-          out->tried++;
-          if (ms < out->ms_per_stage) {
-            out->ms_per_stage = ms;
-            out->ncrit        = nc;
-            out->m2l_batch    = h->m2l_batch;
+        for (int b = 0; b < nbat; b++)
+          for (int c = 0; c < (mixed ? 2 : 1); c++) {
+            if (nbat > 1 && !m2l_batch_fits(h->cfg.p, bat[b]))
+              continue;
+            h->cfg.ncrit     = nc;
+            h->cfg.m2l_batch = nbat > 1 ? bat[b] : forced0;
+            h->cfg.p2p_chunk = mixed ? chk[c] : chunk0;
+            const float ms   = time_stage();
+            out->tried++;
+            if (ms < out->ms_per_stage) {
+              out->ms_per_stage = ms;
+              out->ncrit        = nc;
+              out->m2l_batch    = h->m2l_batch;
+              out->p2p_chunk    = h->cfg.p2p_chunk ? h->cfg.p2p_chunk : 768;
+            }
           }
-        }
     } catch (...) {
       h->cfg.ncrit     = ncrit0;
       h->cfg.m2l_batch = forced0;
+      h->cfg.p2p_chunk = chunk0;
       throw;
     }
     h->cfg.ncrit     = out->ncrit;
-    h->cfg.m2l_batch = mixed ? out->m2l_batch : 0;
+    h->cfg.m2l_batch = nbat > 1 ? out->m2l_batch : forced0;
+    h->cfg.p2p_chunk = mixed ? out->p2p_chunk : chunk0;
     h->has_tree = h->has_eval = false;
     VFMM_CUDA_TRY(cudaStreamSynchronize(s));
   });
@@ -1485,6 +1497,24 @@ int vfmm_direct(vfmm_handle h, vfmm_body *targets, size_t nt, const vfmm_body *s
   });
 }
 
+namespace {
+// The model-consistent direct sum at tree-order bodies `targets` (host) into
+// out (host, nt x 12), on the handle's current tree and lists.
+void direct_model_host(vfmm_handle h, const uint32_t *targets, size_t nt, double *out)
+{
+  cudaStream_t s       = h->stream;
+  const int    nchunks = std::max(1, std::min(64, h->n / 4096));
+  h->dtmp.reserve((size_t)nt * 12 * (nchunks + 2) + nt / 2 + 1);
+  double   *scratch = h->dtmp.p, *dout = scratch + (size_t)nt * 12 * (nchunks + 1);
+  uint32_t *dtgt    = reinterpret_cast<uint32_t *>(dout + (size_t)nt * 12);
+  VFMM_CUDA_TRY(cudaMemcpyAsync(dtgt, targets, nt * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+  direct_model_sum(s, h->soa[h->cur].p, h->cap, h->n, h->tree.view(), h->tree.leaf_cells.p, h->tree.nleaves, h->lists.p2p_start.p,
+                   h->lists.p2p_src.p, dtgt, (int)nt, scratch, nchunks, dout);
+  VFMM_CUDA_TRY(cudaMemcpyAsync(out, dout, nt * 12 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+}
+} // namespace
+
 int vfmm_direct_model(vfmm_handle h, const uint32_t *targets, size_t nt, double *out)
 {
   return guarded(h, [&] {
@@ -1497,16 +1527,62 @@ int vfmm_direct_model(vfmm_handle h, const uint32_t *targets, size_t nt, double 
     for (size_t i = 0; i < nt; i++)
       if (targets[i] >= (uint32_t)h->n)
         throw Error(VFMM_ERR_INVALID, "target index out of range");
-    cudaStream_t s       = h->stream;
-    const int    nchunks = std::max(1, std::min(64, h->n / 4096));
-    h->dtmp.reserve((size_t)nt * 12 * (nchunks + 2) + nt / 2 + 1);
-    double   *scratch = h->dtmp.p, *dout = scratch + (size_t)nt * 12 * (nchunks + 1);
-    uint32_t *dtgt    = reinterpret_cast<uint32_t *>(dout + (size_t)nt * 12);
-    VFMM_CUDA_TRY(cudaMemcpyAsync(dtgt, targets, nt * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    direct_model_sum(s, h->soa[h->cur].p, h->cap, h->n, h->tree.view(), h->tree.leaf_cells.p, h->tree.nleaves, h->lists.p2p_start.p,
-                     h->lists.p2p_src.p, dtgt, (int)nt, scratch, nchunks, dout);
-    VFMM_CUDA_TRY(cudaMemcpyAsync(out, dout, nt * 12 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    VFMM_CUDA_TRY(cudaStreamSynchronize(s));
+    direct_model_host(h, targets, nt, out);
+  });
+}
+
+int vfmm_choose_order(vfmm_handle h, const vfmm_body *bodies, size_t n, double tol, int pmin, int pmax, int targets, int *p_out,
+                      double *err_out)
+{
+  return guarded(h, [&] {
+    if (!bodies || !p_out || n == 0 || targets < 1 || !(tol > 0) || pmin < PMIN || pmax > PMAX || pmin > pmax)
+      throw Error(VFMM_ERR_INVALID, "choose_order: bad argument (orders 2..16, tol > 0, targets >= 1)");
+    upload(h, bodies, n);
+    build_tree_and_lists(h);
+    const size_t          nt = std::min<size_t>((size_t)targets, n);
+    std::vector<uint32_t> tgt(nt);
+    for (size_t i = 0; i < nt; i++)
+      tgt[i] = (uint32_t)(i * n / nt);
+    std::vector<double> ref(nt * 12), u(3 * (size_t)n);
+    direct_model_host(h, tgt.data(), nt, ref.data());
+    double nref = 0;
+    for (size_t i = 0; i < nt; i++)
+      for (int d = 0; d < 3; d++)
+        nref += ref[12 * i + d] * ref[12 * i + d];
+    const int p0     = h->cfg.p;
+    int       chosen = pmax;
+    double    err    = 0;
+    try {
+      for (int p = pmin; p <= pmax; p++) {
+        h->cfg.p = p;
+        calculate(h);
+        VFMM_CUDA_TRY(cudaMemcpyAsync(u.data(), h->soa[h->cur].p + (size_t)F_U * h->cap, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+        VFMM_CUDA_TRY(cudaMemcpyAsync(u.data() + n, h->soa[h->cur].p + (size_t)(F_U + 1) * h->cap, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                      h->stream));
+        VFMM_CUDA_TRY(cudaMemcpyAsync(u.data() + 2 * n, h->soa[h->cur].p + (size_t)(F_U + 2) * h->cap, sizeof(double) * n,
+                                      cudaMemcpyDeviceToHost, h->stream));
+        VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
+        check_eval_err(h);
+        double e2 = 0;
+        for (size_t i = 0; i < nt; i++)
+          for (int d = 0; d < 3; d++) {
+            const double diff = u[(size_t)d * n + tgt[i]] - ref[12 * i + d];
+            e2 += diff * diff;
+          }
+        err = nref > 0 ? std::sqrt(e2 / nref) : 0.0;
+        if (err <= tol || p == pmax) {
+          chosen = p;
+          break;
+        }
+      }
+    } catch (...) {
+      h->cfg.p = p0;
+      throw;
+    }
+    h->cfg.p = chosen;
+    *p_out   = chosen;
+    if (err_out)
+      *err_out = err;
   });
 }
 

@@ -546,12 +546,15 @@ __device__ __forceinline__ zf deriv_coef32(const zf *c, int n, int mu, int axis,
   return {0.5f * (A.i - B.i), -0.5f * (A.r - B.r)};
 }
 
-template <int P>
+// CH_: near-field source bodies staged per chunk (the P2P tile): 768 (six
+// blocks per SM, the default) or 512 (seven blocks per SM; vfmm_config.p2p_chunk)
+template <int P, int CH_>
 struct L2P32Sizes {
   static constexpr int    K  = nterms(P);
   static constexpr int    K1 = nterms(P - 1) > 0 ? nterms(P - 1) : 1;
   static constexpr int    K2 = nterms(P - 2) > 0 ? nterms(P - 2) : 1;
-  static constexpr int    CH = 768; // near-field source bodies staged per chunk (measured best: 6 blocks per SM)
+  static constexpr int    CH = CH_;
+  static constexpr int    BLOCKS = CH == 512 ? 7 : 6; // resident blocks per SM the launch bounds ask for
   static constexpr size_t bytes =
       (size_t)CH * 2 * sizeof(float4) + 128 * (sizeof(float4) + sizeof(int)) + (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zf);
   static_assert((size_t)CH * 2 * sizeof(float4) >= 2 * 128 * 12 * sizeof(float), "the staging buffer holds the reduction");
@@ -639,10 +642,10 @@ __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v)
 // Everything is folded into a two-sum (float-float) accumulator, the G members
 // are combined in a fixed order, and the result becomes FP64 for the
 // stretching epilogue.  All lanes run the same trip counts.
-template <int P>
-__global__ void __launch_bounds__(128, 6) k_l2p_p2p32(DevMixed a, double *out)
+template <int P, int CH_>
+__global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(DevMixed a, double *out)
 {
-  using S = L2P32Sizes<P>;
+  using S = L2P32Sizes<P, CH_>;
   constexpr int K = S::K, K1 = S::K1, K2 = S::K2, CH = S::CH, LG = 128;
   constexpr int D1 = P - 1, D2 = P - 2;
   extern __shared__ float4 smem32[];
@@ -984,16 +987,25 @@ static void m2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   VFMM_LAUNCH_CHECK();
 }
 
+template <int P, int CH>
+static void l2p32_launch(cudaStream_t s, const DevMixed &d, const ExpArgs &e, double *out)
+{
+  const size_t bytes = L2P32Sizes<P, CH>::bytes;
+  VFMM_SMEM_ONCE(bytes, k_l2p_p2p32<P, CH>);
+  if (e.nleaves > 0) {
+    k_l2p_p2p32<P, CH><<<std::min(e.nleaves, 152 * 16), 128, bytes, s>>>(d, out);
+    count_launch();
+  }
+}
+
 template <int P>
 static void l2p32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out)
 {
-  DevMixed     d     = dev_mixed(e, m);
-  const size_t bytes = L2P32Sizes<P>::bytes;
-  VFMM_SMEM_ONCE(bytes, k_l2p_p2p32<P>);
-  if (e.nleaves > 0) {
-    k_l2p_p2p32<P><<<std::min(e.nleaves, 152 * 16), 128, bytes, s>>>(d, out);
-    count_launch();
-  }
+  DevMixed d = dev_mixed(e, m);
+  if (m.p2p_chunk == 512)
+    l2p32_launch<P, 512>(s, d, e, out);
+  else
+    l2p32_launch<P, 768>(s, d, e, out);
   VFMM_LAUNCH_CHECK();
 }
 

@@ -282,6 +282,7 @@ struct MixedArgs {
   const int4   *items32;
   const int4   *lanes32; // k_m2l32v2 lane table, see m2l_lane_table
   int           m2l_batch; // sources staged per batch in k_m2l32v2 (8, 16 or 32)
+  int           p2p_chunk; // near-field sources staged per chunk in the leaf kernel (512 or 768; 0: 768)
   double        R0;
   // tensor-core M2L (null tc: the CUDA-core kernel k_m2l32v2): operand rows
   // written by P2M/M2M, the traversal's sorted (target << key_bits | source)
