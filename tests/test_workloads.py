@@ -8,8 +8,13 @@ def test_wing_wake_shedding_rule():
     """400 particles per step (40 TE panels x 10 segments), 160,000 after 400
     steps; the trailing (side-line) vorticity of one step sums to zero along
     the chord direction (the neighbour halves cancel and the tips close the
-    loop), and the spanwise part is the TE line times Gamma, -integral of
-    Gamma dy, as in the reference driver's rule (src/main.cpp:246-289)."""
+    loop); the spanwise part is the TE line times the change of Gamma (the
+    starting vortex at the first step, none after it for the steady
+    prescribed Gamma), or times Gamma every step under the reference
+    driver's rule (src/main.cpp:246-289)."""
+    r = workloads.WingWake(rule="reference")
+    r.shed()
+    assert np.allclose(r.shed()["alpha"][:, 1], -r.gamma * r.b / r.ns)
     w = workloads.WingWake()
     p = w.shed()
     assert p.size == 400
@@ -21,6 +26,7 @@ def test_wing_wake_shedding_rule():
     # the wing moves by -U dt per step; shed particles sit one step behind its TE
     q = w.shed()
     assert np.allclose(q["X"][:, 0] - p["X"][:, 0], -w.U * w.dt)
+    assert np.all(q["alpha"][:, 1] == 0)
     for _ in range(398):
         w.shed()
     assert w.step_index * w.ns == 160000

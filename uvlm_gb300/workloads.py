@@ -107,12 +107,20 @@ class WingWake:
     `alpha_deg` about the spanwise (y) axis, moving through still fluid with
     velocity -U (U = (|U|, 0, 0)) like the reference driver's wing
     (src/main.cpp:183), and shedding wake particles at its trailing edge every
-    step (the rule of src/main.cpp:246-289):
+    step after the reference driver (src/main.cpp:246-289):
 
     * each trailing-edge (TE) panel p sheds at the TE midpoint plus U dt a
-      particle with alpha = (TE vortex line) * Gamma_p, plus half the
-      circulation differences to its neighbours on the panel's side lines,
-      and the full Gamma on the side line at a wing tip;
+      particle carrying half the circulation differences to its neighbours
+      on the panel's side lines, and the full Gamma on the side line at a wing
+      tip (the trailing vorticity);
+    * its spanwise part is the TE vortex line times the change of the panel's
+      circulation since the last step (rule="unsteady", the default: with a
+      steady prescribed Gamma only the first step sheds it, the starting
+      vortex), or times Gamma_p itself every step (rule="reference", the
+      driver's line 255-257: at 400 particles per step the resulting vortex
+      sheet went unstable within 60 steps in FP64 as in mixed precision,
+      speeds above 500 |U| and then coinciding particles, so it is kept only
+      as an option);
     * here each TE panel is cut into `subdiv` equal spanwise segments that
       shed one particle each (the reference sheds one per panel: 40 x 400 =
       16k particles after 400 steps; subdivided, 400 per step reach ~160k);
@@ -130,7 +138,10 @@ class WingWake:
     pitched wing plane."""
 
     def __init__(self, aspect: float = 8.0, chord: float = 1.0, nspan: int = 40, nchord: int = 10, alpha_deg: float = 5.0,
-                 U: float = 1.0, dt: float = 0.02, subdiv: int = 10):
+                 U: float = 1.0, dt: float = 0.02, subdiv: int = 10, rule: str = "unsteady"):
+        if rule not in ("unsteady", "reference"):
+            raise ValueError("rule must be 'unsteady' or 'reference'")
+        self.rule = rule
         a = np.deg2rad(alpha_deg)
         self.c, self.b, self.U, self.dt = chord, aspect * chord, U, dt
         self.ex = np.array([np.cos(a), 0.0, -np.sin(a)])  # chordwise unit vector in the pitched plane
@@ -159,7 +170,8 @@ class WingWake:
         X[:, 2] = te_x[2]
         te_line = np.zeros((n, 3))
         te_line[:, 1] = -(self.y1 - self.y0)  # trailing line along -y
-        A = te_line * g[:, None]
+        shed = g if (self.rule == "reference" or k == 0) else np.zeros_like(g)  # circulation change (steady after the start)
+        A = te_line * shed[:, None]
         # side lines: left along -x (shared with the left neighbour), right along +x
         gl = np.concatenate([[0.0], g[:-1]])
         gr = np.concatenate([g[1:], [0.0]])
