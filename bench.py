@@ -66,6 +66,8 @@ def parse(argv=None):
                          "of shedding; ring: the 32,512-body ring, 10 RK2 steps with relaxation (FP64)")
     ap.add_argument("--wing-steps", type=int, default=400, help="wing workload: steps")
     ap.add_argument("--wing-check", type=int, default=50, help="wing workload: accuracy check every this many steps")
+    ap.add_argument("--m2l-kernel", default="auto", choices=["auto", "tensor", "cuda"],
+                    help="mixed-mode M2L at p = 8..10: by size (auto), tensor cores, or CUDA cores")
     ap.add_argument("--orders", default="6,14",
                     help="other expansion orders of the cloud reported beside the headline (stage times, errors); '' = none")
     ap.add_argument("--adj-steps", type=int, default=50, help="adjoint workload: RK3 steps")
@@ -238,7 +240,7 @@ def run_ours(args, dist: Dist) -> dict | None:
     from uvlm_gb300._lib import BODY_DTYPE
     n = args.n
     calc = FMMCalculator(p=args.p, ncrit=args.ncrit, theta=args.theta, integration="RK2", precision=args.precision,
-                         device=dist.local_rank)
+                         device=dist.local_rank, m2l_kernel=args.m2l_kernel)
     h = calc.handle
     L = lib()
     bodies = workloads.cloud(n, seed=1000 + dist.rank)

@@ -69,8 +69,13 @@ typedef struct {
   int    m2l_batch;   /* mixed mode: M2L sources per batch, 8, 16, 24, 30 or 32 (at most 227 KB of staging: 32 to p = 14, 30 to p = 15); 0 = by p (30 up to 10, 24 to 12, else 16) */
   double nu;          /* kinematic viscosity for PSE/CSM (the reference leaves its _nu unset, fmmCalculator.hpp:56) */
   int    p2p_chunk; /* mixed mode: near-field source bodies the leaf kernel stages per chunk (its P2P tile), 512 or 768; 0 = 768 */
-  int    reserved;
+  int    m2l_kernel; /* mixed mode, p = 8..10: 0 = by size (tensor cores from VFMM_TC_MIN_PAIRS M2L pairs up), 1 = tensor cores, 2 = CUDA cores */
 } vfmm_config;
+
+/* Below this many M2L pairs an evaluation with m2l_kernel = 0 uses the CUDA-core
+ * M2L: the tensor-core M2L's per-evaluation offset-class table pays only when
+ * a level's many targets share their offset classes (dense sets). */
+#define VFMM_TC_MIN_PAIRS 1500000
 
 /* exafmm::Body (exafmmTypes.hpp:18-32), 296 bytes. J[a][b] = du_a/dx_b. */
 typedef struct {

@@ -109,20 +109,21 @@ def test_seeds_follow_the_bodies(vfmm_lib):
     assert worst(errs) < TOL, errs
 
 
-@pytest.mark.parametrize("kw,tol", [(dict(integration="RK3"), 2e-5), (dict(integration="RK4"), 2e-5),
-                                    (dict(integration="RK2", relax=0.3), 3e-5)])
+@pytest.mark.parametrize("kw,tol", [(dict(integration="RK3"), 1e-5), (dict(integration="RK4"), 1e-5),
+                                    (dict(integration="RK2", relax=0.3), 3e-5),
+                                    (dict(integration="RK3", m2l_kernel="tensor"), 2e-5)])
 def test_mixed_gradient_close_to_fp64(vfmm_lib, kw, tol):
     """Mixed precision (FP32 forward kernels, FP32 P2P^T and M2L^T in the
     reverse sweep): the gradient differs from the all-FP64 one by FP32
     rounding of the trajectory and of the transposed passes (RK3, RK4, and
-    RK2 with relaxation).  The forward M2L at p = 8 runs on the tensor cores
-    in three TF32 products, which hold each operand to about 2^-22 (FP32:
-    2^-24): the forward fields stay as close to FP64 as with FP32 M2L
-    (velocity 2.2e-7 on this case), but the 3-step gradient differs by up to
-    1.0e-5 (6.0e-6 with the CUDA-core M2L).  Relaxation rescales alpha by
-    |alpha| / |w| with w a difference of J entries, which amplifies J's
-    rounding (measured 1.1e-5 on this case; the FP64 relaxation adjoint
-    matches the complex step to 1e-8)."""
+    RK2 with relaxation).  Relaxation rescales alpha by |alpha| / |w| with w
+    a difference of J entries, which amplifies J's rounding (measured 1.1e-5
+    on this case; the FP64 relaxation adjoint matches the complex step to
+    1e-8).  With the forward M2L on the tensor cores (three TF32 products,
+    operands held to about 2^-22 against FP32's 2^-24) the forward fields stay
+    as close to FP64 as with the FP32 M2L (velocity 2.2e-7 on this case) but
+    the 3-step gradient differs by up to 1.0e-5 (6.0e-6 with the CUDA-core
+    M2L)."""
     from uvlm_gb300 import FMMCalculator, workloads
     b = workloads.leapfrog(16, seed=7)
     res = {}

@@ -57,14 +57,14 @@ def test_batch_rejects_repeated_handles(vfmm_lib):
             advance_batch([c, c], [workloads.cloud(100, seed=1), workloads.cloud(100, seed=2)], 0.01)
 
 
-@pytest.mark.parametrize("P,tried", [(8, 18), (12, 72)])
-def test_autotune(vfmm_lib, P, tried):
-    """The opt-in tuner returns a timed leaf size, P2P tile and (where M2L runs
-    on the CUDA cores: p = 12) M2L batch, keeps them, and the tuned calculator
+@pytest.mark.parametrize("P,kernel,tried", [(8, "auto", 72), (10, "tensor", 18)])
+def test_autotune(vfmm_lib, P, kernel, tried):
+    """The opt-in tuner returns a timed leaf size, P2P tile and (where M2L may
+    run on the CUDA cores) M2L batch, keeps them, and the tuned calculator
     still meets the mixed-mode bar against FP64 at that leaf size."""
     from uvlm_gb300 import FMMCalculator, workloads
     b = workloads.cloud(60000, seed=21)
-    with FMMCalculator(p=P, ncrit=64, theta=0.5, integration="Euler", precision="mixed") as c:
+    with FMMCalculator(p=P, ncrit=64, theta=0.5, integration="Euler", precision="mixed", m2l_kernel=kernel) as c:
         t = c.autotune(b, 0.01)
         assert t["tried"] == tried and t["ncrit"] in (16, 24, 32, 48, 64, 96, 128, 192, 256)
         assert t["p2p_chunk"] in (512, 768)
@@ -73,7 +73,7 @@ def test_autotune(vfmm_lib, P, tried):
         cfg = vfmm_config()
         assert vfmm_lib.vfmm_get_config(c.handle, ctypes.byref(cfg)) == 0
         assert (cfg.ncrit, cfg.p2p_chunk) == (t["ncrit"], t["p2p_chunk"])
-        if P == 12:
+        if kernel == "auto":
             assert t["m2l_batch"] in (16, 24, 30, 32)
         assert t["ms_per_stage"] <= t["default_ms_per_stage"]
         bb = b.copy()

@@ -262,6 +262,42 @@ def test_mixed_matches_fp64_fmm(vfmm_lib, kind, n, P, ncrit, theta):
     assert ev < 1e-6 and eJ < 1e-6 and ed < 1e-6, (ev, eJ, ed)
 
 
+@pytest.mark.parametrize("kind,n,P,ncrit,theta", [("cloud", 40000, 10, 64, 0.5), ("cloud", 30000, 9, 64, 0.5), ("cloud", 20000, 8, 32, 0.3),
+                                                  ("ring", 96, 8, 32, 0.5), ("ring", 64, 10, 32, 0.5), ("leapfrog", 64, 10, 32, 0.47),
+                                                  ("wing", 60, 10, 64, 0.5)])
+def test_tensor_m2l_matches_fp64_fmm(vfmm_lib, kind, n, P, ncrit, theta):
+    """The tensor-core M2L (forced: small sets choose the CUDA-core kernel by
+    size) against the FP64 FMM on the same tree, within the mixed-mode bar:
+    uniform clouds, thin rings and two rings (cross-level pairs, many offset
+    classes: some built in the kernel beyond the first evaluation's table),
+    and a wing wake after `n` steps of shedding (an adaptive sheet)."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    if kind == "cloud":
+        b = workloads.cloud(n, seed=5)
+    elif kind == "ring":
+        b = workloads.ring(n, seed=5)
+    elif kind == "leapfrog":
+        b = workloads.leapfrog(n, seed=5)
+    else:
+        w = workloads.WingWake()
+        b = np.concatenate([w.shed() for _ in range(n)])
+        b["X"] += np.random.default_rng(5).normal(0.0, 0.02, b["X"].shape)  # a roughened sheet
+    out = {}
+    for prec, kernel in (("fp64", "auto"), ("mixed", "tensor")):
+        with FMMCalculator(p=P, ncrit=ncrit, theta=theta, precision=prec, m2l_kernel=kernel) as c:
+            bb = b.copy()
+            c.init(bb)
+            c.calculate()
+            c.copyBodies2Host(bb)
+            out[prec] = bb
+    assert (out["fp64"]["X"] == out["mixed"]["X"]).all()
+    ev = rel_l2(out["mixed"]["velocity"], out["fp64"]["velocity"])
+    eJ = rel_l2(out["mixed"]["J"], out["fp64"]["J"])
+    ed = rel_l2(out["mixed"]["dadt"], out["fp64"]["dadt"])
+    print(f"tensor M2L {kind} n={n} P={P}: velocity {ev:.3e}  J {eJ:.3e}  dadt {ed:.3e}")
+    assert ev < 1e-6 and eJ < 1e-6 and ed < 1e-6, (ev, eJ, ed)
+
+
 VISC = {"advance_pse_cloud": "PSE", "advance_pse_rk3_ring": "PSE", "advance_csm_cloud": "CSM"}
 
 

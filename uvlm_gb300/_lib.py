@@ -57,7 +57,7 @@ class vfmm_config(ctypes.Structure):
                 ("precision", ctypes.c_int), ("integrator", ctypes.c_int), ("stretching", ctypes.c_int),
                 ("formulation", ctypes.c_int), ("relax", ctypes.c_double), ("rk4_fixed", ctypes.c_int),
                 ("device", ctypes.c_int), ("viscous", ctypes.c_int), ("m2l_batch", ctypes.c_int),
-                ("nu", ctypes.c_double), ("p2p_chunk", ctypes.c_int), ("reserved", ctypes.c_int)]
+                ("nu", ctypes.c_double), ("p2p_chunk", ctypes.c_int), ("m2l_kernel", ctypes.c_int)]
 
 
 class VfmmError(RuntimeError):

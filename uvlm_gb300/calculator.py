@@ -31,7 +31,7 @@ class FMMCalculator:
     def __init__(self, p: int = 4, ncrit: int = 128, theta: float = 0.3, integration: str = "RK3",
                  viscous: str = "Inviscid", formulation: str = "cVPM", stretching: str = "Transposed",
                  precision: str = "fp64", relax: float = 0.0, rk4_fixed: bool = False, device: int = -1,
-                 nu: float = 0.0, m2l_batch: int = 0, p2p_chunk: int = 0):
+                 nu: float = 0.0, m2l_batch: int = 0, p2p_chunk: int = 0, m2l_kernel: str = "auto"):
         cfg = _lib.vfmm_config()
         lib().vfmm_default_config(ctypes.byref(cfg))
         cfg.p, cfg.ncrit, cfg.theta = int(p), int(ncrit), float(theta)
@@ -46,6 +46,7 @@ class FMMCalculator:
         cfg.nu = float(nu)
         cfg.m2l_batch = int(m2l_batch)
         cfg.p2p_chunk = int(p2p_chunk)
+        cfg.m2l_kernel = {"auto": 0, "tensor": 1, "cuda": 2}[m2l_kernel]
         h = ctypes.c_void_p()
         code = lib().vfmm_create(ctypes.byref(cfg), ctypes.byref(h))
         if code != 0:

@@ -210,6 +210,8 @@ void validate(const vfmm_config &c)
     throw Error(VFMM_ERR_INVALID, "m2l_batch: the batch's staging exceeds a block's shared memory at this p");
   if (c.p2p_chunk != 0 && c.p2p_chunk != 512 && c.p2p_chunk != 768)
     throw Error(VFMM_ERR_INVALID, "p2p_chunk must be 0, 512 or 768");
+  if (c.m2l_kernel < 0 || c.m2l_kernel > 2)
+    throw Error(VFMM_ERR_INVALID, "m2l_kernel must be 0 (by size), 1 (tensor cores) or 2 (CUDA cores)");
   if (c.viscous != VFMM_INVISCID && c.viscous != VFMM_PSE && c.viscous != VFMM_CSM)
     throw Error(VFMM_ERR_INVALID, "unknown viscous scheme");
   if (!(c.nu >= 0) || !(c.nu < 1e300))
@@ -488,15 +490,13 @@ ExpArgs particle_args(vfmm_handle h)
   return e;
 }
 
-// The tensor-core M2L runs for p = 8..10 in mixed mode; VFMM_M2L_TENSOR=0 in
-// the environment selects the CUDA-core kernel instead (for comparisons).
-bool tensor_m2l(int p)
+// Whether this evaluation's M2L runs on the tensor cores (mixed mode, p =
+// 8..10): as vfmm_config.m2l_kernel says, by size when it is 0.
+bool tensor_m2l(vfmm_handle h)
 {
-  static const bool off = [] {
-    const char *v = getenv("VFMM_M2L_TENSOR");
-    return v && v[0] == '0';
-  }();
-  return !off && p >= TC_PMIN && p <= TC_PMAX;
+  if (h->cfg.precision != VFMM_MIXED || h->cfg.p < TC_PMIN || h->cfg.p > TC_PMAX || h->cfg.m2l_kernel == 2)
+    return false;
+  return h->cfg.m2l_kernel == 1 || h->lists.n_m2l >= VFMM_TC_MIN_PAIRS;
 }
 
 // Raise the error an evaluation kernel recorded (after a stream sync).
@@ -534,7 +534,7 @@ void calculate(vfmm_handle h)
     m.lanes32   = h->lanes32.p;
     m.m2l_batch = h->m2l_batch;
     m.p2p_chunk = h->cfg.p2p_chunk;
-    if (tensor_m2l(h->cfg.p)) {
+    if (tensor_m2l(h)) {
       const size_t rows = (size_t)h->tree.ncells * 3 * tc_kp(h->cfg.p);
       h->tcs.B.reserve(2 * rows);
       m.tc           = &h->tcs;
@@ -1080,7 +1080,7 @@ int vfmm_autotune(vfmm_handle h, const vfmm_body *bodies, size_t n, double dt, v
     const int bat[]  = {16, 24, 30, 32};
     const int chk[]  = {768, 512};
     // the CUDA-core M2L's source batch matters only where the tensor-core M2L does not run
-    const int nbat = mixed && !tensor_m2l(h->cfg.p) ? 4 : 1;
+    const int nbat = mixed && !(h->cfg.m2l_kernel == 1 && h->cfg.p >= TC_PMIN && h->cfg.p <= TC_PMAX) ? 4 : 1;
     try {
       for (int nc : leaf)
         for (int b = 0; b < nbat; b++)
