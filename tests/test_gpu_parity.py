@@ -130,7 +130,10 @@ def test_ring_configuration_against_oracle(vfmm_lib):
     1e-10; and ten free-running steps are compared at theta = 0.47.  The
     strengths after relaxation (factor 0.3) are held to 1e-9: relaxation
     turns alpha towards w / |w|, w a difference of J entries, which amplifies
-    the rounding differences of J (measured 1.04e-10 at the first step)."""
+    the rounding differences of J (measured 1.04e-10 at the first step).  J
+    and the velocity of bodies within sin(theta) < 1e-4 of their leaf's z
+    axis in the last stage's tree are held to 1e-6 (the reference's L2P, which
+    the oracle restates, divides by sin(theta) there; see near_axis_mask)."""
     import time
     from oracle import oracle as O
     from uvlm_gb300 import FMMCalculator, workloads
@@ -147,8 +150,14 @@ def test_ring_configuration_against_oracle(vfmm_lib):
             t0 = time.perf_counter()
             c.advance(state, 0.01)
             t_gpu += time.perf_counter() - t0
-            for f in ["X", "alpha", "radius", "velocity", "J"]:
+            # positions of the second stage's tree: x0 + dt u0, u0 = 2 (u0 + u1) / 2 - u1
+            x1 = state["X_old"] + 0.01 * (2.0 * state["velocity_old"] - state["velocity"])
+            axis = near_axis_mask(c.tree(), x1)
+            for f in ["X", "alpha", "radius"]:
                 assert rel(state[f], ref[f]) < (1e-9 if f == "alpha" else TOL), (step, f)
+            for f in ["velocity", "J"]:
+                assert rel(state[f][~axis], ref[f][~axis]) < TOL, (step, f)
+                assert rel(state[f], ref[f]) < 1e-6, (step, f)
     print(f"ring 32,512 bodies, 10 RK2 steps with relaxation, theta 0.5: GPU FP64 {t_gpu:.3f} s, oracle (CPU) {t_cpu:.2f} s")
     ref = O.advance(b, 8, 32, 0.47, 0.01, 10, 1, relax=0.3)
     with FMMCalculator(p=8, ncrit=32, theta=0.47, integration="RK2", relax=0.3) as c:

@@ -112,6 +112,7 @@ struct vfmm_handle_s {
   DevBuf<float4>  pos32, alp32;
   TcScratch       tcs;                // tensor-core M2L (mixed mode, p = 8..10)
   int            *eval_err = nullptr; // device: error raised by an evaluation kernel (bounded waits)
+  int            *eval_err_host = nullptr; // pinned: its copy, read after the handle's stream synchronises
 
   DevBuf<unsigned char> flushbuf;
   DevBuf<double>        dtmp;
@@ -268,7 +269,8 @@ void upload(vfmm_handle h, const vfmm_body *b, size_t n)
   }
 }
 
-void check_eval_err(vfmm_handle h);
+void fetch_eval_err(vfmm_handle h);
+void raise_eval_err(vfmm_handle h);
 
 void download(vfmm_handle h, vfmm_body *b, size_t n)
 {
@@ -280,8 +282,9 @@ void download(vfmm_handle h, vfmm_body *b, size_t n)
     soa_to_aos(h->stream, h->soa[h->cur].p, h->cap, h->aos.p, (int)n);
     VFMM_CUDA_TRY(cudaMemcpyAsync(b, h->aos.p, n * sizeof(vfmm_body), cudaMemcpyDeviceToHost, h->stream));
   }
+  fetch_eval_err(h);
   VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
-  check_eval_err(h);
+  raise_eval_err(h);
 }
 
 void read_info(cudaStream_t s, DevInfo *info, DevInfo *hinfo)
@@ -499,15 +502,30 @@ bool tensor_m2l(vfmm_handle h)
   return h->cfg.m2l_kernel == 1 || h->lists.n_m2l >= VFMM_TC_MIN_PAIRS;
 }
 
-// Raise the error an evaluation kernel recorded (after a stream sync).
-void check_eval_err(vfmm_handle h)
+// Queue the copy of the evaluation error word on the handle's stream (before
+// a synchronisation of that stream; only that stream is involved, so handles
+// on other streams keep running).
+void fetch_eval_err(vfmm_handle h)
 {
-  int e = 0;
-  VFMM_CUDA_TRY(cudaMemcpy(&e, h->eval_err, sizeof(int), cudaMemcpyDeviceToHost));
+  VFMM_CUDA_TRY(cudaMemcpyAsync(h->eval_err_host, h->eval_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+}
+
+// After the synchronisation: raise the error an evaluation kernel recorded.
+void raise_eval_err(vfmm_handle h)
+{
+  const int e = *h->eval_err_host;
   if (e) {
-    VFMM_CUDA_TRY(cudaMemset(h->eval_err, 0, sizeof(int)));
+    *h->eval_err_host = 0;
+    VFMM_CUDA_TRY(cudaMemsetAsync(h->eval_err, 0, sizeof(int), h->stream));
     throw Error(e, e == VFMM_ERR_TIMEOUT ? "a tensor-core M2L wait on the GPU gave up (time limit)" : "tensor-core M2L: more operator classes than its hash holds");
   }
+}
+
+void check_eval_err(vfmm_handle h)
+{
+  fetch_eval_err(h);
+  VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  raise_eval_err(h);
 }
 
 void calculate(vfmm_handle h)
@@ -873,6 +891,8 @@ int vfmm_create(const vfmm_config *cfg, vfmm_handle *out)
     VFMM_CUDA_TRY(cudaMalloc((void **)&h->info, sizeof(DevInfo)));
     VFMM_CUDA_TRY(cudaMalloc((void **)&h->eval_err, sizeof(int)));
     VFMM_CUDA_TRY(cudaMemset(h->eval_err, 0, sizeof(int)));
+    VFMM_CUDA_TRY(cudaMallocHost((void **)&h->eval_err_host, sizeof(int)));
+    *h->eval_err_host = 0;
     VFMM_CUDA_TRY(cudaMallocHost((void **)&h->hinfo, sizeof(DevInfo)));
     std::memset(h->hinfo, 0, sizeof(DevInfo));
     VFMM_CUDA_TRY(cudaMalloc((void **)&h->sinfo, sizeof(DevInfo)));
@@ -937,6 +957,8 @@ int vfmm_destroy(vfmm_handle h)
   h->tcs.cub_tmp.release();
   if (h->eval_err)
     cudaFree(h->eval_err);
+  if (h->eval_err_host)
+    cudaFreeHost(h->eval_err_host);
   if (h->info)
     cudaFree(h->info);
   if (h->hinfo)
@@ -1561,7 +1583,6 @@ int vfmm_choose_order(vfmm_handle h, const vfmm_body *bodies, size_t n, double t
                                       h->stream));
         VFMM_CUDA_TRY(cudaMemcpyAsync(u.data() + 2 * n, h->soa[h->cur].p + (size_t)(F_U + 2) * h->cap, sizeof(double) * n,
                                       cudaMemcpyDeviceToHost, h->stream));
-        VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
         check_eval_err(h);
         double e2 = 0;
         for (size_t i = 0; i < nt; i++)
@@ -1607,10 +1628,7 @@ int vfmm_event_elapsed(vfmm_handle h, int a, int b, float *ms)
 
 int vfmm_synchronize(vfmm_handle h)
 {
-  return guarded(h, [&] {
-    VFMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
-    check_eval_err(h);
-  });
+  return guarded(h, [&] { check_eval_err(h); });
 }
 
 uint64_t vfmm_launch_count(vfmm_handle h) { return h ? h->launches : 0; }
