@@ -184,8 +184,11 @@ def test_direct_model_against_oracle(vfmm_lib):
         c.calculate()
         c.copyBodies2Host(bb)
     ref = O.direct_model(bb, cells, p2p, tgt)
+    # J: the near pairs' (regularised - singular) terms are differences of
+    # values up to ~1/R^3 that cancel to a small remainder, and the device and
+    # host sum them in different orders (measured 7e-12): the FP64 fields' bar
     assert rel(u, ref[:, :3]) < 1e-12
-    assert rel(J.reshape(-1, 9), ref[:, 3:]) < 1e-12
+    assert rel(J.reshape(-1, 9), ref[:, 3:]) < 1e-10
     e_gpu = rel_l2(bb["velocity"][tgt], u)
     fmm = O.calculate(b, 10, 64, 0.5)
     e_cpu = rel_l2(fmm["velocity"][tgt], ref[:, :3])

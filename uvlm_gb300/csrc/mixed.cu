@@ -48,10 +48,15 @@ struct DevMixed {
   float        *Bhi, *Blo; // tensor-core M2L operand rows [cell][3][tc_kp(P)] (null: not used)
 };
 
+// 2^e as a double built from its exponent field (-1022 <= e <= 1023; here
+// |e| <= 21 levels x 16 orders): multiplying by it is exact, like ldexp,
+// without ldexp's range handling on GB300's narrow FP64 pipe.
+__device__ __forceinline__ double exp2i(int e) { return __longlong_as_double((long long)(1023 + e) << 52); }
+
 // R_c^n and R_c^-n for a cell at `level` (R_c = R0 / 2^level): exact
 // power-of-two rescalings of the per-tree tables.
-__device__ __forceinline__ double cell_Rpow(const DevMixed &a, int level, int n) { return ldexp(a.R0pow[n], -level * n); }
-__device__ __forceinline__ double cell_iRpow(const DevMixed &a, int level, int n) { return ldexp(a.iR0pow[n], level * n); }
+__device__ __forceinline__ double cell_Rpow(const DevMixed &a, int level, int n) { return a.R0pow[n] * exp2i(-level * n); }
+__device__ __forceinline__ double cell_iRpow(const DevMixed &a, int level, int n) { return a.iR0pow[n] * exp2i(level * n); }
 
 // Store the scaled multipole Mt_n^m (m >= 0, component d) of cell c in the
 // folded FP32 form read by M2L, [cell][n^2+n+m][d]: M'_n^m = (-1)^m Mt_n^m and,
@@ -546,15 +551,17 @@ __device__ __forceinline__ zf deriv_coef32(const zf *c, int n, int mu, int axis,
   return {0.5f * (A.i - B.i), -0.5f * (A.r - B.r)};
 }
 
-// CH_: near-field source bodies staged per chunk (the P2P tile): 768 (six
-// blocks per SM, the default) or 512 (seven blocks per SM; vfmm_config.p2p_chunk)
+// CH_: near-field source bodies staged per chunk (the P2P tile): 768 (five
+// blocks per SM, 96 registers: the default) or 512 (seven blocks per SM, 72
+// registers with a few spilled; vfmm_config.p2p_chunk).  At 2^20 bodies the
+// unspilled five-block form is 7% faster than six blocks at 80 registers.
 template <int P, int CH_>
 struct L2P32Sizes {
   static constexpr int    K  = nterms(P);
   static constexpr int    K1 = nterms(P - 1) > 0 ? nterms(P - 1) : 1;
   static constexpr int    K2 = nterms(P - 2) > 0 ? nterms(P - 2) : 1;
   static constexpr int    CH = CH_;
-  static constexpr int    BLOCKS = CH == 512 ? 7 : 6; // resident blocks per SM the launch bounds ask for
+  static constexpr int    BLOCKS = CH == 512 ? 7 : 5; // resident blocks per SM the launch bounds ask for
   static constexpr size_t bytes =
       (size_t)CH * 2 * sizeof(float4) + 128 * (sizeof(float4) + sizeof(int)) + (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zf);
   static_assert((size_t)CH * 2 * sizeof(float4) >= 2 * 128 * 12 * sizeof(float), "the staging buffer holds the reduction");
@@ -565,59 +572,95 @@ constexpr float kC2spi  = 1.12837916709551257f; // 2/sqrt(pi)
 constexpr float kKS     = 0.0317468755f;        // (2/sqrt(pi)) / (8 sqrt(2) pi)
 constexpr float kIsq2   = 0.707106781186547524f;
 
-// Weights of one pair of the regularised Biot-Savart kernel
-// (multipoleKernels.hpp:239-283) from R^2, w = 1/(2 sigma^2), is = 1/sigma:
-// velocity G = g(rho) / (4 pi R^3) and gradient A = (t2 / sigma^2 -
-// 3 g / R^2) / (4 pi R^3), rho = R / (sqrt(2) sigma), g = erf(rho) - t2,
-// t2 = (2/sqrt(pi)) rho e^(-rho^2).  For rho^2 < 0.25 the x^3-scaled series
-// replaces the cancelling difference; R^2 = 0 (the body itself) gives zero.
-__device__ __forceinline__ void p2p_weights(float R2, float w, float is, float &Gc, float &Ac)
+// ---- packed FP32 (two sources per lane) --------------------------------------
+// The near-field loop runs on float2 operands with the f32x2 instructions
+// (one instruction, two FP32 FMAs): each lane carries two source bodies.
+__device__ __forceinline__ float2 pk(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 add2(float2 x, float2 y) { return __fadd2_rn(x, y); }
+__device__ __forceinline__ float2 mul2(float2 x, float2 y) { return __fmul2_rn(x, y); }
+__device__ __forceinline__ float2 fma2(float2 x, float2 y, float2 z) { return __ffma2_rn(x, y, z); }
+// 1/sqrt(x) and 2^x, the PTX approximations with subnormals flushed (the
+// operands here are squared distances between bodies and -rho^2 log2(e))
+__device__ __forceinline__ float rsqrt_ftz(float x)
 {
-  const float RS   = R2 * w; // rho^2
-  const float R2s  = R2 != 0.f ? R2 : 1.f;
-  const float rinv = rsqrtf(R2s);
-  const float xs   = R2s * rinv * is * kIsq2;
-  const float erfS = erff(xs);
-  const float t2   = kC2spi * xs * __expf(-RS);
-  const float c4   = kInv4pi * rinv * rinv * rinv;
-  const float gg   = erfS - t2;
-  Gc               = gg * c4;
-  Ac               = (t2 * 2.f * w - 3.f * gg * rinv * rinv) * c4;
-  if (RS < 0.25f) {
-    const float gpoly = ((((((1.f / 5400.f) * RS - 1.f / 780.f) * RS + 1.f / 132.f) * RS - 1.f / 27.f) * RS + 1.f / 7.f) * RS - 0.4f) * RS + 2.f / 3.f;
-    const float hpoly = ((((((-1.f / 6120.f) * RS + 1.f / 900.f) * RS - 1.f / 156.f) * RS + 1.f / 33.f) * RS - 1.f / 9.f) * RS + 2.f / 7.f) * RS - 0.4f;
-    const float is2 = is * is, is3 = is2 * is;
-    Gc              = gpoly * kKS * is3;
-    Ac              = hpoly * kKS * is3 * is2;
-  }
-  if (R2 == 0.f)
-    Gc = Ac = 0.f;
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float ex2_ftz(float x)
+{
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
 
-// sacc += the pair's velocity (0..2) and gradient (3..11, J[a][b] at 3+3a+b)
-// terms, offset d = x_target - x_source, strength al.
-__device__ __forceinline__ void p2p_accum(float dx, float dy, float dz, float4 al, float Gc, float Ac, float *sacc)
+__device__ __forceinline__ float rcp_ftz(float x)
 {
-  const float cr0 = dy * al.z - dz * al.y, cr1 = dz * al.x - dx * al.z, cr2 = dx * al.y - dy * al.x;
-  sacc[0]         = fmaf(Gc, cr0, sacc[0]);
-  sacc[1]         = fmaf(Gc, cr1, sacc[1]);
-  sacc[2]         = fmaf(Gc, cr2, sacc[2]);
-  const float a0 = Ac * cr0, a1 = Ac * cr1, a2 = Ac * cr2;
-  sacc[3]        = fmaf(a0, dx, sacc[3]);
-  sacc[4]        = fmaf(a0, dy, sacc[4]);
-  sacc[5]        = fmaf(a0, dz, sacc[5]);
-  sacc[6]        = fmaf(a1, dx, sacc[6]);
-  sacc[7]        = fmaf(a1, dy, sacc[7]);
-  sacc[8]        = fmaf(a1, dz, sacc[8]);
-  sacc[9]        = fmaf(a2, dx, sacc[9]);
-  sacc[10]       = fmaf(a2, dy, sacc[10]);
-  sacc[11]       = fmaf(a2, dz, sacc[11]);
-  sacc[6]        = fmaf(-Gc, al.z, sacc[6]);
-  sacc[9]        = fmaf(Gc, al.y, sacc[9]);
-  sacc[4]        = fmaf(Gc, al.z, sacc[4]);
-  sacc[10]       = fmaf(-Gc, al.x, sacc[10]);
-  sacc[5]        = fmaf(-Gc, al.y, sacc[5]);
-  sacc[8]        = fmaf(Gc, al.x, sacc[8]);
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// erfcx(rho) = e^(rho^2) erfc(rho) ~ t (c1 + c2 t + c3 t^2 + c4 t^3 + c5 t^4),
+// t = 1 / (1 + a rho), for rho >= 0.5: a weighted least-squares fit whose
+// error, with these FP32 constants, is below 5e-8 relative to g(rho) below
+// (uvlm_gb300/csrc/fit_erfcx.py makes them; tests/test_erfcx_fit.py checks
+// them in FP32 arithmetic)
+constexpr float kErfcxA = 0.49f;
+constexpr float kErfcx1 = 0.26611265540122986f;
+constexpr float kErfcx2 = 0.36194512248039246f;
+constexpr float kErfcx3 = -0.03765244781970978f;
+constexpr float kErfcx4 = 0.6230325698852539f;
+constexpr float kErfcx5 = -0.2134859561920166f;
+
+// Weights of the regularised Biot-Savart kernel (multipoleKernels.hpp:239-283)
+// for two pairs at once, from R^2, w = 1/(2 sigma^2) and s = 1/(sqrt(2) sigma)
+// of the source: velocity G = g(rho) / (4 pi R^3) and half the gradient weight
+// A = (w t2 - 1.5 g / R^2) / (4 pi R^3), rho = R s, g = erf(rho) - t2,
+// t2 = (2/sqrt(pi)) rho e^(-rho^2), evaluated as g = 1 - e^(-rho^2) H(rho),
+// H = erfcx(rho) + (2/sqrt(pi)) rho, from the exponential t2 needs and the fit
+// above (no erf call).  Pairs with rho^2 < 0.25 take the x^3-scaled series
+// instead of the cancelling difference (a branch: about one pair in 250 of a
+// uniform cloud), and R^2 = 0 (the body itself) gives zero.
+__device__ __forceinline__ void p2p_weights2(float2 R2, float2 w, float2 s, float2 &G, float2 &A)
+{
+  const float2 RS = mul2(R2, w); // rho^2
+  const float2 ri = pk(rsqrt_ftz(R2.x), rsqrt_ftz(R2.y));
+  const float2 xs = mul2(mul2(R2, ri), s);
+  const float2 ea = mul2(RS, pk(-1.44269504088896341f, -1.44269504088896341f));
+  const float2 ex = pk(ex2_ftz(ea.x), ex2_ftz(ea.y));
+  const float2 u  = fma2(xs, pk(kErfcxA, kErfcxA), pk(1.f, 1.f));
+  const float2 t  = pk(rcp_ftz(u.x), rcp_ftz(u.y));
+  float2       q  = fma2(pk(kErfcx5, kErfcx5), t, pk(kErfcx4, kErfcx4));
+  q               = fma2(q, t, pk(kErfcx3, kErfcx3));
+  q               = fma2(q, t, pk(kErfcx2, kErfcx2));
+  q               = fma2(q, t, pk(kErfcx1, kErfcx1));
+  const float2 kx = mul2(xs, pk(kC2spi, kC2spi));
+  const float2 t2 = mul2(kx, ex);
+  const float2 gg = fma2(mul2(ex, fma2(q, t, kx)), pk(-1.f, -1.f), pk(1.f, 1.f)); // erf - t2
+  const float2 ri2 = mul2(ri, ri);
+  const float2 c4  = mul2(mul2(ri2, ri), pk(kInv4pi, kInv4pi));
+  G                = mul2(gg, c4);
+  A                = mul2(fma2(mul2(gg, ri2), pk(-1.5f, -1.5f), mul2(t2, w)), c4);
+  if (RS.x < 0.25f || RS.y < 0.25f) {
+    // g / rho^3 and the gradient's (3 g - rho g') / rho^5 as series in rho^2;
+    // is^3 = 2 sqrt(2) s^3 and is^5 / 2 = 2 sqrt(2) s^5 with is = 1/sigma
+    constexpr float kK3 = kKS * 2.82842712474619010f;
+    const float     r2[2] = {RS.x, RS.y}, q2[2] = {R2.x, R2.y}, sv[2] = {s.x, s.y};
+    float           g2[2] = {G.x, G.y}, a2[2] = {A.x, A.y};
+#pragma unroll
+    for (int h = 0; h < 2; h++)
+      if (r2[h] < 0.25f) {
+        const float x = r2[h];
+        const float gpoly = ((((((1.f / 5400.f) * x - 1.f / 780.f) * x + 1.f / 132.f) * x - 1.f / 27.f) * x + 1.f / 7.f) * x - 0.4f) * x + 2.f / 3.f;
+        const float hpoly = ((((((-1.f / 6120.f) * x + 1.f / 900.f) * x - 1.f / 156.f) * x + 1.f / 33.f) * x - 1.f / 9.f) * x + 2.f / 7.f) * x - 0.4f;
+        const float s3 = sv[h] * sv[h] * sv[h];
+        g2[h]          = q2[h] != 0.f ? gpoly * kK3 * s3 : 0.f;
+        a2[h]          = q2[h] != 0.f ? hpoly * kK3 * s3 * sv[h] * sv[h] : 0.f;
+      }
+    G = pk(g2[0], g2[1]);
+    A = pk(a2[0], a2[1]);
+  }
 }
 
 // two-sum: hi + lo accumulates v without losing its low-order bits
@@ -636,9 +679,10 @@ __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v)
 //  * far field: member g evaluates the columns m = g, g+G, ... of the leaf's
 //    derivative expansions at the target;
 //  * near field: the bodies of the leaf's P2P source leaves are staged in
-//    shared memory as one flat array in coordinates relative to the target
-//    leaf's centre (each source leaf's centre offset computed once, in FP64),
-//    and member g takes every G-th staged body; groups of 16 are summed in FP32.
+//    shared memory as one flat sequence of body pairs in coordinates relative
+//    to the target leaf's centre (each source leaf's centre offset computed
+//    once, in FP64), and member g takes every G-th pair, both bodies at once in
+//    packed FP32; groups of 16 pairs are summed in FP32 (per body of a pair).
 // Everything is folded into a two-sum (float-float) accumulator, the G members
 // are combined in a fixed order, and the result becomes FP64 for the
 // stretching epilogue.  All lanes run the same trip counts.
@@ -649,16 +693,15 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
   constexpr int K = S::K, K1 = S::K1, K2 = S::K2, CH = S::CH, LG = 128;
   constexpr int D1 = P - 1, D2 = P - 2;
   extern __shared__ float4 smem32[];
-  float4 *Sp   = smem32;   // staged source positions (rel. to target leaf), w = 1/(2 sigma^2)
-  float4 *Sa   = Sp + CH;  // staged strengths, w = 1/sigma
-  float4 *Loff = Sa + CH;  // per source leaf of the current group: centre offset, w = body start (int bits)
+  float4 *Sq   = smem32;   // staged source pairs, four float4 per pair of bodies
+  float4 *Loff = Sq + 2 * CH; // per source leaf of the current group: centre offset, w = body start (int bits)
   int    *Lcnt = reinterpret_cast<int *>(Loff + LG);
   __shared__ int Lpre[LG + 1]; // exclusive prefix of Lcnt over the group; Lpre[ng] = the group's bodies
   static_assert(CH % 128 == 0, "every thread stages the same number of chunk elements");
   zf     *Lc   = reinterpret_cast<zf *>(Lcnt + LG);
   zf     *U    = Lc + 3 * K;
   zf     *JJ   = U + 3 * K1;
-  float  *rhi  = reinterpret_cast<float *>(Sp); // [128][12] partial sums (hi), reusing the staging buffer
+  float  *rhi  = reinterpret_cast<float *>(Sq); // [128][12] partial sums (hi), reusing the staging buffer
   float  *rlo  = rhi + 128 * 12;                // [128][12] partial sums (lo)
   (void)K1;
   (void)K2;
@@ -791,18 +834,23 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
         }
         __syncthreads();
         // The group's source bodies as one sequence (leaf by leaf) cut into
-        // chunks of CH.  Every thread copies its elements e = tid + 128 i of a
-        // chunk with cp.async (all in flight at once), finds each element's
-        // leaf by binary search over Lpre, and after the copies land moves
-        // its own positions from the source leaf's frame to the target's.
+        // chunks of CH, staged as pairs of consecutive bodies: pair k is four
+        // float4, {-x, -y}, {-z, s}, {alpha_x, alpha_y}, {alpha_z, w} of bodies
+        // 2k and 2k + 1 (each float2 = the two bodies), positions relative to
+        // the target leaf's centre, s = 1/(sqrt(2) sigma), w = 1/(2 sigma^2).
+        // Element e = tid + 128 i finds its leaf by binary search over Lpre,
+        // loads its body, and swaps half of its words with lane e ^ 1, so that
+        // the even lane stores the pair's position words and the odd lane its
+        // strength words.  An odd count is padded with a body of zero strength
+        // far away, whose terms are exactly zero.
         const int total = Lpre[ng];
         for (int c0 = 0; c0 < total; c0 += CH) {
-          const int cnt = min(CH, total - c0);
-          int       lqs[CH / 128];
+          const int cnt = min(CH, total - c0), npair = (cnt + 1) >> 1;
+          const bool odd = threadIdx.x & 1;
 #pragma unroll
           for (int i = 0; i < CH / 128; i++) {
-            const int e = threadIdx.x + 128 * i;
-            lqs[i]      = -1;
+            const int e  = threadIdx.x + 128 * i;
+            float     nx = 1e3f, ny = 1e3f, nz = 1e3f, sv = 1.f, wv = 1.f, ax = 0.f, ay = 0.f, az = 0.f;
             if (e < cnt) {
               const int g = c0 + e;
               int       lb = 0, ub = ng - 1; // the last leaf with Lpre <= g
@@ -813,97 +861,151 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
                 else
                   ub = mid - 1;
               }
-              lqs[i]       = lb;
-              const int bi = __float_as_int(Loff[lb].w) + (g - Lpre[lb]);
-              cp_async16(Sp + e, a.pos32 + bi);
-              cp_async16(Sa + e, a.alp32 + bi);
+              const float4 o  = Loff[lb];
+              const int    bi = __float_as_int(o.w) + (g - Lpre[lb]);
+              const float4 p = __ldg(a.pos32 + bi), q = __ldg(a.alp32 + bi);
+              nx = -(p.x + o.x);
+              ny = -(p.y + o.y);
+              nz = -(p.z + o.z);
+              wv = p.w;
+              sv = q.w * kIsq2;
+              ax = q.x;
+              ay = q.y;
+              az = q.z;
+            }
+            const float v0 = __shfl_xor_sync(0xffffffffu, odd ? nx : ax, 1);
+            const float v1 = __shfl_xor_sync(0xffffffffu, odd ? ny : ay, 1);
+            const float v2 = __shfl_xor_sync(0xffffffffu, odd ? nz : az, 1);
+            const float v3 = __shfl_xor_sync(0xffffffffu, odd ? sv : wv, 1);
+            const int   k  = e >> 1;
+            if (k < npair) {
+              if (!odd) {
+                Sq[4 * k]     = make_float4(nx, v0, ny, v1);
+                Sq[4 * k + 1] = make_float4(nz, v2, sv, v3);
+              } else {
+                Sq[4 * k + 2] = make_float4(v0, ax, v1, ay);
+                Sq[4 * k + 3] = make_float4(v2, az, v3, wv);
+              }
             }
           }
-          cp_async_wait_all();
-#pragma unroll
-          for (int i = 0; i < CH / 128; i++)
-            if (lqs[i] >= 0) {
-              const int    e = threadIdx.x + 128 * i;
-              const float4 o = Loff[lqs[i]];
-              float4       p = Sp[e];
-              p.x += o.x;
-              p.y += o.y;
-              p.z += o.z;
-              Sp[e] = p;
-            }
           __syncthreads();
           if (active) {
-            for (int j0 = g; j0 < cnt; j0 += 16 * Gt) {
-              float sacc[12];
-              for (int k = 0; k < 12; k++)
-                sacc[k] = 0.f;
-              const int jend = min(cnt, j0 + 16 * Gt);
-              // two sources per iteration, straight-line, accumulated in source order
-              for (int jb = j0; jb < jend; jb += 2 * Gt) {
-                const int    jb2 = jb + Gt;
-                const bool   two = jb2 < jend;
-                const float4 ps = Sp[jb], qs = Sp[two ? jb2 : jb];
-                const float4 al = Sa[jb], bl = Sa[two ? jb2 : jb];
-                const float  dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
-                const float  ex = pt.x - qs.x, ey = pt.y - qs.y, ez = pt.z - qs.z;
-                const float  R2 = dx * dx + dy * dy + dz * dz, R2b = ex * ex + ey * ey + ez * ez;
-                float        G1, A1, G2, A2;
-                p2p_weights(R2, ps.w, al.w, G1, A1);
-                p2p_weights(R2b, qs.w, bl.w, G2, A2);
-                if (!two)
-                  G2 = A2 = 0.f;
-                p2p_accum(dx, dy, dz, al, G1, A1, sacc);
-                p2p_accum(ex, ey, ez, bl, G2, A2, sacc);
+            const float2 px = pk(pt.x, pt.x), py = pk(pt.y, pt.y), pz = pk(pt.z, pt.z);
+            for (int k0 = g; k0 < npair; k0 += 16 * Gt) {
+              // velocity V, G alpha (E) and half the gradient's A-part (J),
+              // each as two FP32 partial sums (one per body of a pair)
+              float2 V0{0.f, 0.f}, V1{0.f, 0.f}, V2{0.f, 0.f}, E0{0.f, 0.f}, E1{0.f, 0.f}, E2{0.f, 0.f};
+              float2 J[9];
+#pragma unroll
+              for (int u = 0; u < 9; u++)
+                J[u] = pk(0.f, 0.f);
+              const int kend = min(npair, k0 + 16 * Gt);
+              for (int k = k0; k < kend; k += Gt) {
+                const float4 f0 = Sq[4 * k], f1 = Sq[4 * k + 1], f2 = Sq[4 * k + 2], f3 = Sq[4 * k + 3];
+                const float2 dx = add2(px, pk(f0.x, f0.y)), dy = add2(py, pk(f0.z, f0.w)), dz = add2(pz, pk(f1.x, f1.y));
+                const float2 ax = pk(f2.x, f2.y), ay = pk(f2.z, f2.w), az = pk(f3.x, f3.y);
+                const float2 R2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+                float2       G, A;
+                p2p_weights2(R2, pk(f3.z, f3.w), pk(f1.z, f1.w), G, A);
+                const float2 m1 = pk(-1.f, -1.f);
+                const float2 c0 = fma2(mul2(dz, ay), m1, mul2(dy, az)); // d x alpha
+                const float2 c1 = fma2(mul2(dx, az), m1, mul2(dz, ax));
+                const float2 c2 = fma2(mul2(dy, ax), m1, mul2(dx, ay));
+                V0              = fma2(G, c0, V0);
+                V1              = fma2(G, c1, V1);
+                V2              = fma2(G, c2, V2);
+                E0              = fma2(G, ax, E0);
+                E1              = fma2(G, ay, E1);
+                E2              = fma2(G, az, E2);
+                const float2 a0 = mul2(A, c0), a1 = mul2(A, c1), a2 = mul2(A, c2);
+                J[0]            = fma2(a0, dx, J[0]);
+                J[1]            = fma2(a0, dy, J[1]);
+                J[2]            = fma2(a0, dz, J[2]);
+                J[3]            = fma2(a1, dx, J[3]);
+                J[4]            = fma2(a1, dy, J[4]);
+                J[5]            = fma2(a1, dz, J[5]);
+                J[6]            = fma2(a2, dx, J[6]);
+                J[7]            = fma2(a2, dy, J[7]);
+                J[8]            = fma2(a2, dz, J[8]);
               }
-              for (int k = 0; k < 12; k++)
-                two_sum_add(hi[k], lo[k], -sacc[k]); // the near field enters with a minus sign
+              // velocity (0..2) and gradient (3..11, J[a][b] at 3 + 3a + b):
+              // J[a][b] = 2 J_ab + the G alpha terms of the kernel's
+              // antisymmetric part; the near field enters with a minus sign
+              const float ex = E0.x + E0.y, ey = E1.x + E1.y, ez = E2.x + E2.y;
+              float       v[12];
+              v[0] = V0.x + V0.y;
+              v[1] = V1.x + V1.y;
+              v[2] = V2.x + V2.y;
+#pragma unroll
+              for (int u = 0; u < 9; u++)
+                v[3 + u] = 2.f * (J[u].x + J[u].y);
+              v[4] += ez;
+              v[5] -= ey;
+              v[6] -= ez;
+              v[8] += ex;
+              v[9] += ey;
+              v[10] -= ex;
+#pragma unroll
+              for (int u = 0; u < 12; u++)
+                two_sum_add(hi[u], lo[u], -v[u]);
             }
           }
           __syncthreads();
         }
       }
       __syncthreads(); // staging buffer free: reuse it for the partial sums
+#pragma unroll
       for (int k = 0; k < 12; k++) {
         rhi[threadIdx.x * 12 + k] = hi[k];
         rlo[threadIdx.x * 12 + k] = lo[k];
       }
       __syncthreads();
-      if (threadIdx.x < nt) {
-        const int t = threadIdx.x, b = b0 + tc + t;
-        double    r[12];
-        for (int k = 0; k < 12; k++) {
+      // Four adjacent lanes per target (item w = 4 t + q): q = 0 combines the
+      // velocity, q = 1..3 the three gradient entries that make dadt component
+      // q - 1 (column q - 1 of J for the transposed scheme, row q - 1 for the
+      // classic one) and that component; the rVPM correction's dot product is
+      // summed over the four lanes.  Every lane runs the same trip count.
+      for (int w0 = 0; w0 < 4 * nt; w0 += 128) {
+        const int  w = w0 + threadIdx.x, q = w & 3;
+        const bool ok = w < 4 * nt;
+        const int  t = ok ? w >> 2 : 0, b = b0 + tc + t, Gm = t < full ? G : G - 1;
+        int        comp[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+          comp[c] = q == 0 ? c : (a.stretching == VFMM_TRANSPOSED ? 3 + 3 * c + (q - 1) : 3 + 3 * (q - 1) + c);
+        double r3[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
           float h = 0.f, l = 0.f;
-          const int Gm = t < full ? G : G - 1;
           for (int gg = 0; gg < Gm; gg++) {
-            two_sum_add(h, l, rhi[(gg * nt + t) * 12 + k]);
-            l += rlo[(gg * nt + t) * 12 + k];
+            two_sum_add(h, l, rhi[(gg * nt + t) * 12 + comp[c]]);
+            l += rlo[(gg * nt + t) * 12 + comp[c]];
           }
-          r[k] = (double)h + (double)l;
+          r3[c] = (double)h + (double)l;
         }
         const double al[3] = {a.soa[F_A * a.cap + b], a.soa[(F_A + 1) * a.cap + b], a.soa[(F_A + 2) * a.cap + b]};
-        double       dadt[3];
-        for (int aa = 0; aa < 3; aa++) {
-          double v = 0;
-          for (int cc = 0; cc < 3; cc++)
-            v += (a.stretching == VFMM_TRANSPOSED ? r[3 + 3 * cc + aa] : r[3 + 3 * aa + cc]) * al[cc];
-          dadt[aa] = v;
+        double       da    = q == 0 ? 0. : r3[0] * al[0] + r3[1] * al[1] + r3[2] * al[2];
+        double       drdt  = 0.;
+        if (a.formulation == VFMM_RVPM) { // one reciprocal square root per lane: FP64 is a narrow pipe here
+          const double ina = rsqrt(al[0] * al[0] + al[1] * al[1] + al[2] * al[2]);
+          const double ah  = q == 0 ? 0. : al[q - 1] * ina;
+          double       dot = da * ah;
+          dot += __shfl_xor_sync(0xffffffffu, dot, 1);
+          dot += __shfl_xor_sync(0xffffffffu, dot, 2);
+          if (q == 0)
+            drdt = -1.0 / 5.0 * a.soa[F_R * a.cap + b] * ina * dot;
+          else
+            da -= 3. / 5. * dot * ah;
         }
-        double drdt = 0;
-        if (a.formulation == VFMM_RVPM) {
-          const double na = sqrt(al[0] * al[0] + al[1] * al[1] + al[2] * al[2]);
-          const double ah[3] = {al[0] / na, al[1] / na, al[2] / na};
-          const double dot   = dadt[0] * ah[0] + dadt[1] * ah[1] + dadt[2] * ah[2];
-          for (int aa = 0; aa < 3; aa++)
-            dadt[aa] -= 3. / 5. * dot * ah[aa];
-          drdt -= 1.0 / 5.0 * a.soa[F_R * a.cap + b] / na * dot;
+        if (ok) {
+#pragma unroll
+          for (int c = 0; c < 3; c++)
+            out[((q == 0 ? F_U : F_J) + comp[c] - (q == 0 ? 0 : 3)) * a.cap + b] = r3[c];
+          if (q == 0)
+            out[F_DRDT * a.cap + b] = drdt;
+          else
+            out[(F_DADT + q - 1) * a.cap + b] = da;
         }
-        for (int d = 0; d < 3; d++) {
-          out[(F_U + d) * a.cap + b]    = r[d];
-          out[(F_DADT + d) * a.cap + b] = dadt[d];
-        }
-        for (int k = 0; k < 9; k++)
-          out[(F_J + k) * a.cap + b] = r[3 + k];
-        out[F_DRDT * a.cap + b] = drdt;
       }
     }
   }
