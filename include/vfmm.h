@@ -311,7 +311,8 @@ uint64_t vfmm_launch_count(vfmm_handle h);
  * [1] upward, [2] M2L, [3] downward L2L, [4] L2P+P2P, [5] update. */
 int vfmm_phase_times(vfmm_handle h, float *ms, int n);
 /* Sizes of the last tree: cells, leaves, P2P pairs, M2L pairs, P2P body-body
- * interactions (self pairs excluded), max level. */
+ * interactions (self pairs excluded), max level; [6] is 1 when M2L of an
+ * evaluation on these lists runs on the tensor cores (vfmm_config.m2l_kernel). */
 int vfmm_tree_stats(vfmm_handle h, uint64_t *stats, int n);
 /* Page-lock and map a host range (cudaHostRegister, mapped).  Calls given
  * bodies that lie wholly in such a range read and write them directly from

@@ -203,9 +203,9 @@ class FMMCalculator:
         return M, L
 
     def stats(self) -> dict:
-        v = (ctypes.c_uint64 * 6)()
-        self._check(lib().vfmm_tree_stats(self._h, v, 6))
-        return dict(zip(["cells", "leaves", "p2p_pairs", "m2l_pairs", "p2p_interactions", "max_level"], map(int, v)))
+        v = (ctypes.c_uint64 * 7)()
+        self._check(lib().vfmm_tree_stats(self._h, v, 7))
+        return dict(zip(["cells", "leaves", "p2p_pairs", "m2l_pairs", "p2p_interactions", "max_level", "m2l_tensor"], map(int, v)))
 
     def phase_times(self) -> dict:
         v = (ctypes.c_float * 6)()

@@ -1650,9 +1650,9 @@ int vfmm_tree_stats(vfmm_handle h, uint64_t *st, int n)
     if (!h->has_tree)
       throw Error(VFMM_ERR_STATE, "no tree");
     read_info(h);
-    const uint64_t v[6] = {(uint64_t)h->tree.ncells, (uint64_t)h->tree.nleaves, (uint64_t)h->lists.n_p2p, (uint64_t)h->lists.n_m2l, h->hinfo->p2p_interactions,
-                           (uint64_t)h->tree.maxLevel};
-    for (int i = 0; i < n && i < 6; i++)
+    const uint64_t v[7] = {(uint64_t)h->tree.ncells, (uint64_t)h->tree.nleaves, (uint64_t)h->lists.n_p2p, (uint64_t)h->lists.n_m2l, h->hinfo->p2p_interactions,
+                           (uint64_t)h->tree.maxLevel, (uint64_t)tensor_m2l(h)};
+    for (int i = 0; i < n && i < 7; i++)
       st[i] = v[i];
   });
 }

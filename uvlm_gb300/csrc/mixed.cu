@@ -563,13 +563,12 @@ struct L2P32Sizes {
   static constexpr int    CH = CH_;
   static constexpr int    BLOCKS = CH == 512 ? 7 : 5; // resident blocks per SM the launch bounds ask for
   static constexpr size_t bytes =
-      (size_t)CH * 2 * sizeof(float4) + 128 * (sizeof(float4) + sizeof(int)) + (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zf);
-  static_assert((size_t)CH * 2 * sizeof(float4) >= 2 * 128 * 12 * sizeof(float), "the staging buffer holds the reduction");
+      (size_t)(CH / 2) * 5 * sizeof(float4) + 128 * (sizeof(float4) + sizeof(int)) + (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zf);
+  static_assert((size_t)(CH / 2) * 5 * sizeof(float4) >= 2 * 128 * 12 * sizeof(float), "the staging buffer holds the reduction");
 };
 
 constexpr float kInv4pi = 0.0795774715459476679f;
 constexpr float kC2spi  = 1.12837916709551257f; // 2/sqrt(pi)
-constexpr float kKS     = 0.0317468755f;        // (2/sqrt(pi)) / (8 sqrt(2) pi)
 constexpr float kIsq2   = 0.707106781186547524f;
 
 // ---- packed FP32 (two sources per lane) --------------------------------------
@@ -615,8 +614,9 @@ constexpr float kErfcx5 = -0.2134859561920166f;
 
 // Weights of the regularised Biot-Savart kernel (multipoleKernels.hpp:239-283)
 // for two pairs at once, from R^2, w = 1/(2 sigma^2) and s = 1/(sqrt(2) sigma)
-// of the source: velocity G = g(rho) / (4 pi R^3) and half the gradient weight
-// A = (w t2 - 1.5 g / R^2) / (4 pi R^3), rho = R s, g = erf(rho) - t2,
+// of the source: velocity G = g(rho) / R^3 and half the gradient weight
+// A = (w t2 - 1.5 g / R^2) / R^3 (both without the kernel's 1/(4 pi), which the
+// caller applies to its sums), rho = R s, g = erf(rho) - t2,
 // t2 = (2/sqrt(pi)) rho e^(-rho^2), evaluated as g = 1 - e^(-rho^2) H(rho),
 // H = erfcx(rho) + (2/sqrt(pi)) rho, from the exponential t2 needs and the fit
 // above (no erf call).  Pairs with rho^2 < 0.25 take the x^3-scaled series
@@ -639,13 +639,13 @@ __device__ __forceinline__ void p2p_weights2(float2 R2, float2 w, float2 s, floa
   const float2 t2 = mul2(kx, ex);
   const float2 gg = fma2(mul2(ex, fma2(q, t, kx)), pk(-1.f, -1.f), pk(1.f, 1.f)); // erf - t2
   const float2 ri2 = mul2(ri, ri);
-  const float2 c4  = mul2(mul2(ri2, ri), pk(kInv4pi, kInv4pi));
+  const float2 c4  = mul2(ri2, ri);
   G                = mul2(gg, c4);
   A                = mul2(fma2(mul2(gg, ri2), pk(-1.5f, -1.5f), mul2(t2, w)), c4);
   if (RS.x < 0.25f || RS.y < 0.25f) {
-    // g / rho^3 and the gradient's (3 g - rho g') / rho^5 as series in rho^2;
-    // is^3 = 2 sqrt(2) s^3 and is^5 / 2 = 2 sqrt(2) s^5 with is = 1/sigma
-    constexpr float kK3 = kKS * 2.82842712474619010f;
+    // g / rho^3 and the gradient's (3 g - rho g') / rho^5 as series in
+    // rho^2, times (2/sqrt(pi)) s^3 and (2/sqrt(pi)) s^5
+    constexpr float kK3 = kC2spi;
     const float     r2[2] = {RS.x, RS.y}, q2[2] = {R2.x, R2.y}, sv[2] = {s.x, s.y};
     float           g2[2] = {G.x, G.y}, a2[2] = {A.x, A.y};
 #pragma unroll
@@ -693,8 +693,8 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
   constexpr int K = S::K, K1 = S::K1, K2 = S::K2, CH = S::CH, LG = 128;
   constexpr int D1 = P - 1, D2 = P - 2;
   extern __shared__ float4 smem32[];
-  float4 *Sq   = smem32;   // staged source pairs, four float4 per pair of bodies
-  float4 *Loff = Sq + 2 * CH; // per source leaf of the current group: centre offset, w = body start (int bits)
+  float4 *Sq   = smem32;   // staged source pairs, five float4 per pair of bodies
+  float4 *Loff = Sq + 5 * (CH / 2); // per source leaf of the current group: centre offset, w = body start (int bits)
   int    *Lcnt = reinterpret_cast<int *>(Loff + LG);
   __shared__ int Lpre[LG + 1]; // exclusive prefix of Lcnt over the group; Lpre[ng] = the group's bodies
   static_assert(CH % 128 == 0, "every thread stages the same number of chunk elements");
@@ -835,14 +835,16 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
         __syncthreads();
         // The group's source bodies as one sequence (leaf by leaf) cut into
         // chunks of CH, staged as pairs of consecutive bodies: pair k is four
-        // float4, {-x, -y}, {-z, s}, {alpha_x, alpha_y}, {alpha_z, w} of bodies
-        // 2k and 2k + 1 (each float2 = the two bodies), positions relative to
-        // the target leaf's centre, s = 1/(sqrt(2) sigma), w = 1/(2 sigma^2).
-        // Element e = tid + 128 i finds its leaf by binary search over Lpre,
-        // loads its body, and swaps half of its words with lane e ^ 1, so that
-        // the even lane stores the pair's position words and the odd lane its
-        // strength words.  An odd count is padded with a body of zero strength
-        // far away, whose terms are exactly zero.
+        // five float4, {-x, -y}, {-z, s}, {alpha_x, alpha_y}, {alpha_z, -alpha_x},
+        // {-alpha_y, -alpha_z} of bodies 2k and 2k + 1 (each float2 = the two
+        // bodies), positions relative to the target leaf's centre,
+        // s = 1/(sqrt(2) sigma) (and 1/(2 sigma^2) = s^2); both signs of alpha
+        // make each cross-product component one multiply and one FMA.  Element
+        // e = tid + 128 i finds its leaf by binary search over Lpre, loads its
+        // body, and swaps words with lane e ^ 1, so that the even lane stores
+        // the pair's float4 0, 1, 4 and the odd lane float4 2, 3.  An odd count
+        // is padded with a body of zero strength far away, whose terms are
+        // exactly zero.
         const int total = Lpre[ng];
         for (int c0 = 0; c0 < total; c0 += CH) {
           const int cnt = min(CH, total - c0), npair = (cnt + 1) >> 1;
@@ -850,7 +852,7 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
 #pragma unroll
           for (int i = 0; i < CH / 128; i++) {
             const int e  = threadIdx.x + 128 * i;
-            float     nx = 1e3f, ny = 1e3f, nz = 1e3f, sv = 1.f, wv = 1.f, ax = 0.f, ay = 0.f, az = 0.f;
+            float     nx = 1e3f, ny = 1e3f, nz = 1e3f, sv = 1.f, ax = 0.f, ay = 0.f, az = 0.f;
             if (e < cnt) {
               const int g = c0 + e;
               int       lb = 0, ub = ng - 1; // the last leaf with Lpre <= g
@@ -867,7 +869,6 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
               nx = -(p.x + o.x);
               ny = -(p.y + o.y);
               nz = -(p.z + o.z);
-              wv = p.w;
               sv = q.w * kIsq2;
               ax = q.x;
               ay = q.y;
@@ -876,15 +877,18 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
             const float v0 = __shfl_xor_sync(0xffffffffu, odd ? nx : ax, 1);
             const float v1 = __shfl_xor_sync(0xffffffffu, odd ? ny : ay, 1);
             const float v2 = __shfl_xor_sync(0xffffffffu, odd ? nz : az, 1);
-            const float v3 = __shfl_xor_sync(0xffffffffu, odd ? sv : wv, 1);
+            const float v3 = __shfl_xor_sync(0xffffffffu, odd ? sv : -ax, 1);
+            const float v4 = __shfl_xor_sync(0xffffffffu, -ay, 1);
+            const float v5 = __shfl_xor_sync(0xffffffffu, -az, 1);
             const int   k  = e >> 1;
             if (k < npair) {
               if (!odd) {
-                Sq[4 * k]     = make_float4(nx, v0, ny, v1);
-                Sq[4 * k + 1] = make_float4(nz, v2, sv, v3);
+                Sq[5 * k]     = make_float4(nx, v0, ny, v1);
+                Sq[5 * k + 1] = make_float4(nz, v2, sv, v3);
+                Sq[5 * k + 4] = make_float4(-ay, v4, -az, v5);
               } else {
-                Sq[4 * k + 2] = make_float4(v0, ax, v1, ay);
-                Sq[4 * k + 3] = make_float4(v2, az, v3, wv);
+                Sq[5 * k + 2] = make_float4(v0, ax, v1, ay);
+                Sq[5 * k + 3] = make_float4(v2, az, v3, -ax);
               }
             }
           }
@@ -895,22 +899,22 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
               // velocity V, G alpha (E) and half the gradient's A-part (J),
               // each as two FP32 partial sums (one per body of a pair)
               float2 V0{0.f, 0.f}, V1{0.f, 0.f}, V2{0.f, 0.f}, E0{0.f, 0.f}, E1{0.f, 0.f}, E2{0.f, 0.f};
-              float2 J[9];
+              float2 J[8];
 #pragma unroll
-              for (int u = 0; u < 9; u++)
+              for (int u = 0; u < 8; u++)
                 J[u] = pk(0.f, 0.f);
               const int kend = min(npair, k0 + 16 * Gt);
               for (int k = k0; k < kend; k += Gt) {
-                const float4 f0 = Sq[4 * k], f1 = Sq[4 * k + 1], f2 = Sq[4 * k + 2], f3 = Sq[4 * k + 3];
+                const float4 f0 = Sq[5 * k], f1 = Sq[5 * k + 1], f2 = Sq[5 * k + 2], f3 = Sq[5 * k + 3], f4 = Sq[5 * k + 4];
                 const float2 dx = add2(px, pk(f0.x, f0.y)), dy = add2(py, pk(f0.z, f0.w)), dz = add2(pz, pk(f1.x, f1.y));
                 const float2 ax = pk(f2.x, f2.y), ay = pk(f2.z, f2.w), az = pk(f3.x, f3.y);
                 const float2 R2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+                const float2 sv = pk(f1.z, f1.w);
                 float2       G, A;
-                p2p_weights2(R2, pk(f3.z, f3.w), pk(f1.z, f1.w), G, A);
-                const float2 m1 = pk(-1.f, -1.f);
-                const float2 c0 = fma2(mul2(dz, ay), m1, mul2(dy, az)); // d x alpha
-                const float2 c1 = fma2(mul2(dx, az), m1, mul2(dz, ax));
-                const float2 c2 = fma2(mul2(dy, ax), m1, mul2(dx, ay));
+                p2p_weights2(R2, mul2(sv, sv), sv, G, A);
+                const float2 c0 = fma2(dz, pk(f4.x, f4.y), mul2(dy, az)); // d x alpha
+                const float2 c1 = fma2(dx, pk(f4.z, f4.w), mul2(dz, ax));
+                const float2 c2 = fma2(dy, pk(f3.z, f3.w), mul2(dx, ay));
                 V0              = fma2(G, c0, V0);
                 V1              = fma2(G, c1, V1);
                 V2              = fma2(G, c2, V2);
@@ -926,19 +930,21 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
                 J[5]            = fma2(a1, dz, J[5]);
                 J[6]            = fma2(a2, dx, J[6]);
                 J[7]            = fma2(a2, dy, J[7]);
-                J[8]            = fma2(a2, dz, J[8]);
               }
               // velocity (0..2) and gradient (3..11, J[a][b] at 3 + 3a + b):
               // J[a][b] = 2 J_ab + the G alpha terms of the kernel's
-              // antisymmetric part; the near field enters with a minus sign
-              const float ex = E0.x + E0.y, ey = E1.x + E1.y, ez = E2.x + E2.y;
+              // antisymmetric part, all times 1/(4 pi); the A-part is
+              // trace-free ((d x alpha) . d = 0), so J_22 = -(J_00 + J_11); the
+              // near field enters with a minus sign
+              const float ex = kInv4pi * (E0.x + E0.y), ey = kInv4pi * (E1.x + E1.y), ez = kInv4pi * (E2.x + E2.y);
               float       v[12];
-              v[0] = V0.x + V0.y;
-              v[1] = V1.x + V1.y;
-              v[2] = V2.x + V2.y;
+              v[0] = kInv4pi * (V0.x + V0.y);
+              v[1] = kInv4pi * (V1.x + V1.y);
+              v[2] = kInv4pi * (V2.x + V2.y);
 #pragma unroll
-              for (int u = 0; u < 9; u++)
-                v[3 + u] = 2.f * (J[u].x + J[u].y);
+              for (int u = 0; u < 8; u++)
+                v[3 + u] = (2.f * kInv4pi) * (J[u].x + J[u].y);
+              v[11] = -(v[3] + v[7]);
               v[4] += ez;
               v[5] -= ey;
               v[6] -= ez;
