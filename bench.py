@@ -176,7 +176,7 @@ P2P_FLOPS = 84  # per body-body interaction, counted from multipoleKernels.hpp:2
 # per M2L pair for the CUDA-core and the tensor-core M2L, per body for the leaf
 # kernel (profiles/k_m2l32v2_k_l2p_p2p32_cloud512K_p10.md,
 # profiles/k_m2l_tc_cloud512K_p10.md, profiles/k_l2p_p2p32_cloud512K_p10.md).
-NCU_TRAFFIC_MIXED_P10 = {"m2l": 359.0e6 / 3881744, "m2l_tc": (578.5e6 + 91.3e6) / 3881744, "l2p_p2p": (129.3e6 + 45.4e6) / 524288}
+NCU_TRAFFIC_MIXED_P10 = {"m2l": 359.0e6 / 3881744, "m2l_tc": (578.5e6 + 91.3e6) / 3881744, "l2p_p2p": (125.1e6 + 40.5e6) / 524288}
 # tensor-pipe share of the tensor M2L's cycles in the same capture
 NCU_TC_PIPE_ACTIVE = 0.241
 # dense TF32 tensor rate relative to dense BF16 (nominal GB300 figures, 1.1 and

@@ -273,6 +273,31 @@ def test_mixed_matches_fp64_fmm(vfmm_lib, kind, n, P, ncrit, theta):
     assert ev < 1e-6 and eJ < 1e-6 and ed < 1e-6, (ev, eJ, ed)
 
 
+@pytest.mark.parametrize("ncrit,formulation,stretching", [(256, "rVPM", "Transposed"), (128, "cVPM", "Classic"), (64, "rVPM", "Classic"),
+                                                         (16, "rVPM", "Transposed")])
+def test_mixed_leaf_sizes_and_stretching(vfmm_lib, ncrit, formulation, stretching):
+    """The mixed leaf kernel's per-body epilogue (four lanes per body: velocity
+    and one dadt component each, the rVPM dot product summed across the four)
+    against the FP64 path: leaves of up to 256 bodies (target chunks of 128, so
+    several passes of the four-lane loop), classic and transposed stretching,
+    cVPM and rVPM."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(40000, seed=9)
+    out = {}
+    for prec in ["fp64", "mixed"]:
+        with FMMCalculator(p=10, ncrit=ncrit, theta=0.5, precision=prec, formulation=formulation, stretching=stretching) as c:
+            bb = b.copy()
+            c.init(bb)
+            c.calculate()
+            c.copyBodies2Host(bb)
+            out[prec] = bb
+    assert (out["fp64"]["X"] == out["mixed"]["X"]).all()
+    ev = rel_l2(out["mixed"]["velocity"], out["fp64"]["velocity"])
+    eJ = rel_l2(out["mixed"]["J"], out["fp64"]["J"])
+    ed = rel_l2(out["mixed"]["dadt"], out["fp64"]["dadt"])
+    assert ev < 1e-6 and eJ < 1e-6 and ed < 1e-6, (ev, eJ, ed)
+
+
 @pytest.mark.parametrize("kind,n,P,ncrit,theta", [("cloud", 40000, 10, 64, 0.5), ("cloud", 30000, 9, 64, 0.5), ("cloud", 20000, 8, 32, 0.3),
                                                   ("ring", 96, 8, 32, 0.5), ("ring", 64, 10, 32, 0.5), ("leapfrog", 64, 10, 32, 0.47),
                                                   ("wing", 60, 10, 64, 0.5)])
