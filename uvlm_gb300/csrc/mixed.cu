@@ -673,9 +673,10 @@ __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v)
   lo += e;
 }
 
-// One block (128 threads) per target leaf.  Thread l works for target
-// t = l % nt (nt targets in this chunk) as member g = l / nt of G = 128 / nt
-// threads:
+// One block (128 threads) per target leaf.  Each thread works for one target
+// t of the chunk (nt targets) as member g of its G or G - 1 members (G =
+// ceil(128 / nt)); lanes are ordered so that a warp serves targets with the
+// same member count where it can:
 //  * far field: member g evaluates the columns m = g, g+G, ... of the leaf's
 //    derivative expansions at the target;
 //  * near field: the bodies of the leaf's P2P source leaves are staged in
@@ -744,9 +745,28 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
     for (int tc = 0; tc < nb; tc += 128) {
       // every thread works: the first `full` targets of the chunk have G members,
       // the others G - 1; member g of target tt takes every Gt-th column / source
-      const int  nt = min(128, nb - tc);
-      const int  G = (128 + nt - 1) / nt, full = 128 - (G - 1) * nt;
-      const int  tt = threadIdx.x % nt, g = threadIdx.x / nt, Gt = tt < full ? G : G - 1;
+      const int nt = min(128, nb - tc);
+      const int G = (128 + nt - 1) / nt, full = 128 - (G - 1) * nt;
+      // With at most five members per target (26 or more targets), lanes
+      // 0 .. full G - 1 serve the targets with G members and the others the
+      // targets with G - 1, so that a warp's lanes mostly share a trip count
+      // (a 32-body leaf: 96% of the near-field lane slots busy instead of
+      // 88%).  With more members per target a warp would then read too many
+      // different staged pairs, and lane l serves target l % nt as member
+      // l / nt.  Member g of target tt keeps partial-sum slot g nt + tt.
+      int tt, g;
+      if (G > 5 || full == nt) {
+        tt = threadIdx.x % nt;
+        g  = threadIdx.x / nt;
+      } else if (threadIdx.x < full * G) {
+        tt = threadIdx.x % full;
+        g  = threadIdx.x / full;
+      } else {
+        const int l = threadIdx.x - full * G;
+        tt          = full + l % (nt - full);
+        g           = l / (nt - full);
+      }
+      const int  Gt = tt < full ? G : G - 1, slot = g * nt + tt;
       const bool active = g < Gt;
       float      hi[12], lo[12];
       for (int k = 0; k < 12; k++)
@@ -962,8 +982,8 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
       __syncthreads(); // staging buffer free: reuse it for the partial sums
 #pragma unroll
       for (int k = 0; k < 12; k++) {
-        rhi[threadIdx.x * 12 + k] = hi[k];
-        rlo[threadIdx.x * 12 + k] = lo[k];
+        rhi[slot * 12 + k] = hi[k];
+        rlo[slot * 12 + k] = lo[k];
       }
       __syncthreads();
       // Four adjacent lanes per target (item w = 4 t + q): q = 0 combines the
