@@ -505,8 +505,9 @@ def run_rings64(args, dist: Dist) -> dict | None:
     kw = dict(p=8, ncrit=32, theta=0.5, integration="RK2", precision=args.precision, device=dist.local_rank)
     tuned = None
     if args.autotune:
-        # leaf size and M2L batch tuned per size bucket (N within a factor of 2)
-        # on the bucket's median system, then used by every handle of the bucket
+        # leaf size, P2P tile and M2L batch tuned per size bucket (N within a
+        # factor of 2) on the bucket's median system, then used by every handle
+        # of the bucket
         buckets = {}
         for i, b in enumerate(systems):
             buckets.setdefault(int(np.log2(b.size)), []).append(i)
@@ -515,10 +516,12 @@ def run_rings64(args, dist: Dist) -> dict | None:
             med = sorted(idx, key=lambda i: systems[i].size)[len(idx) // 2]
             with FMMCalculator(**kw) as c:
                 t = c.autotune(systems[med], args.dt)
-            tuned[key] = {"systems": len(idx), "ncrit": t["ncrit"], "m2l_batch": t["m2l_batch"],
+            tuned[key] = {"systems": len(idx), "ncrit": t["ncrit"], "m2l_batch": t["m2l_batch"], "p2p_chunk": t["p2p_chunk"],
                           "ms_per_stage": t["ms_per_stage"], "default_ms_per_stage": t["default_ms_per_stage"]}
+        mixed = args.precision == "mixed"
         calcs = [FMMCalculator(**dict(kw, ncrit=tuned[int(np.log2(b.size))]["ncrit"],
-                                      m2l_batch=tuned[int(np.log2(b.size))]["m2l_batch"] if args.precision == "mixed" else 0))
+                                      m2l_batch=tuned[int(np.log2(b.size))]["m2l_batch"] if mixed else 0,
+                                      p2p_chunk=tuned[int(np.log2(b.size))]["p2p_chunk"] if mixed else 0))
                  for b in systems]
     else:
         calcs = [FMMCalculator(**kw) for _ in systems]
