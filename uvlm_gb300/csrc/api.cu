@@ -72,6 +72,10 @@ struct vfmm_handle_s {
   vfmm_config  cfg;
   int          device = 0;
   cudaStream_t stream = nullptr;
+  // second stream of the tensor-core M2L's pre-pass, beside the upward pass,
+  // and its fork/join events (made on first use)
+  cudaStream_t side = nullptr;
+  cudaEvent_t  side_go = nullptr, side_done = nullptr;
   cudaEvent_t  ev[16]{};
   cudaEvent_t  ph[8]{};
   bool         ph_valid = false;
@@ -566,11 +570,26 @@ void calculate(vfmm_handle h)
     // the FP32 kernels' scaling length: any positive value is exact; R0 = 0
     // (every body at one point, a single root leaf without far field) uses 1
     m.R0      = h->tree.R0 > 0 ? h->tree.R0 : 1.0;
+    if (m.tc) { // the tensor M2L's pre-pass needs only the tree and lists: beside P2M/M2M
+      if (!h->side) {
+        VFMM_CUDA_TRY(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        VFMM_CUDA_TRY(cudaEventCreateWithFlags(&h->side_go, cudaEventDisableTiming));
+        VFMM_CUDA_TRY(cudaEventCreateWithFlags(&h->side_done, cudaEventDisableTiming));
+      }
+      VFMM_CUDA_TRY(cudaEventRecord(h->side_go, s));
+      VFMM_CUDA_TRY(cudaStreamWaitEvent(h->side, h->side_go, 0));
+      m2l_tensor_prepare(h->side, e, m);
+      VFMM_CUDA_TRY(cudaEventRecord(h->side_done, h->side));
+    }
     p2m_mixed(s, e, m);
     m2m_mixed(s, e, m);
     if (h->timing)
       VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
-    m2l_mixed(s, e, m);
+    if (m.tc) {
+      VFMM_CUDA_TRY(cudaStreamWaitEvent(s, h->side_done, 0));
+      m2l_tensor_run(s, e, m);
+    } else
+      m2l_mixed(s, e, m);
     if (h->timing)
       VFMM_CUDA_TRY(cudaEventRecord(h->ph[3], s));
     l2l_mixed(s, e, m);
@@ -949,6 +968,7 @@ int vfmm_destroy(vfmm_handle h)
     b->release();
   h->tcs.hid.release();
   h->tcs.cidq.release();
+  h->tcs.coords.release();
   h->tcs.table.release();
   if (h->tcs.ncls_host)
     cudaFreeHost(h->tcs.ncls_host);
@@ -973,6 +993,12 @@ int vfmm_destroy(vfmm_handle h)
   for (auto &e : h->ph)
     if (e)
       cudaEventDestroy(e);
+  if (h->side_go)
+    cudaEventDestroy(h->side_go);
+  if (h->side_done)
+    cudaEventDestroy(h->side_done);
+  if (h->side)
+    cudaStreamDestroy(h->side);
   if (h->stream)
     cudaStreamDestroy(h->stream);
   delete h;

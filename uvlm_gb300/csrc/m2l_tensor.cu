@@ -149,6 +149,7 @@ struct TcArgs {
   const int                *tile_cells; // [ntiles][32], -1 = none
   const int                *tile_level;
   const int                *ntiles;     // device scalar
+  int                      *tile_next;  // tiles handed out beyond the first gridDim.x (zeroed per evaluation)
   const float              *Bhi, *Blo;  // [cell][3][KP]
   const float4             *table;      // operators, see k_tc_class_ops
   const int                *cidq;       // table index of each group, at its first pair
@@ -396,8 +397,9 @@ struct TcMeta {
   int    src[32];
 };
 
-// One block (384 threads, one per SM: 512 TMEM columns) walks its tiles'
-// classes in order.  Warp w writes and reads TMEM lanes 32 (w % 4) .. + 31
+// One block (384 threads, one per SM: 512 TMEM columns) walks the classes of
+// its tiles in order: tile blockIdx.x first, then the next unclaimed tile
+// (an atomic counter), so that blocks finish together.  Warp w writes and reads TMEM lanes 32 (w % 4) .. + 31
 // (rows of A and D); warps w, w + 4, w + 8 split each row's A chunks and D
 // columns.  Iteration c:
 //   1. B(c) and A(c) complete -> barrier -> one thread of warp 3 issues the MMAs of
@@ -485,8 +487,11 @@ __global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
     wp1 = a.tile_start[wT + 1];
   }
   auto decode = [&](TcMeta &M) { // decoder warp: the class at the walker into M
-    while (wT < ntiles && we >= wp1) {
-      wT += gridDim.x;
+    while (wT < ntiles && we >= wp1) { // next tile: the first gridDim.x by block index, then whoever is free
+      int next = 0;
+      if (lane == 0)
+        next = (int)gridDim.x + atomicAdd(a.tile_next, 1);
+      wT = __shfl_sync(0xffffffffu, next, 0);
       if (wT < ntiles) {
         we  = a.tile_start[wT];
         wp1 = a.tile_start[wT + 1];
@@ -782,16 +787,32 @@ __global__ void k_tc_assign(const unsigned long long *__restrict__ sk, int n, co
   }
 }
 
-// Pair (t, s) -> key tile(t) << 38 | class, value column(t) << 27 | s.
-__global__ void k_tc_pair_keys(const unsigned long long *__restrict__ pk, int n, int kb, CellsView cv, const int *__restrict__ tile_of,
+// Lattice coordinates of each cell: (x - x0) / R, an odd integer (2 i + 1 for
+// the cell's index i along each axis at its level), with x0 the root cell's
+// lower corner; w = level.  The centres come from the reference's FP64 chain,
+// so the quotient is an odd integer to within far less than 1/2.
+__global__ void k_tc_cell_coords(CellsView cv, int nc, int4 *cc)
+{
+  const double x0 = cv.x[0] - cv.R[0], y0 = cv.y[0] - cv.R[0], z0 = cv.z[0] - cv.R[0];
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const double iR = 1.0 / cv.R[c];
+    cc[c]           = make_int4((int)llrint((cv.x[c] - x0) * iR), (int)llrint((cv.y[c] - y0) * iR), (int)llrint((cv.z[c] - z0) * iR), cv.level[c]);
+  }
+}
+
+// Pair (t, s) -> key tile(t) << 38 | class, value column(t) << 27 | s; the
+// class offset (x_t - x_s) / R_f in units of the finer cell's half-width R_f,
+// from the lattice coordinates in integer arithmetic.
+__global__ void k_tc_pair_keys(const unsigned long long *__restrict__ pk, int n, int kb, const int4 *__restrict__ cc, const int *__restrict__ tile_of,
                                const int *__restrict__ col_of, unsigned long long *keys, uint32_t *vals)
 {
   const unsigned long long smask = (1ull << kb) - 1;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int          t = (int)(pk[q] >> kb), s = (int)(pk[q] & smask);
-    const int          dl = cv.level[t] - cv.level[s];
-    const double       iRf = 1.0 / fmin(cv.R[t], cv.R[s]);
-    const long long    ox = llrint((cv.x[t] - cv.x[s]) * iRf), oy = llrint((cv.y[t] - cv.y[s]) * iRf), oz = llrint((cv.z[t] - cv.z[s]) * iRf);
+    const int4         ct = cc[t], cs = cc[s];
+    const int          dl = ct.w - cs.w, lf = max(ct.w, cs.w), st = lf - ct.w, ss = lf - cs.w;
+    const long long    ox = ((long long)ct.x << st) - ((long long)cs.x << ss), oy = ((long long)ct.y << st) - ((long long)cs.y << ss),
+                    oz = ((long long)ct.z << st) - ((long long)cs.z << ss);
     unsigned long long cls = TC_SENTINEL;
     if (dl >= -14 && dl <= 14 && llabs(ox) <= 1022 && llabs(oy) <= 1022 && llabs(oz) <= 1022)
       cls = ((unsigned long long)(dl + 16) << 33) | ((unsigned long long)(ox + 1024) << 22) | ((unsigned long long)(oy + 1024) << 11) |
@@ -813,13 +834,16 @@ __global__ void k_tc_tile_ranges(const unsigned long long *__restrict__ keys, in
   }
 }
 
+// The pre-pass of one evaluation (tiles, pair keys, class table), which needs
+// only the tree and the lists; it leaves what the kernel launch needs in S.
 template <int P>
-static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+static void m2l_tc_prepare_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
 {
   using G     = TcM2L<P>;
   TcScratch &S = *m.tc;
   const int  nc = e.ncells, np = m.n_m2l;
   VFMM_CUDA_TRY(cudaMemsetAsync(e.L, 0, sizeof(double2) * (size_t)nc * 3 * nterms(P), s));
+  S.launch_tiles = 0;
   if (np == 0 || nc == 0)
     return;
   if (nc >= (1 << TC_COL_SHIFT))
@@ -833,8 +857,9 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   S.tkeys.reserve(nc);
   S.tkeys_sorted.reserve(nc);
   S.tile_of.reserve(nc);
+  S.coords.reserve(nc);
   S.col_of.reserve(nc);
-  S.meta.reserve(3 * TC_L + 2);
+  S.meta.reserve(3 * TC_L + 3);
   S.tile_cells.reserve((size_t)ntmax * 32);
   S.tile_level.reserve(ntmax);
   S.tile_start.reserve(ntmax + 1);
@@ -849,6 +874,7 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   S.cub_tmp.reserve(std::max(b1, b2));
 
   VFMM_CUDA_TRY(cudaMemsetAsync(S.meta.p, 0xFF, sizeof(int) * (3 * TC_L + 2), s));
+  VFMM_CUDA_TRY(cudaMemsetAsync(S.meta.p + 3 * TC_L + 2, 0, sizeof(int), s)); // the tile counter
   VFMM_CUDA_TRY(cudaMemsetAsync(S.tile_cells.p, 0xFF, sizeof(int) * (size_t)ntmax * 32, s));
   k_tc_target_keys<<<grid_for(nc, 256), 256, 0, s>>>(e.cells, e.m2l_start, nc, S.tkeys.p);
   count_launch();
@@ -861,7 +887,9 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   count_launch();
   k_tc_assign<<<grid_for(nc, 256), 256, 0, s>>>(S.tkeys_sorted.p, nc, S.meta.p, S.tile_cells.p, S.tile_level.p, S.tile_of.p, S.col_of.p);
   count_launch();
-  k_tc_pair_keys<<<grid_for(np, 256), 256, 0, s>>>(m.m2l_keys, np, m.m2l_key_bits, e.cells, S.tile_of.p, S.col_of.p, S.pkeys.p, S.pvals.p);
+  k_tc_cell_coords<<<grid_for(nc, 256), 256, 0, s>>>(e.cells, nc, S.coords.p);
+  count_launch();
+  k_tc_pair_keys<<<grid_for(np, 256), 256, 0, s>>>(m.m2l_keys, np, m.m2l_key_bits, S.coords.p, S.tile_of.p, S.col_of.p, S.pkeys.p, S.pvals.p);
   count_launch();
   bytes = S.cub_tmp.cap;
   VFMM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(S.cub_tmp.p, bytes, S.pkeys.p, S.pkeys_sorted.p, S.pvals.p, S.pvals_sorted.p, np, 0,
@@ -900,7 +928,22 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   k_tc_class_index<<<grid_for(np, 256), 256, 0, s>>>(S.pkeys_sorted.p, np, S.hkeys.p, S.hid.p, count, S.cap, S.cidq.p);
   count_launch();
   VFMM_CUDA_TRY(cudaMemcpyAsync(S.ncls_host, count, sizeof(int), cudaMemcpyDeviceToHost, s));
+  S.launch_tiles = ntmax;
+}
 
+// The kernel of one evaluation, after its pre-pass (m2l_tc_prepare_P) and the
+// upward pass that wrote the operand rows.
+template <int P>
+static void m2l_tc_run_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+{
+  using G      = TcM2L<P>;
+  TcScratch &S = *m.tc;
+  const int  np = m.n_m2l, ntmax = S.launch_tiles;
+  if (ntmax == 0)
+    return;
+  int nsm = 0, dev = 0;
+  VFMM_CUDA_TRY(cudaGetDevice(&dev));
+  VFMM_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   TcArgs a{};
   a.keys       = S.pkeys_sorted.p;
   a.vals       = S.pvals_sorted.p;
@@ -909,6 +952,7 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   a.tile_cells = S.tile_cells.p;
   a.tile_level = S.tile_level.p;
   a.ntiles     = S.meta.p + 3 * TC_L;
+  a.tile_next  = S.meta.p + 3 * TC_L + 2;
   a.Bhi        = m.Bhi;
   a.Blo        = m.Blo;
   a.table      = S.table.p;
@@ -926,14 +970,30 @@ static void m2l_tc_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   VFMM_LAUNCH_CHECK();
 }
 
-void m2l_tensor(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+void m2l_tensor_prepare(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
 {
   switch (e.P) {
-  case 8: m2l_tc_P<8>(s, e, m); break;
-  case 9: m2l_tc_P<9>(s, e, m); break;
-  case 10: m2l_tc_P<10>(s, e, m); break;
+  case 8: m2l_tc_prepare_P<8>(s, e, m); break;
+  case 9: m2l_tc_prepare_P<9>(s, e, m); break;
+  case 10: m2l_tc_prepare_P<10>(s, e, m); break;
   default: throw Error(VFMM_ERR_UNSUPPORTED, "tensor-core M2L: order outside 8..10");
   }
+}
+
+void m2l_tensor_run(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+{
+  switch (e.P) {
+  case 8: m2l_tc_run_P<8>(s, e, m); break;
+  case 9: m2l_tc_run_P<9>(s, e, m); break;
+  case 10: m2l_tc_run_P<10>(s, e, m); break;
+  default: throw Error(VFMM_ERR_UNSUPPORTED, "tensor-core M2L: order outside 8..10");
+  }
+}
+
+void m2l_tensor(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
+{
+  m2l_tensor_prepare(s, e, m);
+  m2l_tensor_run(s, e, m);
 }
 
 } // namespace vfmm

@@ -260,6 +260,8 @@ struct TcScratch {
   DevBuf<unsigned long long> tkeys, tkeys_sorted, pkeys, pkeys_sorted;
   DevBuf<uint32_t>           pvals, pvals_sorted;
   DevBuf<int>                tile_of, col_of, tile_cells, tile_level, tile_start, meta;
+  DevBuf<int4>               coords; // per cell: lattice coordinates (odd integers) and level
+  int                        launch_tiles = 0; // tile bound of the prepared evaluation (0: nothing to launch)
   DevBuf<unsigned char>      cub_tmp;
   // operator classes: hash (keys, index per slot), keys by index, index per
   // pair group, operator table for the first `cap` classes; the class count
@@ -293,7 +295,11 @@ struct MixedArgs {
   int                       m2l_key_bits, n_m2l;
   int                      *eval_err;
 };
-// The tensor-core M2L for P in TC_PMIN..TC_PMAX (m2l_tensor.cu).
+// The tensor-core M2L for P in TC_PMIN..TC_PMAX (m2l_tensor.cu): its pre-pass
+// (needs the tree and lists only; zeroes the local expansions), the kernel
+// (needs the pre-pass and the operand rows of the upward pass), or both.
+void m2l_tensor_prepare(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
+void m2l_tensor_run(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
 void m2l_tensor(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
 // Columns per half-tile of the mixed M2L lane tiles: at most 32 tiles per degree.
 __host__ __device__ constexpr int m2l_half_width(int P) { return P >= 16 ? 4 : 2; }
