@@ -176,9 +176,9 @@ P2P_FLOPS = 84  # per body-body interaction, counted from multipoleKernels.hpp:2
 # per M2L pair for the CUDA-core and the tensor-core M2L, per body for the leaf
 # kernel (profiles/k_m2l32v2_k_l2p_p2p32_cloud512K_p10.md,
 # profiles/k_m2l_tc_cloud512K_p10.md, profiles/k_l2p_p2p32_cloud512K_p10.md).
-NCU_TRAFFIC_MIXED_P10 = {"m2l": 359.0e6 / 3881744, "m2l_tc": (578.5e6 + 91.3e6) / 3881744, "l2p_p2p": (125.1e6 + 40.5e6) / 524288}
+NCU_TRAFFIC_MIXED_P10 = {"m2l": 359.0e6 / 3881744, "m2l_tc": (939.6e6 + 93.4e6) / 3881744, "l2p_p2p": (125.1e6 + 40.5e6) / 524288}
 # tensor-pipe share of the tensor M2L's cycles in the same capture
-NCU_TC_PIPE_ACTIVE = 0.241
+NCU_TC_PIPE_ACTIVE = 0.256
 # dense TF32 tensor rate relative to dense BF16 (nominal GB300 figures, 1.1 and
 # 2.25 PFLOP/s), applied to the measured BF16 rate
 TF32_PER_BF16 = 1.1 / 2.25
@@ -313,7 +313,7 @@ def run_ours(args, dist: Dist) -> dict | None:
                       "tensor_pipe_active_ncu": NCU_TC_PIPE_ACTIVE,
                       "note": "achieved counts the algorithmic M2L flops (24 T(p) per pair); the tensor core "
                               "executes about 3x that for the TF32 splits and the dense 128-row operator, and "
-                              "the kernel is latency-bound (tensor pipe 24% busy in ncu), not pipe-bound"})
+                              "the kernel is staging-bound (tensor pipe 26% busy in ncu), not pipe-bound"})
         else:
             r.update({"bound": "fp64" if args.precision == "fp64" else "fp32", "peak": peak_fp.value,
                       "frac": achieved / peak_fp.value if peak_fp.value else None,
