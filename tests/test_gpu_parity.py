@@ -273,6 +273,35 @@ def test_mixed_matches_fp64_fmm(vfmm_lib, kind, n, P, ncrit, theta):
     assert ev < 1e-6 and eJ < 1e-6 and ed < 1e-6, (ev, eJ, ed)
 
 
+def test_tensor_m2l_repeatable(vfmm_lib):
+    """The tensor-core M2L is bit-reproducible: repeated evaluations on one
+    handle (the first builds the classes beyond its initial operator table
+    inside the kernel, later ones read the grown table; tiles go to whichever
+    block is free, and the pre-pass runs on a second stream) and an evaluation
+    on a fresh handle give identical fields."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(200000, seed=41)
+    outs = []
+    kw = dict(p=10, ncrit=64, theta=0.5, precision="mixed", m2l_kernel="tensor")
+    with FMMCalculator(**kw) as c:
+        for _ in range(3):
+            bb = b.copy()
+            c.init(bb)
+            c.calculate()
+            c.copyBodies2Host(bb)
+            outs.append(bb)
+        assert c.stats()["m2l_tensor"] == 1
+    with FMMCalculator(**kw) as c:
+        bb = b.copy()
+        c.init(bb)
+        c.calculate()
+        c.copyBodies2Host(bb)
+        outs.append(bb)
+    for o in outs[1:]:
+        for f in ("velocity", "J", "dadt"):
+            assert np.array_equal(o[f], outs[0][f]), f
+
+
 @pytest.mark.parametrize("ncrit,formulation,stretching", [(256, "rVPM", "Transposed"), (128, "cVPM", "Classic"), (64, "rVPM", "Classic"),
                                                          (16, "rVPM", "Transposed")])
 def test_mixed_leaf_sizes_and_stretching(vfmm_lib, ncrit, formulation, stretching):
