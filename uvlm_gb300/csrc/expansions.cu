@@ -446,9 +446,11 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(DevExp a, double *out)
             if (R2 != 0) {
               const double ax = src[F_A * scap + jb], ay = src[(F_A + 1) * scap + jb], az = src[(F_A + 2) * scap + jb];
               const double sg = src[F_R * scap + jb];
-              const double S2 = sg * sg, RS = R2 / S2 / 2.0, sqrtRS = sqrt(RS);
-              const double erfS = erf(sqrtRS), expm = exp(-RS), invSqrtR2 = 1.0 / sqrt(R2);
-              const double t2 = 2.0 * inv_sqrtpi * sqrtRS * expm, c4 = 0.25 * inv_pi / R2 * invSqrtR2;
+              // one FP64 division and one reciprocal square root per pair (GB300's
+              // FP64 pipe is narrow): w2 = 1/(2 sigma^2), 1/R and 1/R^2
+              const double w2 = 0.5 / (sg * sg), RS = R2 * w2, sqrtRS = sqrt(RS);
+              const double erfS = erf(sqrtRS), expm = exp(-RS), invSqrtR2 = rsqrt(R2), iR2 = invSqrtR2 * invSqrtR2;
+              const double t2 = 2.0 * inv_sqrtpi * sqrtRS * expm, c4 = 0.25 * inv_pi * iR2 * invSqrtR2;
               const double cr0 = c4 * (dy * az - dz * ay), cr1 = c4 * (dz * ax - dx * az), cr2 = c4 * (dx * ay - dy * ax);
               const double gg  = erfS - t2;
               s[0] += cr0 * gg;
@@ -456,7 +458,7 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(DevExp a, double *out)
               s[2] += cr2 * gg;
               if (SENS)
                 continue;
-              double aux = t2 / S2 - 3.0 * gg / R2;
+              double aux = t2 * (2.0 * w2) - 3.0 * gg * iR2;
               s[3] += aux * cr0 * dx;
               s[4] += aux * cr0 * dy;
               s[5] += aux * cr0 * dz;
