@@ -109,6 +109,7 @@ struct vfmm_handle_s {
 
   // expansions
   DevBuf<double2> M, L, Mprep;
+  DevBuf<double2> srcw; // FP64 P2P: per particle 1/(2 sigma^2), 1/(sqrt(2) sigma)
   DevBuf<int4>    items, items32, lanes32;
   int             m2l_batch = 16; // sources per mixed-M2L batch (set per p); VFMM_M2L_BATCH = 8, 16, 24, 30 or 32 overrides
   int             items_P = 0, items_per_lane = 0, items_batch = 0;
@@ -494,6 +495,11 @@ ExpArgs particle_args(vfmm_handle h)
   e.m2l_nitems_per_lane = h->items_per_lane;
   e.stretching          = h->cfg.stretching;
   e.formulation         = h->cfg.formulation;
+  // the FP64 P2P's source weights (the particles; sensors use the FP64
+  // kernels in both precision modes)
+  h->srcw.reserve(h->n);
+  e.srcw = h->srcw.p;
+  e.nsrc = h->n;
   return e;
 }
 
@@ -943,6 +949,7 @@ int vfmm_destroy(vfmm_handle h)
   h->M.release();
   h->L.release();
   h->Mprep.release();
+  h->srcw.release();
   h->items.release();
   h->items32.release();
   h->lanes32.release();

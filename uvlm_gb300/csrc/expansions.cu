@@ -39,6 +39,7 @@ struct DevExp {
   size_t        cap;
   const double *ssoa; // source bodies of P2P; soa except for sensors
   size_t        scap;
+  const double2 *srcw; // per source body: 1/(2 sigma^2), 1/(sqrt(2) sigma)
   double2      *M, *L, *Mprep;
   const int    *leaf_cells;
   int           nleaves;
@@ -445,11 +446,13 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(DevExp a, double *out)
             const double R2 = dx * dx + dy * dy + dz * dz;
             if (R2 != 0) {
               const double ax = src[F_A * scap + jb], ay = src[(F_A + 1) * scap + jb], az = src[(F_A + 2) * scap + jb];
-              const double sg = src[F_R * scap + jb];
-              // one FP64 division and one reciprocal square root per pair (GB300's
-              // FP64 pipe is narrow): w2 = 1/(2 sigma^2), 1/R and 1/R^2
-              const double w2 = 0.5 / (sg * sg), RS = R2 * w2, sqrtRS = sqrt(RS);
-              const double erfS = erf(sqrtRS), expm = exp(-RS), invSqrtR2 = rsqrt(R2), iR2 = invSqrtR2 * invSqrtR2;
+              // the source's w2 = 1/(2 sigma^2) and s = sqrt(w2) made once per
+              // evaluation (k_src_weights): no FP64 division or square root per
+              // pair on GB300's narrow FP64 pipe, only one reciprocal square root
+              const double2 ws = a.srcw[jb];
+              const double  w2 = ws.x, RS = R2 * w2, invSqrtR2 = rsqrt(R2), iR2 = invSqrtR2 * invSqrtR2;
+              const double  sqrtRS = R2 * invSqrtR2 * ws.y;
+              const double  erfS = erf(sqrtRS), expm = exp(-RS);
               const double t2 = 2.0 * inv_sqrtpi * sqrtRS * expm, c4 = 0.25 * inv_pi * iR2 * invSqrtR2;
               const double cr0 = c4 * (dy * az - dz * ay), cr1 = c4 * (dz * ax - dx * az), cr2 = c4 * (dx * ay - dy * ax);
               const double gg  = erfS - t2;
@@ -530,6 +533,15 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(DevExp a, double *out)
   }
 }
 
+// Per P2P source body: w2 = 1/(2 sigma^2) and s = sqrt(w2) = 1/(sqrt(2) sigma).
+__global__ void k_src_weights(const double *__restrict__ soa, size_t cap, int n, double2 *w)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double sg = soa[F_R * cap + i], w2 = 0.5 / (sg * sg);
+    w[i]            = make_double2(w2, sqrt(w2));
+  }
+}
+
 // ------------------------------------------------------------------ host side
 static DevExp dev_args(const ExpArgs &e)
 {
@@ -540,6 +552,7 @@ static DevExp dev_args(const ExpArgs &e)
   d.cap         = e.cap;
   d.ssoa        = e.src_soa ? e.src_soa : e.soa;
   d.scap        = e.src_soa ? e.src_cap : e.cap;
+  d.srcw        = e.srcw;
   d.M           = e.M;
   d.L           = e.L;
   d.Mprep       = e.Mprep;
@@ -641,6 +654,10 @@ static void l2p_P(cudaStream_t s, const ExpArgs &e, double *out)
   DevExp       d     = dev_args(e);
   const size_t bytes = L2PSizes<P>::bytes;
   VFMM_SMEM_ONCE(bytes, k_l2p_p2p<P, SENS>);
+  if (e.nsrc > 0) {
+    k_src_weights<<<grid_for(e.nsrc, 256), 256, 0, s>>>(d.ssoa, d.scap, e.nsrc, e.srcw);
+    count_launch();
+  }
   if (e.nleaves > 0) {
     k_l2p_p2p<P, SENS><<<std::min(e.nleaves, 152 * 16), 128, bytes, s>>>(d, out);
     count_launch();

@@ -236,6 +236,10 @@ struct ExpArgs {
   CellsView     src_cells;
   const double *src_soa;
   size_t        src_cap;
+  // FP64 P2P: per-source-body weights (1/(2 sigma^2), 1/(sqrt(2) sigma)),
+  // written by the leaf pass for its nsrc source bodies
+  double2      *srcw = nullptr;
+  int           nsrc = 0;
 };
 void upward_pass(cudaStream_t s, const ExpArgs &a); // P2M + M2M (FP64)
 void m2m_pass(cudaStream_t s, const ExpArgs &a);    // M2M only (FP64)
