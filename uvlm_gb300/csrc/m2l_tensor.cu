@@ -166,15 +166,6 @@ __device__ __forceinline__ float tc_scale2(float v, int e)
   return (e >= -126 && e <= 127) ? v * __int_as_float((e + 127) << 23) : ldexpf(v, e);
 }
 
-// Two-sum accumulation: hi + lo gains v without losing its low-order bits.
-__device__ __forceinline__ void tc_two_sum(float &hi, float &lo, float v)
-{
-  const float s  = hi + v;
-  const float bb = s - hi;
-  lo += (hi - (s - bb)) + (v - bb);
-  hi = s;
-}
-
 // Operator classes of one evaluation: an open-addressing hash of the class
 // keys (TC_HASH slots) gives each class an index; the operators of the first
 // `cap` indices are built once into a table, in the order the M2L kernel

@@ -51,18 +51,6 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&v)[8])
                : "r"(taddr)
                : "memory");
 }
-// 32 lanes x 32 bits, 32 consecutive columns per thread.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32])
-{
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-               "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
-                 "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
-                 "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
-                 "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-               : "r"(taddr)
-               : "memory");
-}
 __device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -73,22 +61,6 @@ __device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence
 // Shared-memory writes of this thread (generic proxy) visible to the tensor
 // core's reads (async proxy).
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// x with the 13 low mantissa bits cleared: exactly representable in TF32; x -
-// tf32_trunc(x) is exact in FP32 and carries the next 13 bits.
-__host__ __device__ __forceinline__ float tf32_trunc(float v)
-{
-#ifdef __CUDA_ARCH__
-  return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
-#else
-  unsigned u;
-  __builtin_memcpy(&u, &v, 4);
-  u &= 0xFFFFE000u;
-  float r;
-  __builtin_memcpy(&r, &u, 4);
-  return r;
-#endif
-}
 
 // x rounded to the nearest TF32 value (ties away from zero), as an FP32 bit
 // pattern with the 13 low mantissa bits zero; x - tf32_rn(x) is exact in FP32.
