@@ -365,7 +365,9 @@ def run_ours(args, dist: Dist) -> dict | None:
             "config": config_of(args, "flushed between steps (256 MB write)"),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * BODY_DTYPE.itemsize,
                     "d2h_bytes_per_step": n * BODY_DTYPE.itemsize,
-                    "note": f"vfmm_advance (RK2 = {stages} stages) on pinned host exafmm::Body arrays, wall clock"},
+                    "note": f"vfmm_advance (RK2 = {stages} stages) on pinned host exafmm::Body arrays, wall clock; "
+                            "h2d counts the whole records, of which the step reads X, alpha and the radius "
+                            "(the host-link lines those fields touch)"},
             "gpu_launches": int(launches),
             "roofline": roof, "clocks": clk, "phases_ms": phases, "tree": stats}
     if accuracy:

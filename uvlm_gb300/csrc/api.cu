@@ -262,16 +262,48 @@ void *mapped_host(const void *p, size_t bytes)
 
 // Bodies in: from pinned, mapped host memory the transposing kernel reads the
 // records directly over the host link (one pass); otherwise a copy to the
-// device staging buffer first.
-void upload(vfmm_handle h, const vfmm_body *b, size_t n)
+// device staging buffer first.  `fields`: the fields the caller's computation
+// reads (the others are set to NaN on the device).
+void upload(vfmm_handle h, const vfmm_body *b, size_t n, uint64_t fields = ~0ull)
 {
   ensure_bodies(h, n);
   if (const void *d = mapped_host(b, n * sizeof(vfmm_body)))
-    aos_to_soa(h->stream, static_cast<const double *>(d), h->soa[h->cur].p, h->cap, (int)n);
+    aos_to_soa(h->stream, static_cast<const double *>(d), h->soa[h->cur].p, h->cap, (int)n, fields);
   else {
     VFMM_CUDA_TRY(cudaMemcpyAsync(h->aos.p, b, n * sizeof(vfmm_body), cudaMemcpyHostToDevice, h->stream));
-    aos_to_soa(h->stream, h->aos.p, h->soa[h->cur].p, h->cap, (int)n);
+    aos_to_soa(h->stream, h->aos.p, h->soa[h->cur].p, h->cap, (int)n, fields);
   }
+}
+
+// The fields of the caller's records that an advance reads.  The first
+// stage's evaluation stores velocity, J, dadt and dr/dt of every body before
+// anything reads them (both leaf kernels write all four for each body), and
+// its stage update stores RK registers before reading them: all six with
+// storeInitialState (RK2, RK4), the velocity, dadt and dr/dt registers for
+// RK3, whose first stage assigns them.  The other registers pass through to
+// the output unchanged, so they are read (Euler keeps all six).
+uint64_t advance_input_fields(int scheme)
+{
+  uint64_t m    = (1ull << NFIELD) - 1;
+  auto     drop = [&](int f0, int k) {
+    for (int f = f0; f < f0 + k; f++)
+      m &= ~(1ull << f);
+  };
+  drop(F_J, 9);
+  drop(F_U, 3);
+  drop(F_DADT, 3);
+  drop(F_DRDT, 1);
+  if (scheme == VFMM_RK2 || scheme == VFMM_RK4 || scheme == VFMM_RK3) {
+    drop(F_VOLD, 3);
+    drop(F_DOLD, 3);
+    drop(F_DRDTOLD, 1);
+  }
+  if (scheme == VFMM_RK2 || scheme == VFMM_RK4) {
+    drop(F_XOLD, 3);
+    drop(F_AOLD, 3);
+    drop(F_ROLD, 1);
+  }
+  return m;
 }
 
 void fetch_eval_err(vfmm_handle h);
@@ -836,7 +868,7 @@ void advance_batch(vfmm_handle *hs, vfmm_body *const *bodies, const size_t *ns, 
         VFMM_CUDA_TRY(cudaSetDevice(h->device));
         g_launch_counter = &h->launches;
         h->timing        = false;
-        upload(h, bodies[b], ns[b]);
+        upload(h, bodies[b], ns[b], advance_input_fields(h->cfg.integrator));
         const int S = stages_of(h->cfg.integrator);
         for (int st = 0; st < S; st++)
           run_stage(h, st, dt);
@@ -1055,7 +1087,7 @@ int vfmm_advance(vfmm_handle h, vfmm_body *bodies, size_t n, double dt)
   return guarded(h, [&] {
     if (!bodies)
       throw Error(VFMM_ERR_INVALID, "null bodies");
-    upload(h, bodies, n);
+    upload(h, bodies, n, advance_input_fields(h->cfg.integrator));
     const int ns = stages_of(h->cfg.integrator);
     for (int st = 0; st < ns; st++)
       run_stage(h, st, dt);

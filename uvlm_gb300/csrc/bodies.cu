@@ -39,9 +39,50 @@ __global__ void k_soa_to_aos(const double *__restrict__ soa, size_t cap, double 
   }
 }
 
-void aos_to_soa(cudaStream_t s, const double *aos, double *soa, size_t cap, int n)
+// The fields of `mask` only: the host link moves whole 128-byte lines, so a
+// record read in part costs the lines its fields touch (X, alpha and the
+// radius of 2^20 records: 0.75 ms against 1.48 ms for whole records).  The
+// other fields of each body are set to a quiet NaN, so that a field left out
+// that the caller's computation does read shows up in its results.
+struct FieldList {
+  uint64_t      mask;
+  int           n;
+  unsigned char f[NFIELD];
+};
+__global__ void k_aos_to_soa_fields(const double *__restrict__ aos, double *__restrict__ soa, size_t cap, int n, FieldList fl)
 {
-  k_aos_to_soa<<<grid_for(n, 32, 152 * 32), 128, 0, s>>>(aos, soa, cap, n);
+  __shared__ double t[32 * NFIELD + 1];
+  const double      qnan = __longlong_as_double(0x7ff8000000000000LL);
+  for (int b0 = blockIdx.x * 32; b0 < n; b0 += gridDim.x * 32) {
+    const int nb = min(32, n - b0);
+    for (int k = threadIdx.x; k < nb * fl.n; k += blockDim.x) {
+      const int i = k / fl.n, f = fl.f[k % fl.n];
+      t[i * NFIELD + f] = aos[(size_t)(b0 + i) * NFIELD + f];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nb * NFIELD; k += blockDim.x) {
+      const int f = k / nb, i = k % nb;
+      soa[(size_t)f * cap + b0 + i] = ((fl.mask >> f) & 1) ? t[i * NFIELD + f] : qnan;
+    }
+    __syncthreads();
+  }
+}
+
+void aos_to_soa(cudaStream_t s, const double *aos, double *soa, size_t cap, int n, uint64_t mask)
+{
+  mask &= (1ull << NFIELD) - 1;
+  if (mask == (1ull << NFIELD) - 1)
+    k_aos_to_soa<<<grid_for(n, 32, 152 * 32), 128, 0, s>>>(aos, soa, cap, n);
+  else {
+    FieldList fl{};
+    fl.mask = mask;
+    for (int f = 0; f < NFIELD; f++)
+      if ((mask >> f) & 1)
+        fl.f[fl.n++] = (unsigned char)f;
+    if (fl.n == 0)
+      throw Error(VFMM_ERR_INVALID, "no body fields to load");
+    k_aos_to_soa_fields<<<grid_for(n, 32, 152 * 32), 128, 0, s>>>(aos, soa, cap, n, fl);
+  }
   count_launch();
   VFMM_LAUNCH_CHECK();
 }

@@ -192,7 +192,9 @@ void lists_transpose(cudaStream_t s, ListScratch &ls, int n_p2p, int n_m2l, int 
                      int *p2p_start, int *p2p_tgt, int *m2l_start, int *m2l_tgt);
 
 // ---- bodies.cu
-void aos_to_soa(cudaStream_t s, const double *aos, double *soa, size_t cap, int n);
+// Records to field-major arrays; with a mask, only those fields are read and
+// the others are set to NaN.
+void aos_to_soa(cudaStream_t s, const double *aos, double *soa, size_t cap, int n, uint64_t mask = ~0ull);
 void soa_to_aos(cudaStream_t s, const double *soa, size_t cap, double *aos, int n);
 void gather_bodies(cudaStream_t s, const double *src, double *dst, size_t cap, const uint32_t *perm, int n, uint64_t fieldMask);
 void check_finite(cudaStream_t s, const double *soa, size_t cap, int n, DevInfo *info);
