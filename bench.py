@@ -289,7 +289,12 @@ def run_ours(args, dist: Dist) -> dict | None:
     m2l_flops = m2l_flops_per_pair(args.p) * stats["m2l_pairs"]
     p2p_flops = P2P_FLOPS * stats["p2p_interactions"]
     tensor = args.precision == "mixed" and stats.get("m2l_tensor", 0) == 1
-    cand = {"m2l": (phases["m2l"], m2l_flops), "l2p_p2p": (phases["l2p_p2p"], p2p_flops)}
+    split = phases.get("p2p_near", 0.0) > 0
+    # with the split leaf kernel the near pass runs on a second stream beside
+    # M2L: its own events time it (near pass + far pass), and M2L stays the
+    # phase on the critical path
+    cand = {"m2l": (phases["m2l"], m2l_flops),
+            "l2p_p2p": (phases["p2p_near"] + phases["l2p_far"] if split else phases["l2p_p2p"], p2p_flops)}
 
     def roof_of(kern):
         t_k, f_k = cand[kern]
@@ -315,13 +320,19 @@ def run_ours(args, dist: Dist) -> dict | None:
                               "executes about 3x that for the TF32 splits and the dense 128-row operator, and "
                               "the kernel is staging-bound (tensor pipe 26% busy in ncu), not pipe-bound"})
         else:
+            if kern == "l2p_p2p" and split:
+                r.update({"kernel": "l2p_p2p: k_l2p_p2p32 split, near pass (MODE 1) + far pass (MODE 2)",
+                          "near_ms": phases["p2p_near"], "far_ms": phases["l2p_far"],
+                          "note": "the near pass shares every SM with the tensor M2L for the M2L's duration (one "
+                                  "leaf block beside the M2L block), then runs alone; achieved is over the two "
+                                  "passes' own event times, so it includes the shared stretch"})
             r.update({"bound": "fp64" if args.precision == "fp64" else "fp32", "peak": peak_fp.value,
                       "frac": achieved / peak_fp.value if peak_fp.value else None,
                       "peak_source": "measured on this GPU in this run: FMA-chain probe kernel "
                                      "(vfmm_measure_fma_peak); MEASURED_PEAKS.json has no CUDA-core figure"})
         return r
 
-    dom = max(cand, key=lambda k: cand[k][0])
+    dom = "m2l" if split else max(cand, key=lambda k: cand[k][0])
     roof = roof_of(dom)
     roof["other"] = roof_of("l2p_p2p" if dom == "m2l" else "m2l")
 

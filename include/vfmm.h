@@ -308,7 +308,11 @@ int vfmm_synchronize(vfmm_handle h);
 /* Kernel launches issued by this handle since creation. */
 uint64_t vfmm_launch_count(vfmm_handle h);
 /* Per-phase device time of the last calculate/stage, ms: [0] tree+lists,
- * [1] upward, [2] M2L, [3] downward L2L, [4] L2P+P2P, [5] update. */
+ * [1] upward, [2] M2L, [3] downward L2L, [4] L2P+P2P, [5] update.  When the
+ * leaf kernel ran split (mixed mode with the tensor-core M2L: the near field
+ * on a second stream beside M2L, the far field after L2L), [6] is the near
+ * pass from its start to its end and [7] the far pass; both 0 otherwise, and
+ * [3] and [4] then include waits for the near pass. */
 int vfmm_phase_times(vfmm_handle h, float *ms, int n);
 /* Sizes of the last tree: cells, leaves, P2P pairs, M2L pairs, P2P body-body
  * interactions (self pairs excluded), max level; [6] is 1 when M2L of an

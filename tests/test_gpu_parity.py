@@ -302,6 +302,35 @@ def test_tensor_m2l_repeatable(vfmm_lib):
             assert np.array_equal(o[f], outs[0][f]), f
 
 
+@pytest.mark.parametrize("P,formulation,stretching", [(10, "cVPM", "Transposed"), (9, "rVPM", "Classic"), (8, "rVPM", "Transposed")])
+def test_split_leaf_kernel_matches_fused(vfmm_lib, monkeypatch, P, formulation, stretching):
+    """With the tensor-core M2L the leaf kernel runs in two passes: the near
+    field on a second stream beside M2L (its combined sums kept per body as
+    float-float pairs), then the far field, those sums and the epilogue after
+    L2L; VFMM_P2P_OVERLAP=0 keeps the fused kernel.  The two add the same terms
+    in another order: they agree to FP32 rounding, and the split form is
+    bit-reproducible."""
+    from uvlm_gb300 import FMMCalculator, workloads
+    b = workloads.cloud(150000, seed=8)
+    out = {}
+    for ov in ("0", "1", "1"):
+        monkeypatch.setenv("VFMM_P2P_OVERLAP", ov)
+        with FMMCalculator(p=P, ncrit=64, theta=0.5, precision="mixed", m2l_kernel="tensor", formulation=formulation,
+                           stretching=stretching) as c:
+            bb = b.copy()
+            c.init(bb)
+            c.calculate()
+            c.copyBodies2Host(bb)
+            assert c.stats()["m2l_tensor"] == 1
+        if ov in out:
+            for f in ("velocity", "J", "dadt", "drdt"):
+                assert np.array_equal(bb[f], out[ov][f]), f
+        out[ov] = bb
+    fields = ("velocity", "J", "dadt") + (("drdt",) if formulation == "rVPM" else ())
+    for f in fields:
+        assert rel_l2(out["1"][f], out["0"][f]) < 1e-6, f
+
+
 @pytest.mark.parametrize("ncrit,formulation,stretching", [(256, "rVPM", "Transposed"), (128, "cVPM", "Classic"), (64, "rVPM", "Classic"),
                                                          (16, "rVPM", "Transposed")])
 def test_mixed_leaf_sizes_and_stretching(vfmm_lib, ncrit, formulation, stretching):

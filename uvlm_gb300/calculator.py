@@ -208,9 +208,9 @@ class FMMCalculator:
         return dict(zip(["cells", "leaves", "p2p_pairs", "m2l_pairs", "p2p_interactions", "max_level", "m2l_tensor"], map(int, v)))
 
     def phase_times(self) -> dict:
-        v = (ctypes.c_float * 6)()
-        self._check(lib().vfmm_phase_times(self._h, v, 6))
-        return dict(zip(["tree_lists", "upward", "m2l", "l2l", "l2p_p2p", "update"], map(float, v)))
+        v = (ctypes.c_float * 8)()
+        self._check(lib().vfmm_phase_times(self._h, v, 8))
+        return dict(zip(["tree_lists", "upward", "m2l", "l2l", "l2p_p2p", "update", "p2p_near", "l2p_far"], map(float, v)))
 
     # -- device-resident stepping
     def load(self, bodies: np.ndarray) -> None:

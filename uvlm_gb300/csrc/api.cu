@@ -76,6 +76,14 @@ struct vfmm_handle_s {
   // and its fork/join events (made on first use)
   cudaStream_t side = nullptr;
   cudaEvent_t  side_go = nullptr, side_done = nullptr;
+  // the split leaf kernel: near field on the second stream beside the tensor
+  // M2L (VFMM_P2P_OVERLAP=0 keeps the fused kernel), its fork/join events and
+  // the per-body near-field sums it hands to the far-field pass
+  int            overlap = 1;
+  cudaEvent_t    near_go = nullptr, near_done = nullptr;
+  DevBuf<float>  near32;
+  cudaEvent_t    pn[3]{};           // timing: near pass start and end (second stream), far pass start
+  bool           split_ran = false; // the last timed evaluation ran the split leaf kernel
   cudaEvent_t  ev[16]{};
   cudaEvent_t  ph[8]{};
   bool         ph_valid = false;
@@ -608,11 +616,19 @@ void calculate(vfmm_handle h)
     // the FP32 kernels' scaling length: any positive value is exact; R0 = 0
     // (every body at one point, a single root leaf without far field) uses 1
     m.R0      = h->tree.R0 > 0 ? h->tree.R0 : 1.0;
+    const bool split = m.tc && h->overlap > 0;
+    h->split_ran     = split;
     if (m.tc) { // the tensor M2L's pre-pass needs only the tree and lists: beside P2M/M2M
       if (!h->side) {
         VFMM_CUDA_TRY(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
         VFMM_CUDA_TRY(cudaEventCreateWithFlags(&h->side_go, cudaEventDisableTiming));
         VFMM_CUDA_TRY(cudaEventCreateWithFlags(&h->side_done, cudaEventDisableTiming));
+        VFMM_CUDA_TRY(cudaEventCreateWithFlags(&h->near_go, cudaEventDisableTiming));
+        VFMM_CUDA_TRY(cudaEventCreateWithFlags(&h->near_done, cudaEventDisableTiming));
+      }
+      if (split) {
+        h->near32.reserve((size_t)h->n * 24);
+        m.near32 = h->near32.p;
       }
       VFMM_CUDA_TRY(cudaEventRecord(h->side_go, s));
       VFMM_CUDA_TRY(cudaStreamWaitEvent(h->side, h->side_go, 0));
@@ -625,7 +641,18 @@ void calculate(vfmm_handle h)
       VFMM_CUDA_TRY(cudaEventRecord(h->ph[2], s));
     if (m.tc) {
       VFMM_CUDA_TRY(cudaStreamWaitEvent(s, h->side_done, 0));
+      if (split)
+        VFMM_CUDA_TRY(cudaEventRecord(h->near_go, s));
       m2l_tensor_run(s, e, m);
+      if (split) { // the near field (no local expansion needed) beside the M2L kernel
+        VFMM_CUDA_TRY(cudaStreamWaitEvent(h->side, h->near_go, 0));
+        if (h->timing)
+          VFMM_CUDA_TRY(cudaEventRecord(h->pn[0], h->side));
+        l2p_p2p_mixed_split(h->side, e, m, h->soa[h->cur].p, 1);
+        if (h->timing)
+          VFMM_CUDA_TRY(cudaEventRecord(h->pn[1], h->side));
+        VFMM_CUDA_TRY(cudaEventRecord(h->near_done, h->side));
+      }
     } else
       m2l_mixed(s, e, m);
     if (h->timing)
@@ -633,7 +660,13 @@ void calculate(vfmm_handle h)
     l2l_mixed(s, e, m);
     if (h->timing)
       VFMM_CUDA_TRY(cudaEventRecord(h->ph[4], s));
-    l2p_p2p_mixed(s, e, m, h->soa[h->cur].p);
+    if (split) {
+      VFMM_CUDA_TRY(cudaStreamWaitEvent(s, h->near_done, 0));
+      if (h->timing)
+        VFMM_CUDA_TRY(cudaEventRecord(h->pn[2], s));
+      l2p_p2p_mixed_split(s, e, m, h->soa[h->cur].p, 2);
+    } else
+      l2p_p2p_mixed(s, e, m, h->soa[h->cur].p);
     if (h->timing)
       VFMM_CUDA_TRY(cudaEventRecord(h->ph[5], s));
   } else {
@@ -940,10 +973,14 @@ int vfmm_create(const vfmm_config *cfg, vfmm_handle *out)
     if (h->cfg.device >= 0)
       VFMM_CUDA_TRY(cudaSetDevice(h->cfg.device));
     VFMM_CUDA_TRY(cudaGetDevice(&h->device));
+    if (const char *ov = getenv("VFMM_P2P_OVERLAP"))
+      h->overlap = atoi(ov);
     VFMM_CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     for (auto &e : h->ev)
       VFMM_CUDA_TRY(cudaEventCreate(&e));
     for (auto &e : h->ph)
+      VFMM_CUDA_TRY(cudaEventCreate(&e));
+    for (auto &e : h->pn)
       VFMM_CUDA_TRY(cudaEventCreate(&e));
     VFMM_CUDA_TRY(cudaMalloc((void **)&h->info, sizeof(DevInfo)));
     VFMM_CUDA_TRY(cudaMalloc((void **)&h->eval_err, sizeof(int)));
@@ -1032,6 +1069,13 @@ int vfmm_destroy(vfmm_handle h)
   for (auto &e : h->ph)
     if (e)
       cudaEventDestroy(e);
+  for (auto &e : h->pn)
+    if (e)
+      cudaEventDestroy(e);
+  if (h->near_go)
+    cudaEventDestroy(h->near_go);
+  if (h->near_done)
+    cudaEventDestroy(h->near_done);
   if (h->side_go)
     cudaEventDestroy(h->side_go);
   if (h->side_done)
@@ -1706,6 +1750,15 @@ int vfmm_phase_times(vfmm_handle h, float *ms, int n)
     VFMM_CUDA_TRY(cudaEventSynchronize(h->ph[6]));
     for (int i = 0; i < n && i < 6; i++)
       VFMM_CUDA_TRY(cudaEventElapsedTime(&ms[i], h->ph[i], h->ph[i + 1]));
+    // the split leaf kernel's own passes: near field (beside M2L), far field
+    if (n > 6)
+      ms[6] = 0.f;
+    if (n > 7)
+      ms[7] = 0.f;
+    if (h->split_ran && n > 6)
+      VFMM_CUDA_TRY(cudaEventElapsedTime(&ms[6], h->pn[0], h->pn[1]));
+    if (h->split_ran && n > 7)
+      VFMM_CUDA_TRY(cudaEventElapsedTime(&ms[7], h->pn[2], h->ph[5]));
   });
 }
 

@@ -406,8 +406,13 @@ struct TcMeta {
 // A fresh D per class keeps the tensor core's truncating FP32 accumulation
 // to a few units in the last place of each class's sum; the classes are
 // summed in FP32 in two levels (groups of 8, then the groups).
+// 384 threads at 136 registers (52,224 of the SM's 65,536; no spills) and
+// 161 KB of shared memory leave room on every SM for one block of the leaf
+// kernel's near pass (128 threads x 96 registers, 39 KB), which runs on a
+// second stream beside this kernel: at 168 registers the kernel alone is 8%
+// faster, but the near field it hides is worth more.
 template <int P>
-__global__ void __launch_bounds__(384, 1) k_m2l_tc(TcArgs a)
+__global__ void __maxnreg__(136) k_m2l_tc(TcArgs a)
 {
   using G = TcM2L<P>;
   constexpr int K = nterms(P), KP = G::KP, N = G::N, NCH = KP / 8;
@@ -956,6 +961,7 @@ static void m2l_tc_run_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   for (int k = 1; k < PMAX + 2; k++)
     a.iR0pow[k] = a.iR0pow[k - 1] * iR0;
   VFMM_SMEM_ONCE(G::smem, k_m2l_tc<P>);
+  VFMM_CARVEOUT_MAX_ONCE(k_m2l_tc<P>);
   k_m2l_tc<P><<<std::max(1, std::min(nsm, ntmax)), 384, G::smem, s>>>(a);
   count_launch();
   VFMM_LAUNCH_CHECK();

@@ -29,6 +29,23 @@ typedef cx<double> zd;
 
 static __constant__ HarmRecip<float> kHarmRecipF = make_harm_recip<float>();
 
+// (n, m) of triangle index tri(n, m) for n <= PMAX: a table read instead of
+// jk_of_m's search, whose trip count differs from lane to lane
+struct TriNM {
+  unsigned char n[nterms(PMAX + 1)], m[nterms(PMAX + 1)];
+};
+constexpr TriNM make_tri_nm()
+{
+  TriNM t{};
+  for (int n = 0; n <= PMAX; n++)
+    for (int m = 0; m <= n; m++) {
+      t.n[tri(n, m)] = (unsigned char)n;
+      t.m[tri(n, m)] = (unsigned char)m;
+    }
+  return t;
+}
+static __device__ const TriNM kTriNM = make_tri_nm();
+
 struct DevMixed {
   CellsView     cv;
   const double *soa;
@@ -46,6 +63,7 @@ struct DevMixed {
   double        R0pow[PMAX + 1], iR0pow[PMAX + 1]; // R0^n, R0^-n
   int           stretching, formulation;
   float        *Bhi, *Blo; // tensor-core M2L operand rows [cell][3][tc_kp(P)] (null: not used)
+  float        *near32;    // near-field sums of the split leaf kernel, [body][hi 12, lo 12]
 };
 
 // 2^e as a double built from its exponent field (-1022 <= e <= 1023; here
@@ -144,7 +162,7 @@ __global__ void __launch_bounds__(64) k_p2m32(DevMixed a)
       continue; // the reference's upward pass skips level 0 (fmmCalculator.hpp:427)
     const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
     const int   lev = a.cv.level[c];
-    const float iR  = (float)ldexp(a.iR0, lev);
+    const float iR  = (float)(a.iR0 * exp2i(lev)); // = ldexp(iR0, lev), exact
     zf          acc[NO];
 #pragma unroll
     for (int i = 0; i < NO; i++)
@@ -220,7 +238,7 @@ __global__ void __launch_bounds__(128) k_m2m32(DevMixed a, const int *cells, int
     }
     if (threadIdx.x < nch) {
       const int    ch = ch0 + threadIdx.x;
-      const double iR = ldexp(a.iR0, lev);
+      const double iR = a.iR0 * exp2i(lev); // = ldexp(iR0, lev), exact
       regular_harmonics<float, P>((float)((a.cv.x[c] - a.cv.x[ch]) * iR), (float)((a.cv.y[c] - a.cv.y[ch]) * iR),
                                   (float)((a.cv.z[c] - a.cv.z[ch]) * iR), Ys + threadIdx.x * K);
     }
@@ -265,7 +283,7 @@ __global__ void __launch_bounds__(128) k_l2l32(DevMixed a, const int *cells, int
     }
     if (threadIdx.x < nch) {
       const int    ch = ch0 + threadIdx.x;
-      const double iR = ldexp(a.iR0, lev);
+      const double iR = a.iR0 * exp2i(lev); // = ldexp(iR0, lev), exact
       regular_harmonics<float, P>((float)((a.cv.x[ch] - a.cv.x[p]) * iR), (float)((a.cv.y[ch] - a.cv.y[p]) * iR),
                                   (float)((a.cv.z[ch] - a.cv.z[p]) * iR), Ys + threadIdx.x * K);
     }
@@ -365,7 +383,7 @@ __global__ void __launch_bounds__(P * 32) k_m2l32v2(DevMixed a, const int4 *__re
       if (lane < cnt) {
         const int    s   = a.m2l_src[qb + lane];
         const int    ls  = a.cv.level[s];
-        const double iRs = ldexp(a.iR0, ls);
+        const double iRs = a.iR0 * exp2i(ls); // = ldexp(iR0, ls), exact
         SrcB[buf][lane]  = s;
         LvlB[buf][lane]  = ls;
         OffB[buf][lane]  = make_float4((float)((tx - a.cv.x[s]) * iRs), (float)((ty - a.cv.y[s]) * iRs), (float)((tz - a.cv.z[s]) * iRs),
@@ -555,16 +573,20 @@ __device__ __forceinline__ zf deriv_coef32(const zf *c, int n, int mu, int axis,
 // blocks per SM, 96 registers: the default) or 512 (seven blocks per SM, 72
 // registers with a few spilled; vfmm_config.p2p_chunk).  At 2^20 bodies the
 // unspilled five-block form is 7% faster than six blocks at 80 registers.
-template <int P, int CH_>
+// MODE 2 (the far-field pass of the split kernel) stages no source pairs: its
+// first buffer only holds the members' partial sums, and more of its blocks
+// fit on an SM to hide the latency of its per-leaf steps.
+template <int P, int CH_, int MODE = 0>
 struct L2P32Sizes {
   static constexpr int    K  = nterms(P);
   static constexpr int    K1 = nterms(P - 1) > 0 ? nterms(P - 1) : 1;
   static constexpr int    K2 = nterms(P - 2) > 0 ? nterms(P - 2) : 1;
   static constexpr int    CH = CH_;
-  static constexpr int    BLOCKS = CH == 512 ? 7 : 5; // resident blocks per SM the launch bounds ask for
+  static constexpr int    SQ4 = MODE == 2 ? 2 * 128 * 12 / 4 : (CH / 2) * 5; // float4 of the first buffer
+  static constexpr int    BLOCKS = MODE == 2 ? 8 : (CH == 512 ? 7 : 5);   // resident blocks per SM the launch bounds ask for
   static constexpr size_t bytes =
-      (size_t)(CH / 2) * 5 * sizeof(float4) + 128 * (sizeof(float4) + sizeof(int)) + (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zf);
-  static_assert((size_t)(CH / 2) * 5 * sizeof(float4) >= 2 * 128 * 12 * sizeof(float), "the staging buffer holds the reduction");
+      (size_t)SQ4 * sizeof(float4) + 128 * (sizeof(float4) + sizeof(int)) + (size_t)(3 * K + 3 * K1 + 9 * K2) * sizeof(zf);
+  static_assert((size_t)SQ4 * sizeof(float4) >= 2 * 128 * 12 * sizeof(float), "the staging buffer holds the reduction");
 };
 
 constexpr float kInv4pi = 0.0795774715459476679f;
@@ -687,15 +709,20 @@ __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v)
 // Everything is folded into a two-sum (float-float) accumulator, the G members
 // are combined in a fixed order, and the result becomes FP64 for the
 // stretching epilogue.  All lanes run the same trip counts.
-template <int P, int CH_>
-__global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(DevMixed a, double *out)
+// MODE 0 does both fields.  The split form runs the near field (MODE 1, which
+// needs no local expansion) beside the tensor-core M2L and stores each body's
+// combined near-field sum as a float-float pair in a.near32; MODE 2 then
+// evaluates the far field, adds it to that pair member by member, and runs
+// the epilogue.
+template <int P, int CH_, int MODE = 0>
+__global__ void __launch_bounds__(128, L2P32Sizes<P, CH_, MODE>::BLOCKS) k_l2p_p2p32(DevMixed a, double *out)
 {
-  using S = L2P32Sizes<P, CH_>;
+  using S = L2P32Sizes<P, CH_, MODE>;
   constexpr int K = S::K, K1 = S::K1, K2 = S::K2, CH = S::CH, LG = 128;
   constexpr int D1 = P - 1, D2 = P - 2;
   extern __shared__ float4 smem32[];
   float4 *Sq   = smem32;   // staged source pairs, five float4 per pair of bodies
-  float4 *Loff = Sq + 5 * (CH / 2); // per source leaf of the current group: centre offset, w = body start (int bits)
+  float4 *Loff = Sq + S::SQ4;      // per source leaf of the current group: centre offset, w = body start (int bits)
   int    *Lcnt = reinterpret_cast<int *>(Loff + LG);
   __shared__ int Lpre[LG + 1]; // exclusive prefix of Lcnt over the group; Lpre[ng] = the group's bodies
   static_assert(CH % 128 == 0, "every thread stages the same number of chunk elements");
@@ -712,32 +739,31 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
     const int    c = a.leaf_cells[li];
     const int    b0 = a.cv.body[c], nb = a.cv.nbody[c];
     const int    lev = a.cv.level[c];
-    const float  iR  = (float)ldexp(a.iR0, lev);
-    const int    q0 = a.p2p_start[c], q1 = a.p2p_start[c + 1];
+    const float  iR  = (float)(a.iR0 * exp2i(lev)); // = ldexp(iR0, lev): a power-of-two scaling, exact
+    const int    q0 = MODE == 2 ? 0 : a.p2p_start[c], q1 = MODE == 2 ? 0 : a.p2p_start[c + 1];
     __syncthreads();
-    for (int e = threadIdx.x; e < 3 * K; e += 128) {
-      int n, m;
-      jk_of_m(e / 3, n, m);
+    for (int e = threadIdx.x; MODE != 1 && e < 3 * K; e += 128) {
+      const int     n = __ldg(&kTriNM.n[e / 3]), m = __ldg(&kTriNM.m[e / 3]);
       const double2 v = a.L[(size_t)c * 3 * K + e];
       const double  s = cell_Rpow(a, lev, n); // scaled local Lt = L R^n
       Lc[e]           = {(float)(v.x * s), (float)(v.y * s)};
     }
     __syncthreads();
-    if (D1 > 0)
+    // component-major (a warp's lanes mostly share the derivative axis, and
+    // so the branches of deriv_coef32); each entry's arithmetic as before
+    if (D1 > 0 && MODE != 1)
       for (int e = threadIdx.x; e < 3 * nterms(D1); e += 128) {
-        const int idx = e / 3, ax = e % 3;
-        int       n, mu;
-        jk_of_m(idx, n, mu);
+        const int ax = e / K1, idx = e % K1; // K1 = nterms(D1)
+        const int n = __ldg(&kTriNM.n[idx]), mu = __ldg(&kTriNM.m[idx]);
         const int b1 = (ax + 1) % 3, c1 = (ax + 2) % 3;
         const zf  p = deriv_coef32(Lc, n, mu, b1, 3, c1), q = deriv_coef32(Lc, n, mu, c1, 3, b1);
         U[idx * 3 + ax] = {inv4pi * (p.r - q.r), inv4pi * (p.i - q.i)};
       }
     __syncthreads();
-    if (D2 > 0)
+    if (D2 > 0 && MODE != 1)
       for (int e = threadIdx.x; e < 9 * nterms(D2); e += 128) {
-        const int idx = e / 9, ae = e % 9, ax = ae / 3, ex = ae % 3;
-        int       n, mu;
-        jk_of_m(idx, n, mu);
+        const int ae = e / K2, idx = e % K2, ax = ae / 3, ex = ae % 3; // K2 = nterms(D2) here
+        const int n = __ldg(&kTriNM.n[idx]), mu = __ldg(&kTriNM.m[idx]);
         JJ[idx * 9 + ae] = deriv_coef32(U, n, mu, ex, 3, ax);
       }
     __syncthreads();
@@ -772,8 +798,9 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
       for (int k = 0; k < 12; k++)
         hi[k] = lo[k] = 0.f;
       float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (active) {
+      if (active)
         pt = a.pos32[b0 + tc + tt];
+      if (active && MODE != 1) {
         // far field: columns m = g, g + G, ... (u scaled by 1/R, J by 1/R^2)
         const float x = pt.x * iR, y = pt.y * iR, z = pt.z * iR;
         const float r2 = x * x + y * y + z * z;
@@ -986,12 +1013,25 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
         rlo[slot * 12 + k] = lo[k];
       }
       __syncthreads();
+      if (MODE == 1) { // the members' near-field sums combined in a fixed order, per body and component
+        for (int w = threadIdx.x; w < 12 * nt; w += 128) {
+          const int t = w / 12, k = w % 12, Gm = t < full ? G : G - 1;
+          float     h = 0.f, l = 0.f;
+          for (int gg = 0; gg < Gm; gg++) {
+            two_sum_add(h, l, rhi[(gg * nt + t) * 12 + k]);
+            l += rlo[(gg * nt + t) * 12 + k];
+          }
+          float *dst = a.near32 + (size_t)(b0 + tc + t) * 24;
+          dst[k]      = h;
+          dst[12 + k] = l;
+        }
+      }
       // Four adjacent lanes per target (item w = 4 t + q): q = 0 combines the
       // velocity, q = 1..3 the three gradient entries that make dadt component
       // q - 1 (column q - 1 of J for the transposed scheme, row q - 1 for the
       // classic one) and that component; the rVPM correction's dot product is
       // summed over the four lanes.  Every lane runs the same trip count.
-      for (int w0 = 0; w0 < 4 * nt; w0 += 128) {
+      for (int w0 = 0; MODE != 1 && w0 < 4 * nt; w0 += 128) {
         const int  w = w0 + threadIdx.x, q = w & 3;
         const bool ok = w < 4 * nt;
         const int  t = ok ? w >> 2 : 0, b = b0 + tc + t, Gm = t < full ? G : G - 1;
@@ -1003,6 +1043,10 @@ __global__ void __launch_bounds__(128, L2P32Sizes<P, CH_>::BLOCKS) k_l2p_p2p32(D
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           float h = 0.f, l = 0.f;
+          if (MODE == 2) { // the body's near-field sum first, then the members' far-field parts
+            h = a.near32[(size_t)b * 24 + comp[c]];
+            l = a.near32[(size_t)b * 24 + 12 + comp[c]];
+          }
           for (int gg = 0; gg < Gm; gg++) {
             two_sum_add(h, l, rhi[(gg * nt + t) * 12 + comp[c]]);
             l += rlo[(gg * nt + t) * 12 + comp[c]];
@@ -1068,6 +1112,7 @@ static DevMixed dev_mixed(const ExpArgs &e, const MixedArgs &m)
   d.formulation = e.formulation;
   d.Bhi         = m.Bhi;
   d.Blo         = m.Blo;
+  d.near32      = m.near32;
   return d;
 }
 
@@ -1115,13 +1160,15 @@ static void m2l32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
   VFMM_LAUNCH_CHECK();
 }
 
-template <int P, int CH>
+template <int P, int CH, int MODE = 0>
 static void l2p32_launch(cudaStream_t s, const DevMixed &d, const ExpArgs &e, double *out)
 {
-  const size_t bytes = L2P32Sizes<P, CH>::bytes;
-  VFMM_SMEM_ONCE(bytes, k_l2p_p2p32<P, CH>);
+  const size_t bytes = L2P32Sizes<P, CH, MODE>::bytes;
+  VFMM_SMEM_ONCE(bytes, k_l2p_p2p32<P, CH, MODE>);
+  if (MODE == 1)
+    VFMM_CARVEOUT_MAX_ONCE(k_l2p_p2p32<P, CH, MODE>);
   if (e.nleaves > 0) {
-    k_l2p_p2p32<P, CH><<<std::min(e.nleaves, 152 * 16), 128, bytes, s>>>(d, out);
+    k_l2p_p2p32<P, CH, MODE><<<std::min(e.nleaves, 152 * 16), 128, bytes, s>>>(d, out);
     count_launch();
   }
 }
@@ -1134,6 +1181,21 @@ static void l2p32_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double
     l2p32_launch<P, 512>(s, d, e, out);
   else
     l2p32_launch<P, 768>(s, d, e, out);
+  VFMM_LAUNCH_CHECK();
+}
+
+// The split leaf kernel (the orders of the tensor-core M2L): MODE 1 near
+// field into m.near32, MODE 2 far field plus that sum and the epilogue.
+template <int P, int MODE>
+static void l2p32_split_P(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out)
+{
+  DevMixed d = dev_mixed(e, m);
+  if (!m.near32)
+    throw Error(VFMM_ERR_INVALID, "split leaf kernel without its near-field buffer");
+  if (m.p2p_chunk == 512)
+    l2p32_launch<P, 512, MODE>(s, d, e, out);
+  else
+    l2p32_launch<P, 768, MODE>(s, d, e, out);
   VFMM_LAUNCH_CHECK();
 }
 
@@ -1203,5 +1265,16 @@ void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m)
 void m2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(m2m32_P, s, e, m) }
 void l2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m) { VFMM_DISPATCH_M(l2l32_P, s, e, m) }
 void l2p_p2p_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out) { VFMM_DISPATCH_M(l2p32_P, s, e, m, out) }
+void l2p_p2p_mixed_split(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out, int mode)
+{
+  if (mode != 1 && mode != 2)
+    throw Error(VFMM_ERR_INVALID, "split leaf kernel: mode must be 1 (near) or 2 (far)");
+  switch (e.P) {
+  case 8: mode == 1 ? l2p32_split_P<8, 1>(s, e, m, out) : l2p32_split_P<8, 2>(s, e, m, out); break;
+  case 9: mode == 1 ? l2p32_split_P<9, 1>(s, e, m, out) : l2p32_split_P<9, 2>(s, e, m, out); break;
+  case 10: mode == 1 ? l2p32_split_P<10, 1>(s, e, m, out) : l2p32_split_P<10, 2>(s, e, m, out); break;
+  default: throw Error(VFMM_ERR_UNSUPPORTED, "the split leaf kernel serves p = 8..10");
+  }
+}
 
 } // namespace vfmm

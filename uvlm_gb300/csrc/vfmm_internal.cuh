@@ -121,6 +121,16 @@ struct PerDeviceOnce {
                                                        (int)(bytes)); });                                        \
   } while (0)
 
+// The shared-memory carveout of a kernel that shares its SMs with another
+// one: the largest shared-memory configuration, so that a tensor M2L block
+// and a leaf block fit on one SM together.
+#define VFMM_CARVEOUT_MAX_ONCE(...)                                                                              \
+  do {                                                                                                          \
+    static ::vfmm::PerDeviceOnce vfmm_once_;                                                                    \
+    vfmm_once_.run([&]() { return cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributePreferredSharedMemoryCarveout, \
+                                                       (int)cudaSharedmemCarveoutMaxShared); });                 \
+  } while (0)
+
 
 // Grow-only device buffer.
 template <class T>
@@ -300,6 +310,7 @@ struct MixedArgs {
   const unsigned long long *m2l_keys;
   int                       m2l_key_bits, n_m2l;
   int                      *eval_err;
+  float                    *near32 = nullptr; // the split leaf kernel's near-field sums, 24 floats per body
 };
 // The tensor-core M2L for P in TC_PMIN..TC_PMAX (m2l_tensor.cu): its pre-pass
 // (needs the tree and lists only; zeroes the local expansions), the kernel
@@ -326,6 +337,9 @@ void m2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m);
 void m2m_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m); // FP32, scaled
 void l2l_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m); // FP32, scaled
 void l2p_p2p_mixed(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out);
+// The leaf kernel in two passes (p = 8..10): mode 1 the near field into
+// m.near32, mode 2 the far field, that sum and the epilogue into out.
+void l2p_p2p_mixed_split(cudaStream_t s, const ExpArgs &e, const MixedArgs &m, double *out, int mode);
 
 // ---- viscous.cu: PSE over the P2P lists, added to dadt in soa (FP64 from the
 // soa fields when pos32 is null, else FP32 from the mixed-mode body records)
