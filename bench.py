@@ -172,13 +172,15 @@ def m2l_flops_per_pair(p: int) -> int:
 P2P_FLOPS = 84  # per body-body interaction, counted from multipoleKernels.hpp:239-283
 
 # DRAM bytes (read + write) per unit of the mixed-precision evaluation kernels
-# at p = 10, from ncu captures of a 2^19-body cloud (3,881,744 M2L pairs):
-# per M2L pair for the CUDA-core and the tensor-core M2L, per body for the leaf
-# kernel (profiles/k_m2l32v2_k_l2p_p2p32_cloud512K_p10.md,
-# profiles/k_m2l_tc_cloud512K_p10.md, profiles/k_l2p_p2p32_cloud512K_p10.md).
-NCU_TRAFFIC_MIXED_P10 = {"m2l": 359.0e6 / 3881744, "m2l_tc": (939.6e6 + 93.4e6) / 3881744, "l2p_p2p": (125.1e6 + 40.5e6) / 524288}
+# at p = 10, from ncu captures of 2^19-body clouds: per M2L pair for the
+# CUDA-core M2L (3,881,744 pairs) and the tensor-core M2L (3,847,952 pairs), per
+# body for the fused leaf kernel and for the split one's near + far passes
+# (profiles/k_m2l32v2_k_l2p_p2p32_cloud512K_p10.md, profiles/k_m2l_tc_cloud512K_p10.md,
+# profiles/k_l2p_p2p32_cloud512K_p10.md, profiles/k_l2p_p2p32_split_cloud512K_p10.md).
+NCU_TRAFFIC_MIXED_P10 = {"m2l": 359.0e6 / 3881744, "m2l_tc": (961.3e6 + 93.5e6) / 3847952,
+                         "l2p_p2p": (125.1e6 + 40.5e6) / 524288, "l2p_p2p_split": (24.2e6 + 201.5e6) / 524288}
 # tensor-pipe share of the tensor M2L's cycles in the same capture
-NCU_TC_PIPE_ACTIVE = 0.256
+NCU_TC_PIPE_ACTIVE = 0.233
 # dense TF32 tensor rate relative to dense BF16 (nominal GB300 figures, 1.1 and
 # 2.25 PFLOP/s), applied to the measured BF16 rate
 TF32_PER_BF16 = 1.1 / 2.25
@@ -301,7 +303,7 @@ def run_ours(args, dist: Dist) -> dict | None:
         achieved = f_k / (t_k * 1e-3) / 1e12
         traffic = None
         if args.precision == "mixed" and args.p == 10:
-            key = "m2l_tc" if kern == "m2l" and tensor else kern
+            key = "m2l_tc" if kern == "m2l" and tensor else ("l2p_p2p_split" if kern == "l2p_p2p" and split else kern)
             traffic = NCU_TRAFFIC_MIXED_P10[key] * (stats["m2l_pairs"] if kern == "m2l" else n)
         r = {"kernel": kern, "achieved": achieved, "unit": "TFLOP/s", "traffic": traffic,
              "traffic_source": "DRAM bytes per unit from an ncu capture of a 2^19-body cloud at p = 10, scaled by "
@@ -318,7 +320,7 @@ def run_ours(args, dist: Dist) -> dict | None:
                       "tensor_pipe_active_ncu": NCU_TC_PIPE_ACTIVE,
                       "note": "achieved counts the algorithmic M2L flops (24 T(p) per pair); the tensor core "
                               "executes about 3x that for the TF32 splits and the dense 128-row operator, and "
-                              "the kernel is staging-bound (tensor pipe 26% busy in ncu), not pipe-bound"})
+                              "the kernel is staging-bound (tensor pipe 23% busy in ncu), not pipe-bound"})
         else:
             if kern == "l2p_p2p" and split:
                 r.update({"kernel": "l2p_p2p: k_l2p_p2p32 split, near pass (MODE 1) + far pass (MODE 2)",
