@@ -137,7 +137,10 @@ int vfmm_copy_bodies_to_host(vfmm_handle h, vfmm_body *bodies, size_t n);
  * configured scheme; each stage rebuilds the tree from the current
  * positions.  `bodies` is read, then overwritten with the bodies after the
  * step in the last stage's tree order (velocity, J, dadt from the last stage's
- * evaluation).  With relax > 0, relaxation follows the step (using that J). */
+ * evaluation).  With relax > 0, relaxation follows the step (using that J).
+ * Only the fields the step reads are loaded: X, alpha and the radius (Euler
+ * and RK3 also the RK registers they carry through); velocity, J, dadt, drdt
+ * and the other registers are written before they are read. */
 int vfmm_advance(vfmm_handle h, vfmm_body *bodies, size_t n, double dt);
 
 /* advance (fmmCalculator.hpp:919-1005) for `count` independent systems at
