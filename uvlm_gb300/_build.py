@@ -2,7 +2,8 @@
 
 Translation units compile in parallel into uvlm_gb300/_build/ and link into
 one shared library; a unit is recompiled when it or a header is newer than its
-object.  No CMake and no torch extension machinery: plain nvcc, so that the
+object.  Each unit's ptxas resource report (registers, spills, static shared
+memory per kernel) is kept beside its object.  No CMake and no torch extension machinery: plain nvcc, so that the
 library has a C ABI (include/vfmm.h) and no dependency on PyTorch.
 """
 from __future__ import annotations
@@ -10,8 +11,10 @@ from __future__ import annotations
 import concurrent.futures as cf
 import glob
 import os
+import re
 import shutil
 import subprocess
+import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
@@ -35,14 +38,30 @@ def _newest_header() -> float:
     return max((os.path.getmtime(h) for h in hdrs), default=0.0)
 
 
+def ptxas_report(name: str) -> str:
+    """Path of the ptxas resource report (registers, spills, static shared
+    memory per kernel) that the build keeps beside csrc/<name>.cu's object."""
+    return os.path.join(OUT_DIR, name + ".ptxas.txt")
+
+
 def _compile(src: str, extra: list[str], verbose: bool) -> str:
     obj = os.path.join(OUT_DIR, os.path.basename(src).replace(".cu", ".o"))
-    if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _newest_header()):
+    report = ptxas_report(os.path.basename(src)[:-3])
+    if os.path.exists(obj) and os.path.exists(report) and \
+            os.path.getmtime(obj) >= max(os.path.getmtime(src), _newest_header()):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-Xptxas", "-v", *extra, "-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
-    subprocess.run(cmd, check=True)
+    r = subprocess.run(cmd, stderr=subprocess.PIPE, text=True)
+    with open(report, "w") as f:
+        f.write(r.stderr)
+    # the resource lines go to the report; anything else the compiler says is shown
+    other = [ln for ln in r.stderr.splitlines() if not ln.startswith("ptxas info") and not re.match(r"^\s+\d+ bytes", ln)]
+    if other:
+        sys.stderr.write("\n".join(other) + "\n")
+    if r.returncode != 0:
+        raise subprocess.CalledProcessError(r.returncode, cmd)
     return obj
 
 
